@@ -1,0 +1,86 @@
+"""Generate golden vectors from the reference library itself.
+
+Runs only where the AHMED sources are available and oracle/ref/build_ref.sh
+has produced oracle/_ref/libahmed_ref.so.  The outputs (small .npz files next
+to this script) are committed; the tests read them on any host.
+
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from ahmed_gb300 import geometry as G  # noqa: E402
+
+EPS = 1e-6
+ETA = 0.8
+
+# name -> (points, bmin)
+CASES = {
+    "fib4096": (lambda: G.fibonacci_sphere(4096), 32),
+    "cube3000": (lambda: G.cube_surface(3000, 5), 32),
+    "ell2500": (lambda: G.ellipsoid_surface(2500, 7), 32),
+    "sph360": (lambda: G.sphere_surface(360, 11), 12),
+    "fib50": (lambda: G.fibonacci_sphere(50), 32),   # single-leaf tree edge case
+}
+FULL_DATA = {"sph360"}          # complete leaf arena committed for these
+GMRES = {"fib4096", "cube3000"}
+
+
+def main():
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    for name, (gen, bmin) in CASES.items():
+        P = gen()
+        h = O.mean_nn(P)
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin),
+               "eta": np.float64(ETA), "eps": np.float64(EPS)}
+        n = P.shape[0]
+        rng = np.random.default_rng(0)
+        x = rng.uniform(-1.0, 1.0, n)
+        X = rng.uniform(-1.0, 1.0, (4, n))
+        for kind, kname in ((O.TREE_BBX, "bbx"), (O.TREE_PCA, "pca")):
+            R = O.RefH(P, kind, bmin, ETA, h)
+            op, po = R.perm()
+            out[f"{kname}_op_perm"] = op
+            out[f"{kname}_po_perm"] = po
+            out[f"{kname}_leaves"] = R.leaves()
+            R.assemble(EPS, nthreads=1)
+            out[f"{kname}_ranks"] = R.ranks()
+            out[f"{kname}_y"] = R.matvec(x, np.zeros(n))
+            Y = np.zeros((4, n))
+            R.matvec(X, Y, d=-0.5)
+            out[f"{kname}_Y4"] = Y
+            if name in FULL_DATA:
+                chunks = [R.leaf_data(l) for l in range(R.nleaves)]
+                offs = np.zeros(R.nleaves + 1, np.uint64)
+                offs[1:] = np.cumsum([c.size for c in chunks])
+                out[f"{kname}_data"] = np.concatenate(chunks) if chunks else np.zeros(0)
+                out[f"{kname}_offsets"] = offs
+            if name in GMRES and kind == O.TREE_BBX:
+                b = np.random.default_rng(3).standard_normal(n)
+                for tag, hh in (("spec", h), ("spd", h / 2.0)):
+                    R2 = O.RefH(P, kind, bmin, ETA, hh)
+                    R2.assemble(EPS, nthreads=1)
+                    xg = np.zeros(n)
+                    ret, e, ns = R2.gmres(b, xg, 1e-8, 30, 150)
+                    out[f"gmres_{tag}"] = np.array([ret, e, ns], np.float64)
+                    out[f"gmres_{tag}_x"] = xg
+                    out[f"gmres_{tag}_h"] = np.float64(hh)
+                out["gmres_b"] = b
+        out["x"] = x
+        out["X4"] = X
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
+if __name__ == "__main__":
+    main()
