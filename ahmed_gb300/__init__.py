@@ -1,0 +1,18 @@
+"""GB300-native H-matrix hot path: ACA assembly, H-matvec and GMRES/CG on sm_103a.
+
+The compute path is libahx.so (hand-written CUDA kernels behind a C ABI,
+include/ahx.h); this package is the host-side mirror of the reference's
+interface.
+"""
+from . import geometry  # noqa: F401
+from .hmatrix import (  # noqa: F401
+    CG,
+    GMRes,
+    HBatch,
+    HMatrix,
+    matgenGeH_omp,
+    mean_nn,
+    mltaGeHGeM,
+    mltaGeHVec,
+)
+from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA  # noqa: F401

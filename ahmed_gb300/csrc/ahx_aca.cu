@@ -1,0 +1,575 @@
+// Batched adaptive cross approximation (ACA) with SVD recompression, FP64.
+//
+// One cooperative group per admissible leaf: a warp for leaves up to 256 rows
+// and columns, a whole CTA for larger ones.  Every per-index array (rows of U,
+// the row counters Z, columns of V, the column counters S) is owned by the
+// thread with index % G == rank, so the only cross-thread traffic is through
+// the group's all-reduces plus one barrier per cross.
+//
+// Algorithm (same control flow, same stopping rule and counters as the
+// reference):
+//   ACA row/column steps      Include/ACA.h:29-213
+//   ACA driver                Include/ACA.h:217-350
+//   leaf policy (maxk, i0)    Include/apprx.h:136-172
+//   recompression addtrll     H/mblock_D.cpp:356-465 (Householder QR in place of
+//                             dgeqrf/dormqr, one-sided Jacobi in place of dgesvd)
+#include <climits>
+
+#include "ahx_aca.cuh"
+
+namespace ahx {
+namespace {
+
+constexpr int KSM = 32;        // ranks up to KSM keep the k x k SVD in shared memory
+constexpr int LDS = KSM + 1;   // padded row stride of the shared k x k arrays
+constexpr int kSmallWarps = 4; // warps (= leaves) per CTA of the small-leaf kernel
+
+// per-group shared scratch (doubles)
+constexpr int kSmemPerGroup = 2 * KSM * LDS + KSM + 2 * KSM + KSM;
+
+struct Blk {
+  PointsSoA P;
+  double diag;
+  uint32_t b1, n1, b2, n2;
+  double* U;
+  double* V;
+  int* Z;
+  int* S;
+};
+
+template <class Grp>
+__device__ __forceinline__ bool owns(const Grp& g, uint32_t i, int G) {
+  return (i % (uint32_t)G) == g.rank;
+}
+
+// next index >= j (cyclic) whose counter is not -1 (ACA.h:29-36)
+template <int G, class Grp>
+__device__ uint32_t nexti(const Grp& g, const int* Z, uint32_t n, uint32_t j) {
+  uint32_t d = 0xffffffffu;
+  for (uint32_t i = g.rank; i < n; i += G)
+    if (Z[i] != -1) d = min(d, i >= j ? i - j : i + n - j);
+  d = g.umin(d);
+  return d == 0xffffffffu ? j : (j + d) % n;
+}
+
+// ACA_row_step (ACA.h:46-130)
+template <int G, class Grp>
+__device__ bool row_step(const Grp& g, const Blk& B, uint32_t& klast, uint32_t& i0, uint32_t k,
+                         uint32_t& no, double& nrmlsk2, double scale) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  double* const pu = B.U + (size_t)k * n1;
+  double* const pv = B.V + (size_t)k * n2;
+  ArgMax am;
+  for (;;) {
+    g.sync();
+    const uint32_t gi = B.b1 + i0;
+    const double xi = B.P.x[gi], yi = B.P.y[gi], zi = B.P.z[gi];
+    am = ArgMax{0.0, 0xffffffffu, 0.0};
+    for (uint32_t j = g.rank; j < n2; j += G) {
+      double v = lap_entry(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
+      for (uint32_t l = 0; l < k; ++l) v = fma(-B.U[(size_t)l * n1 + i0], B.V[(size_t)l * n2 + j], v);
+      pv[j] = v;
+      if (B.S[j] >= 0) {
+        const double a = fabs(v);
+        if (a > am.v) am = ArgMax{a, j, v};
+      }
+    }
+    am = g.argmax(am);
+    if (!(am.v < 1e-14 * scale)) break;
+    if (owns(g, i0, G)) B.Z[i0] = -1;
+    if (++no >= n1) return false;
+    g.sync();
+    i0 = nexti<G>(g, B.Z, n1, i0);
+  }
+  const uint32_t j0 = am.idx;
+  const double sqrtpiv = sqrt(am.v);
+  const double sca = sqrtpiv / am.sv;
+  const double thr = 1e-8 * scale * sqrtpiv;
+  double nrmv2 = 0.0;
+  for (uint32_t j = g.rank; j < n2; j += G) {
+    if (B.S[j] >= 0) {
+      const double e = pv[j] * sca;
+      pv[j] = e;
+      nrmv2 += e * e;
+      if (fabs(e) > thr) ++B.S[j];
+    }
+  }
+  const uint32_t gj = B.b2 + j0;
+  const double xj = B.P.x[gj], yj = B.P.y[gj], zj = B.P.z[gj];
+  for (uint32_t i = g.rank; i < n1; i += G) {
+    double u = lap_entry(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
+    for (uint32_t l = 0; l < k; ++l) u = fma(-B.V[(size_t)l * n2 + j0], B.U[(size_t)l * n1 + i], u);
+    pu[i] = u;
+  }
+  klast = (uint32_t)g.imax(owns(g, i0, G) ? B.Z[i0] : INT_MIN);
+  if (owns(g, i0, G)) B.Z[i0] = -1;
+  if (owns(g, j0, G)) B.S[j0] = -1;
+  ++no;
+  const double dsca = 1.0 / sqrtpiv;
+  double nrmu2 = 0.0;
+  ArgMax nm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t i = g.rank; i < n1; i += G) {
+    const double e = pu[i] * dsca;
+    pu[i] = e;
+    const double ea = fabs(e);
+    if (B.Z[i] >= 0 && ea > thr) ++B.Z[i];
+    nrmu2 += ea * ea;
+    if (B.Z[i] >= 0 && ea > nm.v) nm = ArgMax{ea, i, e};
+  }
+  g.sum2(nrmu2, nrmv2);
+  nm = g.argmax(nm);
+  if (nm.v > 0.0) i0 = nm.idx;
+  nrmlsk2 = nrmu2 * nrmv2;
+  return true;
+}
+
+// ACA_col_step (ACA.h:134-213)
+template <int G, class Grp>
+__device__ bool col_step(const Grp& g, const Blk& B, uint32_t& j0, uint32_t k, uint32_t& no,
+                         double& nrmlsk2, double scale) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  double* const pu = B.U + (size_t)k * n1;
+  double* const pv = B.V + (size_t)k * n2;
+  ArgMax am;
+  for (;;) {
+    g.sync();
+    const uint32_t gj = B.b2 + j0;
+    const double xj = B.P.x[gj], yj = B.P.y[gj], zj = B.P.z[gj];
+    am = ArgMax{0.0, 0xffffffffu, 0.0};
+    for (uint32_t i = g.rank; i < n1; i += G) {
+      double u = lap_entry(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
+      for (uint32_t l = 0; l < k; ++l) u = fma(-B.V[(size_t)l * n2 + j0], B.U[(size_t)l * n1 + i], u);
+      pu[i] = u;
+      if (B.Z[i] >= 0) {
+        const double a = fabs(u);
+        if (a > am.v) am = ArgMax{a, i, u};
+      }
+    }
+    am = g.argmax(am);
+    if (!(am.v < 1e-14 * scale)) break;
+    if (owns(g, j0, G)) B.S[j0] = -1;
+    if (++no >= n2) return false;
+    g.sync();
+    j0 = nexti<G>(g, B.S, n2, j0);
+  }
+  const uint32_t i0 = am.idx;
+  const double sqrtpiv = sqrt(am.v);
+  const double sca = sqrtpiv / am.sv;
+  const double thr = 1e-8 * scale * sqrtpiv;
+  double nrmu2 = 0.0;
+  for (uint32_t i = g.rank; i < n1; i += G) {
+    if (B.Z[i] >= 0) {
+      const double e = pu[i] * sca;
+      pu[i] = e;
+      nrmu2 += e * e;
+      if (fabs(e) > thr) ++B.Z[i];
+    }
+  }
+  const uint32_t gi = B.b1 + i0;
+  const double xi = B.P.x[gi], yi = B.P.y[gi], zi = B.P.z[gi];
+  for (uint32_t j = g.rank; j < n2; j += G) {
+    double v = lap_entry(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
+    for (uint32_t l = 0; l < k; ++l) v = fma(-B.U[(size_t)l * n1 + i0], B.V[(size_t)l * n2 + j], v);
+    pv[j] = v;
+  }
+  if (owns(g, i0, G)) B.Z[i0] = -1;
+  if (owns(g, j0, G)) B.S[j0] = -1;
+  ++no;
+  const double dsca = 1.0 / sqrtpiv;
+  double nrmv2 = 0.0;
+  ArgMax nm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t j = g.rank; j < n2; j += G) {
+    const double e = pv[j] * dsca;
+    pv[j] = e;
+    const double ea = fabs(e);
+    if (B.S[j] >= 0 && ea > thr) ++B.S[j];
+    nrmv2 += ea * ea;
+    if (ea > nm.v) nm = ArgMax{ea, j, e};  // no S filter here, as in the reference
+  }
+  g.sum2(nrmu2, nrmv2);
+  nm = g.argmax(nm);
+  if (nm.v > 0.0) j0 = nm.idx;
+  nrmlsk2 = nrmu2 * nrmv2;
+  return true;
+}
+
+// ACA driver (ACA.h:217-350).  Returns the status, the rank in k.
+template <int G, class Grp>
+__device__ int aca(const Grp& g, const Blk& B, uint32_t i0, uint32_t kmax, uint32_t kcap,
+                   double eps, uint32_t& kout) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  for (uint32_t i = g.rank; i < n1; i += G) B.Z[i] = 0;
+  for (uint32_t j = g.rank; j < n2; j += G) B.S[j] = 0;
+  double scale;
+  {
+    const uint32_t a = B.b1, b = B.b2;
+    scale = fabs(lap_entry(B.P, a, b, B.P.x[a], B.P.y[a], B.P.z[a], B.diag));
+  }
+  uint32_t k = 0, no = 0, klast = 0, inext = i0, j0 = 0;
+  int kmin = -2, keps = -1;
+  double nrmlsk2 = 0.0, nrms2 = 0.0;
+  int outcome = -1;  // 0 NSUCC, 1 SUCC, 2 overflow
+  do {
+    if (k >= kcap) { outcome = kAcaOverflow; break; }
+    inext = i0;
+    if (!row_step<G>(g, B, klast, inext, k, no, nrmlsk2, scale)) {
+      nrmlsk2 = 0.0;
+      outcome = kAcaOk;
+      break;
+    }
+    double sum = 0.0;
+    const double* uk = B.U + (size_t)k * n1;
+    const double* vk = B.V + (size_t)k * n2;
+    for (uint32_t l = 0; l < k; ++l) {
+      double du = 0.0, dv = 0.0;
+      for (uint32_t i = g.rank; i < n1; i += G) du += B.U[(size_t)l * n1 + i] * uk[i];
+      for (uint32_t j = g.rank; j < n2; j += G) dv += B.V[(size_t)l * n2 + j] * vk[j];
+      g.sum2(du, dv);
+      sum += du * dv;
+    }
+    nrms2 += 2.0 * sum + nrmlsk2;
+    const bool stpcrit = nrmlsk2 < eps * eps * nrms2;
+    if (stpcrit && keps == -1) keps = (int)klast + 1;
+    ++k;
+    scale = sqrt(nrmlsk2 / (double)(uint32_t)(n1 * n2));
+    if (keps > 0) {
+      ArgMinI m{INT_MAX, 0xffffffffu};
+      for (uint32_t i = g.rank; i < n1; i += G)
+        if (B.Z[i] >= 0 && B.Z[i] < m.v) m = ArgMinI{B.Z[i], i};
+      m = g.argmin(m);
+      if (m.v == INT_MAX) {
+        nrmlsk2 = 0.0;
+        outcome = kAcaOk;
+        break;
+      }
+      kmin = m.v;
+      i0 = m.idx;
+      if ((uint32_t)kmin == k) i0 = inext;
+    } else {
+      i0 = inext;
+    }
+  } while (no < n1 && k < kmax && kmin < keps);
+
+  if (outcome < 0) {
+    if ((no == n1 || k == kmax) && kmin < keps) {
+      outcome = kAcaFail;
+    } else {
+      do {
+        ArgMinI m{INT_MAX, 0xffffffffu};
+        for (uint32_t j = g.rank; j < n2; j += G)
+          if (B.S[j] >= 0 && B.S[j] < m.v) m = ArgMinI{B.S[j], j};
+        m = g.argmin(m);
+        if (m.v == INT_MAX) {
+          nrmlsk2 = 0.0;
+          outcome = kAcaOk;
+          break;
+        }
+        kmin = m.v;
+        j0 = m.idx;
+        if (kmin >= keps) { outcome = kAcaOk; break; }
+        if (k >= kcap) { outcome = kAcaOverflow; break; }
+        if (!col_step<G>(g, B, j0, k, no, nrmlsk2, scale)) {
+          nrmlsk2 = 0.0;
+          outcome = kAcaOk;
+          break;
+        }
+        ++k;
+      } while (no < n2 && k < kmax);
+      if (outcome < 0) outcome = kAcaFail;
+    }
+  }
+  if (outcome == kAcaOk) {
+    const double epsa = sqrt(nrmlsk2 / nrms2);
+    if (epsa >= eps) outcome = kAcaFail;  // NaN (0/0) stays a success, as in the reference
+  }
+  kout = k;
+  g.sync();
+  return outcome;
+}
+
+// In-place Householder QR of A (m x k, column-major) by the group; tau[k].
+template <int G, class Grp>
+__device__ void group_qr(const Grp& g, uint32_t m, uint32_t k, double* A, double* tau) {
+  const uint32_t kk = min(m, k);
+  for (uint32_t c = 0; c < kk; ++c) {
+    double* a = A + (size_t)c * m;
+    double xn2 = 0.0, alpha = 0.0;
+    for (uint32_t i = g.rank; i < m; i += G) {
+      if (i > c) xn2 += a[i] * a[i];
+      else if (i == c) alpha = a[i];
+    }
+    g.sum2(xn2, alpha);
+    if (xn2 == 0.0) {
+      if (g.rank == 0) tau[c] = 0.0;
+      continue;
+    }
+    const double nrm = sqrt(alpha * alpha + xn2);
+    const double beta = alpha >= 0.0 ? -nrm : nrm;
+    const double t = (beta - alpha) / beta;
+    const double sc = 1.0 / (alpha - beta);
+    if (g.rank == 0) tau[c] = t;
+    for (uint32_t i = g.rank; i < m; i += G) {
+      if (i > c) a[i] *= sc;
+      else if (i == c) a[i] = beta;
+    }
+    for (uint32_t q = c + 1; q < k; ++q) {
+      double* b = A + (size_t)q * m;
+      double s = 0.0;
+      for (uint32_t i = g.rank; i < m; i += G) {
+        if (i > c) s += a[i] * b[i];
+        else if (i == c) s += b[i];
+      }
+      s = g.sum(s) * t;
+      for (uint32_t i = g.rank; i < m; i += G) {
+        if (i > c) b[i] -= s * a[i];
+        else if (i == c) b[i] -= s;
+      }
+    }
+  }
+}
+
+// C (m x nc, column-major, ldc m) := Q C, Q = H_0 ... H_{kr-1} stored in A/tau.
+// Rows of C are owned like rows of A; tau is read from memory written by rank 0
+// before a group barrier.
+template <int G, class Grp>
+__device__ void group_apply_q(const Grp& g, uint32_t m, uint32_t kr, const double* A,
+                              const double* tau, uint32_t nc, double* C) {
+  for (int c = (int)kr - 1; c >= 0; --c) {
+    const double t = tau[c];
+    if (t == 0.0) continue;
+    const double* a = A + (size_t)c * m;
+    for (uint32_t q = 0; q < nc; ++q) {
+      double* b = C + (size_t)q * m;
+      double s = 0.0;
+      for (uint32_t i = g.rank; i < m; i += G) {
+        if (i > (uint32_t)c) s += a[i] * b[i];
+        else if (i == (uint32_t)c) s += b[i];
+      }
+      s = g.sum(s) * t;
+      for (uint32_t i = g.rank; i < m; i += G) {
+        if (i > (uint32_t)c) b[i] -= s * a[i];
+        else if (i == (uint32_t)c) b[i] -= s;
+      }
+    }
+  }
+}
+
+// addtrll (H/mblock_D.cpp:356-465) for a fresh low-rank block: recompress U V^T
+// of rank k to kt <= k columns (relative threshold delta, absolute 1e-64).
+// Results in Un (n1 x kt) and Vn (n2 x kt).
+template <int G, class Grp>
+__device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t k, double* U,
+                               double* V, double* Un, double* Vn, double delta, double* R,
+                               double* Vs, uint32_t ld, double* sig, double* tau, int* perm) {
+  if (k == 0) return 0;
+  const uint32_t mmin = min(n1, k), nmin = min(n2, k), amin = min(mmin, nmin);
+  double* tau1 = tau;
+  double* tau2 = tau + k;
+  group_qr<G>(g, n1, k, U, tau1);
+  group_qr<G>(g, n2, k, V, tau2);
+  g.sync();
+  // R = R1 R2^T (Include/blas.h:2767-2781), rows owned by i % G
+  double fro = 0.0;
+  for (uint32_t i = g.rank; i < mmin; i += G) {
+    for (uint32_t j = 0; j < nmin; ++j) {
+      double d = 0.0;
+      for (uint32_t l = max(i, j); l < k; ++l) d += U[i + (size_t)l * n1] * V[j + (size_t)l * n2];
+      R[i * ld + j] = d;
+      fro += d * d;
+    }
+  }
+  fro = g.sum(fro);
+  const double thresh = delta * sqrt(fro) / (double)sqrtf((float)mmin * (float)nmin);
+  for (uint32_t i = g.rank; i < mmin; i += G)
+    for (uint32_t j = 0; j < nmin; ++j)
+      if (fabs(R[i * ld + j]) < thresh) R[i * ld + j] = 0.0;
+  for (uint32_t i = g.rank; i < nmin; i += G)
+    for (uint32_t j = 0; j < nmin; ++j) Vs[i * ld + j] = (i == j) ? 1.0 : 0.0;
+  // one-sided Jacobi on the columns of R (Hestenes), rotations accumulated in Vs
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    bool rotated = false;
+    for (uint32_t p = 0; p + 1 < nmin; ++p) {
+      for (uint32_t q = p + 1; q < nmin; ++q) {
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (uint32_t i = g.rank; i < mmin; i += G) {
+          const double x = R[i * ld + p], y = R[i * ld + q];
+          al += x * x;
+          be += y * y;
+          ga += x * y;
+        }
+        g.sum3(al, be, ga);
+        if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+        rotated = true;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double s = c * t;
+        for (uint32_t i = g.rank; i < mmin; i += G) {
+          const double x = R[i * ld + p], y = R[i * ld + q];
+          R[i * ld + p] = c * x - s * y;
+          R[i * ld + q] = s * x + c * y;
+        }
+        for (uint32_t i = g.rank; i < nmin; i += G) {
+          const double x = Vs[i * ld + p], y = Vs[i * ld + q];
+          Vs[i * ld + p] = c * x - s * y;
+          Vs[i * ld + q] = s * x + c * y;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  for (uint32_t j = 0; j < nmin; ++j) {
+    double s = 0.0;
+    for (uint32_t i = g.rank; i < mmin; i += G) s += R[i * ld + j] * R[i * ld + j];
+    s = g.sum(s);
+    if (g.rank == 0) sig[j] = sqrt(s);
+  }
+  g.sync();
+  if (g.rank == 0) {
+    for (uint32_t j = 0; j < nmin; ++j) perm[j] = (int)j;
+    for (uint32_t j = 0; j < nmin; ++j) {
+      uint32_t b = j;
+      for (uint32_t q = j + 1; q < nmin; ++q)
+        if (sig[perm[q]] > sig[perm[b]]) b = q;
+      const int t = perm[j];
+      perm[j] = perm[b];
+      perm[b] = t;
+    }
+    uint32_t kt = min(amin, k);
+    const double s0 = sig[perm[0]];
+    while (kt > 0 && (sig[perm[kt - 1]] <= delta * s0 || sig[perm[kt - 1]] < 1e-64)) --kt;
+    perm[nmin] = (int)kt;  // the slot after the permutation holds kt
+  }
+  g.sync();
+  const uint32_t kt = (uint32_t)perm[nmin];
+  // Un = Q1 [R(:, perm[:kt]); 0],  Vn = Q2 [Vs(:, perm[:kt]); 0]
+  for (uint32_t j = 0; j < kt; ++j) {
+    const int pj = perm[j];
+    for (uint32_t i = g.rank; i < n1; i += G) Un[i + (size_t)j * n1] = i < mmin ? R[i * ld + pj] : 0.0;
+    for (uint32_t i = g.rank; i < n2; i += G) Vn[i + (size_t)j * n2] = i < nmin ? Vs[i * ld + pj] : 0.0;
+  }
+  group_apply_q<G>(g, n1, mmin, U, tau1, kt, Un);
+  group_apply_q<G>(g, n2, nmin, V, tau2, kt, Vn);
+  return kt;
+}
+
+template <int G, class Grp>
+__device__ void aca_task(const Grp& g, const AcaParams& p, uint32_t ti, double* smem) {
+  const AcaTask t = p.tasks[ti];
+  Blk B;
+  B.P = p.pts;
+  B.diag = p.diag;
+  B.b1 = t.b1;
+  B.n1 = t.n1;
+  B.b2 = t.b2;
+  B.n2 = t.n2;
+  double* ws = p.ws + t.ws;
+  const uint32_t kc = t.kcap;
+  B.U = ws;
+  B.V = B.U + (size_t)t.n1 * kc;
+  double* Un = B.V + (size_t)t.n2 * kc;
+  double* Vn = Un + (size_t)t.n1 * kc;
+  double* Rg = Vn + (size_t)t.n2 * kc;
+  double* Vsg = Rg + (size_t)kc * kc;
+  double* sigg = Vsg + (size_t)kc * kc;
+  double* taug = sigg + kc;
+  B.Z = p.zs + t.zs;
+  B.S = B.Z + t.n1;
+  uint32_t k = 0;
+  const int st = aca<G>(g, B, t.i0, t.kmax, t.kcap, p.eps, k);
+  uint32_t kt = 0;
+  if (st == kAcaOk && k > 0) {
+    // small ranks: k x k work arrays in shared memory; larger: in the workspace
+    const bool sm = k <= (uint32_t)KSM;
+    double* R = sm ? smem : Rg;
+    double* Vs = sm ? smem + KSM * LDS : Vsg;
+    double* sig = sm ? smem + 2 * KSM * LDS : sigg;
+    double* tau = sm ? smem + 2 * KSM * LDS + KSM : taug;
+    // perm needs nmin+1 ints: shared memory when small, else the dead Z/S counters
+    // (n1 + n2 ints >= nmin + 1)
+    int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : B.Z;
+    g.sync();
+    kt = recompress<G>(g, t.n1, t.n2, k, B.U, B.V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau,
+                       perm);
+  }
+  if (g.rank == 0) p.res[ti] = AcaResult{st, k, kt, 0u};
+}
+
+__global__ void __launch_bounds__(32 * kSmallWarps) aca_small_kernel(AcaParams p) {
+  extern __shared__ double smem_all[];
+  const uint32_t w = threadIdx.x >> 5;
+  const uint32_t task = blockIdx.x * kSmallWarps + w;
+  if (task >= p.ntasks) return;
+  Group<32> g(threadIdx.x & 31);
+  aca_task<32>(g, p, task, smem_all + (size_t)w * kSmemPerGroup);
+}
+
+constexpr int kLargeThreads = 256;
+
+__global__ void __launch_bounds__(kLargeThreads) aca_large_kernel(AcaParams p) {
+  extern __shared__ double smem_all[];
+  const uint32_t task = blockIdx.x;
+  if (task >= p.ntasks) return;
+  Group<kLargeThreads> g(threadIdx.x, smem_all + kSmemPerGroup);
+  aca_task<kLargeThreads>(g, p, task, smem_all);
+}
+
+__global__ void dense_fill_kernel(PointsSoA P, double diag, const DenseTask* __restrict__ tasks,
+                                  double* __restrict__ arena) {
+  const DenseTask t = tasks[blockIdx.x];
+  const uint64_t cnt = (uint64_t)t.n1 * t.n2;
+  double* out = arena + t.off;
+  for (uint64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const uint32_t i = (uint32_t)(e % t.n1), j = (uint32_t)(e / t.n1);
+    const uint32_t gj = t.b2 + j;
+    out[e] = lap_entry(P, gj, t.b1 + i, P.x[gj], P.y[gj], P.z[gj], diag);
+  }
+}
+
+__global__ void copy_factors_kernel(const CopyTask* __restrict__ tasks, const double* __restrict__ ws,
+                                    double* __restrict__ arena) {
+  const CopyTask t = tasks[blockIdx.x];
+  const uint64_t nu = (uint64_t)t.n1 * t.kt, nv = (uint64_t)t.n2 * t.kt;
+  double* dst = arena + t.dst;
+  for (uint64_t e = threadIdx.x; e < nu; e += blockDim.x) dst[e] = ws[t.src_u + e];
+  for (uint64_t e = threadIdx.x; e < nv; e += blockDim.x) dst[nu + e] = ws[t.src_v + e];
+}
+
+}  // namespace
+
+cudaError_t launch_aca_small(const AcaParams& p, cudaStream_t s) {
+  if (p.ntasks == 0) return cudaSuccess;
+  const size_t smem = sizeof(double) * kSmemPerGroup * kSmallWarps;
+  cudaError_t e = cudaFuncSetAttribute(aca_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  const uint32_t grid = (p.ntasks + kSmallWarps - 1) / kSmallWarps;
+  aca_small_kernel<<<grid, 32 * kSmallWarps, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_aca_large(const AcaParams& p, cudaStream_t s) {
+  if (p.ntasks == 0) return cudaSuccess;
+  const size_t smem = sizeof(double) * (kSmemPerGroup + 3 * (kLargeThreads / 32) + 8);
+  cudaError_t e = cudaFuncSetAttribute(aca_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  aca_large_kernel<<<p.ntasks, kLargeThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask* tasks,
+                              uint32_t ntasks, double* arena, cudaStream_t s) {
+  if (ntasks == 0) return cudaSuccess;
+  dense_fill_kernel<<<ntasks, 256, 0, s>>>(pts, diag, tasks, arena);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_factors(const CopyTask* tasks, uint32_t ntasks, const double* ws,
+                                double* arena, cudaStream_t s) {
+  if (ntasks == 0) return cudaSuccess;
+  copy_factors_kernel<<<ntasks, 256, 0, s>>>(tasks, ws, arena);
+  return cudaGetLastError();
+}
+
+}  // namespace ahx

@@ -1,0 +1,67 @@
+// Batched ACA assembly of admissible leaves with SVD recompression, and the
+// dense fill of inadmissible leaves (FP64 throughout).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ahx_device.cuh"
+
+namespace ahx {
+
+// One admissible leaf to approximate.  Workspace layout at `ws` (doubles):
+//   U[n1*kcap] V[n2*kcap] Un[n1*kcap] Vn[n2*kcap] R[kcap*kcap] Vs[kcap*kcap] sig[kcap]
+//   tau[2*kcap]
+// and at `zs` (ints): Z[n1] S[n2]  (ACA.h:38-42 row/column success counters).
+struct AcaTask {
+  uint32_t b1, n1, b2, n2;
+  uint32_t i0, kmax, kcap, leaf;
+  uint64_t ws;
+  uint64_t zs;
+};
+
+enum AcaStatus : int32_t { kAcaFail = 0, kAcaOk = 1, kAcaOverflow = 2 };
+
+struct AcaResult {
+  int32_t status;
+  uint32_t k_aca;  // rank returned by ACA (before recompression)
+  uint32_t kt;     // rank after recompression
+  uint32_t pad;
+};
+
+inline uint64_t aca_ws_doubles(uint32_t n1, uint32_t n2, uint32_t kcap) {
+  return 2ull * (uint64_t)(n1 + n2) * kcap + 2ull * kcap * kcap + 3ull * kcap;
+}
+
+struct AcaParams {
+  PointsSoA pts;
+  double diag;  // 1/(4 pi h)
+  double eps;
+  const AcaTask* tasks;
+  uint32_t ntasks;
+  double* ws;
+  int* zs;
+  AcaResult* res;
+};
+
+// Launchers (ahx_aca.cu)
+cudaError_t launch_aca_small(const AcaParams& p, cudaStream_t s);  // one warp per leaf
+cudaError_t launch_aca_large(const AcaParams& p, cudaStream_t s);  // one CTA per leaf
+
+// Dense leaves: fill n1 x n2 column-major blocks of the generator.
+struct DenseTask {
+  uint32_t b1, n1, b2, n2;
+  uint64_t off;  // element offset in the arena
+};
+cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask* tasks,
+                              uint32_t ntasks, double* arena, cudaStream_t s);
+
+// Copy recompressed factors (Un, Vn, kt columns) from the workspace into the arena.
+struct CopyTask {
+  uint64_t src_u, src_v;  // workspace offsets (doubles)
+  uint64_t dst;           // arena offset
+  uint32_t n1, n2, kt, pad;
+};
+cudaError_t launch_copy_factors(const CopyTask* tasks, uint32_t ntasks, const double* ws,
+                                double* arena, cudaStream_t s);
+
+}  // namespace ahx

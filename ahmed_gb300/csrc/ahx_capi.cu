@@ -1,0 +1,677 @@
+// C ABI of libahx: handle management, trees, assembly driver, product.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <numeric>
+
+#include <cuda_bf16.h>
+
+#include "ahx_aca.cuh"
+#include "ahx_hmat.hpp"
+
+namespace ahx {
+
+namespace {
+thread_local std::string g_err;
+
+// Workspace budget of one ACA batch (bytes); AHX_ACA_WS_BYTES overrides.
+size_t aca_ws_budget() {
+  const char* e = std::getenv("AHX_ACA_WS_BYTES");
+  if (e && *e) return (size_t)std::strtoull(e, nullptr, 10);
+  return (size_t)4 << 30;
+}
+
+// first capacity of the ACA rank workspace per leaf; AHX_ACA_KCAP overrides
+uint32_t aca_kcap_default() {
+  const char* e = std::getenv("AHX_ACA_KCAP");
+  if (e && *e) return std::max<uint32_t>(1u, (uint32_t)std::strtoul(e, nullptr, 10));
+  return 48u;
+}
+// leaves with more rows or columns than this use the CTA-per-leaf kernel
+constexpr uint32_t kLargeLeaf = 256;
+
+template <class T>
+int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  if (v.empty()) return AHX_OK;
+  int rc = b.reserve(v.size() * sizeof(T));
+  if (rc) return rc;
+  AHX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return AHX_OK;
+}
+
+__global__ void cvt_kernel_f32(const double* __restrict__ src, float* __restrict__ dst, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+struct CvtTask {
+  uint64_t src, dst, count;
+};
+
+template <typename D>
+__global__ void cvt_tasks_kernel(const CvtTask* __restrict__ t, const double* __restrict__ src,
+                                 D* __restrict__ dst) {
+  const CvtTask c = t[blockIdx.x];
+  for (uint64_t i = threadIdx.x; i < c.count; i += blockDim.x) {
+    if constexpr (sizeof(D) == 2) dst[c.dst + i] = __double2bfloat16(src[c.src + i]);
+    else dst[c.dst + i] = (D)src[c.src + i];
+  }
+}
+
+uint32_t maxk_of(uint32_t n1, uint32_t n2, uint32_t rankmax) {
+  // unsigned arithmetic as in Include/apprx.h:143-144
+  uint32_t maxk = (uint32_t)(n1 * n2) / (n1 + n2) + 4u;
+  return maxk > rankmax ? rankmax : maxk;
+}
+
+// Append-only growable FP64 arena.
+int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
+  const uint64_t need = (H->arena64_elems + count) * sizeof(double);
+  if (need > H->arena64.bytes) {
+    size_t nb = std::max<size_t>(need, H->arena64.bytes * 2);
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, nb);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      nb = need;
+      e = cudaMalloc(&np, nb);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation of the leaf arena failed");
+        return AHX_ERR_NOMEM;
+      }
+    }
+    if (H->arena64_elems)
+      AHX_CUDA(cudaMemcpyAsync(np, H->arena64.p, H->arena64_elems * sizeof(double),
+                               cudaMemcpyDeviceToDevice, H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    if (H->arena64.p) cudaFree(H->arena64.p);
+    H->arena64.p = np;
+    H->arena64.bytes = nb;
+  }
+  off = H->arena64_elems;
+  H->arena64_elems += count;
+  return AHX_OK;
+}
+
+// Runs ACA + recompression for `tasks` in workspace-bounded batches, appends the
+// factors to the arena; failed leaves go to `dense`, capacity overflows to `retry`.
+int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
+            std::vector<uint32_t>& dense, std::vector<AcaTask>& retry) {
+  const size_t budget = aca_ws_budget();
+  std::sort(tasks.begin(), tasks.end(), [](const AcaTask& a, const AcaTask& b) {
+    return (uint64_t)(a.n1 + a.n2) * a.kcap > (uint64_t)(b.n1 + b.n2) * b.kcap;
+  });
+  DevBuf ws, zs, dtasks, dres, dcopy;
+  size_t i = 0;
+  while (i < tasks.size()) {
+    // gather one batch
+    std::vector<AcaTask> small, large;
+    uint64_t wsd = 0, zsi = 0;
+    size_t j = i;
+    while (j < tasks.size()) {
+      AcaTask t = tasks[j];
+      const uint64_t w = aca_ws_doubles(t.n1, t.n2, t.kcap);
+      if (j > i && (wsd + w) * 8 + (zsi + t.n1 + t.n2) * 4 > budget) break;
+      t.ws = wsd;
+      t.zs = zsi;
+      wsd += w;
+      zsi += t.n1 + t.n2;
+      (std::max(t.n1, t.n2) > kLargeLeaf ? large : small).push_back(t);
+      ++j;
+    }
+    i = j;
+    int rc = ws.reserve(std::max<uint64_t>(wsd, 1) * sizeof(double));
+    if (rc) return rc;
+    rc = zs.reserve(std::max<uint64_t>(zsi, 1) * sizeof(int));
+    if (rc) return rc;
+    std::vector<AcaTask> all(large);
+    all.insert(all.end(), small.begin(), small.end());
+    if ((rc = upload(dtasks, all, H->stream))) return rc;
+    rc = dres.reserve(all.size() * sizeof(AcaResult));
+    if (rc) return rc;
+    AcaParams p;
+    const double* pts = H->pts.as<double>();
+    p.pts = PointsSoA{pts, pts + H->tree.n, pts + 2 * (size_t)H->tree.n};
+    p.diag = diag;
+    p.eps = eps;
+    p.ws = ws.as<double>();
+    p.zs = zs.as<int>();
+    p.tasks = dtasks.as<AcaTask>();
+    p.res = dres.as<AcaResult>();
+    p.ntasks = (uint32_t)large.size();
+    AHX_CUDA(launch_aca_large(p, H->stream));
+    p.tasks = dtasks.as<AcaTask>() + large.size();
+    p.res = dres.as<AcaResult>() + large.size();
+    p.ntasks = (uint32_t)small.size();
+    AHX_CUDA(launch_aca_small(p, H->stream));
+    std::vector<AcaResult> res(all.size());
+    AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, res.size() * sizeof(AcaResult),
+                             cudaMemcpyDeviceToHost, H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    std::vector<CopyTask> copies;
+    for (size_t q = 0; q < all.size(); ++q) {
+      const AcaTask& t = all[q];
+      const AcaResult& r = res[q];
+      if (r.status == kAcaOverflow) {
+        AcaTask u = t;
+        u.kcap = std::min(t.kmax, t.kcap * 4);
+        retry.push_back(u);
+        continue;
+      }
+      if (r.status != kAcaOk) {
+        dense.push_back(t.leaf);
+        continue;
+      }
+      H->aca_rank[t.leaf] = (int32_t)r.k_aca;
+      H->rank[t.leaf] = (int32_t)r.kt;
+      if (r.kt == 0) continue;
+      uint64_t off = 0;
+      if ((rc = arena_append(H, (uint64_t)r.kt * (t.n1 + t.n2), off))) return rc;
+      H->off[t.leaf] = off;
+      const uint64_t un = t.ws + (uint64_t)(t.n1 + t.n2) * t.kcap;  // Un follows U and V
+      CopyTask c;
+      c.src_u = un;
+      c.src_v = un + (uint64_t)t.n1 * t.kcap;
+      c.dst = off;
+      c.n1 = t.n1;
+      c.n2 = t.n2;
+      c.kt = r.kt;
+      c.pad = 0;
+      copies.push_back(c);
+    }
+    if (!copies.empty()) {
+      if ((rc = upload(dcopy, copies, H->stream))) return rc;
+      AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), ws.as<double>(),
+                                   H->arena64.as<double>(), H->stream));
+    }
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+  }
+  ws.release();
+  zs.release();
+  dtasks.release();
+  dres.release();
+  dcopy.release();
+  return AHX_OK;
+}
+
+void invalidate_products(ahx_hmat* H) {
+  for (auto& pc : H->prod) {
+    pc.lr.release();
+    pc.dn.release();
+    pc.leaves.release();
+    pc.order.release();
+    pc.valid = false;
+    pc.bytes = 0;
+  }
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? AHX_ERR_NOMEM : AHX_ERR_CUDA;
+}
+
+int DevBuf::reserve(size_t b) {
+  if (b <= bytes) return AHX_OK;
+  release();
+  cudaError_t e = cudaMalloc(&p, b);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return cuda_fail(e, "cudaMalloc");
+  }
+  bytes = b;
+  return AHX_OK;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+bool is_device_ptr(const void* ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int prepare_product(ahx_hmat* H, int prec) {
+  if (prec < 0 || prec > 2) {
+    set_error("unknown precision");
+    return AHX_ERR_ARG;
+  }
+  ProdCopy& pc = H->prod[prec];
+  if (pc.valid) return AHX_OK;
+  const auto& Ls = H->tree.leaves;
+  const uint32_t nl = (uint32_t)Ls.size();
+  std::vector<MvLeaf> mv;
+  std::vector<uint64_t> cost;
+  mv.reserve(nl);
+  std::vector<CvtTask> lr_tasks, dn_tasks;
+  uint64_t lr_off = 0, dn_off = 0;
+  for (uint32_t l = 0; l < nl; ++l) {
+    const Leaf& L = Ls[l];
+    const int32_t r = H->rank[l];
+    if (r == 0) continue;
+    MvLeaf m;
+    m.b1 = L.b1;
+    m.n1 = L.n1;
+    m.b2 = L.b2;
+    m.n2 = L.n2;
+    m.rank = r;
+    const uint64_t cnt = r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
+    if (prec == kBF16FP32) {
+      if (r < 0) {
+        m.dense_in_lr_arena = 0;
+        m.off = dn_off;
+        dn_tasks.push_back(CvtTask{H->off[l], dn_off, cnt});
+        dn_off += cnt;
+      } else {
+        m.dense_in_lr_arena = 1;
+        m.off = lr_off;
+        lr_tasks.push_back(CvtTask{H->off[l], lr_off, cnt});
+        lr_off += cnt;
+      }
+    } else {
+      m.dense_in_lr_arena = 1;
+      m.off = H->off[l];
+    }
+    mv.push_back(m);
+    cost.push_back(cnt);
+  }
+  std::vector<uint32_t> order(mv.size());
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  int rc;
+  if ((rc = upload(pc.leaves, mv, H->stream))) return rc;
+  if ((rc = upload(pc.order, order, H->stream))) return rc;
+  pc.nleaves = (uint32_t)mv.size();
+  const double* a64 = H->arena64.as<double>();
+  if (prec == kFP64) {
+    pc.bytes = H->arena64_elems * sizeof(double);
+  } else if (prec == kFP32) {
+    if ((rc = pc.lr.reserve(std::max<uint64_t>(H->arena64_elems, 1) * sizeof(float)))) return rc;
+    if (H->arena64_elems)
+      cvt_kernel_f32<<<1216, 256, 0, H->stream>>>(a64, pc.lr.as<float>(), H->arena64_elems);
+    AHX_CUDA(cudaGetLastError());
+    pc.bytes = H->arena64_elems * sizeof(float);
+  } else {
+    if ((rc = pc.lr.reserve(std::max<uint64_t>(lr_off, 1) * sizeof(__nv_bfloat16)))) return rc;
+    if ((rc = pc.dn.reserve(std::max<uint64_t>(dn_off, 1) * sizeof(float)))) return rc;
+    DevBuf tl, td;
+    if ((rc = upload(tl, lr_tasks, H->stream))) return rc;
+    if ((rc = upload(td, dn_tasks, H->stream))) return rc;
+    if (!lr_tasks.empty())
+      cvt_tasks_kernel<__nv_bfloat16><<<(unsigned)lr_tasks.size(), 256, 0, H->stream>>>(
+          tl.as<CvtTask>(), a64, pc.lr.as<__nv_bfloat16>());
+    if (!dn_tasks.empty())
+      cvt_tasks_kernel<float><<<(unsigned)dn_tasks.size(), 256, 0, H->stream>>>(
+          td.as<CvtTask>(), a64, pc.dn.as<float>());
+    AHX_CUDA(cudaGetLastError());
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    pc.bytes = lr_off * sizeof(__nv_bfloat16) + dn_off * sizeof(float);
+  }
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  pc.valid = true;
+  return AHX_OK;
+}
+
+int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
+                   double* Y, uint64_t ldY) {
+  int rc = prepare_product(H, prec);
+  if (rc) return rc;
+  ProdCopy& pc = H->prod[prec];
+  MvArgs a;
+  a.leaves = pc.leaves.as<MvLeaf>();
+  a.order = pc.order.as<uint32_t>();
+  a.nleaves = pc.nleaves;
+  a.arena_lr = prec == kFP64 ? H->arena64.p : pc.lr.p;
+  a.arena_dn = pc.dn.p;
+  a.d = d;
+  a.p = p;
+  a.X = X;
+  a.ldX = ldX;
+  a.Y = Y;
+  a.ldY = ldY;
+  AHX_CUDA(launch_matvec(prec, a, H->stream));
+  return AHX_OK;
+}
+
+int ensure_device(ahx_hmat* H) {
+  AHX_CUDA(cudaSetDevice(H->device));
+  if (!H->stream) {
+    AHX_CUDA(cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking));
+    H->own_stream = true;
+  }
+  if (!H->pts.p) {
+    const uint32_t n = H->tree.n;
+    std::vector<double> soa(3 * (size_t)n);
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint32_t o = H->tree.op_perm[i];
+      for (int j = 0; j < 3; ++j) soa[(size_t)j * n + i] = H->tree.pts[3 * (size_t)o + j];
+    }
+    int rc = upload(H->pts, soa, H->stream);
+    if (rc) return rc;
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+  }
+  return AHX_OK;
+}
+
+}  // namespace ahx
+
+using namespace ahx;
+
+extern "C" {
+
+const char* ahx_last_error(void) { return g_err.c_str(); }
+
+int ahx_version(void) { return 10000; }
+
+double ahx_mean_nn(const double* pts, uint32_t n) {
+  if (!pts) return 0.0;
+  return mean_nn(pts, n);
+}
+
+int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
+                    int device, void* stream, ahx_hmat** out) {
+  if (!out || !pts || n == 0 || bmin == 0 || (tree_kind != AHX_TREE_BBX && tree_kind != AHX_TREE_PCA) ||
+      !(eta2 >= 0.0) || device < 0) {
+    set_error("ahx_hmat_create: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  *out = nullptr;
+  ahx_hmat* H = new (std::nothrow) ahx_hmat;
+  if (!H) {
+    set_error("host allocation failed");
+    return AHX_ERR_NOMEM;
+  }
+  H->device = device;
+  H->stream = (cudaStream_t)stream;
+  // trees are host work; the device is touched on the first device call
+  build_tree(H->tree, pts, n, tree_kind, bmin, eta2);
+  *out = H;
+  return AHX_OK;
+}
+
+int ahx_hmat_destroy(ahx_hmat* H) {
+  if (!H) return AHX_OK;
+  const bool touched = H->stream || H->pts.p;
+  if (touched) cudaSetDevice(H->device);
+  if (H->stream) cudaStreamSynchronize(H->stream);
+  invalidate_products(H);
+  H->pts.release();
+  H->arena64.release();
+  H->stage_x.release();
+  H->stage_y.release();
+  H->scratch.release();
+  if (H->own_stream && H->stream) cudaStreamDestroy(H->stream);
+  delete H;
+  return AHX_OK;
+}
+
+int ahx_hmat_set_stream(ahx_hmat* H, void* stream) {
+  if (!H) return AHX_ERR_ARG;
+  if (H->stream) {
+    AHX_CUDA(cudaSetDevice(H->device));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    if (H->own_stream) cudaStreamDestroy(H->stream);
+  }
+  H->own_stream = false;
+  H->stream = (cudaStream_t)stream;  // NULL: a private stream is created on next use
+  return AHX_OK;
+}
+
+void* ahx_hmat_stream(const ahx_hmat* H) { return H ? (void*)H->stream : nullptr; }
+uint32_t ahx_hmat_n(const ahx_hmat* H) { return H ? H->tree.n : 0; }
+uint32_t ahx_hmat_nleaves(const ahx_hmat* H) { return H ? (uint32_t)H->tree.leaves.size() : 0; }
+
+int ahx_hmat_perm(const ahx_hmat* H, uint32_t* op_perm, uint32_t* po_perm) {
+  if (!H) return AHX_ERR_ARG;
+  if (op_perm) std::memcpy(op_perm, H->tree.op_perm.data(), H->tree.n * sizeof(uint32_t));
+  if (po_perm) std::memcpy(po_perm, H->tree.po_perm.data(), H->tree.n * sizeof(uint32_t));
+  return AHX_OK;
+}
+
+int ahx_hmat_leaves(const ahx_hmat* H, uint32_t* out) {
+  if (!H || !out) return AHX_ERR_ARG;
+  for (size_t l = 0; l < H->tree.leaves.size(); ++l) {
+    const Leaf& L = H->tree.leaves[l];
+    uint32_t* o = out + 7 * l;
+    o[0] = L.b1;
+    o[1] = L.n1;
+    o[2] = L.b2;
+    o[3] = L.n2;
+    o[4] = L.adm;
+    o[5] = L.idx;
+    o[6] = L.i0;
+  }
+  return AHX_OK;
+}
+
+int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax) {
+  if (!H || !(h > 0.0) || !(eps > 0.0)) {
+    set_error("ahx_assemble: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  invalidate_products(H);
+  H->assembled = false;
+  H->h = h;
+  H->eps = eps;
+  const auto& Ls = H->tree.leaves;
+  const uint32_t nl = (uint32_t)Ls.size();
+  H->rank.assign(nl, -1);
+  H->aca_rank.assign(nl, -1);
+  H->off.assign(nl, 0);
+  H->arena64_elems = 0;
+  const double diag = 1.0 / (kFourPi * h);
+  std::vector<AcaTask> tasks;
+  std::vector<uint32_t> dense;
+  const uint32_t kcap0 = aca_kcap_default();
+  for (uint32_t l = 0; l < nl; ++l) {
+    const Leaf& L = Ls[l];
+    const uint32_t maxk = maxk_of(L.n1, L.n2, rankmax);
+    if (L.adm && maxk) {
+      AcaTask t{};
+      t.b1 = L.b1;
+      t.n1 = L.n1;
+      t.b2 = L.b2;
+      t.n2 = L.n2;
+      t.i0 = L.i0;
+      t.kmax = maxk;
+      t.kcap = std::min(maxk, kcap0);
+      t.leaf = l;
+      tasks.push_back(t);
+    } else {
+      dense.push_back(l);
+    }
+  }
+  // estimated arena capacity: dense leaves plus about 16 columns per low-rank leaf
+  uint64_t est = 0;
+  for (uint32_t l : dense) est += (uint64_t)Ls[l].n1 * Ls[l].n2;
+  for (const AcaTask& t : tasks) est += (uint64_t)(t.n1 + t.n2) * std::min(t.kmax, 16u);
+  if (H->arena64.bytes < est * sizeof(double)) {
+    H->arena64.release();
+    rc = H->arena64.reserve(std::max<uint64_t>(est, 1) * sizeof(double));
+    if (rc) return rc;
+  }
+  while (!tasks.empty()) {
+    std::vector<AcaTask> retry;
+    if ((rc = run_aca(H, tasks, diag, eps, dense, retry))) return rc;
+    tasks.swap(retry);
+  }
+  // dense leaves (inadmissible and failed ACA), filled in leaf order
+  std::sort(dense.begin(), dense.end());
+  std::vector<DenseTask> dt;
+  for (uint32_t l : dense) {
+    const Leaf& L = Ls[l];
+    uint64_t off = 0;
+    if ((rc = arena_append(H, (uint64_t)L.n1 * L.n2, off))) return rc;
+    H->off[l] = off;
+    H->rank[l] = -1;
+    H->aca_rank[l] = -1;
+    dt.push_back(DenseTask{L.b1, L.n1, L.b2, L.n2, off});
+  }
+  if (!dt.empty()) {
+    DevBuf ddt;
+    if ((rc = upload(ddt, dt, H->stream))) return rc;
+    const double* pts = H->pts.as<double>();
+    PointsSoA P{pts, pts + H->tree.n, pts + 2 * (size_t)H->tree.n};
+    AHX_CUDA(launch_dense_fill(P, diag, ddt.as<DenseTask>(), (uint32_t)dt.size(),
+                               H->arena64.as<double>(), H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+  }
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  H->assembled = true;
+  return AHX_OK;
+}
+
+int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks) {
+  if (!H || !ranks) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("not assembled");
+    return AHX_ERR_STATE;
+  }
+  std::memcpy(ranks, H->rank.data(), H->rank.size() * sizeof(int32_t));
+  return AHX_OK;
+}
+
+int ahx_hmat_aca_ranks(const ahx_hmat* H, int32_t* ranks) {
+  if (!H || !ranks) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("not assembled");
+    return AHX_ERR_STATE;
+  }
+  std::memcpy(ranks, H->aca_rank.data(), H->aca_rank.size() * sizeof(int32_t));
+  return AHX_OK;
+}
+
+uint64_t ahx_hmat_leaf_size(const ahx_hmat* H, uint32_t l) {
+  if (!H || !H->assembled || l >= H->tree.leaves.size()) return 0;
+  const Leaf& L = H->tree.leaves[l];
+  const int32_t r = H->rank[l];
+  return r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
+}
+
+int ahx_hmat_get_leaf(const ahx_hmat* H, uint32_t l, double* out) {
+  if (!H || !out || l >= H->tree.leaves.size()) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("not assembled");
+    return AHX_ERR_STATE;
+  }
+  const uint64_t cnt = ahx_hmat_leaf_size(H, l);
+  if (!cnt) return AHX_OK;
+  AHX_CUDA(cudaSetDevice(H->device));
+  AHX_CUDA(cudaMemcpyAsync(out, H->arena64.as<double>() + H->off[l], cnt * sizeof(double),
+                           cudaMemcpyDeviceToHost, H->stream));
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  return AHX_OK;
+}
+
+int ahx_hmat_set_leaves(ahx_hmat* H, const int32_t* ranks, const double* data,
+                        const uint64_t* offsets) {
+  if (!H || !ranks || !offsets) return AHX_ERR_ARG;
+  const auto& Ls = H->tree.leaves;
+  const uint32_t nl = (uint32_t)Ls.size();
+  for (uint32_t l = 0; l < nl; ++l) {
+    const uint64_t want = ranks[l] < 0 ? (uint64_t)Ls[l].n1 * Ls[l].n2
+                                       : (uint64_t)ranks[l] * (Ls[l].n1 + Ls[l].n2);
+    if (offsets[l + 1] < offsets[l] || offsets[l + 1] - offsets[l] != want) {
+      set_error("ahx_hmat_set_leaves: offsets do not match the leaf sizes");
+      return AHX_ERR_ARG;
+    }
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  invalidate_products(H);
+  const uint64_t total = offsets[nl];
+  H->arena64.release();
+  rc = H->arena64.reserve(std::max<uint64_t>(total, 1) * sizeof(double));
+  if (rc) return rc;
+  if (total) {
+    if (!data) return AHX_ERR_ARG;
+    AHX_CUDA(cudaMemcpyAsync(H->arena64.p, data, total * sizeof(double), cudaMemcpyHostToDevice,
+                             H->stream));
+  }
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  H->arena64_elems = total;
+  H->rank.assign(ranks, ranks + nl);
+  H->aca_rank.assign(ranks, ranks + nl);
+  H->off.assign(offsets, offsets + nl);
+  H->assembled = true;
+  return AHX_OK;
+}
+
+uint64_t ahx_hmat_storage_bytes(ahx_hmat* H, int precision) {
+  if (!H || !H->assembled) return 0;
+  if (ensure_device(H)) return 0;
+  if (prepare_product(H, precision)) return 0;
+  return H->prod[precision].bytes;
+}
+
+int ahx_hmat_prepare(ahx_hmat* H, int precision) {
+  if (!H) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  return prepare_product(H, precision);
+}
+
+int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX,
+               double* Y, uint64_t ldY) {
+  if (!H || !X || !Y || ldX < H->tree.n || ldY < H->tree.n) {
+    set_error("ahx_matvec: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  if (!H->assembled) {
+    set_error("ahx_matvec: H-matrix not assembled");
+    return AHX_ERR_STATE;
+  }
+  if (p == 0) return AHX_OK;
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  const uint64_t n = H->tree.n;
+  const bool xd = is_device_ptr(X), yd = is_device_ptr(Y);
+  const double* Xd = X;
+  double* Yd = Y;
+  uint64_t lx = ldX, ly = ldY;
+  if (!xd) {
+    if ((rc = H->stage_x.reserve(n * p * sizeof(double)))) return rc;
+    AHX_CUDA(cudaMemcpy2DAsync(H->stage_x.p, n * sizeof(double), X, ldX * sizeof(double),
+                               n * sizeof(double), p, cudaMemcpyHostToDevice, H->stream));
+    Xd = H->stage_x.as<double>();
+    lx = n;
+  }
+  if (!yd) {
+    if ((rc = H->stage_y.reserve(n * p * sizeof(double)))) return rc;
+    AHX_CUDA(cudaMemcpy2DAsync(H->stage_y.p, n * sizeof(double), Y, ldY * sizeof(double),
+                               n * sizeof(double), p, cudaMemcpyHostToDevice, H->stream));
+    Yd = H->stage_y.as<double>();
+    ly = n;
+  }
+  if ((rc = product_device(H, precision, d, p, Xd, lx, Yd, ly))) return rc;
+  if (!yd) {
+    AHX_CUDA(cudaMemcpy2DAsync(Y, ldY * sizeof(double), Yd, n * sizeof(double), n * sizeof(double),
+                               p, cudaMemcpyDeviceToHost, H->stream));
+  }
+  if (!xd || !yd) AHX_CUDA(cudaStreamSynchronize(H->stream));
+  return AHX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,71 @@
+// Internal state of an H-matrix handle (shared by the C-ABI translation units).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/ahx.h"
+#include "ahx_matvec.cuh"
+#include "ahx_tree.hpp"
+
+namespace ahx {
+
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+#define AHX_CUDA(call)                                    \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return ::ahx::cuda_fail(e_, #call); \
+  } while (0)
+
+// Device buffer owned by a handle.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int reserve(size_t b);  // grow-only
+  void release();
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// The product's view of one storage precision.
+struct ProdCopy {
+  bool valid = false;
+  DevBuf lr, dn;           // low-rank (and, for FP64/FP32, dense) arena; dense arena for BF16
+  DevBuf leaves, order;    // MvLeaf[nleaves], uint32 launch order
+  uint32_t nleaves = 0;
+  uint64_t bytes = 0;      // arena bytes
+};
+
+}  // namespace ahx
+
+struct ahx_hmat {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  ahx::Tree tree;
+  ahx::DevBuf pts;  // permuted SoA: x[n] y[n] z[n]
+  // assembly
+  bool assembled = false;
+  double h = 0.0, eps = 0.0;
+  std::vector<int32_t> rank, aca_rank;
+  std::vector<uint64_t> off;  // element offset of each leaf in arena64
+  ahx::DevBuf arena64;
+  uint64_t arena64_elems = 0;
+  ahx::ProdCopy prod[3];
+  // staging buffers for host vectors
+  ahx::DevBuf stage_x, stage_y;
+  ahx::DevBuf scratch;  // solver scratch
+};
+
+namespace ahx {
+int prepare_product(ahx_hmat* H, int prec);
+int ensure_device(ahx_hmat* H);
+// Y += d A X on device pointers
+int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
+                   double* Y, uint64_t ldY);
+bool is_device_ptr(const void* p);
+}  // namespace ahx

@@ -1,0 +1,182 @@
+// Batched H-matrix product Y += d A X (mltaGeHVec / mltaGeHGeM semantics:
+// H/mltaGeHVec.cpp:16-59, H/mblock.cpp:126-154, Include/mblock.h:99-109).
+//
+// One CTA per leaf, leaves launched in descending cost order so that the
+// large coarse-level leaves start first.  Right-hand sides are processed in
+// groups of PG; the X rows of a leaf are staged in shared memory (coalesced
+// column-major loads); dense leaves and the U-phase of low-rank leaves have
+// one output row per thread (coalesced arena reads, broadcast shared reads);
+// the V-phase T = V^T X splits each output over several threads and sums the
+// partial results in a fixed order (run-to-run deterministic per leaf).
+// Contributions are added to Y with FP64 atomics (leaves sharing rows).
+#include <cuda_bf16.h>
+
+#include "ahx_matvec.cuh"
+
+namespace ahx {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kCh = 128;  // X rows per staged chunk
+constexpr int kKt = 32;   // low-rank columns per pass
+
+template <typename S, typename A>
+__device__ __forceinline__ A ldcvt(const S* p);
+template <>
+__device__ __forceinline__ double ldcvt<double, double>(const double* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ float ldcvt<float, float>(const float* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ float ldcvt<__nv_bfloat16, float>(const __nv_bfloat16* p) {
+  return __bfloat162float(__ldg(p));
+}
+
+template <typename A, int PG>
+__device__ __forceinline__ void stage_x(A (*Xs)[PG + 1], const MvArgs& a, uint32_t r0, uint32_t pg,
+                                        uint32_t b2, uint32_t jb, uint32_t jn) {
+  for (uint32_t e = threadIdx.x; e < jn * PG; e += kThreads) {
+    const uint32_t j = e % jn, r = e / jn;
+    Xs[j][r] = r < pg ? (A)a.X[(uint64_t)(r0 + r) * a.ldX + b2 + jb + j] : (A)0;
+  }
+}
+
+template <typename SL, typename SD, typename A, int PG>
+__global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
+  __shared__ A Xs[kCh][PG + 1];
+  __shared__ A Ts[kKt][PG];
+  __shared__ A red[kThreads];
+  const MvLeaf L = a.leaves[a.order[blockIdx.x]];
+  const uint32_t tid = threadIdx.x;
+  const double d = a.d;
+  for (uint32_t r0 = 0; r0 < a.p; r0 += PG) {
+    const uint32_t pg = min((uint32_t)PG, a.p - r0);
+    if (L.rank < 0) {
+      const SD* Ad = L.dense_in_lr_arena ? reinterpret_cast<const SD*>(
+                                               reinterpret_cast<const SL*>(a.arena_lr) + L.off)
+                                         : reinterpret_cast<const SD*>(a.arena_dn) + L.off;
+      for (uint32_t ib = 0; ib < L.n1; ib += kThreads) {
+        const uint32_t i = ib + tid;
+        A acc[PG];
+#pragma unroll
+        for (int r = 0; r < PG; ++r) acc[r] = 0;
+        for (uint32_t jb = 0; jb < L.n2; jb += kCh) {
+          const uint32_t jn = min((uint32_t)kCh, L.n2 - jb);
+          __syncthreads();
+          stage_x<A, PG>(Xs, a, r0, pg, L.b2, jb, jn);
+          __syncthreads();
+          if (i < L.n1) {
+            const SD* col = Ad + i + (uint64_t)jb * L.n1;
+            for (uint32_t j = 0; j < jn; ++j) {
+              const A av = ldcvt<SD, A>(col + (uint64_t)j * L.n1);
+#pragma unroll
+              for (int r = 0; r < PG; ++r) acc[r] = fma(av, Xs[j][r], acc[r]);
+            }
+          }
+        }
+        if (i < L.n1)
+          for (uint32_t r = 0; r < pg; ++r)
+            atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
+      }
+    } else if (L.rank > 0) {
+      const uint32_t k = (uint32_t)L.rank;
+      const SL* U = reinterpret_cast<const SL*>(a.arena_lr) + L.off;
+      const SL* V = U + (uint64_t)L.n1 * k;
+      for (uint32_t lb = 0; lb < k; lb += kKt) {
+        const uint32_t kn = min((uint32_t)kKt, k - lb);
+        const uint32_t nout = kn * PG;
+        // phase 1: Ts[l][r] = sum_j V[j, lb+l] X[b2+j, r0+r]
+        const uint32_t ns = nout >= kThreads ? 1u : kThreads / nout;  // threads per output
+        const uint32_t nq = (nout + kThreads - 1) / kThreads;         // outputs per thread
+        A tacc[(kKt * PG + kThreads - 1) / kThreads];
+#pragma unroll
+        for (int q = 0; q < (kKt * PG + kThreads - 1) / kThreads; ++q) tacc[q] = 0;
+        const uint32_t sub = tid / nout, o1 = tid % nout;
+        for (uint32_t jb = 0; jb < L.n2; jb += kCh) {
+          const uint32_t jn = min((uint32_t)kCh, L.n2 - jb);
+          __syncthreads();
+          stage_x<A, PG>(Xs, a, r0, pg, L.b2, jb, jn);
+          __syncthreads();
+          if (ns > 1) {
+            if (sub < ns) {
+              const uint32_t l = o1 / PG, r = o1 % PG;
+              const SL* vc = V + (uint64_t)(lb + l) * L.n2 + jb;
+              for (uint32_t j = sub; j < jn; j += ns) tacc[0] = fma(ldcvt<SL, A>(vc + j), Xs[j][r], tacc[0]);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < (kKt * PG + kThreads - 1) / kThreads; ++q) {
+              const uint32_t o = tid + q * kThreads;
+              if (q < (int)nq && o < nout) {
+                const uint32_t l = o / PG, r = o % PG;
+                const SL* vc = V + (uint64_t)(lb + l) * L.n2 + jb;
+                A s = tacc[q];
+                for (uint32_t j = 0; j < jn; ++j) s = fma(ldcvt<SL, A>(vc + j), Xs[j][r], s);
+                tacc[q] = s;
+              }
+            }
+          }
+        }
+        __syncthreads();
+        if (ns > 1) {
+          red[tid] = tacc[0];
+          __syncthreads();
+          if (tid < nout) {
+            A s = red[tid];
+            for (uint32_t q = 1; q < ns; ++q) s += red[tid + q * nout];
+            Ts[tid / PG][tid % PG] = s;
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < (kKt * PG + kThreads - 1) / kThreads; ++q) {
+            const uint32_t o = tid + q * kThreads;
+            if (q < (int)nq && o < nout) Ts[o / PG][o % PG] = tacc[q];
+          }
+        }
+        __syncthreads();
+        // phase 2: Y[b1+i, r] += d sum_l U[i, lb+l] Ts[l][r]
+        for (uint32_t ib = 0; ib < L.n1; ib += kThreads) {
+          const uint32_t i = ib + tid;
+          if (i < L.n1) {
+            A acc[PG];
+#pragma unroll
+            for (int r = 0; r < PG; ++r) acc[r] = 0;
+            const SL* uc = U + (uint64_t)lb * L.n1 + i;
+            for (uint32_t l = 0; l < kn; ++l) {
+              const A uv = ldcvt<SL, A>(uc + (uint64_t)l * L.n1);
+#pragma unroll
+              for (int r = 0; r < PG; ++r) acc[r] = fma(uv, Ts[l][r], acc[r]);
+            }
+            for (uint32_t r = 0; r < pg; ++r)
+              atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+template <typename SL, typename SD, typename A>
+cudaError_t launch_typed(const MvArgs& a, cudaStream_t s) {
+  if (a.nleaves == 0 || a.p == 0) return cudaSuccess;
+  const uint32_t grid = a.nleaves;
+  if (a.p == 1) mv_kernel<SL, SD, A, 1><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p == 2) mv_kernel<SL, SD, A, 2><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p <= 4) mv_kernel<SL, SD, A, 4><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p <= 8) mv_kernel<SL, SD, A, 8><<<grid, kThreads, 0, s>>>(a);
+  else mv_kernel<SL, SD, A, 16><<<grid, kThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_matvec(int prec, const MvArgs& a, cudaStream_t s) {
+  switch (prec) {
+    case kFP64: return launch_typed<double, double, double>(a, s);
+    case kFP32: return launch_typed<float, float, float>(a, s);
+    case kBF16FP32: return launch_typed<__nv_bfloat16, float, float>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace ahx

@@ -1,0 +1,214 @@
+"""Host-side mirror of the reference's H-matrix interface over libahx.
+
+Names and argument meanings follow AHMED: ``matgenGeH_omp`` (assembly,
+Include/matgen_omp.h:197), ``mltaGeHVec`` / ``mltaGeHGeM`` (y += d A x,
+H/mltaGeHVec.cpp:567-577), ``GMRes`` (solvers/GMRES.cpp:80) and ``CG``
+(solvers/CG.cpp:31).  Vectors are in the permuted (cluster) ordering.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, check, lib, ptr
+
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16_FP32}
+TREES = {"bbx": TREE_BBX, "pca": TREE_PCA}
+
+
+def mean_nn(points):
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    return lib().ahx_mean_nn(ptr(pts), pts.shape[0])
+
+
+def _prec(p):
+    return PRECISIONS[p] if isinstance(p, str) else int(p)
+
+
+def _ncols(a, n):
+    if a.ndim == 1:
+        return 1, n
+    # numpy (p, n) C-contiguous rows == column-major n x p
+    return a.shape[0], a.shape[1]
+
+
+class HMatrix:
+    """Cluster tree, block-cluster tree and (after assembly) device leaves."""
+
+    def __init__(self, points, tree="bbx", bmin=32, eta=0.8, device=0, stream=None):
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        if pts.ndim != 2 or pts.shape[1] != 3:
+            raise ValueError("points must have shape (n, 3)")
+        self.n = pts.shape[0]
+        self.points = pts
+        kind = TREES[tree] if isinstance(tree, str) else int(tree)
+        h = C.c_void_p()
+        check(lib().ahx_hmat_create(ptr(pts), self.n, kind, bmin, float(eta) ** 2, device,
+                                    C.c_void_p(stream) if stream else None, C.byref(h)))
+        self._h = h
+        self.h = None
+        self.eps = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ahx_hmat_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def nleaves(self):
+        return lib().ahx_hmat_nleaves(self._h)
+
+    @property
+    def stream(self):
+        return lib().ahx_hmat_stream(self._h)
+
+    def set_stream(self, stream):
+        check(lib().ahx_hmat_set_stream(self._h, C.c_void_p(stream) if stream else None))
+
+    def perm(self):
+        op = np.zeros(self.n, np.uint32)
+        po = np.zeros(self.n, np.uint32)
+        check(lib().ahx_hmat_perm(self._h, ptr(op), ptr(po)))
+        return op, po
+
+    def leaves(self):
+        out = np.zeros((self.nleaves, 7), np.uint32)
+        check(lib().ahx_hmat_leaves(self._h, ptr(out)))
+        return out
+
+    # -- assembly ---------------------------------------------------------
+    def matgenGeH_omp(self, h=None, eps=1e-6, rankmax=2**32 - 1):
+        """ACA assembly of every leaf on the GPU (h: diagonal 1/(4 pi h); default mean NN)."""
+        self.h = mean_nn(self.points) if h is None else float(h)
+        self.eps = float(eps)
+        check(lib().ahx_assemble(self._h, self.h, self.eps, min(int(rankmax), 2**32 - 1)))
+        return self
+
+    assemble = matgenGeH_omp
+
+    def ranks(self):
+        out = np.zeros(self.nleaves, np.int32)
+        check(lib().ahx_hmat_ranks(self._h, ptr(out)))
+        return out
+
+    def aca_ranks(self):
+        out = np.zeros(self.nleaves, np.int32)
+        check(lib().ahx_hmat_aca_ranks(self._h, ptr(out)))
+        return out
+
+    def leaf_data(self, l):
+        cnt = lib().ahx_hmat_leaf_size(self._h, l)
+        out = np.zeros(cnt, np.float64)
+        if cnt:
+            check(lib().ahx_hmat_get_leaf(self._h, l, ptr(out)))
+        return out
+
+    def set_leaves(self, ranks, data, offsets):
+        ranks = np.ascontiguousarray(ranks, dtype=np.int32)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        check(lib().ahx_hmat_set_leaves(self._h, ptr(ranks), ptr(data), ptr(offsets)))
+        self.eps = self.eps or 0.0
+
+    def storage_bytes(self, precision="fp64"):
+        return lib().ahx_hmat_storage_bytes(self._h, _prec(precision))
+
+    def prepare(self, precision="fp64"):
+        check(lib().ahx_hmat_prepare(self._h, _prec(precision)))
+
+    # -- product ----------------------------------------------------------
+    def mltaGeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
+        """Y += d A X with X, Y column-major (numpy / torch, host or CUDA)."""
+        check(lib().ahx_matvec(self._h, _prec(precision), float(d), int(p), ptr(X), int(ldX),
+                               ptr(Y), int(ldY)))
+        return Y
+
+    def mltaGeHVec(self, d, x, y, precision="fp64"):
+        """y += d A x; x, y of shape (n,) or (p, n) (rows are right-hand sides)."""
+        p, ld = _ncols(x, self.n)
+        return self.mltaGeHGeM(d, p, x, ld, y, ld, precision)
+
+    # -- solvers ----------------------------------------------------------
+    def GMRes(self, b, x, eps, m, nsteps, precision="fp64"):
+        """Restarted GMRES(m); b, x of shape (n,) or (p, n).  Returns (status, eps[], nsteps[])."""
+        p, ld = _ncols(b, self.n)
+        iters = np.zeros(p, np.uint32)
+        res = np.zeros(p, np.float64)
+        code = check(lib().ahx_gmres(self._h, _prec(precision), p, ptr(b), ld, ptr(x), ld,
+                                     float(eps), int(m), int(nsteps), ptr(iters), ptr(res)))
+        return (0 if code == _capi.AHX_OK else 1), res, iters
+
+    def CG(self, b, x, eps, nsteps):
+        p, ld = _ncols(b, self.n)
+        iters = np.zeros(p, np.uint32)
+        res = np.zeros(p, np.float64)
+        code = check(lib().ahx_cg(self._h, p, ptr(b), ld, ptr(x), ld, float(eps), int(nsteps),
+                                  ptr(iters), ptr(res)))
+        return (0 if code == _capi.AHX_OK else 1), res, iters
+
+
+class HBatch:
+    """Many assembled H-matrices as one product / one batched GMRES."""
+
+    def __init__(self, mats, precision="fp64"):
+        self.mats = list(mats)
+        arr = (C.c_void_p * len(self.mats))(*[m.handle.value for m in self.mats])
+        h = C.c_void_p()
+        check(lib().ahx_batch_create(arr, len(self.mats), _prec(precision), C.byref(h)))
+        self._h = h
+        self.n = lib().ahx_batch_n(h)
+        self.offsets = np.concatenate([[0], np.cumsum([m.n for m in self.mats])]).astype(np.int64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ahx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def matvec(self, d, X, Y, p=1):
+        check(lib().ahx_batch_matvec(self._h, float(d), int(p), ptr(X), ptr(Y)))
+        return Y
+
+    def gmres(self, b, x, eps, m, nsteps):
+        k = len(self.mats)
+        iters = np.zeros(k, np.uint32)
+        res = np.zeros(k, np.float64)
+        code = check(lib().ahx_batch_gmres(self._h, ptr(b), ptr(x), float(eps), int(m),
+                                           int(nsteps), ptr(iters), ptr(res)))
+        return (0 if code == _capi.AHX_OK else 1), res, iters
+
+
+# functional forms with the reference's argument order
+def matgenGeH_omp(H, h=None, eps=1e-6, rankmax=2**32 - 1):
+    return H.matgenGeH_omp(h, eps, rankmax)
+
+
+def mltaGeHVec(d, H, x, y, precision="fp64"):
+    return H.mltaGeHVec(d, x, y, precision)
+
+
+def mltaGeHGeM(d, H, p, X, ldX, Y, ldY, precision="fp64"):
+    return H.mltaGeHGeM(d, p, X, ldX, Y, ldY, precision)
+
+
+def GMRes(H, b, x, eps, m, nsteps, precision="fp64"):
+    return H.GMRes(b, x, eps, m, nsteps, precision)
+
+
+def CG(H, b, x, eps, nsteps):
+    return H.CG(b, x, eps, nsteps)

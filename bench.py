@@ -1,0 +1,290 @@
+"""Benchmark: batched H-matvec on one GB300 (and the CPU reference path beside it).
+
+Workload (Laplace single-layer collocation on the unit sphere):
+  N = 65,536 Fibonacci-sphere points, K(x,y) = 1/(4 pi |x-y|), diagonal
+  1/(4 pi h) with h the mean nearest-neighbour distance; bounding-box cluster
+  tree, leaf size 32, eta = 0.8, ACA eps = 1e-6; 16 right-hand sides
+  X ~ U[-1, 1] (numpy PCG64 seed 1).
+A step is one product Y += A X of the assembled H-matrix with all 16
+right-hand sides; `value` counts vector products (16 per step) per second.
+The leaf arena (>= 0.5 GB) is larger than L2, so no flush is needed between
+steps.  `value` uses FP32 leaf storage (the mixed form); the plain FP64 form
+is timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_POINTS = 65536
+NRHS = 16
+BMIN = 32
+ETA = 0.8
+EPS = 1e-6
+METRIC = "H-matvec/s"
+UNIT = "vector products/s"
+WORKLOAD = {
+    "workload": "laplace-sphere-65536-16rhs",
+    "points": "fibonacci sphere", "n": N_POINTS, "rhs": NRHS, "tree": "bbx", "leaf": BMIN,
+    "eta": ETA, "eps": EPS, "kernel": "1/(4 pi r), diag 1/(4 pi h)",
+    "l2": "inputs larger than L2 (no flush)",
+}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            sm = [float(r[0]) for r in rows]
+            out["sm_mhz"] = statistics.median(sm) if sm else None
+            out["sm_max_mhz"] = float(rows[0][1]) if rows else None
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for k, nm in enumerate(names):
+                if any("Active" in r[3 + k] or r[3 + k].strip() == "1" for r in rows):
+                    out["reasons"].append(nm)
+            out["samples"] = len(rows)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        return out
+
+
+def algorithmic_bytes(H, prec, p):
+    """Leaf bytes read once per product + X read once + Y read and written once."""
+    arena = H.storage_bytes(prec)
+    return arena + p * H.n * (8 + 2 * 8)
+
+
+def cpu_reference_run(steps, warmup, threads):
+    """The reference path on the host cores (oracle restatement; full product per step)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from ahmed_gb300 import geometry as G
+
+    P = G.fibonacci_sphere(N_POINTS)
+    h = O.mean_nn(P)
+    Ho = O.OracleH(P, O.TREE_BBX, BMIN, ETA, h)
+    Ho.assemble(EPS, nthreads=threads)
+    X = np.random.default_rng(1).uniform(-1.0, 1.0, (NRHS, N_POINTS))
+    Y = np.zeros_like(X)
+    for _ in range(warmup):
+        Ho.matvec(X, Y, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        Ho.matvec(X, Y, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return NRHS * steps / dt, dt / steps
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    val, sec = cpu_reference_run(args.steps, args.warmup, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": WORKLOAD,
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full 16-RHS products of the N=65536 H-matrix "
+                                   "(oracle C restatement, OpenMP over right-hand sides)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import ahmed_gb300 as A
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P = A.geometry.fibonacci_sphere(N_POINTS)
+    h = A.mean_nn(P)
+    H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA, device=local)
+    stream = torch.cuda.current_stream(dev)
+    H.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    H.matgenGeH_omp(h, EPS)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    ranks = H.ranks()
+    X = torch.from_numpy(np.random.default_rng(1).uniform(-1.0, 1.0, (NRHS, N_POINTS))).to(dev)
+    Y = torch.zeros_like(X)
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if ws > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+    H.prepare("fp64")
+    H.prepare("fp32")
+    ms64 = timed("fp64", max(2, args.steps // 4), args.warmup)
+    with ClockSampler(local) as cs:
+        ms32 = timed("fp32", args.steps, args.warmup)
+    clocks = cs.summary()
+
+    # end to end through the public API with pinned host buffers
+    Xh = torch.from_numpy(np.random.default_rng(1).uniform(-1.0, 1.0, (NRHS, N_POINTS))).pin_memory()
+    Yh = torch.zeros_like(Xh).pin_memory()
+    for _ in range(args.warmup):
+        H.mltaGeHVec(1.0, Xh.numpy(), Yh.numpy(), precision="fp32")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        H.mltaGeHVec(1.0, Xh.numpy(), Yh.numpy(), precision="fp32")
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+
+    # accuracy of the measured forms against the FP64 product (per right-hand side)
+    Y64 = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Y64, precision="fp64")
+    Y32 = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Y32, precision="fp32")
+    torch.cuda.synchronize()
+    err32 = float(((Y32 - Y64).norm(dim=1) / Y64.norm(dim=1)).max())
+
+    peak, peak_kind = _peaks()
+    bytes32 = algorithmic_bytes(H, "fp32", NRHS)
+    bytes64 = algorithmic_bytes(H, "fp64", NRHS)
+    achieved = bytes32 / (ms32 * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("mv_kernel_fp32_16rhs_c2")
+        except Exception:
+            traffic = None
+    value = ws * NRHS / (ms32 * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, parallelism=("replicas%d" % ws),
+                       leaves=int(H.nleaves), lowrank_leaves=int((ranks >= 0).sum()),
+                       avg_rank=float(ranks[ranks >= 0].mean()),
+                       fp32_arena_bytes=int(H.storage_bytes("fp32")),
+                       fp64_arena_bytes=int(H.storage_bytes("fp64")),
+                       plain_fp64_value=ws * NRHS / (ms64 * 1e-3), plain_fp64_ms=ms64,
+                       mixed_over_plain=ms64 / ms32, fp32_max_rel_err_per_rhs=err32,
+                       assembly_s=t_asm),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_kind": peak_kind, "algorithmic_bytes": bytes32,
+                     "fp64_algorithmic_bytes": bytes64},
+        "e2e": {"value": ws * NRHS / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": 2 * NRHS * N_POINTS * 8,
+                "d2h_bytes_per_step": NRHS * N_POINTS * 8},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cval, _ = cpu_reference_run(max(2, min(args.steps, 8)), 1, threads)
+        line["cpu_baseline"] = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "full 16-RHS products of the same N=65536 H-matrix "
+                                          "assembled by the oracle (C restatement)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ahx", choices=["ahx", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

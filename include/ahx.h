@@ -1,0 +1,134 @@
+/* ahx -- GB300-native H-matrix hot path (ACA assembly, H-matvec, GMRES/CG).
+ *
+ * C ABI of libahx.so.  Plain pointers and sizes only.  Every function returns
+ * an int status (AHX_OK on success) and never aborts; ahx_last_error() gives
+ * the message of the last failure on the calling thread.  Vectors are in the
+ * permuted (cluster) ordering, exactly as the reference's products expect
+ * them; ahx_hmat_perm() gives the permutation.
+ *
+ * Each entry point names the reference interface (AHMED 1.0, paths relative
+ * to its source tree) that it replaces on the GPU.
+ */
+#ifndef AHX_H
+#define AHX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AHX_OK 0
+#define AHX_ERR_ARG 1      /* invalid argument / size */
+#define AHX_ERR_CUDA 2     /* CUDA runtime error (message in ahx_last_error) */
+#define AHX_ERR_STATE 3    /* call order (e.g. product before assembly) */
+#define AHX_ERR_NOMEM 4    /* device allocation failed */
+#define AHX_NOT_CONVERGED 5 /* solver stopped at its iteration limit */
+
+/* cluster-tree kinds */
+#define AHX_TREE_BBX 0 /* bounding-box bisection: Include/cluster_bbx.h:24-133 (cluster3d_bbx) */
+#define AHX_TREE_PCA 1 /* PCA bisection + centroid ACA start: Include/bemcluster.h:16-59 */
+
+/* storage precisions of the product */
+#define AHX_FP64 0      /* plain form: FP64 leaves (mblock<double>) */
+#define AHX_FP32 1      /* all leaves FP32, FP32 accumulation */
+#define AHX_BF16_FP32 2 /* low-rank factors BF16, dense leaves FP32, FP32 accumulation */
+
+typedef struct ahx_hmat ahx_hmat;
+typedef struct ahx_batch ahx_batch;
+
+const char* ahx_last_error(void);
+int ahx_version(void);
+
+/* Mean nearest-neighbour distance h of a point cloud (3*n doubles, xyz). */
+double ahx_mean_nn(const double* pts, uint32_t n);
+
+/* Cluster tree + block-cluster tree.  Replaces
+ *   cluster3d_bbx / bemcluster ctor + createClusterTree  Include/cluster_bbx.h:100,
+ *                                                         Include/cluster_pca.h:204
+ *   blcluster::subdivide(cl1, cl2, eta2, nblcks)          Include/blcluster.h:382
+ *   gen_BlSequence                                        parallel/gen_blseq.cpp:68
+ * pts: 3*n doubles in the original order; eta2 = eta*eta as the reference
+ * callers pass it.  device: CUDA device ordinal; stream: cudaStream_t or NULL
+ * (a private stream is created). */
+int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
+                    int device, void* stream, ahx_hmat** out);
+int ahx_hmat_destroy(ahx_hmat* H);
+int ahx_hmat_set_stream(ahx_hmat* H, void* stream);
+void* ahx_hmat_stream(const ahx_hmat* H);
+uint32_t ahx_hmat_n(const ahx_hmat* H);
+uint32_t ahx_hmat_nleaves(const ahx_hmat* H);
+/* op_perm[permuted] = original, po_perm[original] = permuted (either may be NULL) */
+int ahx_hmat_perm(const ahx_hmat* H, uint32_t* op_perm, uint32_t* po_perm);
+/* 7 words per leaf in DFS (idx) order: b1, n1, b2, n2, adm, idx, i0 */
+int ahx_hmat_leaves(const ahx_hmat* H, uint32_t* out);
+
+/* ACA assembly of all leaves with the Laplace collocation generator
+ * K(x,y) = 1/(4 pi |x-y|), diagonal 1/(4 pi h); replaces
+ *   matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A)  Include/matgen_omp.h:197-213
+ *   matgenGeH_sqntl(..., recmpr = false, ...)           Include/matgen_sqntl.h:88-102
+ *   apprx_unsym / ::ACA / mblock::cpyLrM_cmpr           Include/apprx.h:136-172
+ * The assembled leaves live on the device in FP64. */
+int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax);
+/* per leaf: rank after recompression, -1 for dense leaves (mblock::isLrM/rank) */
+int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks);
+/* per leaf: ACA rank before recompression, -1 for dense */
+int ahx_hmat_aca_ranks(const ahx_hmat* H, int32_t* ranks);
+/* number of doubles of leaf l (mblock data: U then V, or the dense block) */
+uint64_t ahx_hmat_leaf_size(const ahx_hmat* H, uint32_t l);
+/* copy leaf l into out (mblock<double>::getdata() layout) */
+int ahx_hmat_get_leaf(const ahx_hmat* H, uint32_t l, double* out);
+/* upload a whole leaf set (e.g. from host mblock<double>** A): ranks[l] (-1 dense),
+ * data = concatenation in leaf order, offsets[l] = start of leaf l in data (nleaves+1). */
+int ahx_hmat_set_leaves(ahx_hmat* H, const int32_t* ranks, const double* data,
+                        const uint64_t* offsets);
+/* bytes of the leaf arena used by the product at a precision */
+uint64_t ahx_hmat_storage_bytes(ahx_hmat* H, int precision);
+/* prepare the product copy at a precision (done lazily by the product otherwise) */
+int ahx_hmat_prepare(ahx_hmat* H, int precision);
+
+/* Y += d A X for p right-hand sides, column-major with leading dimensions ldX, ldY.
+ * X and Y may be host or device pointers (host data are staged through the
+ * device; pinned host memory is copied asynchronously).  Replaces
+ *   mltaGeHVec(d, bl, A, x, y)                     H/mltaGeHVec.cpp:567-571 (p == 1)
+ *   mltaGeHGeM(d, bl, A, p, X, ldX, Y, ldY)        H/mltaGeHVec.cpp:573-577 */
+int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX,
+               double* Y, uint64_t ldY);
+
+/* Restarted GMRES(m) for p right-hand sides (each with its own Krylov space),
+ * right-preconditioner free.  Replaces GMRes(A, b, x, eps, m, nsteps)
+ * solvers/GMRES.cpp:80-181.  B, X column-major n x p (host or device), X holds
+ * the initial guess.  tol: relative residual target; maxit: iteration limit
+ * (the reference's nsteps on input).  precision: storage of the inner
+ * product; with AHX_FP32 or AHX_BF16_FP32 the solve is wrapped in FP64
+ * iterative refinement (residual and orthogonalisation in FP64 with the FP64
+ * leaves).  iters[p], resid[p] (may be NULL) receive per-RHS iteration counts
+ * and final relative residuals (the reference's nsteps and eps on output).
+ * Returns AHX_OK if every RHS converged, AHX_NOT_CONVERGED otherwise. */
+int ahx_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t ldB, double* X,
+              uint64_t ldX, double tol, uint32_t m, uint32_t maxit, uint32_t* iters,
+              double* resid);
+
+/* Conjugate gradients for p right-hand sides; replaces CG(A, b, x, eps, nsteps)
+ * solvers/CG.cpp:31-113 (FP64 product). */
+int ahx_cg(ahx_hmat* H, uint32_t p, const double* B, uint64_t ldB, double* X, uint64_t ldX,
+           double tol, uint32_t maxit, uint32_t* iters, double* resid);
+
+/* Many independent H-matrices of uneven size as one product: all leaves of all
+ * instances run in one launch per product.  Vectors are the concatenation of
+ * the instances' vectors (instance i at offset sum_{j<i} n_j), p columns with
+ * leading dimension = total length.  The instances must be assembled. */
+int ahx_batch_create(ahx_hmat* const* mats, uint32_t count, int precision, ahx_batch** out);
+int ahx_batch_destroy(ahx_batch* b);
+uint64_t ahx_batch_n(const ahx_batch* b);
+int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double* Y);
+/* batched GMRES(m): one right-hand side per instance (b: concatenated), FP64
+ * refinement around the batch's storage precision; iters/resid per instance. */
+int ahx_batch_gmres(ahx_batch* b, const double* B, double* X, double tol, uint32_t m,
+                    uint32_t maxit, uint32_t* iters, double* resid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AHX_H */

@@ -872,28 +872,45 @@ void or_set_leaf(or_hmat* H, uint32_t l, int32_t rank, const double* data) {
 /* product: mltaGeHVec_ / mblock::mltaLrMVec_ / mltaGeMVec                    */
 /* (H/mltaGeHVec.cpp:16-35, H/mblock.cpp:126-138, Include/mblock.h:99-102)    */
 
-static void leaf_mv(const or_hmat* H, uint32_t l, double d, const double* x, double* y) {
+/* one leaf, all p right-hand sides: low rank as mltaLrMGeM_ (t = V^T X, Y += d U t,
+ * H/mblock.cpp:141-154), dense as mltaGeMGeM (Include/mblock.h:105-109) */
+static void leaf_mm(const or_hmat* H, uint32_t l, double d, uint32_t p, const double* X,
+                    double* Y, size_t ld) {
   const or_leaf* L = &H->leaves[l];
   const double* A = H->data[l];
   const uint32_t n1 = L->n1, n2 = L->n2;
-  const double* xp = x + L->b2;
-  double* yp = y + L->b1;
-  if (H->rank[l] >= 0) {
+  if (H->rank[l] > 0) {
     const uint32_t k = (uint32_t)H->rank[l];
-    for (uint32_t r = 0; r < k; ++r) {
-      const double e = d * dot(n2, A + (size_t)k * n1 + (size_t)r * n2, xp);
-      const double* u = A + (size_t)r * n1;
-      for (uint32_t i = 0; i < n1; ++i) yp[i] += e * u[i];
+    const double* V = A + (size_t)k * n1;
+    double tb[256];
+    double* t = (size_t)k * p <= 256 ? tb : (double*)malloc(sizeof(double) * (size_t)k * p);
+    for (uint32_t c = 0; c < p; ++c)
+      for (uint32_t r = 0; r < k; ++r)
+        t[r + (size_t)c * k] = d * dot(n2, V + (size_t)r * n2, X + c * ld + L->b2);
+    for (uint32_t c = 0; c < p; ++c) {
+      double* yp = Y + c * ld + L->b1;
+      for (uint32_t r = 0; r < k; ++r) {
+        const double e = t[r + (size_t)c * k];
+        const double* u = A + (size_t)r * n1;
+        for (uint32_t i = 0; i < n1; ++i) yp[i] += e * u[i];
+      }
     }
-  } else {
-    for (uint32_t j = 0; j < n2; ++j) {
-      const double t = d * xp[j];
-      const double* a = A + (size_t)j * n1;
-      for (uint32_t i = 0; i < n1; ++i) yp[i] += t * a[i];
+    if (t != tb) free(t);
+  } else if (H->rank[l] < 0) {
+    for (uint32_t c = 0; c < p; ++c) {
+      const double* xp = X + c * ld + L->b2;
+      double* yp = Y + c * ld + L->b1;
+      for (uint32_t j = 0; j < n2; ++j) {
+        const double t = d * xp[j];
+        const double* a = A + (size_t)j * n1;
+        for (uint32_t i = 0; i < n1; ++i) yp[i] += t * a[i];
+      }
     }
   }
 }
 
+/* H/mltaGeHVec.cpp:16-59 visits every leaf once; here the leaves are shared
+ * among threads with private accumulators summed in thread order. */
 void or_matvec(const or_hmat* H, double d, uint32_t p, const double* X, double* Y, int nthreads) {
   const size_t n = H->n;
   set_threads(nthreads);
@@ -902,35 +919,25 @@ void or_matvec(const or_hmat* H, double d, uint32_t p, const double* X, double* 
   nt = nthreads > 0 ? nthreads : omp_get_max_threads();
 #endif
   if (nt <= 1) {
-    for (uint32_t r = 0; r < p; ++r)
-      for (uint32_t l = 0; l < H->nleaves; ++l) leaf_mv(H, l, d, X + r * n, Y + r * n);
+    for (uint32_t l = 0; l < H->nleaves; ++l) leaf_mm(H, l, d, p, X, Y, n);
     return;
   }
-  if ((int)p >= nt) {
-#pragma omp parallel for schedule(static)
-    for (int64_t r = 0; r < (int64_t)p; ++r)
-      for (uint32_t l = 0; l < H->nleaves; ++l) leaf_mv(H, l, d, X + r * n, Y + r * n);
-    return;
-  }
-  /* fewer right-hand sides than threads: leaf-parallel with private accumulators */
-  double* acc = (double*)calloc((size_t)nt * n, sizeof(double));
-  for (uint32_t r = 0; r < p; ++r) {
-#pragma omp parallel
-    {
-      int t = 0;
+  double* acc = (double*)malloc(sizeof(double) * (size_t)nt * n * p);
+#pragma omp parallel num_threads(nt)
+  {
+    int t = 0;
 #ifdef _OPENMP
-      t = omp_get_thread_num();
+    t = omp_get_thread_num();
 #endif
-      double* ya = acc + (size_t)t * n;
-      memset(ya, 0, sizeof(double) * n);
-#pragma omp for schedule(dynamic, 16)
-      for (int64_t l = 0; l < (int64_t)H->nleaves; ++l) leaf_mv(H, (uint32_t)l, d, X + r * n, ya);
+    double* ya = acc + (size_t)t * n * p;
+    memset(ya, 0, sizeof(double) * n * p);
+#pragma omp for schedule(dynamic, 8)
+    for (int64_t l = 0; l < (int64_t)H->nleaves; ++l) leaf_mm(H, (uint32_t)l, d, p, X, ya, n);
 #pragma omp for schedule(static)
-      for (int64_t i = 0; i < (int64_t)n; ++i) {
-        double s = 0.0;
-        for (int q = 0; q < nt; ++q) s += acc[(size_t)q * n + i];
-        Y[r * n + i] += s;
-      }
+    for (int64_t i = 0; i < (int64_t)(n * p); ++i) {
+      double s = 0.0;
+      for (int q = 0; q < nt; ++q) s += acc[(size_t)q * n * p + i];
+      Y[i] += s;
     }
   }
   free(acc);

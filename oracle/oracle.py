@@ -158,9 +158,12 @@ class OracleH:
         """Full matrix in permuted order (small n only)."""
         op, _ = self.perm()
         P = self.pts[op]
-        D = np.sqrt(((P[:, None, :] - P[None, :, :]) ** 2).sum(-1))
+        dx = P[:, None, 0] - P[None, :, 0]
+        dy = P[:, None, 1] - P[None, :, 1]
+        dz = P[:, None, 2] - P[None, :, 2]
+        D = np.sqrt((dx * dx + dy * dy) + dz * dz)  # same rounding as or_entry
         np.fill_diagonal(D, self.h)
-        return 1.0 / (4.0 * np.pi * D)
+        return 1.0 / ((4.0 * np.pi) * D)
 
 
 def ref_available():

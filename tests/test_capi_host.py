@@ -1,0 +1,64 @@
+"""Host-side checks of libahx that need no GPU: exports, trees, permutations, h."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ahmed_gb300 as A
+from ahmed_gb300 import _capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASES = ["fib4096", "cube3000", "ell2500", "sph360", "fib50"]
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "ahx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ahx_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _capi.lib()
+    names = _declared()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(L, name), name
+    bound = {s[0] for s in _capi.SIGNATURES}
+    assert set(names) <= bound, set(names) - bound
+
+
+def test_version_and_error_channel():
+    assert _capi.lib().ahx_version() >= 10000
+    with pytest.raises(_capi.AhxError):
+        A.HMatrix(np.zeros((0, 3)))
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("kind", ["bbx", "pca"])
+def test_product_tree_matches_reference(golden, case, kind):
+    g = golden(case)
+    H = A.HMatrix(g["points"], kind, bmin=int(g["bmin"]), eta=float(g["eta"]))
+    op, po = H.perm()
+    assert np.array_equal(op, g[f"{kind}_op_perm"])
+    assert np.array_equal(po, g[f"{kind}_po_perm"])
+    assert np.array_equal(H.leaves(), g[f"{kind}_leaves"])
+
+
+def test_mean_nn_matches_oracle_bitwise(golden):
+    for case in ("fib4096", "cube3000", "ell2500"):
+        g = golden(case)
+        assert A.mean_nn(g["points"]) == float(g["h"])
+
+
+def test_leaf_list_is_a_partition():
+    """Every (row, col) pair of the matrix is covered by exactly one leaf."""
+    P = A.geometry.cube_surface(1500, 3)
+    for kind in ("bbx", "pca"):
+        H = A.HMatrix(P, kind, bmin=16)
+        lv = H.leaves().astype(np.int64)
+        cover = np.zeros((H.n, H.n), np.int8)
+        for b1, n1, b2, n2 in lv[:, :4]:
+            cover[b1:b1 + n1, b2:b2 + n2] += 1
+        assert (cover == 1).all()
+        assert np.array_equal(lv[:, 5], np.arange(len(lv)))

@@ -1,0 +1,116 @@
+"""H-matvec on the GPU through the C ABI against the reference and the oracle.
+
+Plain form: FP64 leaves, results within 1e-12 relative of the reference's
+mltaGeHVec / mltaGeHGeM on the same leaves.  Mixed forms: error against the
+FP64 product stated per right-hand side (FP32 <= 2e-6, BF16/FP32 <= 2e-2).
+"""
+import numpy as np
+import pytest
+
+import ahmed_gb300 as A
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_FP32 = 2e-6
+TOL_BF16 = 2e-2
+
+
+def _relerr(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _with_leaves(g, kind, src_ranks, chunks):
+    H = A.HMatrix(g["points"], kind, bmin=int(g["bmin"]), eta=float(g["eta"]))
+    offs = np.zeros(len(chunks) + 1, np.uint64)
+    offs[1:] = np.cumsum([c.size for c in chunks])
+    data = np.concatenate(chunks) if chunks else np.zeros(0)
+    H.set_leaves(src_ranks, data, offs)
+    return H
+
+
+@pytest.mark.parametrize("kind", ["bbx", "pca"])
+def test_fp64_product_on_reference_leaves(golden, kind):
+    """The reference's own leaf data (sph360): y = A x to 1e-12 of mltaGeHVec."""
+    g = golden("sph360")
+    offs = g[f"{kind}_offsets"]
+    data = g[f"{kind}_data"]
+    chunks = [data[offs[l]:offs[l + 1]] for l in range(len(offs) - 1)]
+    H = _with_leaves(g, kind, g[f"{kind}_ranks"], chunks)
+    n = H.n
+    y = H.mltaGeHVec(1.0, g["x"], np.zeros(n))
+    assert _relerr(y, g[f"{kind}_y"]) <= TOL_FP64
+    Y = H.mltaGeHVec(-0.5, g["X4"], np.zeros((4, n)))
+    for r in range(4):
+        assert _relerr(Y[r], g[f"{kind}_Y4"][r]) <= TOL_FP64
+
+
+@pytest.fixture(scope="module")
+def oracle_pair(golden):
+    """fib4096 assembled by the oracle; the same leaves uploaded to the GPU."""
+    out = {}
+    g = golden("fib4096")
+    for kind, k in (("bbx", O.TREE_BBX), ("pca", O.TREE_PCA)):
+        Ho = O.OracleH(g["points"], k, 32, 0.8, float(g["h"]))
+        Ho.assemble(1e-6, nthreads=4)
+        chunks = [Ho.leaf_data(l) for l in range(Ho.nleaves)]
+        out[kind] = (Ho, _with_leaves(g, kind, Ho.ranks(), chunks))
+    return out
+
+
+@pytest.mark.parametrize("kind", ["bbx", "pca"])
+@pytest.mark.parametrize("p", [1, 3, 16, 37])
+def test_fp64_product_matches_oracle(oracle_pair, kind, p):
+    Ho, H = oracle_pair[kind]
+    n = H.n
+    rng = np.random.default_rng(p)
+    X = rng.uniform(-1, 1, (p, n))
+    Y0 = rng.uniform(-1, 1, (p, n))
+    Yo = Ho.matvec(X, Y0.copy(), d=0.75)
+    Yg = H.mltaGeHGeM(0.75, p, X, n, Y0.copy(), n)
+    for r in range(p):
+        assert _relerr(Yg[r] - Y0[r], Yo[r] - Y0[r]) <= TOL_FP64
+
+
+def test_leading_dimensions_and_device_pointers(oracle_pair):
+    torch = pytest.importorskip("torch")
+    Ho, H = oracle_pair["bbx"]
+    n, p, ld = H.n, 5, H.n + 7
+    rng = np.random.default_rng(9)
+    Xw = rng.uniform(-1, 1, (p, ld))
+    Yw = np.zeros((p, ld))
+    H.mltaGeHGeM(1.0, p, Xw, ld, Yw, ld)
+    Yo = Ho.matvec(np.ascontiguousarray(Xw[:, :n]), np.zeros((p, n)))
+    for r in range(p):
+        assert _relerr(Yw[r, :n], Yo[r]) <= TOL_FP64
+    assert (Yw[:, n:] == 0).all()
+    Xd = torch.from_numpy(Xw).cuda()
+    Yd = torch.zeros((p, ld), dtype=torch.float64, device="cuda")
+    H.mltaGeHGeM(1.0, p, Xd, ld, Yd, ld)
+    torch.cuda.synchronize()
+    assert np.allclose(Yd.cpu().numpy(), Yw, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", TOL_FP32), ("bf16", TOL_BF16)])
+def test_mixed_precision_error_per_rhs(oracle_pair, prec, tol):
+    Ho, H = oracle_pair["pca"]
+    n, p = H.n, 16
+    X = np.random.default_rng(1).uniform(-1, 1, (p, n))
+    Y64 = H.mltaGeHVec(1.0, X, np.zeros((p, n)))
+    Ym = H.mltaGeHVec(1.0, X, np.zeros((p, n)), precision=prec)
+    errs = [_relerr(Ym[r], Y64[r]) for r in range(p)]
+    assert max(errs) <= tol, errs
+    assert H.storage_bytes(prec) < H.storage_bytes("fp64")
+
+
+def test_accumulates_and_zero_rhs(oracle_pair):
+    _, H = oracle_pair["bbx"]
+    n = H.n
+    x = np.random.default_rng(2).uniform(-1, 1, n)
+    y1 = H.mltaGeHVec(1.0, x, np.zeros(n))
+    y2 = H.mltaGeHVec(1.0, x, y1.copy())
+    assert _relerr(y2, 2 * y1) <= TOL_FP64
+    H.mltaGeHGeM(1.0, 0, x, n, y2, n)  # p = 0 is a no-op
+    y3 = H.mltaGeHVec(-1.0, x, y1.copy())
+    assert np.linalg.norm(y3) <= 1e-13 * np.linalg.norm(y1)
