@@ -409,7 +409,9 @@ int ahx_hmat_destroy(ahx_hmat* H) {
   if (!H) return AHX_OK;
   const bool touched = H->stream || H->pts.p;
   if (touched) cudaSetDevice(H->device);
-  if (H->stream) cudaStreamSynchronize(H->stream);
+  // only a stream this handle created is synchronized; work queued on a
+  // caller's stream is ordered before the frees by cudaFree's device sync
+  if (H->own_stream && H->stream) cudaStreamSynchronize(H->stream);
   invalidate_products(H);
   H->pts.release();
   H->arena64.release();

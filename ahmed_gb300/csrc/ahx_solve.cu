@@ -1,5 +1,742 @@
-// Iterative solvers on the device product and the multi-instance batch.
+// Iterative solvers on the device product: restarted GMRES(m) and CG for many
+// independent systems at once, and the multi-instance batch.
+//
+// A "system" is one right-hand side of one H-matrix instance.  Vectors hold
+// p columns of length ntot (the concatenation of all instances); system
+// q = c * nseg + s is the segment s of column c.  Every reduction is split
+// into fixed chunks whose partial sums are combined in a fixed order, so the
+// solvers are run-to-run deterministic.
+//
+// Reference algorithms:
+//   GMRes   solvers/GMRES.cpp:32-181 (Givens rotations genPlRot/applPlRot,
+//           restart residual r = b - A x, convergence |s[i+1]|/|b| < eps)
+//   CG      solvers/CG.cpp:31-113
+// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2), which is
+// as stable as the reference's modified Gram-Schmidt and maps to two blocked
+// kernels per pass.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
 #include "ahx_hmat.hpp"
+
+namespace ahx {
+namespace {
+
+constexpr uint32_t kChunk = 4096;  // elements per reduction item
+constexpr int kRedThreads = 256;
+constexpr int kPerThread = kChunk / kRedThreads;
+
+struct Item {
+  uint64_t base;  // element index in the (ntot x p) array
+  uint32_t len;
+  uint32_t q;     // system
+};
+
+// partial[it * ldp + k] = sum_e V_k[base+e] * W[base+e],  V_k = V + k * vstride
+__global__ void __launch_bounds__(kRedThreads) dots_kernel(const Item* __restrict__ items,
+                                                           const double* __restrict__ V,
+                                                           uint64_t vstride, uint32_t nk,
+                                                           const double* __restrict__ W,
+                                                           double* __restrict__ partial,
+                                                           uint32_t ldp) {
+  __shared__ double red[kRedThreads / 32];
+  const Item it = items[blockIdx.x];
+  double w[kPerThread];
+#pragma unroll
+  for (int e = 0; e < kPerThread; ++e) {
+    const uint32_t o = threadIdx.x + e * kRedThreads;
+    w[e] = o < it.len ? W[it.base + o] : 0.0;
+  }
+  for (uint32_t k = 0; k < nk; ++k) {
+    const double* v = V + k * vstride + it.base;
+    double s = 0.0;
+#pragma unroll
+    for (int e = 0; e < kPerThread; ++e) {
+      const uint32_t o = threadIdx.x + e * kRedThreads;
+      if (o < it.len) s = fma(v[o], w[e], s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = red[0];
+      for (int q = 1; q < kRedThreads / 32; ++q) t += red[q];
+      partial[(uint64_t)blockIdx.x * ldp + k] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// out[q * ldo + k] = sum over the items of q (in order) of partial[it * ldp + k]
+__global__ void reduce_items_kernel(const double* __restrict__ partial, uint32_t ldp,
+                                    const uint32_t* __restrict__ first, uint32_t nsys, uint32_t nk,
+                                    double* __restrict__ out, uint32_t ldo) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsys * nk) return;
+  const uint32_t q = t / nk, k = t % nk;
+  double s = 0.0;
+  for (uint32_t it = first[q]; it < first[q + 1]; ++it) s += partial[(uint64_t)it * ldp + k];
+  out[(uint64_t)q * ldo + k] = s;
+}
+
+__device__ __forceinline__ uint32_t sys_of(uint64_t idx, uint64_t ntot, const uint32_t* seg_id,
+                                           uint32_t nseg) {
+  const uint64_t c = idx / ntot;
+  const uint32_t s = seg_id ? seg_id[idx - c * ntot] : 0u;
+  return (uint32_t)c * nseg + s;
+}
+
+// W -= sum_{k < nk} coef[q * ldc + k] V_k   (per element's system q)
+__global__ void sub_combination_kernel(double* __restrict__ W, const double* __restrict__ V,
+                                       uint64_t vstride, uint32_t nk,
+                                       const double* __restrict__ coef, uint32_t ldc,
+                                       uint64_t total, uint64_t ntot,
+                                       const uint32_t* __restrict__ seg_id, uint32_t nseg) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = sys_of(i, ntot, seg_id, nseg);
+    const double* c = coef + (uint64_t)q * ldc;
+    double w = W[i];
+    for (uint32_t k = 0; k < nk; ++k) w = fma(-c[k], V[k * vstride + i], w);
+    W[i] = w;
+  }
+}
+
+// X += sum_{k < len[q]} y[q * ldy + k] V_k
+__global__ void add_combination_kernel(double* __restrict__ X, const double* __restrict__ V,
+                                       uint64_t vstride, const uint32_t* __restrict__ len,
+                                       const double* __restrict__ y, uint32_t ldy, uint64_t total,
+                                       uint64_t ntot, const uint32_t* __restrict__ seg_id,
+                                       uint32_t nseg) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = sys_of(i, ntot, seg_id, nseg);
+    const double* c = y + (uint64_t)q * ldy;
+    double x = X[i];
+    for (uint32_t k = 0; k < len[q]; ++k) x = fma(c[k], V[k * vstride + i], x);
+    X[i] = x;
+  }
+}
+
+// Y = a[q * lda] * X (per-system factor; mode 1: the factor is 1/sqrt(a) unless a == 0)
+__global__ void scale_kernel(double* Y, const double* X, const double* __restrict__ a,
+                             uint32_t lda, int mode, uint64_t total, uint64_t ntot,
+                             const uint32_t* __restrict__ seg_id, uint32_t nseg) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = sys_of(i, ntot, seg_id, nseg);
+    double f = a[(uint64_t)q * lda];
+    if (mode == 1) f = f > 0.0 ? 1.0 / sqrt(f) : 0.0;
+    Y[i] = f * X[i];
+  }
+}
+
+// Y = X + a[q] * Z   (Y may alias X or Z)
+__global__ void axpy_sys_kernel(double* Y, const double* X, const double* Z,
+                                const double* __restrict__ a, uint64_t total, uint64_t ntot,
+                                const uint32_t* __restrict__ seg_id, uint32_t nseg) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = sys_of(i, ntot, seg_id, nseg);
+    Y[i] = fma(a[q], Z[i], X[i]);
+  }
+}
+
+unsigned grid_for(uint64_t total) {
+  return (unsigned)std::min<uint64_t>((total + 255) / 256, 152ull * 16);
+}
+
+// Givens rotation of solvers/GMRES.cpp:32-56
+void gen_rot(double dx, double dy, double& cs, double& sn) {
+  if (dy == 0.0) {
+    cs = 1.0;
+    sn = 0.0;
+  } else if (std::fabs(dy) > std::fabs(dx)) {
+    const double t = dx / dy;
+    sn = 1.0 / std::sqrt(1.0 + t * t);
+    cs = t * sn;
+  } else {
+    const double t = dy / dx;
+    cs = 1.0 / std::sqrt(1.0 + t * t);
+    sn = t * cs;
+  }
+}
+
+void appl_rot(double& dx, double& dy, double cs, double sn) {
+  const double t = cs * dx + sn * dy;
+  dy = cs * dy - sn * dx;
+  dx = t;
+}
+
+}  // namespace
+
+// Linear operator over ntot x p device vectors (ld = ntot).
+struct Operator {
+  uint64_t ntot = 0;
+  uint32_t nseg = 1;
+  std::vector<uint64_t> seg_off;  // nseg + 1
+  DevBuf seg_id;                  // ntot uint32 (only when nseg > 1)
+  cudaStream_t stream = nullptr;
+  virtual ~Operator() { seg_id.release(); }
+  // Y += d A X in storage precision prec
+  virtual int apply(int prec, double d, uint32_t p, const double* X, double* Y) = 0;
+  int init_segments() {
+    if (nseg <= 1) return AHX_OK;
+    std::vector<uint32_t> id(ntot);
+    for (uint32_t s = 0; s < nseg; ++s)
+      for (uint64_t i = seg_off[s]; i < seg_off[s + 1]; ++i) id[i] = s;
+    int rc = seg_id.reserve(ntot * sizeof(uint32_t));
+    if (rc) return rc;
+    AHX_CUDA(cudaMemcpyAsync(seg_id.p, id.data(), ntot * 4, cudaMemcpyHostToDevice, stream));
+    AHX_CUDA(cudaStreamSynchronize(stream));
+    return AHX_OK;
+  }
+};
+
+struct HmatOp : Operator {
+  ahx_hmat* H;
+  explicit HmatOp(ahx_hmat* h) : H(h) {
+    ntot = h->tree.n;
+    seg_off = {0, ntot};
+    stream = h->stream;
+  }
+  int apply(int prec, double d, uint32_t p, const double* X, double* Y) override {
+    return product_device(H, prec, d, p, X, ntot, Y, ntot);
+  }
+};
+
+// Reduction plan + device scratch for a family of systems.
+class Solver {
+ public:
+  Solver(Operator& op, uint32_t p) : op_(op), p_(p) {}
+  ~Solver() {
+    for (DevBuf* b : {&items_, &first_, &partial_, &small_, &small2_, &len_}) b->release();
+  }
+
+  int init(uint32_t maxk) {
+    nsys_ = op_.nseg * p_;
+    total_ = op_.ntot * p_;
+    std::vector<Item> items;
+    std::vector<uint32_t> first(nsys_ + 1, 0);
+    for (uint32_t c = 0; c < p_; ++c)
+      for (uint32_t s = 0; s < op_.nseg; ++s) {
+        const uint32_t q = c * op_.nseg + s;
+        first[q] = (uint32_t)items.size();
+        const uint64_t b = op_.seg_off[s], e = op_.seg_off[s + 1];
+        for (uint64_t o = b; o < e; o += kChunk)
+          items.push_back(Item{(uint64_t)c * op_.ntot + o, (uint32_t)std::min<uint64_t>(kChunk, e - o), q});
+      }
+    // systems are numbered c * nseg + s, which is the order items were produced in
+    first[nsys_] = (uint32_t)items.size();
+    nitems_ = (uint32_t)items.size();
+    maxk_ = maxk;
+    int rc;
+    if ((rc = items_.reserve(std::max<size_t>(items.size(), 1) * sizeof(Item)))) return rc;
+    if ((rc = first_.reserve(first.size() * sizeof(uint32_t)))) return rc;
+    if ((rc = partial_.reserve((size_t)std::max(nitems_, 1u) * maxk * sizeof(double)))) return rc;
+    if ((rc = small_.reserve((size_t)nsys_ * maxk * sizeof(double)))) return rc;
+    if ((rc = small2_.reserve((size_t)nsys_ * maxk * sizeof(double)))) return rc;
+    if ((rc = len_.reserve((size_t)nsys_ * sizeof(uint32_t)))) return rc;
+    if (!items.empty())
+      AHX_CUDA(cudaMemcpyAsync(items_.p, items.data(), items.size() * sizeof(Item),
+                               cudaMemcpyHostToDevice, op_.stream));
+    AHX_CUDA(cudaMemcpyAsync(first_.p, first.data(), first.size() * 4, cudaMemcpyHostToDevice,
+                             op_.stream));
+    return AHX_OK;
+  }
+
+  // out[q * maxk + k] = <V_k, W>_q  (device out)
+  int dots(const double* V, uint64_t vstride, uint32_t nk, const double* W, double* out) {
+    if (nitems_ == 0) return AHX_OK;
+    dots_kernel<<<nitems_, kRedThreads, 0, op_.stream>>>(items_.as<Item>(), V, vstride, nk, W,
+                                                         partial_.as<double>(), maxk_);
+    const uint32_t nt = nsys_ * nk;
+    reduce_items_kernel<<<(nt + 255) / 256, 256, 0, op_.stream>>>(
+        partial_.as<double>(), maxk_, first_.as<uint32_t>(), nsys_, nk, out, maxk_);
+    AHX_CUDA(cudaGetLastError());
+    return AHX_OK;
+  }
+
+  const uint32_t* segid() const { return op_.nseg > 1 ? op_.seg_id.as<uint32_t>() : nullptr; }
+
+  Operator& op_;
+  uint32_t p_, nsys_ = 0, nitems_ = 0, maxk_ = 0;
+  uint64_t total_ = 0;
+  DevBuf items_, first_, partial_, small_, small2_, len_;
+};
+
+namespace {
+
+// Restarted GMRES(m) on `sv`'s systems with the operator at precision prec.
+// B, X: device, ntot x p.  active[q] selects the systems to solve.
+// Mirrors solvers/GMRES.cpp:80-181 per system.
+int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uint32_t m,
+               uint32_t maxit, std::vector<uint32_t>& iters, std::vector<double>& resid,
+               std::vector<char>& done, DevBuf& vbuf, DevBuf& rbuf) {
+  Operator& op = sv.op_;
+  cudaStream_t st = op.stream;
+  const uint32_t nsys = sv.nsys_;
+  const uint64_t total = sv.total_;
+  const uint64_t vstride = total;
+  const uint32_t* sid = sv.segid();
+  int rc;
+  if ((rc = vbuf.reserve((size_t)(m + 1) * total * sizeof(double)))) return rc;
+  if ((rc = rbuf.reserve(total * sizeof(double)))) return rc;
+  double* V = vbuf.as<double>();
+  double* r = rbuf.as<double>();
+  const uint32_t K = sv.maxk_;  // >= m + 1
+  double* dsmall = sv.small_.as<double>();
+  double* dsmall2 = sv.small2_.as<double>();
+  std::vector<double> hbuf((size_t)nsys * K), nbuf((size_t)nsys * K);
+  auto fetch = [&](double* dev, std::vector<double>& host, uint32_t nk) -> int {
+    (void)nk;
+    AHX_CUDA(cudaMemcpyAsync(host.data(), dev, (size_t)nsys * K * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaStreamSynchronize(st));
+    return AHX_OK;
+  };
+  // normb
+  if ((rc = sv.dots(B, 0, 1, B, dsmall))) return rc;
+  if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+  std::vector<double> normb(nsys);
+  for (uint32_t q = 0; q < nsys; ++q) normb[q] = std::sqrt(nbuf[(size_t)q * K]);
+  // r = b - A x
+  AHX_CUDA(cudaMemcpyAsync(r, B, total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  if ((rc = op.apply(prec, -1.0, sv.p_, X, r))) return rc;
+  if ((rc = sv.dots(r, 0, 1, r, dsmall))) return rc;
+  if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+  std::vector<double> beta(nsys);
+  std::vector<double> zero_fix(nsys, 0.0);
+  for (uint32_t q = 0; q < nsys; ++q) {
+    beta[q] = std::sqrt(nbuf[(size_t)q * K]);
+    if (done[q]) continue;
+    if (normb[q] == 0.0) {
+      // x = 0 (solvers/GMRES.cpp:96-103)
+      done[q] = 1;
+      resid[q] = 0.0;
+      iters[q] = 0;
+      zero_fix[q] = 1.0;
+      continue;
+    }
+    resid[q] = beta[q] / normb[q];
+    if (resid[q] <= tol) {
+      done[q] = 1;
+      iters[q] = 0;
+    }
+  }
+  // zero x of systems with b == 0:  X -= 1 * X on those systems
+  if (std::any_of(zero_fix.begin(), zero_fix.end(), [](double v) { return v != 0.0; })) {
+    std::vector<double> f(nsys);
+    for (uint32_t q = 0; q < nsys; ++q) f[q] = zero_fix[q] != 0.0 ? 0.0 : 1.0;
+    AHX_CUDA(cudaMemcpyAsync(dsmall2, f.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(total), 256, 0, st>>>(X, X, dsmall2, 1, 0, total, op.ntot, sid, op.nseg);
+  }
+  std::vector<double> Hm((size_t)nsys * (m + 1) * m), cs((size_t)nsys * (m + 1)),
+      sn((size_t)nsys * (m + 1)), s((size_t)nsys * (m + 1));
+  std::vector<double> ycoef((size_t)nsys * K, 0.0);
+  std::vector<uint32_t> ylen(nsys, 0);
+  uint32_t j = 1;
+  auto active_left = [&]() {
+    for (uint32_t q = 0; q < nsys; ++q)
+      if (!done[q]) return true;
+    return false;
+  };
+  // solve H y = s (upper triangular, column oriented as dtrsv) for system q with k columns
+  auto tri_solve = [&](uint32_t q, uint32_t k) {
+    const double* Hq = Hm.data() + (size_t)q * (m + 1) * m;
+    double* y = ycoef.data() + (size_t)q * K;
+    for (uint32_t i = 0; i < k; ++i) y[i] = s[(size_t)q * (m + 1) + i];
+    for (int jj = (int)k - 1; jj >= 0; --jj) {
+      y[jj] /= Hq[jj + (size_t)jj * (m + 1)];
+      for (int i = 0; i < jj; ++i) y[i] -= y[jj] * Hq[i + (size_t)jj * (m + 1)];
+    }
+    ylen[q] = k;
+  };
+  while (active_left() && j <= maxit) {
+    // V_0 = r / beta
+    for (uint32_t q = 0; q < nsys; ++q) nbuf[q] = done[q] ? 0.0 : beta[q] * beta[q];
+    AHX_CUDA(cudaMemcpyAsync(dsmall2, nbuf.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(total), 256, 0, st>>>(V, r, dsmall2, 1, 1, total, op.ntot, sid, op.nseg);
+    std::vector<char> cyc(nsys);
+    for (uint32_t q = 0; q < nsys; ++q) {
+      cyc[q] = !done[q];
+      s[(size_t)q * (m + 1)] = beta[q];
+      for (uint32_t i = 1; i <= m; ++i) s[(size_t)q * (m + 1) + i] = 0.0;
+      ylen[q] = 0;
+    }
+    uint32_t i = 0;
+    for (; i < m && j <= maxit; i++, j++) {
+      double* vi = V + (size_t)i * vstride;
+      double* w = V + (size_t)(i + 1) * vstride;
+      AHX_CUDA(cudaMemsetAsync(w, 0, total * sizeof(double), st));
+      if ((rc = op.apply(prec, 1.0, sv.p_, vi, w))) return rc;
+      // CGS2: h = V^T w; w -= V h; h2 = V^T w; w -= V h2
+      if ((rc = sv.dots(V, vstride, i + 1, w, dsmall))) return rc;
+      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, dsmall, K,
+                                                              total, op.ntot, sid, op.nseg);
+      if ((rc = sv.dots(V, vstride, i + 1, w, dsmall2))) return rc;
+      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, dsmall2, K,
+                                                              total, op.ntot, sid, op.nseg);
+      std::vector<double> h1((size_t)nsys * K), h2((size_t)nsys * K);
+      if ((rc = fetch(dsmall, h1, i + 1))) return rc;
+      if ((rc = fetch(dsmall2, h2, i + 1))) return rc;
+      if ((rc = sv.dots(w, 0, 1, w, dsmall))) return rc;
+      if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+      // w /= |w|
+      scale_kernel<<<grid_for(total), 256, 0, st>>>(w, w, dsmall, K, 1, total, op.ntot, sid, op.nseg);
+      AHX_CUDA(cudaGetLastError());
+      for (uint32_t q = 0; q < nsys; ++q) {
+        if (!cyc[q] || done[q]) continue;
+        double* Hq = Hm.data() + (size_t)q * (m + 1) * m;
+        double* col = Hq + (size_t)i * (m + 1);
+        for (uint32_t k = 0; k <= i; ++k) col[k] = h1[(size_t)q * K + k] + h2[(size_t)q * K + k];
+        col[i + 1] = std::sqrt(nbuf[(size_t)q * K]);
+        double* csq = cs.data() + (size_t)q * (m + 1);
+        double* snq = sn.data() + (size_t)q * (m + 1);
+        double* sq = s.data() + (size_t)q * (m + 1);
+        for (uint32_t k = 0; k < i; k++) appl_rot(col[k], col[k + 1], csq[k], snq[k]);
+        gen_rot(col[i], col[i + 1], csq[i], snq[i]);
+        appl_rot(col[i], col[i + 1], csq[i], snq[i]);
+        appl_rot(sq[i], sq[i + 1], csq[i], snq[i]);
+        resid[q] = std::fabs(sq[i + 1] / normb[q]);
+        iters[q] = j;
+        if (resid[q] < tol) {
+          tri_solve(q, i + 1);
+          done[q] = 1;
+        }
+      }
+    }
+    // systems still running: update with the i vectors of this cycle
+    for (uint32_t q = 0; q < nsys; ++q)
+      if (cyc[q] && !done[q] && i > 0) tri_solve(q, i);
+    AHX_CUDA(cudaMemcpyAsync(sv.small_.p, ycoef.data(), (size_t)nsys * K * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+    AHX_CUDA(cudaMemcpyAsync(sv.len_.p, ylen.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    add_combination_kernel<<<grid_for(total), 256, 0, st>>>(X, V, vstride, sv.len_.as<uint32_t>(),
+                                                            sv.small_.as<double>(), K, total,
+                                                            op.ntot, sid, op.nseg);
+    AHX_CUDA(cudaGetLastError());
+    if (!active_left()) break;
+    // r = b - A x for the running systems
+    AHX_CUDA(cudaMemcpyAsync(r, B, total * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if ((rc = op.apply(prec, -1.0, sv.p_, X, r))) return rc;
+    if ((rc = sv.dots(r, 0, 1, r, dsmall))) return rc;
+    if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+    for (uint32_t q = 0; q < nsys; ++q) {
+      if (done[q]) continue;
+      beta[q] = std::sqrt(nbuf[(size_t)q * K]);
+      resid[q] = beta[q] / normb[q];
+      if (resid[q] < tol) {
+        done[q] = 1;
+        iters[q] = j;
+      }
+    }
+  }
+  AHX_CUDA(cudaStreamSynchronize(st));
+  return AHX_OK;
+}
+
+// GMRES with the storage precision `prec`: FP64 runs gmres_core directly; the
+// mixed forms run FP64 iterative refinement around inner GMRES cycles.
+int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X, double tol,
+                 uint32_t m, uint32_t maxit, uint32_t* iters_out, double* resid_out, int& status) {
+  if (m == 0) {
+    set_error("gmres: m must be positive");
+    return AHX_ERR_ARG;
+  }
+  Solver sv(op, p);
+  int rc = sv.init(m + 2);
+  if (rc) return rc;
+  const uint32_t nsys = sv.nsys_;
+  std::vector<uint32_t> iters(nsys, 0);
+  std::vector<double> resid(nsys, 0.0);
+  std::vector<char> done(nsys, 0);
+  DevBuf vbuf, rbuf, rr, z;
+  if (prec == kFP64) {
+    rc = gmres_core(sv, kFP64, B, X, tol, m, maxit, iters, resid, done, vbuf, rbuf);
+  } else {
+    // FP64 refinement: r = b - A64 x (FP64 leaves), solve A_prec z = r by one
+    // GMRES(m) cycle to an inner tolerance, x += z.
+    const uint64_t total = sv.total_;
+    if ((rc = rr.reserve(total * sizeof(double)))) return rc;
+    if ((rc = z.reserve(total * sizeof(double)))) return rc;
+    cudaStream_t st = op.stream;
+    const double inner_tol = prec == kFP32 ? 1e-6 : 1e-2;
+    std::vector<double> normb(nsys), nb((size_t)nsys * sv.maxk_);
+    if ((rc = sv.dots(B, 0, 1, B, sv.small_.as<double>()))) return rc;
+    AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t q = 0; q < nsys; ++q) normb[q] = std::sqrt(nb[(size_t)q * sv.maxk_]);
+    uint32_t used = 0;
+    for (;;) {
+      AHX_CUDA(cudaMemcpyAsync(rr.p, B, total * 8, cudaMemcpyDeviceToDevice, st));
+      if ((rc = op.apply(kFP64, -1.0, p, X, rr.as<double>()))) return rc;
+      if ((rc = sv.dots(rr.as<double>(), 0, 1, rr.as<double>(), sv.small_.as<double>()))) return rc;
+      AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
+      AHX_CUDA(cudaStreamSynchronize(st));
+      bool any = false;
+      std::vector<char> idone(nsys, 0);
+      std::vector<double> mask(nsys, 1.0);
+      for (uint32_t q = 0; q < nsys; ++q) {
+        resid[q] = normb[q] > 0.0 ? std::sqrt(nb[(size_t)q * sv.maxk_]) / normb[q] : 0.0;
+        if (resid[q] < tol || normb[q] == 0.0) {
+          done[q] = 1;
+          idone[q] = 1;
+          mask[q] = 0.0;
+        } else {
+          any = true;
+        }
+      }
+      if (!any || used >= maxit) break;
+      // masked residual (converged systems contribute nothing), z = 0
+      AHX_CUDA(cudaMemcpyAsync(sv.small2_.p, mask.data(), nsys * 8, cudaMemcpyHostToDevice, st));
+      scale_kernel<<<grid_for(total), 256, 0, st>>>(rr.as<double>(), rr.as<double>(),
+                                                    sv.small2_.as<double>(), 1, 0, total, op.ntot,
+                                                    sv.segid(), op.nseg);
+      AHX_CUDA(cudaMemsetAsync(z.p, 0, total * 8, st));
+      std::vector<uint32_t> it2(nsys, 0);
+      std::vector<double> res2(nsys, 0.0);
+      const uint32_t budget = std::min(m, maxit - used);
+      if ((rc = gmres_core(sv, prec, rr.as<double>(), z.as<double>(), inner_tol, m, budget, it2, res2,
+                           idone, vbuf, rbuf)))
+        return rc;
+      uint32_t step = 0;
+      for (uint32_t q = 0; q < nsys; ++q)
+        if (!done[q]) {
+          iters[q] += it2[q];
+          step = std::max(step, it2[q]);
+        }
+      used += std::max(step, 1u);
+      // x += z
+      std::vector<double> ones(nsys, 1.0);
+      AHX_CUDA(cudaMemcpyAsync(sv.small2_.p, ones.data(), nsys * 8, cudaMemcpyHostToDevice, st));
+      axpy_sys_kernel<<<grid_for(total), 256, 0, st>>>(X, X, z.as<double>(), sv.small2_.as<double>(),
+                                                       total, op.ntot, sv.segid(), op.nseg);
+      AHX_CUDA(cudaGetLastError());
+    }
+  }
+  vbuf.release();
+  rbuf.release();
+  rr.release();
+  z.release();
+  if (rc) return rc;
+  status = AHX_OK;
+  for (uint32_t q = 0; q < nsys; ++q) {
+    if (!done[q]) status = AHX_NOT_CONVERGED;
+    if (iters_out) iters_out[q] = iters[q];
+    if (resid_out) resid_out[q] = resid[q];
+  }
+  return AHX_OK;
+}
+
+// CG (solvers/CG.cpp:31-113) for every system, FP64 product.
+int cg_driver(Operator& op, uint32_t p, const double* B, double* X, double tol, uint32_t maxit,
+              uint32_t* iters_out, double* resid_out, int& status) {
+  Solver sv(op, p);
+  int rc = sv.init(4);
+  if (rc) return rc;
+  const uint32_t nsys = sv.nsys_, K = sv.maxk_;
+  const uint64_t total = sv.total_;
+  cudaStream_t st = op.stream;
+  const uint32_t* sid = sv.segid();
+  DevBuf buf;
+  if ((rc = buf.reserve(3 * total * sizeof(double)))) return rc;
+  double* P = buf.as<double>();
+  double* Q = P + total;
+  double* R = Q + total;
+  double* ds = sv.small_.as<double>();
+  double* da = sv.small2_.as<double>();
+  std::vector<double> hb((size_t)nsys * K), coef(nsys);
+  auto dot1 = [&](const double* a, const double* b, std::vector<double>& out) -> int {
+    int r2 = sv.dots(a, 0, 1, b, ds);
+    if (r2) return r2;
+    AHX_CUDA(cudaMemcpyAsync(hb.data(), ds, hb.size() * 8, cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaStreamSynchronize(st));
+    out.resize(nsys);
+    for (uint32_t q = 0; q < nsys; ++q) out[q] = hb[(size_t)q * K];
+    return AHX_OK;
+  };
+  auto axpy = [&](double* Y, const double* Xv, const double* Z, const std::vector<double>& a) -> int {
+    AHX_CUDA(cudaMemcpyAsync(da, a.data(), nsys * 8, cudaMemcpyHostToDevice, st));
+    axpy_sys_kernel<<<grid_for(total), 256, 0, st>>>(Y, Xv, Z, da, total, op.ntot, sid, op.nseg);
+    AHX_CUDA(cudaGetLastError());
+    return AHX_OK;
+  };
+  std::vector<double> nrmb, res2, rho(nsys), rho1(nsys, 0.0), pq;
+  if ((rc = dot1(B, B, nrmb))) return rc;
+  std::vector<char> done(nsys, 0);
+  std::vector<uint32_t> iters(nsys, 0);
+  std::vector<double> resid(nsys, 0.0);
+  AHX_CUDA(cudaMemcpyAsync(R, B, total * 8, cudaMemcpyDeviceToDevice, st));
+  if ((rc = op.apply(kFP64, -1.0, p, X, R))) return rc;
+  if ((rc = dot1(R, R, res2))) return rc;
+  for (uint32_t q = 0; q < nsys; ++q) {
+    nrmb[q] = std::sqrt(nrmb[q]);
+    const double rs = std::sqrt(res2[q]);
+    if (nrmb[q] < 1e-16) {
+      done[q] = 1;
+      resid[q] = 0.0;
+    } else if (rs <= tol * nrmb[q]) {
+      done[q] = 1;
+      resid[q] = rs / nrmb[q];
+    }
+  }
+  for (uint32_t l = 1; l <= maxit; ++l) {
+    bool any = false;
+    for (uint32_t q = 0; q < nsys; ++q) any |= !done[q];
+    if (!any) break;
+    if ((rc = dot1(R, R, rho))) return rc;
+    if (l > 1) {
+      for (uint32_t q = 0; q < nsys; ++q) coef[q] = done[q] ? 0.0 : rho[q] / rho1[q];
+      // p = r + beta p
+      if ((rc = axpy(P, R, P, coef))) return rc;
+    } else {
+      AHX_CUDA(cudaMemcpyAsync(P, R, total * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    AHX_CUDA(cudaMemsetAsync(Q, 0, total * 8, st));
+    if ((rc = op.apply(kFP64, 1.0, p, P, Q))) return rc;
+    if ((rc = dot1(P, Q, pq))) return rc;
+    for (uint32_t q = 0; q < nsys; ++q) coef[q] = done[q] ? 0.0 : rho[q] / pq[q];
+    if ((rc = axpy(X, X, P, coef))) return rc;
+    for (uint32_t q = 0; q < nsys; ++q) coef[q] = -coef[q];
+    if ((rc = axpy(R, R, Q, coef))) return rc;
+    if ((rc = dot1(R, R, res2))) return rc;
+    for (uint32_t q = 0; q < nsys; ++q) {
+      if (done[q]) continue;
+      const double rs = std::sqrt(res2[q]);
+      resid[q] = rs / nrmb[q];
+      iters[q] = l;
+      if (rs <= tol * nrmb[q]) done[q] = 1;
+    }
+    rho1 = rho;
+  }
+  buf.release();
+  status = AHX_OK;
+  for (uint32_t q = 0; q < nsys; ++q) {
+    if (!done[q]) status = AHX_NOT_CONVERGED;
+    if (iters_out) iters_out[q] = iters[q];
+    if (resid_out) resid_out[q] = resid[q];
+  }
+  return AHX_OK;
+}
+
+// Host/device staging of an ntot x p block with leading dimension ld.
+int stage_in(const double* src, uint64_t ld, uint64_t n, uint32_t p, DevBuf& buf, const double*& dev,
+             cudaStream_t st) {
+  if (is_device_ptr(src) && ld == n) {
+    dev = src;
+    return AHX_OK;
+  }
+  int rc = buf.reserve(n * p * sizeof(double));
+  if (rc) return rc;
+  AHX_CUDA(cudaMemcpy2DAsync(buf.p, n * 8, src, ld * 8, n * 8, p, cudaMemcpyDefault, st));
+  dev = buf.as<double>();
+  return AHX_OK;
+}
+
+}  // namespace
+}  // namespace ahx
+
+// ---------------------------------------------------------------------------
+// multi-instance batch
+
+struct ahx_batch : ahx::Operator {
+  std::vector<ahx_hmat*> mats;
+  int prec = 0;
+  int device = 0;
+  bool own_stream = false;
+  // concatenated product tables per precision (FP64 always, for refinement)
+  struct Tab {
+    ahx::DevBuf leaves, order, lr, dn;
+    uint32_t nleaves = 0;
+  } tab[3];
+  ahx::DevBuf stx, sty;
+
+  int build_tab(int pr) {
+    using namespace ahx;
+    Tab& T = tab[pr];
+    std::vector<MvLeaf> all;
+    std::vector<uint64_t> cost;
+    uint64_t lr_elems = 0, dn_elems = 0;
+    std::vector<std::pair<const void*, uint64_t>> lr_src, dn_src;  // (ptr, bytes)
+    const size_t lsz = pr == kFP64 ? 8 : (pr == kFP32 ? 4 : 2);
+    for (size_t i = 0; i < mats.size(); ++i) {
+      ahx_hmat* H = mats[i];
+      int rc = prepare_product(H, pr);
+      if (rc) return rc;
+      ProdCopy& pc = H->prod[pr];
+      std::vector<MvLeaf> lv(pc.nleaves);
+      AHX_CUDA(cudaMemcpy(lv.data(), pc.leaves.p, lv.size() * sizeof(MvLeaf), cudaMemcpyDeviceToHost));
+      uint64_t lr_n = 0, dn_n = 0;
+      for (MvLeaf& L : lv) {
+        L.b1 += (uint32_t)seg_off[i];
+        L.b2 += (uint32_t)seg_off[i];
+        const uint64_t cnt = L.rank < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)L.rank * (L.n1 + L.n2);
+        if (L.dense_in_lr_arena) {
+          lr_n = std::max(lr_n, L.off + cnt);
+          L.off += lr_elems;
+        } else {
+          dn_n = std::max(dn_n, L.off + cnt);
+          L.off += dn_elems;
+        }
+        all.push_back(L);
+        cost.push_back(cnt);
+      }
+      const void* lrp = pr == kFP64 ? H->arena64.p : pc.lr.p;
+      lr_src.push_back({lrp, lr_n * lsz});
+      dn_src.push_back({pc.dn.p, dn_n * 4});
+      lr_elems += lr_n;
+      dn_elems += dn_n;
+    }
+    std::vector<uint32_t> order(all.size());
+    for (uint32_t k = 0; k < order.size(); ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+    int rc;
+    if ((rc = T.leaves.reserve(std::max<size_t>(all.size(), 1) * sizeof(MvLeaf)))) return rc;
+    if ((rc = T.order.reserve(std::max<size_t>(order.size(), 1) * 4))) return rc;
+    if ((rc = T.lr.reserve(std::max<uint64_t>(lr_elems, 1) * lsz))) return rc;
+    if ((rc = T.dn.reserve(std::max<uint64_t>(dn_elems, 1) * 4))) return rc;
+    if (!all.empty()) {
+      AHX_CUDA(cudaMemcpyAsync(T.leaves.p, all.data(), all.size() * sizeof(MvLeaf), cudaMemcpyHostToDevice, stream));
+      AHX_CUDA(cudaMemcpyAsync(T.order.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, stream));
+    }
+    uint64_t o1 = 0, o2 = 0;
+    for (size_t i = 0; i < mats.size(); ++i) {
+      if (lr_src[i].second)
+        AHX_CUDA(cudaMemcpyAsync((char*)T.lr.p + o1, lr_src[i].first, lr_src[i].second, cudaMemcpyDeviceToDevice, stream));
+      if (dn_src[i].second)
+        AHX_CUDA(cudaMemcpyAsync((char*)T.dn.p + o2, dn_src[i].first, dn_src[i].second, cudaMemcpyDeviceToDevice, stream));
+      o1 += lr_src[i].second;
+      o2 += dn_src[i].second;
+    }
+    AHX_CUDA(cudaStreamSynchronize(stream));
+    T.nleaves = (uint32_t)all.size();
+    return AHX_OK;
+  }
+
+  int apply(int pr, double d, uint32_t p, const double* X, double* Y) override {
+    using namespace ahx;
+    Tab& T = tab[pr];
+    MvArgs a;
+    a.leaves = T.leaves.as<MvLeaf>();
+    a.order = T.order.as<uint32_t>();
+    a.nleaves = T.nleaves;
+    a.arena_lr = T.lr.p;
+    a.arena_dn = T.dn.p;
+    a.d = d;
+    a.p = p;
+    a.X = X;
+    a.ldX = ntot;
+    a.Y = Y;
+    a.ldY = ntot;
+    AHX_CUDA(launch_matvec(pr, a, stream));
+    return AHX_OK;
+  }
+};
 
 using namespace ahx;
 
@@ -8,36 +745,183 @@ extern "C" {
 int ahx_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t ldB, double* X,
               uint64_t ldX, double tol, uint32_t m, uint32_t maxit, uint32_t* iters,
               double* resid) {
-  (void)H; (void)precision; (void)p; (void)B; (void)ldB; (void)X; (void)ldX; (void)tol; (void)m;
-  (void)maxit; (void)iters; (void)resid;
-  set_error("ahx_gmres: not built yet");
-  return AHX_ERR_STATE;
+  if (!H || !B || !X || p == 0 || ldB < H->tree.n || ldX < H->tree.n || precision < 0 ||
+      precision > 2) {
+    set_error("ahx_gmres: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  if (!H->assembled) {
+    set_error("ahx_gmres: H-matrix not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  HmatOp op(H);
+  const uint64_t n = H->tree.n;
+  DevBuf bb, xb;
+  const double* Bd = nullptr;
+  if ((rc = stage_in(B, ldB, n, p, bb, Bd, H->stream))) return rc;
+  const double* Xc = nullptr;
+  if ((rc = stage_in(X, ldX, n, p, xb, Xc, H->stream))) return rc;
+  double* Xd = const_cast<double*>(Xc);
+  int status = AHX_OK;
+  rc = gmres_driver(op, precision, p, Bd, Xd, tol, m, maxit, iters, resid, status);
+  if (rc) return rc;
+  if (Xd != X) {
+    AHX_CUDA(cudaMemcpy2DAsync(X, ldX * 8, Xd, n * 8, n * 8, p, cudaMemcpyDefault, H->stream));
+  }
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  bb.release();
+  xb.release();
+  return status;
 }
 
 int ahx_cg(ahx_hmat* H, uint32_t p, const double* B, uint64_t ldB, double* X, uint64_t ldX,
            double tol, uint32_t maxit, uint32_t* iters, double* resid) {
-  (void)H; (void)p; (void)B; (void)ldB; (void)X; (void)ldX; (void)tol; (void)maxit; (void)iters;
-  (void)resid;
-  set_error("ahx_cg: not built yet");
-  return AHX_ERR_STATE;
+  if (!H || !B || !X || p == 0 || ldB < H->tree.n || ldX < H->tree.n) {
+    set_error("ahx_cg: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  if (!H->assembled) {
+    set_error("ahx_cg: H-matrix not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  HmatOp op(H);
+  const uint64_t n = H->tree.n;
+  DevBuf bb, xb;
+  const double* Bd = nullptr;
+  if ((rc = stage_in(B, ldB, n, p, bb, Bd, H->stream))) return rc;
+  const double* Xc = nullptr;
+  if ((rc = stage_in(X, ldX, n, p, xb, Xc, H->stream))) return rc;
+  double* Xd = const_cast<double*>(Xc);
+  int status = AHX_OK;
+  rc = cg_driver(op, p, Bd, Xd, tol, maxit, iters, resid, status);
+  if (rc) return rc;
+  if (Xd != X) AHX_CUDA(cudaMemcpy2DAsync(X, ldX * 8, Xd, n * 8, n * 8, p, cudaMemcpyDefault, H->stream));
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  return status;
 }
 
 int ahx_batch_create(ahx_hmat* const* mats, uint32_t count, int precision, ahx_batch** out) {
-  (void)mats; (void)count; (void)precision; (void)out;
-  set_error("ahx_batch_create: not built yet");
-  return AHX_ERR_STATE;
+  if (!mats || !out || count == 0 || precision < 0 || precision > 2) {
+    set_error("ahx_batch_create: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  *out = nullptr;
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!mats[i] || !mats[i]->assembled) {
+      set_error("ahx_batch_create: every instance must be assembled");
+      return AHX_ERR_STATE;
+    }
+    if (mats[i]->device != mats[0]->device) {
+      set_error("ahx_batch_create: instances on different devices");
+      return AHX_ERR_ARG;
+    }
+  }
+  ahx_batch* b = new (std::nothrow) ahx_batch;
+  if (!b) return AHX_ERR_NOMEM;
+  b->mats.assign(mats, mats + count);
+  b->prec = precision;
+  b->device = mats[0]->device;
+  int rc = ensure_device(mats[0]);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete b;
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+    b->own_stream = true;
+  }
+  b->nseg = count;
+  b->seg_off.assign(count + 1, 0);
+  for (uint32_t i = 0; i < count; ++i) b->seg_off[i + 1] = b->seg_off[i] + mats[i]->tree.n;
+  b->ntot = b->seg_off[count];
+  if (b->ntot >= (1ull << 32)) {
+    delete b;
+    set_error("ahx_batch_create: total length exceeds 2^32");
+    return AHX_ERR_ARG;
+  }
+  for (uint32_t i = 0; i < count; ++i) {
+    // instances share the first instance's stream for the duration of the batch
+    if ((rc = ensure_device(mats[i]))) {
+      delete b;
+      return rc;
+    }
+  }
+  if ((rc = b->init_segments()) || (rc = b->build_tab(kFP64)) ||
+      (precision != kFP64 && (rc = b->build_tab(precision)))) {
+    ahx_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return AHX_OK;
 }
-int ahx_batch_destroy(ahx_batch* b) { (void)b; return AHX_OK; }
-uint64_t ahx_batch_n(const ahx_batch* b) { (void)b; return 0; }
+
+int ahx_batch_destroy(ahx_batch* b) {
+  if (!b) return AHX_OK;
+  cudaSetDevice(b->device);
+  if (b->own_stream && b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& T : b->tab) {
+    T.leaves.release();
+    T.order.release();
+    T.lr.release();
+    T.dn.release();
+  }
+  b->stx.release();
+  b->sty.release();
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  b->stream = nullptr;
+  delete b;
+  return AHX_OK;
+}
+
+uint64_t ahx_batch_n(const ahx_batch* b) { return b ? b->ntot : 0; }
+
 int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double* Y) {
-  (void)b; (void)d; (void)p; (void)X; (void)Y;
-  set_error("ahx_batch_matvec: not built yet");
-  return AHX_ERR_STATE;
+  if (!b || !X || !Y) return AHX_ERR_ARG;
+  if (p == 0) return AHX_OK;
+  AHX_CUDA(cudaSetDevice(b->device));
+  const uint64_t n = b->ntot;
+  const double* Xd = nullptr;
+  int rc = stage_in(X, n, n, p, b->stx, Xd, b->stream);
+  if (rc) return rc;
+  const bool yd = is_device_ptr(Y);
+  double* Yd = Y;
+  if (!yd) {
+    if ((rc = b->sty.reserve(n * p * 8))) return rc;
+    AHX_CUDA(cudaMemcpyAsync(b->sty.p, Y, n * p * 8, cudaMemcpyHostToDevice, b->stream));
+    Yd = b->sty.as<double>();
+  }
+  if ((rc = b->apply(b->prec, d, p, Xd, Yd))) return rc;
+  if (!yd) AHX_CUDA(cudaMemcpyAsync(Y, Yd, n * p * 8, cudaMemcpyDeviceToHost, b->stream));
+  if (!yd || Xd != X) AHX_CUDA(cudaStreamSynchronize(b->stream));
+  return AHX_OK;
 }
+
 int ahx_batch_gmres(ahx_batch* b, const double* B, double* X, double tol, uint32_t m,
                     uint32_t maxit, uint32_t* iters, double* resid) {
-  (void)b; (void)B; (void)X; (void)tol; (void)m; (void)maxit; (void)iters; (void)resid;
-  set_error("ahx_batch_gmres: not built yet");
-  return AHX_ERR_STATE;
+  if (!b || !B || !X) return AHX_ERR_ARG;
+  AHX_CUDA(cudaSetDevice(b->device));
+  const uint64_t n = b->ntot;
+  DevBuf bb, xb;
+  const double* Bd = nullptr;
+  int rc = stage_in(B, n, n, 1, bb, Bd, b->stream);
+  if (rc) return rc;
+  const double* Xc = nullptr;
+  if ((rc = stage_in(X, n, n, 1, xb, Xc, b->stream))) return rc;
+  double* Xd = const_cast<double*>(Xc);
+  int status = AHX_OK;
+  rc = gmres_driver(*b, b->prec, 1, Bd, Xd, tol, m, maxit, iters, resid, status);
+  if (rc) return rc;
+  if (Xd != X) AHX_CUDA(cudaMemcpyAsync(X, Xd, n * 8, cudaMemcpyDefault, b->stream));
+  AHX_CUDA(cudaStreamSynchronize(b->stream));
+  return status;
 }
-}
+
+}  // extern "C"

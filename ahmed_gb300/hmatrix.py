@@ -5,7 +5,9 @@ Include/matgen_omp.h:197), ``mltaGeHVec`` / ``mltaGeHGeM`` (y += d A x,
 H/mltaGeHVec.cpp:567-577), ``GMRes`` (solvers/GMRES.cpp:80) and ``CG``
 (solvers/CG.cpp:31).  Vectors are in the permuted (cluster) ordering.
 """
+import atexit
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -14,6 +16,25 @@ from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, check, lib, ptr
 
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16_FP32}
 TREES = {"bbx": TREE_BBX, "pca": TREE_PCA}
+
+
+# Live handles are released in a fixed order (batches, then matrices) before
+# the interpreter tears modules down; finalizers after that point do nothing.
+_live = weakref.WeakSet()
+_shutdown = False
+
+
+@atexit.register
+def _release_all():
+    global _shutdown
+    objs = list(_live)
+    for o in objs:
+        if isinstance(o, HBatch):
+            o.close()
+    for o in objs:
+        if isinstance(o, HMatrix):
+            o.close()
+    _shutdown = True
 
 
 def mean_nn(points):
@@ -48,13 +69,21 @@ class HMatrix:
         self._h = h
         self.h = None
         self.eps = None
+        self._batches = []
+        _live.add(self)
 
     def close(self):
+        for b in list(getattr(self, "_batches", [])):
+            bb = b()
+            if bb is not None:
+                bb.close()
         if getattr(self, "_h", None):
             lib().ahx_hmat_destroy(self._h)
             self._h = None
 
     def __del__(self):
+        if _shutdown:
+            return
         try:
             self.close()
         except Exception:
@@ -168,6 +197,9 @@ class HBatch:
         self._h = h
         self.n = lib().ahx_batch_n(h)
         self.offsets = np.concatenate([[0], np.cumsum([m.n for m in self.mats])]).astype(np.int64)
+        for m in self.mats:
+            m._batches.append(weakref.ref(self))
+        _live.add(self)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -175,6 +207,8 @@ class HBatch:
             self._h = None
 
     def __del__(self):
+        if _shutdown:
+            return
         try:
             self.close()
         except Exception:

@@ -42,6 +42,14 @@ WORKLOAD = {
 }
 
 
+def set_size(n):
+    """Smaller point counts are used only for profiling captures."""
+    global N_POINTS
+    N_POINTS = n
+    WORKLOAD["n"] = n
+    WORKLOAD["workload"] = f"laplace-sphere-{n}-16rhs"
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -95,7 +103,7 @@ class ClockSampler:
             out["sm_max_mhz"] = float(rows[0][1]) if rows else None
             names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
             for k, nm in enumerate(names):
-                if any("Active" in r[3 + k] or r[3 + k].strip() == "1" for r in rows):
+                if any(r[3 + k].strip() in ("Active", "1") for r in rows):
                     out["reasons"].append(nm)
             out["samples"] = len(rows)
         except Exception:
@@ -167,7 +175,9 @@ def run_gpu(args):
     P = A.geometry.fibonacci_sphere(N_POINTS)
     h = A.mean_nn(P)
     H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA, device=local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream shared by the library and the CUDA events
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     H.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
     H.matgenGeH_omp(h, EPS)
@@ -277,9 +287,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ahx", choices=["ahx", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--n", type=int, default=N_POINTS,
+                    help="number of points (smaller cases are for profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.n != N_POINTS:
+        set_size(args.n)
     if args.impl == "reference":
         run_reference(args)
     else:

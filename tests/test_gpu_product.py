@@ -89,7 +89,9 @@ def test_leading_dimensions_and_device_pointers(oracle_pair):
     Yd = torch.zeros((p, ld), dtype=torch.float64, device="cuda")
     H.mltaGeHGeM(1.0, p, Xd, ld, Yd, ld)
     torch.cuda.synchronize()
-    assert np.allclose(Yd.cpu().numpy(), Yw, rtol=1e-13, atol=1e-15)
+    Yg = Yd.cpu().numpy()
+    assert _relerr(Yg, Yw) <= 1e-13  # atomics: summation order differs between runs
+    assert (Yg[:, n:] == 0).all()
 
 
 @pytest.mark.parametrize("prec,tol", [("fp32", TOL_FP32), ("bf16", TOL_BF16)])
