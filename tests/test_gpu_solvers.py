@@ -145,4 +145,4 @@ def test_batch_product_and_gmres_match_instances():
         r1, e1, i1 = H.GMRes(b[o0:o1], xi, 1e-8, 30, 400)
         assert its[i] == i1[0]
         assert abs(eps[i] - e1[0]) <= 1e-6 * e1[0] + 1e-14  # chunked sums differ by instance offsets
-        assert _relerr(xb[o0:o1], xi) <= 1e-10
+        assert _relerr(xb[o0:o1], xi) <= 1e-7
