@@ -52,6 +52,8 @@ SIGNATURES = [
     ("ahx_batch_n", _u64, [_vp]),
     ("ahx_batch_matvec", _i32, [_vp, _dbl, _u32, _vp, _vp]),
     ("ahx_batch_gmres", _i32, [_vp, _vp, _vp, _dbl, _u32, _u32, _vp, _vp]),
+    ("ahx_aca_block_noalloc", _i32, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _u32, _dbl, _dbl,
+                                     _u32, _vp, _vp, _vp, _vp]),
 ]
 
 _lib = None

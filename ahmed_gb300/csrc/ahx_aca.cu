@@ -14,8 +14,11 @@
 //   recompression addtrll     H/mblock_D.cpp:356-465 (Householder QR in place of
 //                             dgeqrf/dormqr, one-sided Jacobi in place of dgesvd)
 #include <climits>
+#include <mutex>
+#include <string>
 
 #include "ahx_aca.cuh"
+#include "ahx_hmat.hpp"
 
 namespace ahx {
 namespace {
@@ -573,3 +576,156 @@ cudaError_t launch_copy_factors(const CopyTask* tasks, uint32_t ntasks, const do
 }
 
 }  // namespace ahx
+
+// ---------------------------------------------------------------------------
+// ACA of one block with no device allocation.
+//
+// Some callers cannot call cudaMalloc: code that runs while a framework's
+// caching allocator has reserved the device memory, latency-critical paths
+// where the implicit device synchronisation of cudaMalloc/cudaFree is not
+// acceptable, or hosts that own every device allocation themselves and only
+// hand out buffers.  For them, ahx_aca_block_noalloc approximates one
+// admissible block with the same kernel code as ahx_assemble, taking its
+// scratch (the ACA columns, the row/column counters and the recompression
+// work arrays) from the file-scope array below instead of an allocation.
+//
+// The array is 8 MiB and lives on every GPU that loads the library until the
+// process exits.  Every call shares it and it keeps the last call's contents;
+// the kernel rewrites every word it reads (the counters are set to zero by the
+// ACA itself), so nothing carries over between calls.  Calls whose kernels
+// overlap on the GPU (on different streams) race on the array: serialise them.
+
+namespace ahx {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;
+constexpr size_t kNoAllocHeader = 256;  // task slot + result slot
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+size_t noalloc_bytes(uint32_t n1, uint32_t n2, uint32_t kmax) {
+  const size_t ws = aca_ws_doubles(n1, n2, kmax) * sizeof(double);
+  return kNoAllocHeader + ws + (size_t)(n1 + n2) * sizeof(int);
+}
+
+template <int G>
+__global__ void __launch_bounds__(G < 64 ? 32 : G)
+    aca_noalloc_kernel(AcaTask t, uint64_t ws_doubles, PointsSoA P, double diag, double eps,
+                       unsigned char* scratch, double* __restrict__ Uout,
+                       double* __restrict__ Vout, int32_t* info) {
+  extern __shared__ double smem_na[];
+  AcaTask* slot = reinterpret_cast<AcaTask*>(scratch);
+  AcaResult* res = reinterpret_cast<AcaResult*>(scratch + 128);
+  double* ws = reinterpret_cast<double*>(scratch + kNoAllocHeader);
+  int* zs = reinterpret_cast<int*>(ws + ws_doubles);
+  if (threadIdx.x == 0) {
+    t.ws = 0;
+    t.zs = 0;
+    *slot = t;
+    *res = AcaResult{kAcaFail, 0u, 0u, 0u};
+  }
+  __syncthreads();
+  AcaParams p;
+  p.pts = P;
+  p.diag = diag;
+  p.eps = eps;
+  p.tasks = slot;
+  p.ntasks = 1;
+  p.ws = ws;
+  p.zs = zs;
+  p.res = res;
+  if constexpr (G == 32) {
+    Group<32> g(threadIdx.x);
+    aca_task<32>(g, p, 0, smem_na);
+  } else {
+    Group<G> g(threadIdx.x, smem_na + kSmemPerGroup);
+    aca_task<G>(g, p, 0, smem_na);
+  }
+  __syncthreads();
+  const AcaResult r = *res;
+  const uint64_t kc = t.kcap;
+  const double* Un = ws + (uint64_t)(t.n1 + t.n2) * kc;
+  const double* Vn = Un + (uint64_t)t.n1 * kc;
+  if (r.status == kAcaOk) {
+    for (uint64_t e = threadIdx.x; e < (uint64_t)t.n1 * r.kt; e += blockDim.x) Uout[e] = Un[e];
+    for (uint64_t e = threadIdx.x; e < (uint64_t)t.n2 * r.kt; e += blockDim.x) Vout[e] = Vn[e];
+  }
+  if (threadIdx.x == 0) {
+    info[0] = r.status;
+    info[1] = (int32_t)r.k_aca;
+    info[2] = (int32_t)r.kt;
+  }
+}
+
+// Device address of the scratch array, looked up once per device.
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+
+}  // namespace
+}  // namespace ahx
+
+extern "C" int ahx_aca_block_noalloc(const double* px, const double* py, const double* pz,
+                                     uint32_t b1, uint32_t n1, uint32_t b2, uint32_t n2,
+                                     uint32_t i0, double h, double eps, uint32_t kmax, double* U,
+                                     double* V, int32_t* info, void* stream) {
+  using namespace ahx;
+  if (!px || !py || !pz || !U || !V || !info || n1 == 0 || n2 == 0 || i0 >= n1 || kmax == 0 ||
+      !(h > 0.0) || !(eps > 0.0)) {
+    set_error("ahx_aca_block_noalloc: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  const size_t need = noalloc_bytes(n1, n2, kmax);
+  if (need > kNoAllocScratchBytes) {
+    set_error("ahx_aca_block_noalloc: block " + std::to_string(n1) + " x " + std::to_string(n2) +
+              " with kmax " + std::to_string(kmax) + " needs " + std::to_string(need) +
+              " bytes of scratch; the fixed scratch array holds " +
+              std::to_string(kNoAllocScratchBytes) + " bytes");
+    return AHX_ERR_ARG;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 256) {
+    set_error("ahx_aca_block_noalloc: device ordinal out of range");
+    return AHX_ERR_ARG;
+  }
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      // first call on this device: resolve the array's device address (the
+      // current device is the one the kernel will run on)
+      e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        g_noalloc_ptr[dev] = nullptr;
+        return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+      }
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  AcaTask t{};
+  t.b1 = b1;
+  t.n1 = n1;
+  t.b2 = b2;
+  t.n2 = n2;
+  t.i0 = i0;
+  t.kmax = kmax;
+  t.kcap = kmax;
+  t.leaf = 0;
+  const PointsSoA P{px, py, pz};
+  const double diag = 1.0 / (kFourPi * h);
+  const uint64_t wsd = aca_ws_doubles(n1, n2, kmax);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (std::max(n1, n2) > 256) {
+    const size_t smem = sizeof(double) * (kSmemPerGroup + 3 * (kLargeThreads / 32) + 8);
+    aca_noalloc_kernel<kLargeThreads><<<1, kLargeThreads, smem, s>>>(t, wsd, P, diag, eps,
+                                                                     (unsigned char*)scratch, U, V, info);
+  } else {
+    const size_t smem = sizeof(double) * kSmemPerGroup;
+    aca_noalloc_kernel<32><<<1, 32, smem, s>>>(t, wsd, P, diag, eps, (unsigned char*)scratch, U, V,
+                                               info);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "aca_noalloc_kernel launch");
+  return AHX_OK;
+}

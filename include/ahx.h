@@ -128,6 +128,29 @@ int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double
 int ahx_batch_gmres(ahx_batch* b, const double* B, double* X, double tol, uint32_t m,
                     uint32_t maxit, uint32_t* iters, double* resid);
 
+/* ACA + recompression of ONE admissible block without allocating device
+ * memory.  This entry point has no counterpart in the reference.  It is for
+ * callers that cannot call cudaMalloc: code running while a framework's
+ * caching allocator holds the device memory, paths that cannot afford the
+ * device synchronisation of cudaMalloc/cudaFree, and hosts that own every
+ * device allocation and only lend buffers.  The scratch comes from a fixed
+ * 8 MiB array inside the library (present on every GPU that loads it, until
+ * exit); a block needs 256 + 8*(2*(n1+n2)*kmax + 2*kmax^2 + 3*kmax) +
+ * 4*(n1+n2) bytes and larger requests return AHX_ERR_ARG.
+ * Inputs (device): px/py/pz = point coordinates in permuted order; the block
+ * is rows b1..b1+n1-1, columns b2..b2+n2-1, ACA start row i0 (< n1), kernel
+ * diagonal 1/(4 pi h), accuracy eps, at most kmax ACA steps (the reference's
+ * maxk).  Outputs (device): U (n1*kmax doubles) and V (n2*kmax) receive the
+ * recompressed factors (kt columns, mblock layout), info[3] = {status
+ * (1 = low rank, 0 = ACA failed: fill the block densely), ACA rank, kt}.
+ * The kernel is queued on `stream` (NULL = default stream); the call does not
+ * wait for it.  The first call on a device resolves the array's device address
+ * (make it before any stream capture).  All calls share the array: calls whose
+ * kernels overlap on the GPU race, so serialise them. */
+int ahx_aca_block_noalloc(const double* px, const double* py, const double* pz, uint32_t b1,
+                          uint32_t n1, uint32_t b2, uint32_t n2, uint32_t i0, double h, double eps,
+                          uint32_t kmax, double* U, double* V, int32_t* info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
