@@ -41,26 +41,6 @@ int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
   return AHX_OK;
 }
 
-__global__ void cvt_kernel_f32(const double* __restrict__ src, float* __restrict__ dst, uint64_t n) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x)
-    dst[i] = (float)src[i];
-}
-
-struct CvtTask {
-  uint64_t src, dst, count;
-};
-
-template <typename D>
-__global__ void cvt_tasks_kernel(const CvtTask* __restrict__ t, const double* __restrict__ src,
-                                 D* __restrict__ dst) {
-  const CvtTask c = t[blockIdx.x];
-  for (uint64_t i = threadIdx.x; i < c.count; i += blockDim.x) {
-    if constexpr (sizeof(D) == 2) dst[c.dst + i] = __double2bfloat16(src[c.src + i]);
-    else dst[c.dst + i] = (D)src[c.src + i];
-  }
-}
-
 uint32_t maxk_of(uint32_t n1, uint32_t n2, uint32_t rankmax) {
   // unsigned arithmetic as in Include/apprx.h:143-144
   uint32_t maxk = (uint32_t)(n1 * n2) / (n1 + n2) + 4u;
@@ -199,14 +179,7 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
 }
 
 void invalidate_products(ahx_hmat* H) {
-  for (auto& pc : H->prod) {
-    pc.lr.release();
-    pc.dn.release();
-    pc.leaves.release();
-    pc.order.release();
-    pc.valid = false;
-    pc.bytes = 0;
-  }
+  for (auto& pc : H->prod) pc.release_all();
 }
 
 }  // namespace
@@ -255,11 +228,24 @@ int prepare_product(ahx_hmat* H, int prec) {
   if (pc.valid) return AHX_OK;
   const auto& Ls = H->tree.leaves;
   const uint32_t nl = (uint32_t)Ls.size();
+  int rc;
+  if (prec != kFP64) {
+    std::vector<PlanLeaf> pls;
+    pls.reserve(nl);
+    for (uint32_t l = 0; l < nl; ++l) {
+      const Leaf& L = Ls[l];
+      if (H->rank[l] == 0) continue;
+      pls.push_back(PlanLeaf{L.b1, L.n1, L.b2, L.n2, H->rank[l], H->off[l]});
+    }
+    if ((rc = build_mixed_streams(pc, prec, pls, H->arena64.as<double>(), H->tree.n, H->device,
+                                  H->stream)))
+      return rc;
+    pc.valid = true;
+    return AHX_OK;
+  }
   std::vector<MvLeaf> mv;
   std::vector<uint64_t> cost;
   mv.reserve(nl);
-  std::vector<CvtTask> lr_tasks, dn_tasks;
-  uint64_t lr_off = 0, dn_off = 0;
   for (uint32_t l = 0; l < nl; ++l) {
     const Leaf& L = Ls[l];
     const int32_t r = H->rank[l];
@@ -270,61 +256,106 @@ int prepare_product(ahx_hmat* H, int prec) {
     m.b2 = L.b2;
     m.n2 = L.n2;
     m.rank = r;
-    const uint64_t cnt = r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
-    if (prec == kBF16FP32) {
-      if (r < 0) {
-        m.dense_in_lr_arena = 0;
-        m.off = dn_off;
-        dn_tasks.push_back(CvtTask{H->off[l], dn_off, cnt});
-        dn_off += cnt;
-      } else {
-        m.dense_in_lr_arena = 1;
-        m.off = lr_off;
-        lr_tasks.push_back(CvtTask{H->off[l], lr_off, cnt});
-        lr_off += cnt;
-      }
-    } else {
-      m.dense_in_lr_arena = 1;
-      m.off = H->off[l];
-    }
+    m.dense_in_lr_arena = 1;
+    m.off = H->off[l];
     mv.push_back(m);
-    cost.push_back(cnt);
+    cost.push_back(r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2));
   }
   std::vector<uint32_t> order(mv.size());
   std::iota(order.begin(), order.end(), 0u);
   std::stable_sort(order.begin(), order.end(),
                    [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
-  int rc;
   if ((rc = upload(pc.leaves, mv, H->stream))) return rc;
   if ((rc = upload(pc.order, order, H->stream))) return rc;
   pc.nleaves = (uint32_t)mv.size();
-  const double* a64 = H->arena64.as<double>();
-  if (prec == kFP64) {
-    pc.bytes = H->arena64_elems * sizeof(double);
-  } else if (prec == kFP32) {
-    if ((rc = pc.lr.reserve(std::max<uint64_t>(H->arena64_elems, 1) * sizeof(float)))) return rc;
-    if (H->arena64_elems)
-      cvt_kernel_f32<<<1216, 256, 0, H->stream>>>(a64, pc.lr.as<float>(), H->arena64_elems);
-    AHX_CUDA(cudaGetLastError());
-    pc.bytes = H->arena64_elems * sizeof(float);
-  } else {
-    if ((rc = pc.lr.reserve(std::max<uint64_t>(lr_off, 1) * sizeof(__nv_bfloat16)))) return rc;
-    if ((rc = pc.dn.reserve(std::max<uint64_t>(dn_off, 1) * sizeof(float)))) return rc;
-    DevBuf tl, td;
-    if ((rc = upload(tl, lr_tasks, H->stream))) return rc;
-    if ((rc = upload(td, dn_tasks, H->stream))) return rc;
-    if (!lr_tasks.empty())
-      cvt_tasks_kernel<__nv_bfloat16><<<(unsigned)lr_tasks.size(), 256, 0, H->stream>>>(
-          tl.as<CvtTask>(), a64, pc.lr.as<__nv_bfloat16>());
-    if (!dn_tasks.empty())
-      cvt_tasks_kernel<float><<<(unsigned)dn_tasks.size(), 256, 0, H->stream>>>(
-          td.as<CvtTask>(), a64, pc.dn.as<float>());
-    AHX_CUDA(cudaGetLastError());
-    AHX_CUDA(cudaStreamSynchronize(H->stream));
-    pc.bytes = lr_off * sizeof(__nv_bfloat16) + dn_off * sizeof(float);
-  }
+  pc.bytes = H->arena64_elems * sizeof(double);
   AHX_CUDA(cudaStreamSynchronize(H->stream));
   pc.valid = true;
+  return AHX_OK;
+}
+
+int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,
+                        const double* arena64, uint64_t n, int device, cudaStream_t s) {
+  StreamLayout L;
+  build_stream_layout(leaves, prec == kBF16FP32 ? 1 : 0, L);
+  int sms = 0;
+  AHX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const uint32_t grid = (uint32_t)std::max(sms, 1);
+  std::vector<uint64_t> vb(L.vunits.size()), rb(L.units.size());
+  for (size_t i = 0; i < vb.size(); ++i) vb[i] = L.vunits[i].bytes;
+  for (size_t i = 0; i < rb.size(); ++i) rb[i] = L.units[i].bytes;
+  std::vector<uint32_t> vr, rr;
+  balance_ranges(vb, grid, vr);
+  balance_ranges(rb, grid, rr);
+  int rc;
+  if ((rc = pc.vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;
+  if ((rc = pc.rstream.reserve(std::max<uint64_t>(L.rbytes, 16)))) return rc;
+  if ((rc = upload(pc.vunits, L.vunits, s))) return rc;
+  if ((rc = upload(pc.units, L.units, s))) return rc;
+  if ((rc = upload(pc.ents, L.ents, s))) return rc;
+  if ((rc = upload(pc.vranges, vr, s))) return rc;
+  if ((rc = upload(pc.rranges, rr, s))) return rc;
+  if ((rc = upload(pc.treduce, L.treduce, s))) return rc;
+  pc.ntreduce = (uint32_t)L.treduce.size();
+  if ((rc = pc.xr.reserve(std::max<uint64_t>(n, 1) * 16 * sizeof(float)))) return rc;
+  if ((rc = pc.yr.reserve(std::max<uint64_t>(n, 1) * 16 * sizeof(float)))) return rc;
+  if ((rc = pc.t.reserve(std::max<uint64_t>(L.t_rows, 1) * 16 * sizeof(float)))) return rc;
+  if ((rc = pc.err.reserve(sizeof(int)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), s));
+  DevBuf cv;
+  if (!L.vcopies.empty()) {
+    if ((rc = upload(cv, L.vcopies, s))) return rc;
+    AHX_CUDA(launch_stream_copies(cv.as<StreamCopy>(), (uint32_t)L.vcopies.size(), arena64,
+                                  pc.vstream.as<unsigned char>(), s));
+    AHX_CUDA(cudaStreamSynchronize(s));
+  }
+  if (!L.rcopies.empty()) {
+    if ((rc = upload(cv, L.rcopies, s))) return rc;
+    AHX_CUDA(launch_stream_copies(cv.as<StreamCopy>(), (uint32_t)L.rcopies.size(), arena64,
+                                  pc.rstream.as<unsigned char>(), s));
+  }
+  AHX_CUDA(cudaStreamSynchronize(s));
+  cv.release();
+  pc.nvunits = (uint32_t)L.vunits.size();
+  pc.nunits = (uint32_t)L.units.size();
+  pc.grid = grid;
+  pc.t_rows = L.t_rows;
+  pc.bytes = L.payload_bytes;
+  return AHX_OK;
+}
+
+MvPlan mixed_plan(const ProdCopy& pc, uint64_t n) {
+  MvPlan pl;
+  pl.vunits = pc.vunits.as<StreamVUnit>();
+  pl.nvunits = pc.nvunits;
+  pl.units = pc.units.as<StreamUnit>();
+  pl.nunits = pc.nunits;
+  pl.ents = pc.ents.as<StreamEnt>();
+  pl.vranges = pc.vranges.as<uint32_t>();
+  pl.rranges = pc.rranges.as<uint32_t>();
+  pl.treduce = pc.treduce.as<TReduce>();
+  pl.ntreduce = pc.ntreduce;
+  pl.grid = pc.grid;
+  pl.vstream = pc.vstream.as<unsigned char>();
+  pl.rstream = pc.rstream.as<unsigned char>();
+  pl.n = n;
+  pl.xr = pc.xr.as<float>();
+  pl.yr = pc.yr.as<float>();
+  pl.t = pc.t.as<float>();
+  pl.err = pc.err.as<int>();
+  return pl;
+}
+
+int check_stream_error(ProdCopy& pc, cudaStream_t s) {
+  if (!pc.err.p) return AHX_OK;
+  int e = 0;
+  AHX_CUDA(cudaMemcpyAsync(&e, pc.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  AHX_CUDA(cudaStreamSynchronize(s));
+  if (e) {
+    AHX_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), s));
+    set_error("a streaming product kernel timed out waiting for its shared-memory pipeline");
+    return AHX_ERR_CUDA;
+  }
   return AHX_OK;
 }
 
@@ -333,6 +364,11 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   int rc = prepare_product(H, prec);
   if (rc) return rc;
   ProdCopy& pc = H->prod[prec];
+  if (prec != kFP64) {
+    const MvPlan pl = mixed_plan(pc, H->tree.n);
+    AHX_CUDA(launch_matvec_mixed(prec, pl, d, p, X, ldX, Y, ldY, H->stream));
+    return AHX_OK;
+  }
   MvArgs a;
   a.leaves = pc.leaves.as<MvLeaf>();
   a.order = pc.order.as<uint32_t>();
@@ -672,7 +708,10 @@ int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X
     AHX_CUDA(cudaMemcpy2DAsync(Y, ldY * sizeof(double), Yd, n * sizeof(double), n * sizeof(double),
                                p, cudaMemcpyDeviceToHost, H->stream));
   }
-  if (!xd || !yd) AHX_CUDA(cudaStreamSynchronize(H->stream));
+  if (!xd || !yd) {
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    if (precision != kFP64) return check_stream_error(H->prod[precision], H->stream);
+  }
   return AHX_OK;
 }
 

@@ -653,44 +653,44 @@ struct ahx_batch : ahx::Operator {
   struct Tab {
     ahx::DevBuf leaves, order, lr, dn;
     uint32_t nleaves = 0;
+    ahx::ProdCopy plan;  // mixed-precision plan over the concatenated leaves
   } tab[3];
   ahx::DevBuf stx, sty;
 
+  // FP64: concatenated leaf table and arena; mixed precisions: streams built
+  // from the concatenated FP64 arena.
   int build_tab(int pr) {
     using namespace ahx;
     Tab& T = tab[pr];
+    if (pr != kFP64) {
+      Tab& F = tab[kFP64];
+      std::vector<MvLeaf> lv(F.nleaves);
+      AHX_CUDA(cudaMemcpy(lv.data(), F.leaves.p, lv.size() * sizeof(MvLeaf), cudaMemcpyDeviceToHost));
+      std::vector<PlanLeaf> pls;
+      pls.reserve(lv.size());
+      for (const MvLeaf& m : lv) pls.push_back(PlanLeaf{m.b1, m.n1, m.b2, m.n2, m.rank, m.off});
+      return build_mixed_streams(T.plan, pr, pls, F.lr.as<double>(), ntot, device, stream);
+    }
     std::vector<MvLeaf> all;
     std::vector<uint64_t> cost;
-    uint64_t lr_elems = 0, dn_elems = 0;
-    std::vector<std::pair<const void*, uint64_t>> lr_src, dn_src;  // (ptr, bytes)
-    const size_t lsz = pr == kFP64 ? 8 : (pr == kFP32 ? 4 : 2);
+    uint64_t elems = 0;
+    std::vector<std::pair<const void*, uint64_t>> src;  // (ptr, bytes)
     for (size_t i = 0; i < mats.size(); ++i) {
       ahx_hmat* H = mats[i];
-      int rc = prepare_product(H, pr);
+      int rc = prepare_product(H, kFP64);
       if (rc) return rc;
-      ProdCopy& pc = H->prod[pr];
+      ProdCopy& pc = H->prod[kFP64];
       std::vector<MvLeaf> lv(pc.nleaves);
       AHX_CUDA(cudaMemcpy(lv.data(), pc.leaves.p, lv.size() * sizeof(MvLeaf), cudaMemcpyDeviceToHost));
-      uint64_t lr_n = 0, dn_n = 0;
       for (MvLeaf& L : lv) {
         L.b1 += (uint32_t)seg_off[i];
         L.b2 += (uint32_t)seg_off[i];
-        const uint64_t cnt = L.rank < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)L.rank * (L.n1 + L.n2);
-        if (L.dense_in_lr_arena) {
-          lr_n = std::max(lr_n, L.off + cnt);
-          L.off += lr_elems;
-        } else {
-          dn_n = std::max(dn_n, L.off + cnt);
-          L.off += dn_elems;
-        }
+        L.off += elems;
         all.push_back(L);
-        cost.push_back(cnt);
+        cost.push_back(L.rank < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)L.rank * (L.n1 + L.n2));
       }
-      const void* lrp = pr == kFP64 ? H->arena64.p : pc.lr.p;
-      lr_src.push_back({lrp, lr_n * lsz});
-      dn_src.push_back({pc.dn.p, dn_n * 4});
-      lr_elems += lr_n;
-      dn_elems += dn_n;
+      src.push_back({H->arena64.p, H->arena64_elems * sizeof(double)});
+      elems += H->arena64_elems;
     }
     std::vector<uint32_t> order(all.size());
     for (uint32_t k = 0; k < order.size(); ++k) order[k] = k;
@@ -698,20 +698,16 @@ struct ahx_batch : ahx::Operator {
     int rc;
     if ((rc = T.leaves.reserve(std::max<size_t>(all.size(), 1) * sizeof(MvLeaf)))) return rc;
     if ((rc = T.order.reserve(std::max<size_t>(order.size(), 1) * 4))) return rc;
-    if ((rc = T.lr.reserve(std::max<uint64_t>(lr_elems, 1) * lsz))) return rc;
-    if ((rc = T.dn.reserve(std::max<uint64_t>(dn_elems, 1) * 4))) return rc;
+    if ((rc = T.lr.reserve(std::max<uint64_t>(elems, 1) * sizeof(double)))) return rc;
     if (!all.empty()) {
       AHX_CUDA(cudaMemcpyAsync(T.leaves.p, all.data(), all.size() * sizeof(MvLeaf), cudaMemcpyHostToDevice, stream));
       AHX_CUDA(cudaMemcpyAsync(T.order.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, stream));
     }
-    uint64_t o1 = 0, o2 = 0;
-    for (size_t i = 0; i < mats.size(); ++i) {
-      if (lr_src[i].second)
-        AHX_CUDA(cudaMemcpyAsync((char*)T.lr.p + o1, lr_src[i].first, lr_src[i].second, cudaMemcpyDeviceToDevice, stream));
-      if (dn_src[i].second)
-        AHX_CUDA(cudaMemcpyAsync((char*)T.dn.p + o2, dn_src[i].first, dn_src[i].second, cudaMemcpyDeviceToDevice, stream));
-      o1 += lr_src[i].second;
-      o2 += dn_src[i].second;
+    uint64_t o = 0;
+    for (auto& sp : src) {
+      if (sp.second)
+        AHX_CUDA(cudaMemcpyAsync((char*)T.lr.p + o, sp.first, sp.second, cudaMemcpyDeviceToDevice, stream));
+      o += sp.second;
     }
     AHX_CUDA(cudaStreamSynchronize(stream));
     T.nleaves = (uint32_t)all.size();
@@ -721,6 +717,11 @@ struct ahx_batch : ahx::Operator {
   int apply(int pr, double d, uint32_t p, const double* X, double* Y) override {
     using namespace ahx;
     Tab& T = tab[pr];
+    if (pr != kFP64) {
+      const MvPlan pl = mixed_plan(T.plan, ntot);
+      AHX_CUDA(launch_matvec_mixed(pr, pl, d, p, X, ntot, Y, ntot, stream));
+      return AHX_OK;
+    }
     MvArgs a;
     a.leaves = T.leaves.as<MvLeaf>();
     a.order = T.order.as<uint32_t>();
@@ -872,6 +873,7 @@ int ahx_batch_destroy(ahx_batch* b) {
     T.order.release();
     T.lr.release();
     T.dn.release();
+    T.plan.release_all();
   }
   b->stx.release();
   b->sty.release();
