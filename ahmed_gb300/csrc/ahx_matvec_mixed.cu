@@ -228,20 +228,89 @@ __global__ void t_reduce_kernel(const TReduce* __restrict__ items, uint32_t n, f
   }
 }
 
-template <int P>
-__device__ __forceinline__ void fma_row(float (&a0)[P], float (&a1)[P], float u0, float u1,
-                                        const float* row) {
+// One rows unit.  lane = rq * 16 + rr: rr picks rows rr, rr + 16, ... (S row slots,
+// S = ceil(nrows / 16)), rq picks half of the P right-hand sides.
+template <typename SL, int P, int S>
+__device__ __forceinline__ void rows_unit(const StreamUnit& U, const StreamEnt& myent,
+                                          const unsigned char* slot, uint32_t lane, float* __restrict__ yr) {
+  constexpr int H = P / 2;  // right-hand sides per lane (P >= 4 -> H >= 2)
+  const uint32_t nr = U.nrows;
+  const uint32_t rr = lane & 15, rq = lane >> 4;
+  bool ok[S];
 #pragma unroll
-  for (int q = 0; q < P / 4; ++q) {
-    const float4 x = *reinterpret_cast<const float4*>(row + 4 * q);
-    a0[4 * q] = fmaf(u0, x.x, a0[4 * q]);
-    a0[4 * q + 1] = fmaf(u0, x.y, a0[4 * q + 1]);
-    a0[4 * q + 2] = fmaf(u0, x.z, a0[4 * q + 2]);
-    a0[4 * q + 3] = fmaf(u0, x.w, a0[4 * q + 3]);
-    a1[4 * q] = fmaf(u1, x.x, a1[4 * q]);
-    a1[4 * q + 1] = fmaf(u1, x.y, a1[4 * q + 1]);
-    a1[4 * q + 2] = fmaf(u1, x.z, a1[4 * q + 2]);
-    a1[4 * q + 3] = fmaf(u1, x.w, a1[4 * q + 3]);
+  for (int k = 0; k < S; ++k) ok[k] = rr + 16 * k < nr;
+  float a[S][H];
+#pragma unroll
+  for (int k = 0; k < S; ++k)
+#pragma unroll
+    for (int r = 0; r < H; ++r) a[k][r] = 0.f;
+  const float* side = reinterpret_cast<const float*>(slot + kSlotBytes) + rq * H;
+  for (uint32_t e = 0; e < U.ne; ++e) {
+    const uint32_t boff = __shfl_sync(0xffffffffu, myent.boff, e);
+    const uint32_t kind = __shfl_sync(0xffffffffu, myent.kind, e);
+    const uint32_t ncols = __shfl_sync(0xffffffffu, myent.ncols, e);
+    if (kind == 0) {
+      const float* A = reinterpret_cast<const float*>(slot + boff) + rr;
+#pragma unroll 4
+      for (uint32_t j = 0; j < ncols; ++j) {
+        float u[S];
+#pragma unroll
+        for (int k = 0; k < S; ++k) u[k] = ok[k] ? A[j * nr + 16 * k] : 0.f;
+        const float* xrow = side + j * P;
+#pragma unroll
+        for (int q = 0; q < H / 4 + (H % 4 ? 1 : 0); ++q) {
+          float x[4];
+          if (H >= 4) {
+            const float4 v = *reinterpret_cast<const float4*>(xrow + 4 * q);
+            x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+          } else {
+            const float2 v = *reinterpret_cast<const float2*>(xrow);
+            x[0] = v.x; x[1] = v.y; x[2] = 0.f; x[3] = 0.f;
+          }
+#pragma unroll
+          for (int c = 0; c < 4 && 4 * q + c < H; ++c)
+#pragma unroll
+            for (int k = 0; k < S; ++k) a[k][4 * q + c] = fmaf(u[k], x[c], a[k][4 * q + c]);
+        }
+      }
+    } else {
+      const SL* Uc = reinterpret_cast<const SL*>(slot + boff) + rr;
+#pragma unroll 4
+      for (uint32_t l = 0; l < ncols; ++l) {
+        float u[S];
+#pragma unroll
+        for (int k = 0; k < S; ++k) u[k] = ok[k] ? cvt<SL>(Uc[l * nr + 16 * k]) : 0.f;
+        const float* trow = side + l * P;
+#pragma unroll
+        for (int q = 0; q < H / 4 + (H % 4 ? 1 : 0); ++q) {
+          float x[4];
+          if (H >= 4) {
+            const float4 v = *reinterpret_cast<const float4*>(trow + 4 * q);
+            x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+          } else {
+            const float2 v = *reinterpret_cast<const float2*>(trow);
+            x[0] = v.x; x[1] = v.y; x[2] = 0.f; x[3] = 0.f;
+          }
+#pragma unroll
+          for (int c = 0; c < 4 && 4 * q + c < H; ++c)
+#pragma unroll
+            for (int k = 0; k < S; ++k) a[k][4 * q + c] = fmaf(u[k], x[c], a[k][4 * q + c]);
+        }
+      }
+    }
+    side += ncols * P;
+  }
+#pragma unroll
+  for (int k = 0; k < S; ++k) {
+    if (!ok[k]) continue;
+    float* y = yr + (uint64_t)(U.row0 + rr + 16 * k) * P + rq * H;
+    if (H >= 4) {
+#pragma unroll
+      for (int q = 0; q < H / 4; ++q) red4(y + 4 * q, a[k][4 * q], a[k][4 * q + 1], a[k][4 * q + 2], a[k][4 * q + 3]);
+    } else {
+      atomicAdd(y, a[k][0]);
+      atomicAdd(y + 1, a[k][1]);
+    }
   }
 }
 
@@ -288,45 +357,11 @@ __global__ void __launch_bounds__(kThreads, 1) rows_sweep_kernel(MvPlan pl) {
         }
       },
       [&](const RDesc& D, const unsigned char* slot, uint32_t lane) {
-        const uint32_t nr = D.u.nrows;
-        const bool ok0 = lane < nr, ok1 = lane + 32 < nr;
-        float a0[P], a1[P];
-#pragma unroll
-        for (int r = 0; r < P; ++r) a0[r] = a1[r] = 0.f;
-        const float* side = reinterpret_cast<const float*>(slot + kSlotBytes);
-        for (uint32_t e = 0; e < D.u.ne; ++e) {
-          const uint32_t boff = __shfl_sync(0xffffffffu, D.e.boff, e);
-          const uint32_t kind = __shfl_sync(0xffffffffu, D.e.kind, e);
-          const uint32_t ncols = __shfl_sync(0xffffffffu, D.e.ncols, e);
-          if (kind == 0) {
-            const float* A = reinterpret_cast<const float*>(slot + boff);
-#pragma unroll 4
-            for (uint32_t j = 0; j < ncols; ++j) {
-              const float u0v = ok0 ? A[j * nr + lane] : 0.f;
-              const float u1v = ok1 ? A[j * nr + lane + 32] : 0.f;
-              fma_row<P>(a0, a1, u0v, u1v, side + j * P);
-            }
-          } else {
-            const SL* Uc = reinterpret_cast<const SL*>(slot + boff);
-#pragma unroll 4
-            for (uint32_t l = 0; l < ncols; ++l) {
-              const float u0v = ok0 ? cvt<SL>(Uc[l * nr + lane]) : 0.f;
-              const float u1v = ok1 ? cvt<SL>(Uc[l * nr + lane + 32]) : 0.f;
-              fma_row<P>(a0, a1, u0v, u1v, side + l * P);
-            }
-          }
-          side += ncols * P;
-        }
-        if (ok0) {
-          float* y = pl.yr + (uint64_t)(D.u.row0 + lane) * P;
-#pragma unroll
-          for (int q = 0; q < P / 4; ++q) red4(y + 4 * q, a0[4 * q], a0[4 * q + 1], a0[4 * q + 2], a0[4 * q + 3]);
-        }
-        if (ok1) {
-          float* y = pl.yr + (uint64_t)(D.u.row0 + lane + 32) * P;
-#pragma unroll
-          for (int q = 0; q < P / 4; ++q) red4(y + 4 * q, a1[4 * q], a1[4 * q + 1], a1[4 * q + 2], a1[4 * q + 3]);
-        }
+        const uint32_t S = (D.u.nrows + 15) / 16;
+        if (S <= 1) rows_unit<SL, P, 1>(D.u, D.e, slot, lane, pl.yr);
+        else if (S == 2) rows_unit<SL, P, 2>(D.u, D.e, slot, lane, pl.yr);
+        else if (S == 3) rows_unit<SL, P, 3>(D.u, D.e, slot, lane, pl.yr);
+        else rows_unit<SL, P, 4>(D.u, D.e, slot, lane, pl.yr);
       });
 }
 
