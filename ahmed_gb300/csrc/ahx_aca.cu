@@ -69,12 +69,12 @@ __device__ bool row_step(const Grp& g, const Blk& B, uint32_t& klast, uint32_t& 
     const double xi = B.P.x[gi], yi = B.P.y[gi], zi = B.P.z[gi];
     am = ArgMax{0.0, 0xffffffffu, 0.0};
     for (uint32_t j = g.rank; j < n2; j += G) {
-      double v = lap_entry(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
+      double v = lap_entry_aca(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
       for (uint32_t l = 0; l < k; ++l) v = fma(-B.U[(size_t)l * n1 + i0], B.V[(size_t)l * n2 + j], v);
       pv[j] = v;
       if (B.S[j] >= 0) {
         const double a = fabs(v);
-        if (a > am.v) am = ArgMax{a, j, v};
+        if (gt_nonneg(a, am.v)) am = ArgMax{a, j, v};
       }
     }
     am = g.argmax(am);
@@ -94,13 +94,13 @@ __device__ bool row_step(const Grp& g, const Blk& B, uint32_t& klast, uint32_t& 
       const double e = pv[j] * sca;
       pv[j] = e;
       nrmv2 += e * e;
-      if (fabs(e) > thr) ++B.S[j];
+      if (gt_nonneg(fabs(e), thr)) ++B.S[j];
     }
   }
   const uint32_t gj = B.b2 + j0;
   const double xj = B.P.x[gj], yj = B.P.y[gj], zj = B.P.z[gj];
   for (uint32_t i = g.rank; i < n1; i += G) {
-    double u = lap_entry(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
+    double u = lap_entry_aca(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
     for (uint32_t l = 0; l < k; ++l) u = fma(-B.V[(size_t)l * n2 + j0], B.U[(size_t)l * n1 + i], u);
     pu[i] = u;
   }
@@ -115,9 +115,9 @@ __device__ bool row_step(const Grp& g, const Blk& B, uint32_t& klast, uint32_t& 
     const double e = pu[i] * dsca;
     pu[i] = e;
     const double ea = fabs(e);
-    if (B.Z[i] >= 0 && ea > thr) ++B.Z[i];
+    if (B.Z[i] >= 0 && gt_nonneg(ea, thr)) ++B.Z[i];
     nrmu2 += ea * ea;
-    if (B.Z[i] >= 0 && ea > nm.v) nm = ArgMax{ea, i, e};
+    if (B.Z[i] >= 0 && gt_nonneg(ea, nm.v)) nm = ArgMax{ea, i, e};
   }
   g.sum2(nrmu2, nrmv2);
   nm = g.argmax(nm);
@@ -140,12 +140,12 @@ __device__ bool col_step(const Grp& g, const Blk& B, uint32_t& j0, uint32_t k, u
     const double xj = B.P.x[gj], yj = B.P.y[gj], zj = B.P.z[gj];
     am = ArgMax{0.0, 0xffffffffu, 0.0};
     for (uint32_t i = g.rank; i < n1; i += G) {
-      double u = lap_entry(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
+      double u = lap_entry_aca(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
       for (uint32_t l = 0; l < k; ++l) u = fma(-B.V[(size_t)l * n2 + j0], B.U[(size_t)l * n1 + i], u);
       pu[i] = u;
       if (B.Z[i] >= 0) {
         const double a = fabs(u);
-        if (a > am.v) am = ArgMax{a, i, u};
+        if (gt_nonneg(a, am.v)) am = ArgMax{a, i, u};
       }
     }
     am = g.argmax(am);
@@ -165,13 +165,13 @@ __device__ bool col_step(const Grp& g, const Blk& B, uint32_t& j0, uint32_t k, u
       const double e = pu[i] * sca;
       pu[i] = e;
       nrmu2 += e * e;
-      if (fabs(e) > thr) ++B.Z[i];
+      if (gt_nonneg(fabs(e), thr)) ++B.Z[i];
     }
   }
   const uint32_t gi = B.b1 + i0;
   const double xi = B.P.x[gi], yi = B.P.y[gi], zi = B.P.z[gi];
   for (uint32_t j = g.rank; j < n2; j += G) {
-    double v = lap_entry(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
+    double v = lap_entry_aca(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
     for (uint32_t l = 0; l < k; ++l) v = fma(-B.U[(size_t)l * n1 + i0], B.V[(size_t)l * n2 + j], v);
     pv[j] = v;
   }
@@ -185,9 +185,9 @@ __device__ bool col_step(const Grp& g, const Blk& B, uint32_t& j0, uint32_t k, u
     const double e = pv[j] * dsca;
     pv[j] = e;
     const double ea = fabs(e);
-    if (B.S[j] >= 0 && ea > thr) ++B.S[j];
+    if (B.S[j] >= 0 && gt_nonneg(ea, thr)) ++B.S[j];
     nrmv2 += ea * ea;
-    if (ea > nm.v) nm = ArgMax{ea, j, e};  // no S filter here, as in the reference
+    if (gt_nonneg(ea, nm.v)) nm = ArgMax{ea, j, e};  // no S filter here, as in the reference
   }
   g.sum2(nrmu2, nrmv2);
   nm = g.argmax(nm);
@@ -357,6 +357,70 @@ __device__ void group_apply_q(const Grp& g, uint32_t m, uint32_t kr, const doubl
   }
 }
 
+// One-sided Jacobi on the columns of R (m x n, m, n <= 16) by one warp, in
+// tournament order (Brent-Luk round robin): every round rotates n/2 disjoint
+// column pairs at once, one group of 4 lanes per pair, each lane holding rows
+// sub, sub + 4, sub + 8, sub + 12.  Rotations are accumulated in Vs (n x n).
+__device__ void jacobi_warp16(uint32_t m, uint32_t n, double* R, double* Vs, uint32_t ld) {
+  const uint32_t lane = threadIdx.x & 31, grp = lane >> 2, sub = lane & 3;
+  const uint32_t ne = n + (n & 1);  // a dummy column when n is odd
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    bool rotated = false;
+    for (uint32_t r = 0; r + 1 < ne; ++r) {
+      __syncwarp();
+      uint32_t a = 0, b = 0;
+      bool live = grp < ne / 2;
+      if (live) {
+        const uint32_t pa = grp, pb = ne - 1 - grp;
+        a = pa == 0 ? 0 : 1 + (pa - 1 + r) % (ne - 1);
+        b = pb == 0 ? 0 : 1 + (pb - 1 + r) % (ne - 1);
+        if (a > b) {
+          const uint32_t t = a;
+          a = b;
+          b = t;
+        }
+        live = b < n;
+      }
+      double al = 0.0, be = 0.0, ga = 0.0;
+      if (live) {
+        for (uint32_t i = sub; i < m; i += 4) {
+          const double x = R[i * ld + a], y = R[i * ld + b];
+          al = fma(x, x, al);
+          be = fma(y, y, be);
+          ga = fma(x, y, ga);
+        }
+      }
+#pragma unroll
+      for (int o = 1; o < 4; o <<= 1) {
+        al += __shfl_xor_sync(0xffffffffu, al, o);
+        be += __shfl_xor_sync(0xffffffffu, be, o);
+        ga += __shfl_xor_sync(0xffffffffu, ga, o);
+      }
+      // rotate unless |ga| <= 1e-15 sqrt(al be)  (tested without a square root)
+      const bool rot = live && ga != 0.0 && ga * ga > 1e-30 * (al * be);
+      if (rot) {
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
+        const double c = rsqrt(fma(t, t, 1.0));
+        const double s = c * t;
+        for (uint32_t i = sub; i < m; i += 4) {
+          const double x = R[i * ld + a], y = R[i * ld + b];
+          R[i * ld + a] = c * x - s * y;
+          R[i * ld + b] = s * x + c * y;
+        }
+        for (uint32_t i = sub; i < n; i += 4) {
+          const double x = Vs[i * ld + a], y = Vs[i * ld + b];
+          Vs[i * ld + a] = c * x - s * y;
+          Vs[i * ld + b] = s * x + c * y;
+        }
+      }
+      rotated |= rot;
+    }
+    if (!__any_sync(0xffffffffu, rotated)) break;
+  }
+  __syncwarp();
+}
+
 // addtrll (H/mblock_D.cpp:356-465) for a fresh low-rank block: recompress U V^T
 // of rank k to kt <= k columns (relative threshold delta, absolute 1e-64).
 // Results in Un (n1 x kt) and Vn (n2 x kt).
@@ -389,6 +453,10 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   for (uint32_t i = g.rank; i < nmin; i += G)
     for (uint32_t j = 0; j < nmin; ++j) Vs[i * ld + j] = (i == j) ? 1.0 : 0.0;
   // one-sided Jacobi on the columns of R (Hestenes), rotations accumulated in Vs
+  if (G == 32 && mmin <= 16 && nmin <= 16) {
+    g.sync();
+    jacobi_warp16(mmin, nmin, R, Vs, ld);
+  } else
   for (int sweep = 0; sweep < 40; ++sweep) {
     bool rotated = false;
     for (uint32_t p = 0; p + 1 < nmin; ++p) {
@@ -421,6 +489,7 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
     }
     if (!rotated) break;
   }
+  g.sync();
   for (uint32_t j = 0; j < nmin; ++j) {
     double s = 0.0;
     for (uint32_t i = g.rank; i < mmin; i += G) s += R[i * ld + j] * R[i * ld + j];

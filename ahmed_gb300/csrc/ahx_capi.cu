@@ -29,8 +29,9 @@ uint32_t aca_kcap_default() {
   if (e && *e) return std::max<uint32_t>(1u, (uint32_t)std::strtoul(e, nullptr, 10));
   return 48u;
 }
-// leaves with more rows or columns than this use the CTA-per-leaf kernel
-constexpr uint32_t kLargeLeaf = 256;
+// leaves with more rows or columns than this use the CTA-per-leaf kernel; the
+// rest run one warp per leaf (warp reductions; the FP64 pipe is the limit)
+constexpr uint32_t kLargeLeaf = 4096;
 
 template <class T>
 int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {

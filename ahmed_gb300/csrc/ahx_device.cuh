@@ -27,6 +27,25 @@ __device__ __forceinline__ double lap_entry(const PointsSoA& P, uint32_t i, uint
   return __ddiv_rn(1.0, __dmul_rn(kFourPi, __dsqrt_rn(r2)));
 }
 
+// The same kernel inside the ACA steps, evaluated as (1/(4 pi)) * rsqrt(r^2):
+// within an ulp of lap_entry and several times fewer FP64 instructions (the
+// FP64 pipe is what bounds the assembly on this GPU).  Dense leaves use
+// lap_entry.
+__device__ __forceinline__ double lap_entry_aca(const PointsSoA& P, uint32_t i, uint32_t j,
+                                                double xi, double yi, double zi, double diag) {
+  if (i == j) return diag;
+  const double dx = xi - P.x[j];
+  const double dy = yi - P.y[j];
+  const double dz = zi - P.z[j];
+  const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+  return (1.0 / kFourPi) * rsqrt(r2);
+}
+
+// a > b for non-negative doubles, on the integer pipe (IEEE order of the bit patterns)
+__device__ __forceinline__ bool gt_nonneg(double a, double b) {
+  return __double_as_longlong(a) > __double_as_longlong(b);
+}
+
 // ---------------------------------------------------------------------------
 // Cooperative groups of G threads working on one block.  G == 32: one warp
 // (several groups per CTA).  G > 32: the whole CTA.  All reductions are
@@ -41,7 +60,8 @@ struct ArgMax {
 };
 
 __device__ __forceinline__ void argmax_merge(ArgMax& a, const ArgMax& b) {
-  if (b.v > a.v || (b.v == a.v && b.idx < a.idx)) a = b;
+  const long long bv = __double_as_longlong(b.v), av = __double_as_longlong(a.v);
+  if (bv > av || (bv == av && b.idx < a.idx)) a = b;
 }
 
 struct ArgMinI {
