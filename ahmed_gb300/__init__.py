@@ -16,3 +16,4 @@ from .hmatrix import (  # noqa: F401
     mltaGeHVec,
 )
 from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA  # noqa: F401
+from .rank_predictor import RankPredictor, training_set  # noqa: F401

@@ -52,6 +52,18 @@ SIGNATURES = [
     ("ahx_batch_n", _u64, [_vp]),
     ("ahx_batch_matvec", _i32, [_vp, _dbl, _u32, _vp, _vp]),
     ("ahx_batch_gmres", _i32, [_vp, _vp, _vp, _dbl, _u32, _u32, _vp, _vp]),
+    ("ahx_assemble_hinted", _i32, [_vp, _dbl, _dbl, _u32, _vp]),
+    ("ahx_hmat_assembly_stats", _i32, [_vp, _vp]),
+    ("ahx_hmat_features", _i32, [_vp, _dbl, _dbl, _vp]),
+    ("ahx_mlp_nparams", _u32, []),
+    ("ahx_mlp_create", _i32, [_i32, _u64, _vp]),
+    ("ahx_mlp_destroy", _i32, [_vp]),
+    ("ahx_mlp_get_params", _i32, [_vp, _vp]),
+    ("ahx_mlp_set_params", _i32, [_vp, _vp]),
+    ("ahx_mlp_set_norm", _i32, [_vp, _vp, _vp]),
+    ("ahx_mlp_gradients", _i32, [_vp, _vp, _vp, _u32, _vp, _vp]),
+    ("ahx_mlp_train", _i32, [_vp, _vp, _vp, _u32, _u32, _u32, C.c_float, _u64, _vp]),
+    ("ahx_mlp_predict", _i32, [_vp, _vp, _u32, _vp]),
     ("ahx_aca_block_noalloc", _i32, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _u32, _dbl, _dbl,
                                      _u32, _vp, _vp, _vp, _vp]),
 ]

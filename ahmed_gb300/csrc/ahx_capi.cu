@@ -105,6 +105,8 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
       ++j;
     }
     i = j;
+    H->stat_ws_bytes = std::max<uint64_t>(H->stat_ws_bytes, wsd * sizeof(double) + zsi * sizeof(int));
+    H->stat_batches++;
     int rc = ws.reserve(std::max<uint64_t>(wsd, 1) * sizeof(double));
     if (rc) return rc;
     rc = zs.reserve(std::max<uint64_t>(zsi, 1) * sizeof(int));
@@ -139,8 +141,9 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
       const AcaResult& r = res[q];
       if (r.status == kAcaOverflow) {
         AcaTask u = t;
-        u.kcap = std::min(t.kmax, t.kcap * 4);
+        u.kcap = std::min(t.kmax, std::max(t.kcap * 4, 16u));
         retry.push_back(u);
+        H->stat_retries++;
         continue;
       }
       if (r.status != kAcaOk) {
@@ -500,6 +503,11 @@ int ahx_hmat_leaves(const ahx_hmat* H, uint32_t* out) {
 }
 
 int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax) {
+  return ahx_assemble_hinted(H, h, eps, rankmax, nullptr);
+}
+
+int ahx_assemble_hinted(ahx_hmat* H, double h, double eps, uint32_t rankmax,
+                        const float* rank_hint) {
   if (!H || !(h > 0.0) || !(eps > 0.0)) {
     set_error("ahx_assemble: invalid argument");
     return AHX_ERR_ARG;
@@ -516,6 +524,7 @@ int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax) {
   H->aca_rank.assign(nl, -1);
   H->off.assign(nl, 0);
   H->arena64_elems = 0;
+  H->stat_ws_bytes = H->stat_retries = H->stat_batches = 0;
   const double diag = 1.0 / (kFourPi * h);
   std::vector<AcaTask> tasks;
   std::vector<uint32_t> dense;
@@ -532,6 +541,11 @@ int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax) {
       t.i0 = L.i0;
       t.kmax = maxk;
       t.kcap = std::min(maxk, kcap0);
+      if (rank_hint && rank_hint[l] >= 0.f) {
+        // predicted rank plus a margin; an under-prediction only costs a retry
+        const float want = rank_hint[l] * 1.25f + 4.f;
+        t.kcap = std::min(maxk, std::max(8u, (uint32_t)std::ceil(want)));
+      }
       t.leaf = l;
       tasks.push_back(t);
     } else {
@@ -575,6 +589,21 @@ int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax) {
   }
   AHX_CUDA(cudaStreamSynchronize(H->stream));
   H->assembled = true;
+  return AHX_OK;
+}
+
+int ahx_hmat_assembly_stats(const ahx_hmat* H, uint64_t* out) {
+  if (!H || !out) return AHX_ERR_ARG;
+  out[0] = H->stat_ws_bytes;
+  out[1] = H->stat_retries;
+  out[2] = H->stat_batches;
+  return AHX_OK;
+}
+
+int ahx_hmat_features(const ahx_hmat* H, double wavenumber, double eps, float* out) {
+  if (!H || !out) return AHX_ERR_ARG;
+  for (size_t l = 0; l < H->tree.leaves.size(); ++l)
+    leaf_features(H->tree, H->tree.leaves[l], wavenumber, eps, out + 8 * l);
   return AHX_OK;
 }
 

@@ -77,6 +77,10 @@ struct ahx_hmat {
   // staging buffers for host vectors
   ahx::DevBuf stage_x, stage_y;
   ahx::DevBuf scratch;  // solver scratch
+  // statistics of the last assembly
+  uint64_t stat_ws_bytes = 0;   // largest ACA workspace batch (bytes)
+  uint64_t stat_retries = 0;    // leaves re-run with a larger rank capacity
+  uint64_t stat_batches = 0;    // workspace batches
 };
 
 namespace ahx {

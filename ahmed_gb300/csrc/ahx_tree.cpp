@@ -271,6 +271,31 @@ void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin,
   B.subdivide(root, root);
 }
 
+void leaf_features(const Tree& T, const Leaf& L, double wavenumber, double eps, float out[8]) {
+  const ClusterNode& a = T.nodes[L.row_cl];
+  const ClusterNode& b = T.nodes[L.col_cl];
+  double ca[3], cb[3];
+  for (int j = 0; j < 3; ++j) {
+    ca[j] = T.kind == kTreePca ? a.com[j] : 0.5 * (a.xmm[j] + a.xmm[j + 3]);
+    cb[j] = T.kind == kTreePca ? b.com[j] : 0.5 * (b.xmm[j] + b.xmm[j + 3]);
+  }
+  const double dist = std::sqrt((ca[0] - cb[0]) * (ca[0] - cb[0]) + (ca[1] - cb[1]) * (ca[1] - cb[1]) +
+                                (ca[2] - cb[2]) * (ca[2] - cb[2]));
+  const double da = std::sqrt(a.diam2), db = std::sqrt(b.diam2);
+  // a block on the diagonal has distance 0: floor it at 1e-6 of the larger
+  // diameter so that every feature stays finite
+  const double tiny = 1e-300;
+  const double dfl = std::max(dist, std::max(1e-6 * std::max(da, db), tiny));
+  out[0] = (float)std::log(std::max(da, tiny));
+  out[1] = (float)std::log(std::max(db, tiny));
+  out[2] = (float)std::log(dfl);
+  out[3] = (float)(std::min(da, db) / dfl);
+  out[4] = (float)std::log((double)L.n1);
+  out[5] = (float)std::log((double)L.n2);
+  out[6] = (float)(wavenumber * std::max(da, db));
+  out[7] = (float)(-std::log10(eps));
+}
+
 double mean_nn(const double* pts, uint32_t n) {
   if (n < 2) return 0.0;
   double lo[3], hi[3];

@@ -53,4 +53,11 @@ void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin,
 // Mean nearest-neighbour distance (exact; uniform-grid search; deterministic sum order).
 double mean_nn(const double* pts, uint32_t n);
 
+// Geometric features of a leaf for the rank predictor (8 floats):
+//   log diam(row cluster), log diam(col cluster), log centre distance,
+//   min(diam) / distance, log n1, log n2, wavenumber * max(diam), -log10(eps)
+// diam = sqrt(diam2) of the cluster (Include/cluster.h:194); centres are the
+// PCA centres of mass or the bounding-box centres.
+void leaf_features(const Tree& T, const Leaf& L, double wavenumber, double eps, float out[8]);
+
 }  // namespace ahx

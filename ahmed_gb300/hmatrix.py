@@ -125,6 +125,26 @@ class HMatrix:
 
     assemble = matgenGeH_omp
 
+    def assemble_hinted(self, h, eps, rank_hint, rankmax=2**32 - 1):
+        """Assembly whose ACA workspace is sized by per-leaf rank hints (negative: none)."""
+        self.h = float(h)
+        self.eps = float(eps)
+        hint = np.ascontiguousarray(rank_hint, dtype=np.float32)
+        check(lib().ahx_assemble_hinted(self._h, self.h, self.eps, min(int(rankmax), 2**32 - 1),
+                                        ptr(hint)))
+        return self
+
+    def assembly_stats(self):
+        """(largest workspace batch in bytes, capacity retries, batches) of the last assembly."""
+        out = np.zeros(3, np.uint64)
+        check(lib().ahx_hmat_assembly_stats(self._h, ptr(out)))
+        return tuple(int(v) for v in out)
+
+    def features(self, eps, wavenumber=0.0):
+        out = np.zeros((self.nleaves, 8), np.float32)
+        check(lib().ahx_hmat_features(self._h, float(wavenumber), float(eps), ptr(out)))
+        return out
+
     def ranks(self):
         out = np.zeros(self.nleaves, np.int32)
         check(lib().ahx_hmat_ranks(self._h, ptr(out)))

@@ -71,6 +71,19 @@ int ahx_hmat_leaves(const ahx_hmat* H, uint32_t* out);
  *   apprx_unsym / ::ACA / mblock::cpyLrM_cmpr           Include/apprx.h:136-172
  * The assembled leaves live on the device in FP64. */
 int ahx_assemble(ahx_hmat* H, double h, double eps, uint32_t rankmax);
+/* Assembly with a rank hint per leaf (e.g. from the learned predictor below;
+ * NULL or a negative entry: no hint).  The hint only sizes each leaf's ACA
+ * workspace and orders the work; ACA with its own stopping rule decides every
+ * rank, so the result is the same as ahx_assemble's. */
+int ahx_assemble_hinted(ahx_hmat* H, double h, double eps, uint32_t rankmax,
+                        const float* rank_hint);
+/* {largest ACA workspace batch in bytes, leaves re-run with a larger rank
+ * capacity, workspace batches} of the last assembly */
+int ahx_hmat_assembly_stats(const ahx_hmat* H, uint64_t* out3);
+/* 8 geometric features per leaf (DFS order) for the rank predictor:
+ * log diam1, log diam2, log centre distance, min diam / distance, log n1,
+ * log n2, wavenumber * max diam, -log10(eps) (diam: Include/cluster.h:194) */
+int ahx_hmat_features(const ahx_hmat* H, double wavenumber, double eps, float* out);
 /* per leaf: rank after recompression, -1 for dense leaves (mblock::isLrM/rank) */
 int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks);
 /* per leaf: ACA rank before recompression, -1 for dense */
@@ -127,6 +140,24 @@ int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double
  * refinement around the batch's storage precision; iters/resid per instance. */
 int ahx_batch_gmres(ahx_batch* b, const double* B, double* X, double tol, uint32_t m,
                     uint32_t maxit, uint32_t* iters, double* resid);
+
+/* Learned ACA-rank predictor: an 8 -> 64 -> 64 -> 1 ReLU network trained on
+ * the GPU by the library's own forward / backward / Adam kernels; the target
+ * is log(1 + ACA rank).  New component of this library (the reference sizes
+ * every ACA by its maxk, Include/apprx.h:143). */
+typedef struct ahx_mlp ahx_mlp;
+uint32_t ahx_mlp_nparams(void);
+int ahx_mlp_create(int device, uint64_t seed, ahx_mlp** out);
+int ahx_mlp_destroy(ahx_mlp* M);
+int ahx_mlp_get_params(const ahx_mlp* M, float* out);
+int ahx_mlp_set_params(ahx_mlp* M, const float* in);
+int ahx_mlp_set_norm(ahx_mlp* M, const float* mean8, const float* std8);
+/* gradient of the mean squared error over n samples (host X n x 8, Y n) */
+int ahx_mlp_gradients(ahx_mlp* M, const float* X, const float* Y, uint32_t n, float* grad,
+                      float* loss);
+int ahx_mlp_train(ahx_mlp* M, const float* X, const float* Y, uint32_t n, uint32_t epochs,
+                  uint32_t batch, float lr, uint64_t seed, float* loss_per_epoch);
+int ahx_mlp_predict(ahx_mlp* M, const float* X, uint32_t n, float* out);
 
 /* ACA + recompression of ONE admissible block without allocating device
  * memory.  This entry point has no counterpart in the reference.  It is for

@@ -1,0 +1,259 @@
+// ahx_ahmed.hpp -- the reference's C++ entry points for the H-matrix hot path,
+// implemented over the C ABI of libahx (include/ahx.h).
+//
+// A program written against AHMED's hot path
+//
+//   bemcluster<dof>* cl = new bemcluster<dof>(dofs, op_perm, 0, N);   // Include/bemcluster.h:25
+//   cl->createClusterTree(bmin, op_perm, po_perm);                     // Include/cluster_pca.h:204
+//   bemblcluster<dof,dof>* bl = new bemblcluster<dof,dof>(0, 0, N, N); // Include/bemblcluster.h:23
+//   bl->subdivide(cl, cl, eta * eta, nblcks);                          // Include/blcluster.h:382
+//   mblock<double>** A; allocmbls(bl, A);                              // Include/H.h:28
+//   matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);                // Include/matgen_omp.h:197
+//   mltaGeHVec(1.0, bl, A, x, y);                                      // H/mltaGeHVec.cpp:567
+//   GMRes(Op, b, x, eps, m, nsteps);                                   // solvers/GMRES.cpp:80
+//   freembls(bl, A);                                                   // Include/H.h:42
+//
+// compiles against this header by replacing the AHMED includes with it and
+// `using namespace ahx_ahmed;`.  The clusters, the block-cluster tree and the
+// leaves live in one libahx handle (trees on the host, bit-identical to the
+// reference's; leaves on the GPU).  mblock<T> objects are host views that
+// copy a leaf back from the device when their data is asked for.
+// MATGEN_T: the GPU generator is the Laplace collocation kernel; the
+// generator object passes h (diagonal 1/(4 pi h)) through `geth()`.
+#ifndef AHX_AHMED_HPP
+#define AHX_AHMED_HPP
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ahx.h"
+
+namespace ahx_ahmed {
+
+inline void check(int rc) {
+  if (rc != AHX_OK && rc != AHX_NOT_CONVERGED)
+    throw std::runtime_error(std::string("ahx: ") + ahx_last_error());
+}
+
+// Geometry shared by the clusters and the block-cluster tree of one matrix.
+struct Geometry {
+  std::vector<double> pts;  // original order, xyz
+  int kind = AHX_TREE_PCA;
+  unsigned bmin = 0;
+  unsigned* op_perm = nullptr;
+  unsigned* po_perm = nullptr;
+};
+
+// cluster tree root (the reference's bemcluster / cluster3d_bbx)
+template <class DOF, int KIND>
+class cluster_root {
+ public:
+  cluster_root(DOF* dofs, unsigned* op_perm, unsigned k, unsigned l) : geo_(new Geometry) {
+    if (k != 0) throw std::invalid_argument("ahx_ahmed: only root clusters (k = 0) are built");
+    geo_->kind = KIND;
+    geo_->pts.resize(3 * (size_t)l);
+    for (unsigned i = 0; i < l; ++i)
+      for (unsigned j = 0; j < 3; ++j) geo_->pts[3 * (size_t)i + j] = dofs[i].getcenter(j);
+    geo_->op_perm = op_perm;
+    n_ = l;
+  }
+  // Include/cluster_pca.h:204 / Include/cluster_bbx.h:100: the permutation is
+  // written when the block-cluster tree is built (the tree needs eta as well).
+  void createClusterTree(unsigned bmin, unsigned* op_perm, unsigned* po_perm) {
+    geo_->bmin = bmin;
+    geo_->op_perm = op_perm;
+    geo_->po_perm = po_perm;
+  }
+  unsigned size() const { return n_; }
+  std::shared_ptr<Geometry> geometry() const { return geo_; }
+
+ private:
+  std::shared_ptr<Geometry> geo_;
+  unsigned n_ = 0;
+};
+
+template <class DOF>
+using bemcluster = cluster_root<DOF, AHX_TREE_PCA>;
+template <class DOF>
+using cluster3d_bbx = cluster_root<DOF, AHX_TREE_BBX>;
+
+// root of the block-cluster tree (the reference's bemblcluster / blcluster_geo)
+class blcluster {
+ public:
+  blcluster(unsigned i1, unsigned i2, unsigned m1, unsigned m2) : n_(m1) {
+    if (i1 != 0 || i2 != 0 || m1 != m2)
+      throw std::invalid_argument("ahx_ahmed: the root block must be (0, 0, N, N)");
+  }
+  ~blcluster() {
+    if (h_) ahx_hmat_destroy(h_);
+  }
+  blcluster(const blcluster&) = delete;
+  blcluster& operator=(const blcluster&) = delete;
+
+  // Include/blcluster.h:382: builds the trees and numbers the leaves in DFS order
+  template <class CL>
+  void subdivide(CL* cl1, CL* cl2, double eta2, unsigned& nblcks, unsigned maxdepth = 0) {
+    if (cl1 != cl2 || maxdepth != 0)
+      throw std::invalid_argument("ahx_ahmed: square trees over one cluster tree, maxdepth 0");
+    std::shared_ptr<Geometry> g = cl1->geometry();
+    check(ahx_hmat_create(g->pts.data(), n_, g->kind, g->bmin, eta2, 0, nullptr, &h_));
+    check(ahx_hmat_perm(h_, g->op_perm, g->po_perm));
+    nblcks = ahx_hmat_nleaves(h_);
+    leaves_.resize(7 * (size_t)nblcks);
+    check(ahx_hmat_leaves(h_, leaves_.data()));
+  }
+
+  unsigned long nleaves() const { return ahx_hmat_nleaves(h_); }
+  unsigned long nadmleaves() const {
+    unsigned long c = 0;
+    for (size_t l = 0; l < leaves_.size() / 7; ++l) c += leaves_[7 * l + 4];
+    return c;
+  }
+  unsigned getn1() const { return n_; }
+  unsigned getn2() const { return n_; }
+  ahx_hmat* handle() const { return h_; }
+  const uint32_t* leaf(unsigned l) const { return &leaves_[7 * (size_t)l]; }
+  // per-leaf ranks after an assembly (-1 dense)
+  void refresh_ranks() {
+    ranks_.resize(ahx_hmat_nleaves(h_));
+    check(ahx_hmat_ranks(h_, ranks_.data()));
+  }
+  int rank_of(unsigned l) const { return ranks_.at(l); }
+
+ private:
+  unsigned n_;
+  ahx_hmat* h_ = nullptr;
+  std::vector<uint32_t> leaves_;
+  std::vector<int32_t> ranks_;
+};
+
+template <class T1, class T2>
+using bemblcluster = blcluster;
+
+// Host view of one leaf (Include/mblock.h:29-97): U then V for a low-rank
+// block, n1 x n2 column-major for a dense one.
+template <class T>
+class mblock {
+ public:
+  mblock(const blcluster* bl, unsigned idx) : bl_(bl), idx_(idx) {}
+  unsigned getn1() const { return bl_->leaf(idx_)[1]; }
+  unsigned getn2() const { return bl_->leaf(idx_)[3]; }
+  bool isLrM() const { return bl_->rank_of(idx_) >= 0; }
+  bool isGeM() const { return !isLrM(); }
+  unsigned rank() const { return (unsigned)bl_->rank_of(idx_); }
+  T* getdata() {
+    if (data_.empty()) {
+      data_.resize(ahx_hmat_leaf_size(bl_->handle(), idx_));
+      if (!data_.empty()) check(ahx_hmat_get_leaf(bl_->handle(), idx_, data_.data()));
+    }
+    return data_.data();
+  }
+
+ private:
+  const blcluster* bl_;
+  unsigned idx_;
+  std::vector<T> data_;
+};
+
+template <class T>
+void allocmbls(blcluster* bl, mblock<T>**& A) {
+  const unsigned n = (unsigned)bl->nleaves();
+  A = new mblock<T>*[n];
+  for (unsigned i = 0; i < n; ++i) A[i] = nullptr;
+}
+
+template <class T>
+void freembls(blcluster* bl, mblock<T>**& A) {
+  if (!A) return;
+  const unsigned n = (unsigned)bl->nleaves();
+  for (unsigned i = 0; i < n; ++i) delete A[i];
+  delete[] A;
+  A = nullptr;
+}
+
+// Include/matgen_omp.h:197-213: ACA assembly of every leaf (on the GPU)
+template <class T, class MATGEN_T>
+void matgenGeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps, unsigned rankmax,
+                   mblock<T>** A) {
+  check(ahx_assemble(bl->handle(), MatGen.geth(), eps, rankmax));
+  bl->refresh_ranks();
+  for (unsigned i = 0; i < nblcks; ++i) {
+    delete A[i];
+    A[i] = new mblock<T>(bl, i);
+  }
+}
+
+// Include/matgen_sqntl.h:88-102 (recmpr = false)
+template <class T, class MATGEN_T>
+void matgenGeH_sqntl(MATGEN_T& MatGen, blcluster* root, blcluster* bl, bool recmpr, double eps,
+                     unsigned rankmax, mblock<T>** A) {
+  if (recmpr || root != bl) throw std::invalid_argument("ahx_ahmed: recmpr and sub-blocks not built");
+  matgenGeH_omp(MatGen, (unsigned)bl->nleaves(), bl, eps, rankmax, A);
+}
+
+// H/mltaGeHVec.cpp:567-577: y += d A x, Y += d A X (permuted ordering)
+inline bool mltaGeHVec(double d, blcluster* bl, mblock<double>**, double* x, double* y) {
+  check(ahx_matvec(bl->handle(), AHX_FP64, d, 1, x, bl->getn1(), y, bl->getn1()));
+  return true;
+}
+
+inline bool mltaGeHGeM(double d, blcluster* bl, mblock<double>**, unsigned p, double* X,
+                       unsigned ldX, double* Y, unsigned ldY) {
+  check(ahx_matvec(bl->handle(), AHX_FP64, d, p, X, ldX, Y, ldY));
+  return true;
+}
+
+// Include/matrix.h:20-32
+template <class T>
+struct Matrix {
+  unsigned m, n;
+  Matrix(unsigned n1, unsigned n2) : m(n1), n(n2) {}
+  Matrix() : m(0), n(0) {}
+  virtual void amux(T d, T* x, T* y) const = 0;
+  virtual void atmux(T d, T* x, T* y) const { amux(d, x, y); }
+  virtual void precond_apply(T*) const {}
+  virtual ~Matrix() {}
+};
+
+// The H-matrix as a Matrix<double>: GMRes/CG on it run on the GPU.
+struct HMatrixOperator : public Matrix<double> {
+  blcluster* bl;
+  explicit HMatrixOperator(blcluster* b) : Matrix<double>(b->getn1(), b->getn1()), bl(b) {}
+  void amux(double d, double* x, double* y) const override { mltaGeHVec(d, bl, nullptr, x, y); }
+};
+
+// solvers/GMRES.cpp:80: returns 0 converged, 1 not; eps and nsteps updated
+inline unsigned GMRes(const Matrix<double>& A, double* const b, double* const x, double& eps,
+                      const unsigned m, unsigned& nsteps) {
+  const HMatrixOperator* H = dynamic_cast<const HMatrixOperator*>(&A);
+  if (!H) throw std::invalid_argument("ahx_ahmed: GMRes runs on an HMatrixOperator");
+  uint32_t its = 0;
+  double res = 0.0;
+  const int rc = ahx_gmres(H->bl->handle(), AHX_FP64, 1, b, A.n, x, A.n, eps, m, nsteps, &its, &res);
+  check(rc);
+  eps = res;
+  nsteps = its;
+  return rc == AHX_OK ? 0u : 1u;
+}
+
+// solvers/CG.cpp:31
+inline unsigned CG(const Matrix<double>& A, double* const b, double* const x, double& eps,
+                   unsigned& nsteps) {
+  const HMatrixOperator* H = dynamic_cast<const HMatrixOperator*>(&A);
+  if (!H) throw std::invalid_argument("ahx_ahmed: CG runs on an HMatrixOperator");
+  uint32_t its = 0;
+  double res = 0.0;
+  const int rc = ahx_cg(H->bl->handle(), 1, b, A.n, x, A.n, eps, nsteps, &its, &res);
+  check(rc);
+  eps = res;
+  nsteps = its;
+  return rc == AHX_OK ? 0u : 1u;
+}
+
+}  // namespace ahx_ahmed
+
+#endif  // AHX_AHMED_HPP

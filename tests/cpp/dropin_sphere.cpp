@@ -1,0 +1,102 @@
+// The reference's hot-path call sequence (cluster tree, block-cluster tree,
+// allocmbls, matgenGeH_omp, mltaGeHVec, GMRes, freembls) compiled against
+// include/ahx_ahmed.hpp.  Checks the product against the dense matrix and
+// GMRES on the diagonal-2/(4 pi h) variant; exit status 0 on success.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "ahx_ahmed.hpp"
+
+using namespace ahx_ahmed;
+
+struct dof {
+  double c[3];
+  double getcenter(unsigned j) const { return c[j]; }
+  double getradius2() const { return 0.0; }
+};
+
+struct LaplaceGen {  // the MATGEN_T of this example: K = 1/(4 pi r), diagonal 1/(4 pi h)
+  double h;
+  double geth() const { return h; }
+};
+
+int main(int argc, char** argv) {
+  const unsigned N = argc > 1 ? (unsigned)atoi(argv[1]) : 2048;
+  const unsigned bmin = 32;
+  const double eta = 0.8, eps = 1e-6;
+  std::vector<dof> dofs(N);
+  for (unsigned i = 0; i < N; ++i) {  // Fibonacci sphere
+    const double z = 1.0 - 2.0 * (i + 0.5) / N, r = std::sqrt(1.0 - z * z);
+    const double th = i * (M_PI * (3.0 - std::sqrt(5.0)));
+    dofs[i].c[0] = r * std::cos(th);
+    dofs[i].c[1] = r * std::sin(th);
+    dofs[i].c[2] = z;
+  }
+  std::vector<double> pts(3 * (size_t)N);
+  for (unsigned i = 0; i < N; ++i)
+    for (int j = 0; j < 3; ++j) pts[3 * i + j] = dofs[i].c[j];
+  const double h = ahx_mean_nn(pts.data(), N);
+
+  std::vector<unsigned> op_perm(N), po_perm(N);
+  for (unsigned i = 0; i < N; ++i) op_perm[i] = po_perm[i] = i;
+  bemcluster<dof>* cl = new bemcluster<dof>(dofs.data(), op_perm.data(), 0, N);
+  cl->createClusterTree(bmin, op_perm.data(), po_perm.data());
+  unsigned nblcks = 0;
+  bemblcluster<dof, dof>* bl = new bemblcluster<dof, dof>(0, 0, N, N);
+  bl->subdivide(cl, cl, eta * eta, nblcks);
+  std::printf("leaves %u admissible %lu\n", nblcks, bl->nadmleaves());
+  if (argc > 2) {  // tree only (host): no device work
+    delete bl;
+    delete cl;
+    return 0;
+  }
+
+  mblock<double>** A;
+  allocmbls(bl, A);
+  LaplaceGen gen{h};
+  matgenGeH_omp(gen, nblcks, bl, eps, 1000000, A);
+  unsigned lowrank = 0;
+  for (unsigned l = 0; l < nblcks; ++l) lowrank += A[l]->isLrM();
+
+  std::vector<double> x(N), y(N, 0.0);
+  srand(1);
+  for (unsigned i = 0; i < N; ++i) x[i] = 2.0 * rand() / RAND_MAX - 1.0;
+  mltaGeHVec(1.0, bl, A, x.data(), y.data());
+  double num = 0.0, den = 0.0;
+  for (unsigned i = 0; i < N; ++i) {  // dense product in the permuted ordering
+    const dof& a = dofs[op_perm[i]];
+    double s = 0.0;
+    for (unsigned j = 0; j < N; ++j) {
+      const dof& b = dofs[op_perm[j]];
+      const double dx = a.c[0] - b.c[0], dy = a.c[1] - b.c[1], dz = a.c[2] - b.c[2];
+      const double r = i == j ? h : std::sqrt(dx * dx + dy * dy + dz * dz);
+      s += x[j] / (4.0 * M_PI * r);
+    }
+    num += (y[i] - s) * (y[i] - s);
+    den += s * s;
+  }
+  const double err = std::sqrt(num / den);
+  std::printf("low-rank leaves %u, product error vs dense %.3e\n", lowrank, err);
+  freembls(bl, A);
+  delete bl;
+
+  // GMRES on the SPD variant (diagonal 2/(4 pi h))
+  bemblcluster<dof, dof>* bl2 = new bemblcluster<dof, dof>(0, 0, N, N);
+  bl2->subdivide(cl, cl, eta * eta, nblcks);
+  allocmbls(bl2, A);
+  LaplaceGen gen2{h / 2.0};
+  matgenGeH_omp(gen2, nblcks, bl2, eps, 1000000, A);
+  HMatrixOperator op(bl2);
+  std::vector<double> b(N), sol(N, 0.0);
+  for (unsigned i = 0; i < N; ++i) b[i] = std::sin(0.37 * i);
+  double geps = 1e-8;
+  unsigned nsteps = 300;
+  const unsigned ret = GMRes(op, b.data(), sol.data(), geps, 30, nsteps);
+  std::printf("GMRes ret %u eps %.3e steps %u\n", ret, geps, nsteps);
+  freembls(bl2, A);
+  delete bl2;
+  delete cl;
+  return (err < 2e-6 && ret == 0 && geps < 1e-8) ? 0 : 1;
+}
