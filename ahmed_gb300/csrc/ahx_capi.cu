@@ -280,73 +280,84 @@ int prepare_product(ahx_hmat* H, int prec) {
 
 int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,
                         const double* arena64, uint64_t n, int device, cudaStream_t s) {
-  StreamLayout L;
-  build_stream_layout(leaves, prec == kBF16FP32 ? 1 : 0, L);
+  const bool bf = prec == kBF16FP32;
+  const uint32_t pmax = bf ? 64u : 16u;
   int sms = 0;
   AHX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const uint32_t grid = (uint32_t)std::max(sms, 1);
-  std::vector<uint64_t> vb(L.vunits.size()), rb(L.units.size());
-  for (size_t i = 0; i < vb.size(); ++i) vb[i] = L.vunits[i].bytes;
-  for (size_t i = 0; i < rb.size(); ++i) rb[i] = L.units[i].bytes;
-  std::vector<uint32_t> vr, rr;
-  balance_ranges(vb, grid, vr);
-  balance_ranges(rb, grid, rr);
+  TcLayout L;
+  build_tc_layout(leaves, bf, pmax, grid * kTcGroups, L);
   int rc;
   if ((rc = pc.vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;
   if ((rc = pc.rstream.reserve(std::max<uint64_t>(L.rbytes, 16)))) return rc;
   if ((rc = upload(pc.vunits, L.vunits, s))) return rc;
-  if ((rc = upload(pc.units, L.units, s))) return rc;
-  if ((rc = upload(pc.ents, L.ents, s))) return rc;
-  if ((rc = upload(pc.vranges, vr, s))) return rc;
-  if ((rc = upload(pc.rranges, rr, s))) return rc;
+  if ((rc = upload(pc.runits, L.runits, s))) return rc;
+  if ((rc = upload(pc.sides, L.sides, s))) return rc;
+  if ((rc = upload(pc.vranges, L.vranges, s))) return rc;
+  if ((rc = upload(pc.rranges, L.rranges, s))) return rc;
   if ((rc = upload(pc.treduce, L.treduce, s))) return rc;
   pc.ntreduce = (uint32_t)L.treduce.size();
-  if ((rc = pc.xr.reserve(std::max<uint64_t>(n, 1) * 16 * sizeof(float)))) return rc;
-  if ((rc = pc.yr.reserve(std::max<uint64_t>(n, 1) * 16 * sizeof(float)))) return rc;
-  if ((rc = pc.t.reserve(std::max<uint64_t>(L.t_rows, 1) * 16 * sizeof(float)))) return rc;
+  // X / T rows carry 16 zero rows past the end (read as K padding)
+  const uint64_t xrows = std::max<uint64_t>(n, 1) + 16, trows = (uint64_t)L.t_rows + 16;
+  const uint64_t es = bf ? 2 : 4;
+  if ((rc = pc.xf.reserve(xrows * (pmax + 8) * 4))) return rc;
+  if (bf && (rc = pc.xb.reserve(xrows * (pmax + 8) * 2))) return rc;
+  if ((rc = pc.yr.reserve(std::max<uint64_t>(n, 1) * pmax * 4))) return rc;
+  if ((rc = pc.t.reserve(trows * (pmax + 8) * es))) return rc;
   if ((rc = pc.err.reserve(sizeof(int)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.xf.p, 0, xrows * (pmax + 8) * 4, s));
+  if (bf) AHX_CUDA(cudaMemsetAsync(pc.xb.p, 0, xrows * (pmax + 8) * 2, s));
+  AHX_CUDA(cudaMemsetAsync(pc.t.p, 0, trows * (pmax + 8) * es, s));
   AHX_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), s));
-  DevBuf cv;
-  if (!L.vcopies.empty()) {
-    if ((rc = upload(cv, L.vcopies, s))) return rc;
-    AHX_CUDA(launch_stream_copies(cv.as<StreamCopy>(), (uint32_t)L.vcopies.size(), arena64,
-                                  pc.vstream.as<unsigned char>(), s));
+  // fragment-ordered streams (padding stays zero)
+  AHX_CUDA(cudaMemsetAsync(pc.vstream.p, 0, std::max<uint64_t>(L.vbytes, 16), s));
+  AHX_CUDA(cudaMemsetAsync(pc.rstream.p, 0, std::max<uint64_t>(L.rbytes, 16), s));
+  DevBuf dt, dseg;
+  if ((rc = upload(dseg, L.segs, s))) return rc;
+  if (!L.vtasks.empty()) {
+    if ((rc = upload(dt, L.vtasks, s))) return rc;
+    AHX_CUDA(launch_tc_build(dt.as<TcFragTask>(), (uint32_t)L.vtasks.size(), dseg.as<TcSeg>(), arena64,
+                             pc.vstream.as<unsigned char>(), s));
     AHX_CUDA(cudaStreamSynchronize(s));
   }
-  if (!L.rcopies.empty()) {
-    if ((rc = upload(cv, L.rcopies, s))) return rc;
-    AHX_CUDA(launch_stream_copies(cv.as<StreamCopy>(), (uint32_t)L.rcopies.size(), arena64,
-                                  pc.rstream.as<unsigned char>(), s));
+  if (!L.rtasks.empty()) {
+    if ((rc = upload(dt, L.rtasks, s))) return rc;
+    AHX_CUDA(launch_tc_build(dt.as<TcFragTask>(), (uint32_t)L.rtasks.size(), dseg.as<TcSeg>(), arena64,
+                             pc.rstream.as<unsigned char>(), s));
   }
   AHX_CUDA(cudaStreamSynchronize(s));
-  cv.release();
+  dt.release();
+  dseg.release();
   pc.nvunits = (uint32_t)L.vunits.size();
-  pc.nunits = (uint32_t)L.units.size();
+  pc.nrunits = (uint32_t)L.runits.size();
   pc.grid = grid;
   pc.t_rows = L.t_rows;
+  pc.pmax = pmax;
   pc.bytes = L.payload_bytes;
   return AHX_OK;
 }
 
-MvPlan mixed_plan(const ProdCopy& pc, uint64_t n) {
-  MvPlan pl;
-  pl.vunits = pc.vunits.as<StreamVUnit>();
-  pl.nvunits = pc.nvunits;
-  pl.units = pc.units.as<StreamUnit>();
-  pl.nunits = pc.nunits;
-  pl.ents = pc.ents.as<StreamEnt>();
+TcPlan mixed_plan(const ProdCopy& pc, uint64_t n) {
+  TcPlan pl;
+  pl.vunits = pc.vunits.as<TcVUnit>();
+  pl.runits = pc.runits.as<TcRowUnit>();
+  pl.sides = pc.sides.as<TcSide>();
+  pl.treduce = pc.treduce.as<TcTReduce>();
   pl.vranges = pc.vranges.as<uint32_t>();
   pl.rranges = pc.rranges.as<uint32_t>();
-  pl.treduce = pc.treduce.as<TReduce>();
+  pl.nvunits = pc.nvunits;
+  pl.nrunits = pc.nrunits;
   pl.ntreduce = pc.ntreduce;
   pl.grid = pc.grid;
   pl.vstream = pc.vstream.as<unsigned char>();
   pl.rstream = pc.rstream.as<unsigned char>();
   pl.n = n;
-  pl.xr = pc.xr.as<float>();
+  pl.xb = pc.xb.p;
+  pl.xf = pc.xf.as<float>();
+  pl.t = pc.t.p;
   pl.yr = pc.yr.as<float>();
-  pl.t = pc.t.as<float>();
   pl.err = pc.err.as<int>();
+  pl.pmax = pc.pmax;
   return pl;
 }
 
@@ -369,8 +380,8 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   if (rc) return rc;
   ProdCopy& pc = H->prod[prec];
   if (prec != kFP64) {
-    const MvPlan pl = mixed_plan(pc, H->tree.n);
-    AHX_CUDA(launch_matvec_mixed(prec, pl, d, p, X, ldX, Y, ldY, H->stream));
+    const TcPlan pl = mixed_plan(pc, H->tree.n);
+    AHX_CUDA(launch_matvec_tc(prec, pl, d, p, X, ldX, Y, ldY, H->stream));
     return AHX_OK;
   }
   MvArgs a;

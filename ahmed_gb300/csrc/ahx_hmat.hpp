@@ -38,23 +38,23 @@ struct ProdCopy {
   DevBuf leaves, order;    // FP64 product: MvLeaf[nleaves], uint32 launch order
   uint32_t nleaves = 0;
   uint64_t bytes = 0;      // stored leaf bytes of this precision
-  // mixed-precision streams (FP32 / BF16 products)
-  DevBuf vstream, rstream, vunits, units, ents, vranges, rranges, xr, yr, t, err, treduce;
-  uint32_t nvunits = 0, nunits = 0, grid = 0, t_rows = 0, ntreduce = 0;
+  // mixed-precision fragment streams (FP32 / BF16 products, tensor cores)
+  DevBuf vstream, rstream, vunits, runits, sides, vranges, rranges, treduce, xb, xf, yr, t, err;
+  uint32_t nvunits = 0, nrunits = 0, grid = 0, t_rows = 0, ntreduce = 0, pmax = 16;
   void release_all() {
-    for (DevBuf* b : {&lr, &dn, &leaves, &order, &vstream, &rstream, &vunits, &units, &ents,
-                      &vranges, &rranges, &xr, &yr, &t, &err, &treduce})
+    for (DevBuf* b : {&lr, &dn, &leaves, &order, &vstream, &rstream, &vunits, &runits, &sides, &vranges,
+                      &rranges, &treduce, &xb, &xf, &yr, &t, &err})
       b->release();
     valid = false;
     bytes = 0;
-    nleaves = nvunits = nunits = grid = t_rows = ntreduce = 0;
+    nleaves = nvunits = nrunits = grid = t_rows = ntreduce = 0;
   }
 };
 
 // Builds the streams of a mixed precision from FP64 leaves (offsets into arena64).
 int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,
                         const double* arena64, uint64_t n, int device, cudaStream_t s);
-MvPlan mixed_plan(const ProdCopy& pc, uint64_t n);
+TcPlan mixed_plan(const ProdCopy& pc, uint64_t n);
 // Reports (and clears) a timeout raised by a streaming kernel.
 int check_stream_error(ProdCopy& pc, cudaStream_t s);
 

@@ -40,62 +40,6 @@ struct MvArgs {
 
 cudaError_t launch_matvec(int prec, const MvArgs& a, cudaStream_t s);
 
-// ---------------------------------------------------------------------------
-// Mixed-precision product (FP32 or BF16 low-rank factors, FP32 dense leaves,
-// FP32 accumulation) as two linear sweeps over a re-laid-out arena.
-//
-// The product copy stores the leaves in processing order:
-//   V stream:    chunks of <= 256 rows x <= kVRank columns of the V factors
-//   rows stream: for every 64-row tile of every row cluster, the tile's rows of
-//                every leaf of that block row (dense columns or U columns)
-// so every work unit is one contiguous, 16-byte aligned byte range.  A producer
-// warp per CTA moves units into a shared-memory ring with cp.async.bulk
-// (mbarrier completion); consumer warps compute from shared memory.
-//   1. X (FP64, column-major) -> Xr (FP32, row-major n x P),  Yr = 0
-//   2. V sweep:    T = V^T Xr per chunk (partial T rows, no atomics)
-//   3. rows sweep: per unit, one warp accumulates the tile rows in registers
-//                  and adds them to Yr once (vector reductions)
-//   4. Y += d * Yr  (FP64)
-// for groups of P <= 16 right-hand sides.
-
-constexpr uint32_t kTileRows = 64;
-constexpr uint32_t kVRank = 16;           // columns of V per V unit
-constexpr uint32_t kSlotBytes = 12288;    // leaf bytes of one unit (at most)
-constexpr uint32_t kSideBytes = 6144;     // X / T rows staged with a unit (at most, P = 16)
-constexpr uint32_t kSideRows = kSideBytes / 64;
-
-struct StreamVUnit {
-  uint64_t src;    // byte offset in the V stream
-  uint32_t bytes;  // multiple of 16, <= kSlotBytes
-  uint32_t jn;     // rows (ld of the chunk)
-  uint32_t kn;     // columns
-  uint32_t xrow;   // first X row
-  uint32_t t_row;  // T row of the chunk's first column
-  uint32_t pad;
-};
-
-struct StreamEnt {
-  uint32_t boff;   // byte offset of the chunk inside its unit
-  uint32_t kind;   // 0 dense (FP32 columns), 1 low rank (U columns, plan's low-rank type)
-  uint32_t ncols;  // columns in this chunk
-  uint32_t xrow;   // dense: X row of column 0; low rank: T row of column 0 (summed T)
-};
-
-// Low-rank leaves whose V spans several V units: their partial T are summed
-// into the first chunk's rows between the two sweeps.
-struct TReduce {
-  uint32_t t_row, k, nchunk, pad;
-};
-
-struct StreamUnit {
-  uint64_t src;    // byte offset in the rows stream
-  uint32_t bytes;  // multiple of 16, <= kSlotBytes
-  uint32_t row0;   // first Y row
-  uint32_t nrows;  // <= kTileRows (ld of every chunk of the unit)
-  uint32_t e0, ne; // entries
-  uint32_t pad;
-};
-
 // Host description of one leaf for plan building: its data in the FP64 arena.
 struct PlanLeaf {
   uint32_t b1, n1, b2, n2;
@@ -103,55 +47,139 @@ struct PlanLeaf {
   uint64_t off;  // element offset in the FP64 arena (mblock layout)
 };
 
-// Gather-and-convert task building the streams from the FP64 arena.
-struct StreamCopy {
-  uint64_t src;      // FP64 element offset of the sub-block's (0,0)
-  uint64_t dst;      // byte offset in the destination stream
-  uint32_t src_ld;   // column stride in the FP64 arena
-  uint32_t nrows, ncols;
-  uint32_t dtype;    // 0 FP32, 1 BF16
+// ---------------------------------------------------------------------------
+// Tensor-core product (warp-level mma.sync) over fragment-ordered streams.
+//
+// Both sweeps are small GEMMs C[p][n] += sum_k A[p][k] B[k][n] with the
+// right-hand sides p as the M dimension (16 per m-tile) and the stored leaf
+// data as B:
+//   V sweep:    B[k][n] = V[j0 + k][l] of the low-rank leaves of one column
+//               cluster (columns n = the leaves' V columns, <= 64 per unit),
+//               A[p][k] = X[b2 + j0 + k][p]           -> C = T^T (T = V^T X)
+//   rows sweep: B[k][n] = U[r0 + n][l] (group 0, low rank) or D[r0 + n][j]
+//               (group 1, dense), rows n of one 64-row tile of a row cluster,
+//               A[p][k] = T[leaf row + l][p] or X[b2 + j][p] -> C = (A_tile X)^T
+// B is stored in the exact register order of the mma B fragments (one 8-byte
+// load per lane per fragment, k-block major, then n-tile), so every unit is
+// one contiguous, 16-byte aligned byte range moved by one bulk copy; A comes
+// from rows of X / T (stride P + 8 elements: conflict-free fragment loads)
+// staged beside it.
+//   FP32 storage:       TF32 mma with the 3-pass split (hi*hi + hi*lo + lo*hi),
+//                       FP32-level products
+//   BF16/FP32 storage:  low rank BF16 mma (T and X rows in BF16); dense leaves
+//                       in 4-byte words holding their TF32 rounding, one TF32
+//                       pass (the product is the one of FP32 words rounded at
+//                       load)
+#ifndef AHX_TC_SLOT
+#define AHX_TC_SLOT 11264
+#endif
+#ifndef AHX_TC_GROUPS
+#define AHX_TC_GROUPS 5
+#endif
+#ifndef AHX_TC_RING
+#define AHX_TC_RING 4
+#endif
+constexpr uint32_t kTcSlot = AHX_TC_SLOT;     // bytes of one ring slot
+constexpr uint32_t kTcHead = 32;              // the unit's descriptor, copied to the head of its slot
+constexpr uint32_t kTcSlotData = kTcSlot - kTcHead;  // B fragments + A rows of one unit
+constexpr uint32_t kTcGroups = AHX_TC_GROUPS;  // consumer groups per CTA (one ring each)
+constexpr uint32_t kTcRing = AHX_TC_RING;      // slots per group (split evenly between its unit sequences)
+
+struct TcRowUnit {
+  uint64_t src;       // byte offset in the rows stream
+  uint32_t bytes;     // fragment bytes (group 0, then group 1)
+  uint32_t row0;      // first Y row of the tile
+  uint32_t e0;        // first A-row entry
+  uint16_t ne, nr;    // entries (<= 32), rows of the tile (<= 64)
+  uint16_t kp0, kp1;  // K of group 0 / group 1, multiples of 8
+  uint32_t flags;     // bit 0: first unit of a tile run, bit 1: last unit
 };
 
-struct StreamLayout {
-  std::vector<StreamVUnit> vunits;
-  std::vector<StreamUnit> units;
-  std::vector<StreamEnt> ents;
-  std::vector<StreamCopy> vcopies, rcopies;
-  std::vector<TReduce> treduce;
+struct TcSide {
+  uint32_t src_row;  // first row in T (group 0) or in the X rows (group 1)
+  uint32_t nrows;
+  uint32_t dst_k;    // first k of the group
+  uint32_t group;
+};
+
+struct TcVUnit {
+  uint64_t src;     // byte offset in the V stream
+  uint32_t bytes;
+  uint32_t xrow;    // X row of k = 0
+  uint16_t kp;      // K (rows of V), multiple of 8
+  uint16_t ncols;   // columns n (<= 64)
+  uint32_t trow;    // T row of column 0 (final rows or a partial block)
+  uint32_t flags;   // bit 0: first unit of a piece, bit 1: last unit
+  uint32_t pad;
+};
+
+// T[dst + c] += sum_{q < nsrc} T[src + q * ncols + c], c < ncols
+struct TcTReduce {
+  uint32_t dst, src, ncols, nsrc;
+};
+
+// Fragment-ordering copy of one group of one unit from the FP64 arena:
+// segments s = seg0 .. seg0 + nseg - 1 each give `ncols` consecutive columns
+// starting at column `start`; mode 0: B[k][n] = a64[base + (k - start) * ld + n]
+// (k = start ..), mode 1: B[k][n] = a64[base + (n - start) * ld + k].
+struct TcFragTask {
+  uint64_t dst;
+  uint32_t dtype;  // 0 FP32, 1 BF16, 2 FP32 rounded to TF32 (dense leaves beside BF16 factors)
+  uint32_t kp, nt;
+  uint32_t kvalid, nvalid;
+  uint32_t seg0, nseg;
+  uint32_t mode;
+};
+
+struct TcSeg {
+  uint64_t base;
+  uint32_t ld, ncols, start, pad;
+};
+
+struct TcLayout {
+  std::vector<TcVUnit> vunits;
+  std::vector<TcRowUnit> runits;
+  std::vector<TcSide> sides;
+  std::vector<TcTReduce> treduce;
+  std::vector<TcFragTask> vtasks, rtasks;
+  std::vector<TcSeg> segs;
+  std::vector<uint32_t> vranges, rranges;  // per consumer group: first unit (nparts + 1 entries)
   uint64_t vbytes = 0, rbytes = 0;
-  uint32_t t_rows = 0;
-  uint64_t payload_bytes = 0;  // stored leaf bytes (without alignment padding)
+  uint32_t t_rows = 0;        // rows of T (final + partial blocks)
+  uint64_t payload_bytes = 0;  // stored leaf bytes without padding
 };
 
-// lr_dtype: 0 FP32 low-rank factors, 1 BF16
-void build_stream_layout(const std::vector<PlanLeaf>& leaves, int lr_dtype, StreamLayout& L);
+// lr_bf16: low-rank factors in BF16 (else FP32); pmax: right-hand sides the
+// units are sized for; nparts: consumer groups of one sweep launch
+// (grid * kTcGroups), each given a contiguous unit range
+void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t pmax, uint32_t nparts,
+                     TcLayout& L);
 
-struct MvPlan {
-  const StreamVUnit* vunits = nullptr;
-  uint32_t nvunits = 0;
-  const StreamUnit* units = nullptr;
-  uint32_t nunits = 0;
-  const StreamEnt* ents = nullptr;
-  const uint32_t* vranges = nullptr;  // per CTA: first V unit (grid + 1 entries)
-  const uint32_t* rranges = nullptr;  // per CTA: first rows unit (grid + 1 entries)
-  const TReduce* treduce = nullptr;
-  uint32_t ntreduce = 0;
-  uint32_t grid = 0;
+struct TcPlan {
+  const TcVUnit* vunits = nullptr;
+  const TcRowUnit* runits = nullptr;
+  const TcSide* sides = nullptr;
+  const TcTReduce* treduce = nullptr;
+  const uint32_t* vranges = nullptr;
+  const uint32_t* rranges = nullptr;
+  uint32_t nvunits = 0, nrunits = 0, ntreduce = 0, grid = 0;
   const unsigned char* vstream = nullptr;
   const unsigned char* rstream = nullptr;
   uint64_t n = 0;
-  float* xr = nullptr;  // n * 16
-  float* yr = nullptr;  // n * 16
-  float* t = nullptr;   // t_rows * 16
-  int* err = nullptr;   // set when a bounded wait gives up
+  void* xb = nullptr;   // X rows, BF16 (BF16 storage only)
+  float* xf = nullptr;  // X rows, FP32
+  void* t = nullptr;    // T rows (BF16 or FP32)
+  float* yr = nullptr;  // Y rows, FP32, n x P
+  int* err = nullptr;
+  uint32_t pmax = 16;
 };
 
-cudaError_t launch_stream_copies(const StreamCopy* copies, uint32_t n, const double* arena64,
-                                 unsigned char* dst, cudaStream_t s);
-cudaError_t launch_matvec_mixed(int prec, const MvPlan& plan, double d, uint32_t p,
-                                const double* X, uint64_t ldX, double* Y, uint64_t ldY,
-                                cudaStream_t s);
-// Per-CTA unit ranges balancing bytes over `grid` CTAs.
+cudaError_t launch_tc_build(const TcFragTask* tasks, uint32_t ntasks, const TcSeg* segs,
+                            const double* arena64, unsigned char* dst, cudaStream_t s);
+cudaError_t launch_matvec_tc(int prec, const TcPlan& plan, double d, uint32_t p, const double* X,
+                             uint64_t ldX, double* Y, uint64_t ldY, cudaStream_t s);
+
+// Contiguous unit ranges balancing bytes over `grid` parts (grid + 1 boundaries).
 void balance_ranges(const std::vector<uint64_t>& bytes, uint32_t grid, std::vector<uint32_t>& first);
 
 }  // namespace ahx

@@ -718,8 +718,8 @@ struct ahx_batch : ahx::Operator {
     using namespace ahx;
     Tab& T = tab[pr];
     if (pr != kFP64) {
-      const MvPlan pl = mixed_plan(T.plan, ntot);
-      AHX_CUDA(launch_matvec_mixed(pr, pl, d, p, X, ntot, Y, ntot, stream));
+      const TcPlan pl = mixed_plan(T.plan, ntot);
+      AHX_CUDA(launch_matvec_tc(pr, pl, d, p, X, ntot, Y, ntot, stream));
       return AHX_OK;
     }
     MvArgs a;

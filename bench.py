@@ -280,6 +280,114 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def _sample_rows_exact(P, perm, x, rows, h):
+    """Exact FP64 rows of A x (Laplace, permuted order) by direct summation on the host."""
+    Pp = P[perm]
+    out = np.zeros((len(rows), x.shape[0]))
+    for q, i in enumerate(rows):
+        d = Pp - Pp[i]
+        r = np.sqrt((d * d).sum(axis=1))
+        r[i] = 1.0
+        k = 1.0 / (4.0 * np.pi * r)
+        k[i] = 1.0 / (4.0 * np.pi * h)
+        out[q] = x @ k
+    return out
+
+
+def run_large(args):
+    """N = 1,048,576 uniform random points on the unit-cube surface (seed 4), leaf 64,
+    eta 0.8, ACA eps 1e-6; BF16 low-rank factors + FP32 dense leaves; 64 right-hand sides;
+    GMRES(50) to a 1e-8 FP64 residual (FP64 refinement) against the plain FP64 form."""
+    import torch
+    import ahmed_gb300 as A
+
+    n, p, bmin = args.n_large, 64, 64
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    P = A.geometry.cube_surface(n, 4)
+    t0 = time.perf_counter()
+    h = A.mean_nn(P) / args.diag_scale
+    H = A.HMatrix(P, "bbx", bmin=bmin, eta=ETA, device=0)
+    t_tree = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    H.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    H.matgenGeH_omp(h, EPS)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    ranks = H.ranks()
+    op, _ = H.perm()
+    out = {"workload": f"laplace-cube-{n}-64rhs", "n": n, "rhs": p, "leaf": bmin,
+           "diag": f"1/(4 pi h), h = mean nn / {args.diag_scale:g}",
+           "tree_s": t_tree, "assembly_s": t_asm, "leaves": int(H.nleaves),
+           "lowrank_leaves": int((ranks >= 0).sum()), "avg_rank": float(ranks[ranks >= 0].mean()),
+           "fp64_arena_bytes": int(H.storage_bytes("fp64"))}
+    # assembly error on sampled rows against the exact FP64 kernel sums
+    rng = np.random.default_rng(4)
+    x1 = rng.uniform(-1.0, 1.0, n)
+    y1 = torch.zeros(n, dtype=torch.float64, device=dev)
+    H.mltaGeHVec(1.0, torch.from_numpy(x1).to(dev), y1, precision="fp64")
+    rows = rng.choice(n, 32, replace=False)
+    ex = _sample_rows_exact(P, op, x1[None, :], rows, h)[:, 0]
+    out["assembly_rel_err_sampled_rows"] = float(np.linalg.norm(y1.cpu().numpy()[rows] - ex) / np.linalg.norm(ex))
+    H.prepare("bf16")
+    out["bf16_arena_bytes"] = int(H.storage_bytes("bf16"))
+    X = torch.from_numpy(np.random.default_rng(5).uniform(-1.0, 1.0, (p, n))).to(dev)
+    Y = torch.zeros_like(X)
+
+    def timed(prec, steps):
+        for _ in range(3):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    with ClockSampler(0) as cs:
+        ms_bf16 = timed("bf16", args.steps)
+    out["clocks"] = cs.summary()
+    ms_64 = timed("fp64", 2)
+    Y64 = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Y64, precision="fp64")
+    Yb = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Yb, precision="bf16")
+    torch.cuda.synchronize()
+    peak, peak_kind = _peaks()
+    bytes_b = algorithmic_bytes(H, "bf16", p)
+    out["product"] = {"bf16_ms": ms_bf16, "fp64_ms": ms_64, "speedup": ms_64 / ms_bf16,
+                      "bf16_max_rel_err_per_rhs": float(((Yb - Y64).norm(dim=1) / Y64.norm(dim=1)).max()),
+                      "algorithmic_bytes": bytes_b,
+                      "achieved_gbs": bytes_b / (ms_bf16 * 1e-3) / 1e9, "peak_gbs": peak,
+                      "frac": bytes_b / (ms_bf16 * 1e-3) / 1e9 / peak, "peak_kind": peak_kind}
+    del Y, Y64, Yb
+    # GMRES(50) to 1e-8 with 64 right-hand sides b ~ N(0, 1)
+    B = torch.from_numpy(np.random.default_rng(6).standard_normal((p, n))).to(dev)
+    res = {}
+    for prec, cap in (("bf16", args.gmres_cap), ("fp64", args.gmres_cap_fp64)):
+        Xs = torch.zeros_like(B)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, rr, its = H.GMRes(B, Xs, 1e-8, 50, cap, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        # true FP64 residual of the returned solution
+        R = B.clone()
+        H.mltaGeHVec(-1.0, Xs, R, precision="fp64")
+        true = float((R.norm(dim=1) / B.norm(dim=1)).max())
+        res[prec] = {"s": dt, "converged": st == 0, "max_iters": int(its.max()),
+                     "mean_iters": float(its.mean()), "max_resid": float(rr.max()),
+                     "true_max_resid": true, "iters_per_s": float(its.max()) / dt}
+        del Xs, R
+    out["gmres"] = res
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,6 +397,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large"],
+                    help="sphere: the default product benchmark; cube-large: N = 2^20 "
+                         "cube surface, 64 right-hand sides, products and GMRES")
+    ap.add_argument("--n-large", type=int, default=1 << 20)
+    ap.add_argument("--diag-scale", type=float, default=1.0,
+                    help="cube-large: diagonal 1/(4 pi h / s) (s = 2: the SPD variant)")
+    ap.add_argument("--gmres-cap", type=int, default=600)
+    ap.add_argument("--gmres-cap-fp64", type=int, default=600)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -296,6 +412,8 @@ def main():
         set_size(args.n)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "cube-large":
+        run_large(args)
     else:
         run_gpu(args)
 

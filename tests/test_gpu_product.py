@@ -116,3 +116,20 @@ def test_accumulates_and_zero_rhs(oracle_pair):
     H.mltaGeHGeM(1.0, 0, x, n, y2, n)  # p = 0 is a no-op
     y3 = H.mltaGeHVec(-1.0, x, y1.copy())
     assert np.linalg.norm(y3) <= 1e-13 * np.linalg.norm(y1)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", TOL_FP32), ("bf16", TOL_BF16)])
+@pytest.mark.parametrize("p", [1, 5, 16, 17, 33, 64, 70])
+def test_mixed_precision_rhs_counts(prec, tol, p):
+    """Tensor-core sweeps for every right-hand-side group width (16 / 32 / 64 per
+    pass, ragged last group), on a cube whose coarse clusters split the V sweep
+    over several warps (partial T rows reduced between the sweeps)."""
+    P = A.geometry.cube_surface(20000, 1)
+    H = A.HMatrix(P, "bbx", bmin=64, eta=0.8).matgenGeH_omp(A.mean_nn(P), 1e-6)
+    X = np.random.default_rng(p).uniform(-1, 1, (p, H.n))
+    Y0 = np.random.default_rng(p + 1).uniform(-1, 1, (p, H.n))
+    Y64 = H.mltaGeHVec(-0.5, X, Y0.copy())
+    Ym = H.mltaGeHVec(-0.5, X, Y0.copy(), precision=prec)
+    errs = [_relerr(Ym[r] - Y0[r], Y64[r] - Y0[r]) for r in range(p)]
+    assert max(errs) <= tol, errs
+    H.close()
