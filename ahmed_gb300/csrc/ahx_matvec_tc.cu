@@ -37,9 +37,9 @@ constexpr size_t kSmem = (size_t)kG * kR * kTcSlot + (size_t)2 * kG * kR * sizeo
 
 // Launch shapes for P right-hand sides.  Per group one producer warp and two
 // consumer warps.  At 64 right-hand sides the two consumers split the m-tiles
-// (16 right-hand sides each) of every unit; below, each consumer takes every
-// other unit of the group with the whole tile (rows sweep; the V sweep keeps
-// one consumer there: its partial T rows are planned per group range).  The
+// (16 right-hand sides each) of every unit; below, in the rows sweep each
+// consumer takes every other unit of the group with the whole tile, and in
+// the V sweep the two split the unit's n-tiles (distinct T rows).  The
 // units of a group form SEQ sequences (unit i belongs to sequence i % SEQ),
 // each with its own kR / SEQ slots, so every slot is filled and read strictly
 // in order by one sequence and a parity wait never runs two phases ahead.
@@ -47,10 +47,12 @@ constexpr size_t kSmem = (size_t)kG * kR * kTcSlot + (size_t)2 * kG * kR * sizeo
 template <int P, bool ROWS>
 struct Cfg {
   static constexpr bool MSPLIT = P >= 64;                  // consumers split the m-tiles
-  static constexpr int W = MSPLIT ? 2 : (ROWS ? 2 : 1);    // consumer warps per group
-  static constexpr int SEQ = MSPLIT ? 1 : W;               // unit sequences per group
+  static constexpr bool NSPLIT = !MSPLIT && !ROWS;         // consumers split the n-tiles (V sweep)
+  static constexpr int W = 2;                              // consumer warps per group
+  static constexpr int SEQ = (MSPLIT || NSPLIT) ? 1 : W;   // unit sequences per group
   static constexpr int MTW = P / 16 / (MSPLIT ? 2 : 1);    // m-tiles per consumer warp
-  static constexpr int kEmpty = MSPLIT ? 2 : 1;            // releases per unit
+  static constexpr int NTW = NSPLIT ? 4 : 0;               // n-tiles per consumer warp (0: all)
+  static constexpr int kEmpty = SEQ == 1 ? 2 : 1;          // releases per unit
   static constexpr int kConsumers = kG * W;
   static constexpr int kThreads = 32 * (kConsumers + kG);
   // registers per thread the CTA can give (multiple of 8)
@@ -173,8 +175,9 @@ __device__ __forceinline__ void tf32_compute(const TfFrag<MTW, NT>& F, Accs<MTW,
 // side[k][p] (stride P + 8), m-tiles mt0 .. mt0 + MTW - 1, NT n-tiles.
 template <int P, int MTW, bool SPLIT, int NT>
 __device__ __forceinline__ void tf32_group_nt(const unsigned char* frag, const float* side, uint32_t kp,
-                                              uint32_t nt, uint32_t mt0, Accs<MTW, SPLIT>& A, uint32_t lane) {
-  const uint2* fb = reinterpret_cast<const uint2*>(frag) + lane;
+                                              uint32_t nt, uint32_t mt0, uint32_t n0, Accs<MTW, SPLIT>& A,
+                                              uint32_t lane) {
+  const uint2* fb = reinterpret_cast<const uint2*>(frag) + n0 * 32 + lane;
   for (uint32_t kb = 0; kb < kp / 8; ++kb) {
     TfFrag<MTW, NT> F;
     tf32_load<P, MTW, NT>(F, fb, side, kb, nt, mt0, lane);
@@ -213,12 +216,13 @@ __device__ __forceinline__ void bf16_compute(const BfFrag<MTW, NT>& F, Accs<MTW,
 // ldmatrix.trans, m-tiles mt0 .. mt0 + MTW - 1, NT n-tiles.
 template <int P, int MTW, int NT>
 __device__ __forceinline__ void bf16_group_nt(const unsigned char* frag, const unsigned char* side, uint32_t kp,
-                                              uint32_t nt, uint32_t mt0, Accs<MTW, false>& A, uint32_t lane) {
+                                              uint32_t nt, uint32_t mt0, uint32_t n0, Accs<MTW, false>& A,
+                                              uint32_t lane) {
   constexpr uint32_t SB = (P + 8) * 2;
   const uint32_t kfull = kp >> 4;
   const uint32_t m = lane >> 3, r = lane & 7;
   const uint32_t sbase = smem_u32(side) + mt0 * 32;
-  const uint2* fb = reinterpret_cast<const uint2*>(frag) + lane;
+  const uint2* fb = reinterpret_cast<const uint2*>(frag) + n0 * 32 + lane;
   // one register set: a second (loads of block kb + 1 under the mma of kb)
   // exceeds the register budget at 64 right-hand sides
   for (uint32_t kb = 0; kb < kfull; ++kb) {
@@ -227,7 +231,7 @@ __device__ __forceinline__ void bf16_group_nt(const unsigned char* frag, const u
     bf16_compute<MTW, NT>(F, A);
   }
   if (kp & 8) {
-    const uint32_t* ft = reinterpret_cast<const uint32_t*>(frag + (size_t)kfull * nt * 256) + lane;
+    const uint32_t* ft = reinterpret_cast<const uint32_t*>(frag + (size_t)kfull * nt * 256) + n0 * 32 + lane;
     const uint32_t ra = sbase + (kfull * 16 + r) * SB + (m & 1) * 16;
     uint32_t a0[MTW], a1[MTW], b[NT];
 #pragma unroll
@@ -242,39 +246,35 @@ __device__ __forceinline__ void bf16_group_nt(const unsigned char* frag, const u
 }
 
 // The k-loops run NT n-tiles with no per-tile branches, so the independent
-// mma chains of a k-block interleave: NT = nt rounded up to even below 64
-// right-hand sides, NT = 8 at 64 (one code path keeps the register budget).
+// mma chains of a k-block interleave: NT = 4 or 8 below 64 right-hand sides
+// (two code paths: more would thrash the instruction cache), NT = 8 at 64
+// (one code path keeps the register budget).
 // Tiles n >= nt read B words past the group's fragments (inside the slot, or
 // inside the padding after the last slot) into accumulators that are never
 // flushed: those tiles hold no output rows.
-template <int P, int MTW, bool SPLIT>
+// NT > 0: a fixed count of n-tiles starting at n-tile n0 (warps that split a
+// unit's n-tiles); NT == 0: the unit's own count, rounded up to 4 or 8.
+template <int P, int MTW, bool SPLIT, int NT = 0>
 __device__ __forceinline__ void tf32_group(const unsigned char* frag, const float* side, uint32_t kp, uint32_t nt,
-                                           uint32_t mt0, Accs<MTW, SPLIT>& acc, uint32_t lane) {
-  if (P >= 64) {
-    tf32_group_nt<P, MTW, SPLIT, 8>(frag, side, kp, nt, mt0, acc, lane);
+                                           uint32_t mt0, uint32_t n0, Accs<MTW, SPLIT>& acc, uint32_t lane) {
+  if (NT > 0 || P >= 64) {
+    tf32_group_nt<P, MTW, SPLIT, (NT > 0 ? NT : 8)>(frag, side, kp, nt, mt0, n0, acc, lane);
     return;
   }
-  switch ((nt + 1) >> 1) {
-    case 1: tf32_group_nt<P, MTW, SPLIT, 2>(frag, side, kp, nt, mt0, acc, lane); break;
-    case 2: tf32_group_nt<P, MTW, SPLIT, 4>(frag, side, kp, nt, mt0, acc, lane); break;
-    case 3: tf32_group_nt<P, MTW, SPLIT, 6>(frag, side, kp, nt, mt0, acc, lane); break;
-    default: tf32_group_nt<P, MTW, SPLIT, 8>(frag, side, kp, nt, mt0, acc, lane); break;
-  }
+  if (nt <= 4) tf32_group_nt<P, MTW, SPLIT, 4>(frag, side, kp, nt, mt0, 0, acc, lane);
+  else tf32_group_nt<P, MTW, SPLIT, 8>(frag, side, kp, nt, mt0, 0, acc, lane);
 }
 
-template <int P, int MTW>
+template <int P, int MTW, int NT = 0>
 __device__ __forceinline__ void bf16_group(const unsigned char* frag, const unsigned char* side, uint32_t kp,
-                                           uint32_t nt, uint32_t mt0, Accs<MTW, false>& acc, uint32_t lane) {
-  if (P >= 64) {
-    bf16_group_nt<P, MTW, 8>(frag, side, kp, nt, mt0, acc, lane);
+                                           uint32_t nt, uint32_t mt0, uint32_t n0, Accs<MTW, false>& acc,
+                                           uint32_t lane) {
+  if (NT > 0 || P >= 64) {
+    bf16_group_nt<P, MTW, (NT > 0 ? NT : 8)>(frag, side, kp, nt, mt0, n0, acc, lane);
     return;
   }
-  switch ((nt + 1) >> 1) {
-    case 1: bf16_group_nt<P, MTW, 2>(frag, side, kp, nt, mt0, acc, lane); break;
-    case 2: bf16_group_nt<P, MTW, 4>(frag, side, kp, nt, mt0, acc, lane); break;
-    case 3: bf16_group_nt<P, MTW, 6>(frag, side, kp, nt, mt0, acc, lane); break;
-    default: bf16_group_nt<P, MTW, 8>(frag, side, kp, nt, mt0, acc, lane); break;
-  }
+  if (nt <= 4) bf16_group_nt<P, MTW, 4>(frag, side, kp, nt, mt0, 0, acc, lane);
+  else bf16_group_nt<P, MTW, 8>(frag, side, kp, nt, mt0, 0, acc, lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -450,23 +450,26 @@ __global__ void __launch_bounds__((Cfg<P, false>::kThreads), 1) __maxnreg__((Cfg
   TT* T = reinterpret_cast<TT*>(pl.t);
   Accs<MTW, !BF> acc;
   acc.zero();
+  const uint32_t mt0 = C::MSPLIT ? h * MTW : 0, n0 = C::NSPLIT ? h * C::NTW : 0;
   consume<C::SEQ, TcVUnit>(R, pl.vranges, g, 0, pl.err, [&](const TcVUnit& U, const unsigned char* data, uint32_t) {
     if (U.flags & 1u) acc.zero();
     const uint32_t nt = (U.ncols + 7u) >> 3;
-    if constexpr (BF) bf16_group<P, MTW>(data, data + U.bytes, U.kp, nt, h * MTW, acc, lane);
-    else tf32_group<P, MTW, true>(data, reinterpret_cast<const float*>(data + U.bytes), U.kp, nt, h * MTW, acc, lane);
+    if (n0 >= nt) return;  // no columns for this warp in this unit
+    if constexpr (BF) bf16_group<P, MTW, C::NTW>(data, data + U.bytes, U.kp, nt, mt0, n0, acc, lane);
+    else tf32_group<P, MTW, true, C::NTW>(data, reinterpret_cast<const float*>(data + U.bytes), U.kp, nt, mt0, n0,
+                                          acc, lane);
     if (U.flags & 2u) {
 #pragma unroll
       for (int mt = 0; mt < MTW; ++mt)
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          if ((uint32_t)n < nt) {
+        for (int n = 0; n < (C::NTW ? C::NTW : 8); ++n) {
+          if (n0 + n < nt) {
             float v[4], w[4];
             acc.total(mt, n, v);
             transpose4(v, w, j);
-            const uint32_t col = 8 * n + 2 * t + (j & 1);
+            const uint32_t col = 8 * (n0 + n) + 2 * t + (j & 1);
             if (col < U.ncols) {
-              TT* dst = T + (uint64_t)(U.trow + col) * (P + 8) + 16 * (h * MTW + mt) + 8 * (j >> 1) + 4 * q;
+              TT* dst = T + (uint64_t)(U.trow + col) * (P + 8) + 16 * (mt0 + mt) + 8 * (j >> 1) + 4 * q;
               if (BF) {
                 __nv_bfloat162 lo = __floats2bfloat162_rn(w[0], w[1]);
                 __nv_bfloat162 hi = __floats2bfloat162_rn(w[2], w[3]);
@@ -600,12 +603,13 @@ __global__ void __launch_bounds__((Cfg<P, true>::kThreads), 1) __maxnreg__((Cfg<
     const uint32_t nt = (U.nr + 7u) >> 3;
     const unsigned char* side0 = data + U.bytes;
     if (U.kp0) {
-      if constexpr (BF) bf16_group<P, MTW>(data, side0, U.kp0, nt, mt0, acc, lane);
-      else tf32_group<P, MTW, true>(data, reinterpret_cast<const float*>(side0), U.kp0, nt, mt0, acc, lane);
+      if constexpr (BF) bf16_group<P, MTW>(data, side0, U.kp0, nt, mt0, 0, acc, lane);
+      else tf32_group<P, MTW, true>(data, reinterpret_cast<const float*>(side0), U.kp0, nt, mt0, 0, acc, lane);
     }
     if (U.kp1)
       tf32_group<P, MTW, !BF>(data + (size_t)U.kp0 * nt * 8 * ES0,
-                              reinterpret_cast<const float*>(side0 + (size_t)U.kp0 * S0), U.kp1, nt, mt0, acc, lane);
+                              reinterpret_cast<const float*>(side0 + (size_t)U.kp0 * S0), U.kp1, nt, mt0, 0, acc,
+                              lane);
   });
   if (cur_nr) flush();
 }
