@@ -12,8 +12,9 @@ from .hmatrix import (  # noqa: F401
     HMatrix,
     matgenGeH_omp,
     mean_nn,
+    min_nn,
     mltaGeHGeM,
     mltaGeHVec,
 )
-from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA  # noqa: F401
+from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, lib  # noqa: F401
 from .rank_predictor import RankPredictor, training_set  # noqa: F401

@@ -435,6 +435,15 @@ double ahx_mean_nn(const double* pts, uint32_t n) {
   return mean_nn(pts, n);
 }
 
+uint64_t ahx_kernel_launches(void) { return product_launches(); }
+
+double ahx_min_nn(const double* pts, uint32_t n) {
+  if (!pts) return 0.0;
+  double mn = 0.0;
+  mean_nn(pts, n, &mn);
+  return mn;
+}
+
 int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
                     int device, void* stream, ahx_hmat** out) {
   if (!out || !pts || n == 0 || bmin == 0 || (tree_kind != AHX_TREE_BBX && tree_kind != AHX_TREE_PCA) ||

@@ -174,6 +174,10 @@ struct TcPlan {
   uint32_t pmax = 16;
 };
 
+// kernels launched by the products of this process (FP64 and mixed)
+uint64_t product_launches();
+void count_product_launches(uint64_t n);
+
 cudaError_t launch_tc_build(const TcFragTask* tasks, uint32_t ntasks, const TcSeg* segs,
                             const double* arena64, unsigned char* dst, cudaStream_t s);
 cudaError_t launch_matvec_tc(int prec, const TcPlan& plan, double d, uint32_t p, const double* X,

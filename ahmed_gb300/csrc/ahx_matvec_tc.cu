@@ -16,6 +16,7 @@
 // raises the plan's error word, the producer waits (bounded) for the copies it
 // queued, and all warps return.
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <numeric>
 #include <type_traits>
@@ -706,6 +707,8 @@ __global__ void tc_build_kernel(const TcFragTask* __restrict__ tasks, const TcSe
 
 unsigned grid_rows(uint64_t n) { return (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8); }
 
+std::atomic<uint64_t> g_product_launches{0};
+
 template <int P, bool BF>
 cudaError_t run_tc_group(const TcPlan& pl, double d, uint32_t r0, uint32_t pg, const double* X, uint64_t ldX,
                          double* Y, uint64_t ldY, cudaStream_t s) {
@@ -720,6 +723,7 @@ cudaError_t run_tc_group(const TcPlan& pl, double d, uint32_t r0, uint32_t pg, c
   }
   tc_xr_kernel<P, BF><<<grid_rows(pl.n), 256, 0, s>>>(X, ldX, pl.n, r0, pg, pl.xf,
                                                        reinterpret_cast<__nv_bfloat16*>(pl.xb));
+  g_product_launches += 2 + (pl.nvunits ? 1 : 0) + (pl.ntreduce ? 1 : 0) + (pl.nrunits ? 1 : 0);
   cudaError_t e = cudaMemsetAsync(pl.yr, 0, pl.n * P * sizeof(float), s);
   if (e != cudaSuccess) return e;
   if (pl.nvunits) tc_v_kernel<P, BF><<<pl.grid, Cfg<P, false>::kThreads, kSmem, s>>>(pl);
@@ -753,6 +757,9 @@ size_t entry_of(const std::vector<uint32_t>& starts, uint32_t c) {
 }
 
 }  // namespace
+
+uint64_t product_launches() { return g_product_launches.load(); }
+void count_product_launches(uint64_t n) { g_product_launches += n; }
 
 void balance_ranges(const std::vector<uint64_t>& bytes, uint32_t grid, std::vector<uint32_t>& first) {
   first.assign(grid + 1, 0);

@@ -472,17 +472,44 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     AHX_CUDA(cudaStreamSynchronize(st));
     for (uint32_t q = 0; q < nsys; ++q) normb[q] = std::sqrt(nb[(size_t)q * sv.maxk_]);
     uint32_t used = 0;
+    // Safeguard: an outer step that raises a system's FP64 residual is undone
+    // for that system, and the remaining inner solves run on the FP64 leaves
+    // (the storage precision's error can exceed what refinement contracts
+    // when the matrix is ill-conditioned).
+    int inner_prec = prec;
+    bool undone = false;  // the residual just recomputed follows an undo: accept it
+    std::vector<double> prev(nsys, INFINITY), undo(nsys, 0.0);
     for (;;) {
       AHX_CUDA(cudaMemcpyAsync(rr.p, B, total * 8, cudaMemcpyDeviceToDevice, st));
       if ((rc = op.apply(kFP64, -1.0, p, X, rr.as<double>()))) return rc;
       if ((rc = sv.dots(rr.as<double>(), 0, 1, rr.as<double>(), sv.small_.as<double>()))) return rc;
       AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
       AHX_CUDA(cudaStreamSynchronize(st));
+      bool worse = false;
+      for (uint32_t q = 0; q < nsys; ++q) {
+        const double rq = normb[q] > 0.0 ? std::sqrt(nb[(size_t)q * sv.maxk_]) / normb[q] : 0.0;
+        undo[q] = 0.0;
+        if (!undone && !done[q] && rq > prev[q]) {
+          undo[q] = -1.0;
+          worse = true;
+        }
+      }
+      undone = false;
+      if (worse) {
+        // x -= z on the systems whose residual grew, then recompute r
+        AHX_CUDA(cudaMemcpyAsync(sv.small2_.p, undo.data(), nsys * 8, cudaMemcpyHostToDevice, st));
+        axpy_sys_kernel<<<grid_for(total), 256, 0, st>>>(X, X, z.as<double>(), sv.small2_.as<double>(), total,
+                                                         op.ntot, sv.segid(), op.nseg);
+        inner_prec = kFP64;
+        undone = true;
+        continue;
+      }
       bool any = false;
       std::vector<char> idone(nsys, 0);
       std::vector<double> mask(nsys, 1.0);
       for (uint32_t q = 0; q < nsys; ++q) {
         resid[q] = normb[q] > 0.0 ? std::sqrt(nb[(size_t)q * sv.maxk_]) / normb[q] : 0.0;
+        prev[q] = resid[q];
         if (resid[q] < tol || normb[q] == 0.0) {
           done[q] = 1;
           idone[q] = 1;
@@ -501,7 +528,8 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
       std::vector<uint32_t> it2(nsys, 0);
       std::vector<double> res2(nsys, 0.0);
       const uint32_t budget = std::min(m, maxit - used);
-      if ((rc = gmres_core(sv, prec, rr.as<double>(), z.as<double>(), inner_tol, m, budget, it2, res2,
+      if ((rc = gmres_core(sv, inner_prec, rr.as<double>(), z.as<double>(),
+                           inner_prec == kFP64 ? std::max(tol, 1e-12) : inner_tol, m, budget, it2, res2,
                            idone, vbuf, rbuf)))
         return rc;
       uint32_t step = 0;

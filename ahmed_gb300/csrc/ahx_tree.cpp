@@ -296,7 +296,8 @@ void leaf_features(const Tree& T, const Leaf& L, double wavenumber, double eps, 
   out[7] = (float)(-std::log10(eps));
 }
 
-double mean_nn(const double* pts, uint32_t n) {
+double mean_nn(const double* pts, uint32_t n, double* min_out) {
+  if (min_out) *min_out = 0.0;
   if (n < 2) return 0.0;
   double lo[3], hi[3];
   for (int j = 0; j < 3; ++j) lo[j] = hi[j] = pts[j];
@@ -360,8 +361,12 @@ double mean_nn(const double* pts, uint32_t n) {
     }
     dmin[i] = std::sqrt(best);
   }
-  double sum = 0.0;
-  for (uint32_t i = 0; i < n; ++i) sum += dmin[i];
+  double sum = 0.0, mn = INFINITY;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += dmin[i];
+    mn = std::min(mn, dmin[i]);
+  }
+  if (min_out) *min_out = mn;
   return sum / n;
 }
 

@@ -50,8 +50,9 @@ struct Tree {
 // block-cluster tree with the admissibility parameter eta2 (= eta^2).
 void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin, double eta2);
 
-// Mean nearest-neighbour distance (exact; uniform-grid search; deterministic sum order).
-double mean_nn(const double* pts, uint32_t n);
+// Mean nearest-neighbour distance (exact; uniform-grid search; deterministic
+// sum order); *min_out (if given) receives the smallest one.
+double mean_nn(const double* pts, uint32_t n, double* min_out = nullptr);
 
 // Geometric features of a leaf for the rank predictor (8 floats):
 //   log diam(row cluster), log diam(col cluster), log centre distance,

@@ -42,6 +42,12 @@ def mean_nn(points):
     return lib().ahx_mean_nn(ptr(pts), pts.shape[0])
 
 
+def min_nn(points):
+    """Smallest nearest-neighbour distance of the points (n x 3)."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    return lib().ahx_min_nn(ptr(pts), pts.shape[0])
+
+
 def _prec(p):
     return PRECISIONS[p] if isinstance(p, str) else int(p)
 
@@ -70,6 +76,7 @@ class HMatrix:
         self.h = None
         self.eps = None
         self._batches = []
+        self._stream_explicit = stream is not None
         _live.add(self)
 
     def close(self):
@@ -102,7 +109,25 @@ class HMatrix:
         return lib().ahx_hmat_stream(self._h)
 
     def set_stream(self, stream):
+        """Run this matrix's work on `stream` (a cudaStream_t value; None: a private stream)."""
         check(lib().ahx_hmat_set_stream(self._h, C.c_void_p(stream) if stream else None))
+        self._stream_explicit = stream is not None
+
+    def _follow_torch(self, *arrays):
+        """Without an explicit stream, CUDA torch tensors are used on torch's current
+        stream: the library is moved there so that it is ordered after their producers."""
+        if self._stream_explicit:
+            return
+        for a in arrays:
+            if getattr(a, "is_cuda", False):
+                import torch
+
+                # torch's legacy default stream is handle 0, which the library reads
+                # as "private stream": pass cudaStreamLegacy (1) for it
+                cur = torch.cuda.current_stream(a.device).cuda_stream or 1
+                if cur != (self.stream or 0):
+                    check(lib().ahx_hmat_set_stream(self._h, C.c_void_p(cur)))
+                return
 
     def perm(self):
         op = np.zeros(self.n, np.uint32)
@@ -178,6 +203,7 @@ class HMatrix:
     # -- product ----------------------------------------------------------
     def mltaGeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
         """Y += d A X with X, Y column-major (numpy / torch, host or CUDA)."""
+        self._follow_torch(X, Y)
         check(lib().ahx_matvec(self._h, _prec(precision), float(d), int(p), ptr(X), int(ldX),
                                ptr(Y), int(ldY)))
         return Y
@@ -191,6 +217,7 @@ class HMatrix:
     def GMRes(self, b, x, eps, m, nsteps, precision="fp64"):
         """Restarted GMRES(m); b, x of shape (n,) or (p, n).  Returns (status, eps[], nsteps[])."""
         p, ld = _ncols(b, self.n)
+        self._follow_torch(b, x)
         iters = np.zeros(p, np.uint32)
         res = np.zeros(p, np.float64)
         code = check(lib().ahx_gmres(self._h, _prec(precision), p, ptr(b), ld, ptr(x), ld,
@@ -199,6 +226,7 @@ class HMatrix:
 
     def CG(self, b, x, eps, nsteps):
         p, ld = _ncols(b, self.n)
+        self._follow_torch(b, x)
         iters = np.zeros(p, np.uint32)
         res = np.zeros(p, np.float64)
         code = check(lib().ahx_cg(self._h, p, ptr(b), ld, ptr(x), ld, float(eps), int(nsteps),
@@ -234,12 +262,23 @@ class HBatch:
         except Exception:
             pass
 
+    @staticmethod
+    def _torch_sync(*arrays):
+        # the batch runs on its own stream: CUDA torch tensors are synchronized around calls
+        if any(getattr(a, "is_cuda", False) for a in arrays):
+            import torch
+
+            torch.cuda.synchronize()
+
     def matvec(self, d, X, Y, p=1):
+        self._torch_sync(X, Y)
         check(lib().ahx_batch_matvec(self._h, float(d), int(p), ptr(X), ptr(Y)))
+        self._torch_sync(X, Y)
         return Y
 
     def gmres(self, b, x, eps, m, nsteps):
         k = len(self.mats)
+        self._torch_sync(b, x)
         iters = np.zeros(k, np.uint32)
         res = np.zeros(k, np.float64)
         code = check(lib().ahx_batch_gmres(self._h, ptr(b), ptr(x), float(eps), int(m),

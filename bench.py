@@ -187,6 +187,8 @@ def run_gpu(args):
     X = torch.from_numpy(np.random.default_rng(1).uniform(-1.0, 1.0, (NRHS, N_POINTS))).to(dev)
     Y = torch.zeros_like(X)
 
+    launches = {}
+
     def timed(prec, steps, warmup):
         for _ in range(warmup):
             H.mltaGeHVec(1.0, X, Y, precision=prec)
@@ -195,11 +197,13 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        l0 = A.lib().ahx_kernel_launches()
         e0.record(stream)
         for _ in range(steps):
             H.mltaGeHVec(1.0, X, Y, precision=prec)
         e1.record(stream)
         torch.cuda.synchronize()
+        launches[prec] = A.lib().ahx_kernel_launches() - l0
         ms = e0.elapsed_time(e1)
         if ws > 1:
             t = torch.tensor([ms], device=dev)
@@ -265,7 +269,7 @@ def run_gpu(args):
         "e2e": {"value": ws * NRHS / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * NRHS * N_POINTS * 8,
                 "d2h_bytes_per_step": NRHS * N_POINTS * 8},
-        "gpu_launches": args.steps,
+        "gpu_launches": launches.get("fp32"),
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu:
@@ -306,7 +310,7 @@ def run_large(args):
     dev = torch.device("cuda", 0)
     P = A.geometry.cube_surface(n, 4)
     t0 = time.perf_counter()
-    h = A.mean_nn(P) / args.diag_scale
+    h = (A.min_nn(P) if args.diag == "min" else A.mean_nn(P)) / args.diag_scale
     H = A.HMatrix(P, "bbx", bmin=bmin, eta=ETA, device=0)
     t_tree = time.perf_counter() - t0
     stream = torch.cuda.Stream(device=dev)
@@ -319,7 +323,7 @@ def run_large(args):
     ranks = H.ranks()
     op, _ = H.perm()
     out = {"workload": f"laplace-cube-{n}-64rhs", "n": n, "rhs": p, "leaf": bmin,
-           "diag": f"1/(4 pi h), h = mean nn / {args.diag_scale:g}",
+           "diag": f"1/(4 pi h), h = {args.diag} nearest-neighbour distance / {args.diag_scale:g}",
            "tree_s": t_tree, "assembly_s": t_asm, "leaves": int(H.nleaves),
            "lowrank_leaves": int((ranks >= 0).sum()), "avg_rank": float(ranks[ranks >= 0].mean()),
            "fp64_arena_bytes": int(H.storage_bytes("fp64"))}
@@ -382,9 +386,74 @@ def run_large(args):
         true = float((R.norm(dim=1) / B.norm(dim=1)).max())
         res[prec] = {"s": dt, "converged": st == 0, "max_iters": int(its.max()),
                      "mean_iters": float(its.mean()), "max_resid": float(rr.max()),
-                     "true_max_resid": true, "iters_per_s": float(its.max()) / dt}
+                     "true_max_resid": true, "iters_per_s": float(its.max()) / dt,
+                     "solves_per_s": (p / dt) if st == 0 else None}
         del Xs, R
+    if res["bf16"]["solves_per_s"] and res["fp64"]["solves_per_s"]:
+        res["mixed_over_plain"] = res["bf16"]["solves_per_s"] / res["fp64"]["solves_per_s"]
     out["gmres"] = res
+    print(json.dumps(out))
+
+
+def run_batch(args):
+    """Many uneven H-matrices in one launch: `--instances` instances (256), N log-uniform
+    in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
+    ellipsoid (1, 0.5, 0.25) and the unit-cube surface with uniform random surface points;
+    leaf 32, eta 0.8, ACA eps 1e-6; one right-hand side per instance b ~ N(0, 1) (seed 3);
+    GMRES(30) to 1e-8 with BF16/FP32 leaves and FP64 refinement, against plain FP64."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(2)
+    k = args.instances
+    ns = np.exp(rng.uniform(np.log(2048), np.log(32768), k)).astype(np.int64)
+    geos = rng.integers(0, 3, k)
+    names = ["sphere", "ellipsoid", "cube"]
+    mats = []
+    t_asm = 0.0
+    for i in range(k):
+        P = A.geometry.GEOMETRIES[names[geos[i]]](int(ns[i]), 1000 + i)
+        h = (A.min_nn(P) if args.diag == "min" else A.mean_nn(P)) / args.diag_scale
+        H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H.matgenGeH_omp(h, EPS)
+        torch.cuda.synchronize()
+        t_asm += time.perf_counter() - t0
+        mats.append(H)
+    ntot = int(ns.sum())
+    out = {"workload": f"laplace-batch{k}", "instances": k, "points": ntot,
+           "n_min": int(ns.min()), "n_max": int(ns.max()),
+           "diag": f"1/(4 pi h), h = {args.diag} nearest-neighbour distance / {args.diag_scale:g}",
+           "assembly_s_sum": t_asm,
+           "fp64_arena_bytes": int(sum(H.storage_bytes("fp64") for H in mats))}
+    b = np.random.default_rng(3).standard_normal(ntot)
+    peak, _ = _peaks()
+    for prec in ("bf16", "fp64"):
+        Bt = A.HBatch(mats, precision=prec)
+        x = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ntot)).to(dev)
+        y = torch.zeros_like(x)
+        for _ in range(3):
+            Bt.matvec(1.0, x, y)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            Bt.matvec(1.0, x, y)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / args.steps * 1e3
+        X = np.zeros(ntot)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, rr, its = Bt.gmres(b, X, 1e-8, 30, args.gmres_cap)
+        dt = time.perf_counter() - t0
+        out[prec] = {"product_ms": ms, "gmres_s": dt, "converged": st == 0,
+                     "max_iters": int(its.max()), "mean_iters": float(its.mean()),
+                     "max_resid": float(rr.max()), "solves_per_s": k / dt}
+        Bt.close()
+    out["bf16"]["product_over_fp64"] = out["fp64"]["product_ms"] / out["bf16"]["product_ms"]
+    out["gmres_mixed_over_plain"] = out["fp64"]["gmres_s"] / out["bf16"]["gmres_s"]
     print(json.dumps(out))
 
 
@@ -397,12 +466,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch"],
                     help="sphere: the default product benchmark; cube-large: N = 2^20 "
-                         "cube surface, 64 right-hand sides, products and GMRES")
+                         "cube surface, 64 right-hand sides, products and GMRES; batch: "
+                         "256 uneven instances, one launch per product, batched GMRES")
+    ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--n-large", type=int, default=1 << 20)
+    ap.add_argument("--diag", default="mean", choices=["mean", "min"],
+                    help="cube-large / batch: h = mean (configured) or minimum nearest-neighbour "
+                         "distance (random clouds: positive definite, GMRES converges)")
     ap.add_argument("--diag-scale", type=float, default=1.0,
-                    help="cube-large: diagonal 1/(4 pi h / s) (s = 2: the SPD variant)")
+                    help="cube-large / batch: diagonal 1/(4 pi h / s)")
     ap.add_argument("--gmres-cap", type=int, default=600)
     ap.add_argument("--gmres-cap-fp64", type=int, default=600)
     args = ap.parse_args()
@@ -414,6 +488,8 @@ def main():
         run_reference(args)
     elif args.workload == "cube-large":
         run_large(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

@@ -43,6 +43,12 @@ int ahx_version(void);
 
 /* Mean nearest-neighbour distance h of a point cloud (3*n doubles, xyz). */
 double ahx_mean_nn(const double* pts, uint32_t n);
+/* Smallest nearest-neighbour distance of the points (the diagonal 1/(4 pi h)
+ * with this h makes the Laplace matrix of a random point cloud positive
+ * definite enough for GMRES; the mean spacing leaves it indefinite). */
+double ahx_min_nn(const double* pts, uint32_t n);
+/* Product kernels launched by this process so far (plain and mixed forms). */
+uint64_t ahx_kernel_launches(void);
 
 /* Cluster tree + block-cluster tree.  Replaces
  *   cluster3d_bbx / bemcluster ctor + createClusterTree  Include/cluster_bbx.h:100,
