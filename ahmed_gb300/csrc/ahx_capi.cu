@@ -287,6 +287,7 @@ int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& lea
   const uint32_t grid = (uint32_t)std::max(sms, 1);
   TcLayout L;
   build_tc_layout(leaves, bf, pmax, grid * kTcGroups, L);
+  AHX_CUDA(tc_init_attributes());
   int rc;
   if ((rc = pc.vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;
   if ((rc = pc.rstream.reserve(std::max<uint64_t>(L.rbytes, 16)))) return rc;

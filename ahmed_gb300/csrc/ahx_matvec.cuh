@@ -174,6 +174,8 @@ struct TcPlan {
   uint32_t pmax = 16;
 };
 
+cudaError_t tc_init_attributes();
+
 // kernels launched by the products of this process (FP64 and mixed)
 uint64_t product_launches();
 void count_product_launches(uint64_t n);

@@ -710,17 +710,15 @@ unsigned grid_rows(uint64_t n) { return (unsigned)std::min<uint64_t>((n + 255) /
 std::atomic<uint64_t> g_product_launches{0};
 
 template <int P, bool BF>
+cudaError_t set_attributes() {
+  cudaError_t e = cudaFuncSetAttribute(tc_v_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(tc_rows_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+}
+
+template <int P, bool BF>
 cudaError_t run_tc_group(const TcPlan& pl, double d, uint32_t r0, uint32_t pg, const double* X, uint64_t ldX,
                          double* Y, uint64_t ldY, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_v_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kSmem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(tc_rows_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
   tc_xr_kernel<P, BF><<<grid_rows(pl.n), 256, 0, s>>>(X, ldX, pl.n, r0, pg, pl.xf,
                                                        reinterpret_cast<__nv_bfloat16*>(pl.xb));
   g_product_launches += 2 + (pl.nvunits ? 1 : 0) + (pl.ntreduce ? 1 : 0) + (pl.nrunits ? 1 : 0);
@@ -759,6 +757,16 @@ size_t entry_of(const std::vector<uint32_t>& starts, uint32_t c) {
 }  // namespace
 
 uint64_t product_launches() { return g_product_launches.load(); }
+
+// shared-memory opt-in of every sweep kernel of the current device (before any
+// launch, so that products can be captured in CUDA graphs)
+cudaError_t tc_init_attributes() {
+  cudaError_t e;
+  if ((e = set_attributes<16, false>()) != cudaSuccess) return e;
+  if ((e = set_attributes<16, true>()) != cudaSuccess) return e;
+  if ((e = set_attributes<32, true>()) != cudaSuccess) return e;
+  return set_attributes<64, true>();
+}
 void count_product_launches(uint64_t n) { g_product_launches += n; }
 
 void balance_ranges(const std::vector<uint64_t>& bytes, uint32_t grid, std::vector<uint32_t>& first) {

@@ -150,26 +150,98 @@ unsigned grid_for(uint64_t total) {
   return (unsigned)std::min<uint64_t>((total + 255) / 256, 152ull * 16);
 }
 
-// Givens rotation of solvers/GMRES.cpp:32-56
-void gen_rot(double dx, double dy, double& cs, double& sn) {
+// Givens rotations of solvers/GMRES.cpp:32-56, with explicitly rounded
+// operations (no contraction into FMA).
+__device__ __forceinline__ void gen_rot_d(double dx, double dy, double& cs, double& sn) {
   if (dy == 0.0) {
     cs = 1.0;
     sn = 0.0;
-  } else if (std::fabs(dy) > std::fabs(dx)) {
-    const double t = dx / dy;
-    sn = 1.0 / std::sqrt(1.0 + t * t);
-    cs = t * sn;
+  } else if (fabs(dy) > fabs(dx)) {
+    const double t = __ddiv_rn(dx, dy);
+    sn = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(t, t))));
+    cs = __dmul_rn(t, sn);
   } else {
-    const double t = dy / dx;
-    cs = 1.0 / std::sqrt(1.0 + t * t);
-    sn = t * cs;
+    const double t = __ddiv_rn(dy, dx);
+    cs = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(t, t))));
+    sn = __dmul_rn(t, cs);
   }
 }
 
-void appl_rot(double& dx, double& dy, double cs, double sn) {
-  const double t = cs * dx + sn * dy;
-  dy = cs * dy - sn * dx;
+__device__ __forceinline__ void appl_rot_d(double& dx, double& dy, double cs, double sn) {
+  const double t = __dadd_rn(__dmul_rn(cs, dx), __dmul_rn(sn, dy));
+  dy = __dsub_rn(__dmul_rn(cs, dy), __dmul_rn(sn, dx));
   dx = t;
+}
+
+// Device state of restarted GMRES(m) for nsys systems; K >= m + 1 entries per
+// system; R holds the rotated Hessenberg columns, system q column i at
+// R[(q * m + i) * K].
+struct GmDev {
+  double *R, *cs, *sn, *s, *y, *normb, *resid;
+  uint32_t *flags;  // bit 0: running in this cycle, bit 1: converged
+  uint32_t *ylen, *iters, *jbase, *nactive;
+  const double* tol;      // in device memory so that captured graphs stay valid
+  const uint32_t* maxit;  // across calls with other tolerances and step limits
+};
+
+// y = R^{-1} s over the first k columns (solvers/GMRES.cpp:62-78, dtrsv)
+__device__ void tri_solve_d(const GmDev& g, uint32_t q, uint32_t k, uint32_t m, uint32_t K) {
+  const double* Rq = g.R + (size_t)q * m * K;
+  double* y = g.y + (size_t)q * K;
+  for (uint32_t i = 0; i < k; ++i) y[i] = g.s[(size_t)q * K + i];
+  for (int jj = (int)k - 1; jj >= 0; --jj) {
+    y[jj] = __ddiv_rn(y[jj], Rq[(size_t)jj * K + jj]);
+    for (int i = 0; i < jj; ++i) y[i] = __dsub_rn(y[i], __dmul_rn(y[jj], Rq[(size_t)jj * K + i]));
+  }
+  g.ylen[q] = k;
+}
+
+// One Arnoldi step i of every running system: Hessenberg column from the two
+// Gram-Schmidt passes (h1 + h2) and |w|, the rotations, the residual estimate.
+__global__ void arnoldi_kernel(GmDev g, uint32_t i, uint32_t m, uint32_t K, const double* __restrict__ h1,
+                               const double* __restrict__ h2, const double* __restrict__ nrm, uint32_t nsys) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsys) return;
+  const uint32_t f = g.flags[q];
+  if (!(f & 1u) || (f & 2u)) return;
+  const uint32_t j = g.jbase[0] + i + 1;
+  if (j > g.maxit[0]) return;
+  double* col = g.R + ((size_t)q * m + i) * K;
+  for (uint32_t k = 0; k <= i; ++k) col[k] = __dadd_rn(h1[(size_t)q * K + k], h2[(size_t)q * K + k]);
+  col[i + 1] = __dsqrt_rn(nrm[(size_t)q * K]);
+  double* csq = g.cs + (size_t)q * K;
+  double* snq = g.sn + (size_t)q * K;
+  double* sq = g.s + (size_t)q * K;
+  for (uint32_t k = 0; k < i; ++k) appl_rot_d(col[k], col[k + 1], csq[k], snq[k]);
+  gen_rot_d(col[i], col[i + 1], csq[i], snq[i]);
+  appl_rot_d(col[i], col[i + 1], csq[i], snq[i]);
+  appl_rot_d(sq[i], sq[i + 1], csq[i], snq[i]);
+  const double r = fabs(__ddiv_rn(sq[i + 1], g.normb[q]));
+  g.resid[q] = r;
+  g.iters[q] = j;
+  if (r < g.tol[0]) {
+    tri_solve_d(g, q, i + 1, m, K);
+    g.flags[q] = f | 2u;
+  }
+}
+
+// running systems at the end of a cycle of `icount` steps: y from those steps
+__global__ void cycle_end_kernel(GmDev g, uint32_t icount, uint32_t m, uint32_t K, uint32_t nsys) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsys) return;
+  const uint32_t f = g.flags[q];
+  if ((f & 1u) && !(f & 2u) && icount > 0) tri_solve_d(g, q, icount, m, K);
+}
+
+__global__ void count_active_kernel(GmDev g, uint32_t nsys) {
+  __shared__ uint32_t c;
+  if (threadIdx.x == 0) c = 0;
+  __syncthreads();
+  uint32_t mine = 0;
+  for (uint32_t q = threadIdx.x; q < nsys; q += blockDim.x) mine += ((g.flags[q] & 3u) == 1u) ? 1u : 0u;
+  atomicAdd(&c, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) g.nactive[0] = c;
 }
 
 }  // namespace
@@ -184,6 +256,8 @@ struct Operator {
   virtual ~Operator() { seg_id.release(); }
   // Y += d A X in storage precision prec
   virtual int apply(int prec, double d, uint32_t p, const double* X, double* Y) = 0;
+  // everything apply(prec, ...) allocates, done ahead (graph capture allows no allocation)
+  virtual int prepare(int prec) { (void)prec; return AHX_OK; }
   int init_segments() {
     if (nseg <= 1) return AHX_OK;
     std::vector<uint32_t> id(ntot);
@@ -207,6 +281,7 @@ struct HmatOp : Operator {
   int apply(int prec, double d, uint32_t p, const double* X, double* Y) override {
     return product_device(H, prec, d, p, X, ntot, Y, ntot);
   }
+  int prepare(int prec) override { return prepare_product(H, prec); }
 };
 
 // Reduction plan + device scratch for a family of systems.
@@ -214,7 +289,7 @@ class Solver {
  public:
   Solver(Operator& op, uint32_t p) : op_(op), p_(p) {}
   ~Solver() {
-    for (DevBuf* b : {&items_, &first_, &partial_, &small_, &small2_, &len_}) b->release();
+    for (DevBuf* b : {&items_, &first_, &partial_, &small_, &small2_, &small3_, &len_, &gm_}) b->release();
   }
 
   int init(uint32_t maxk) {
@@ -240,6 +315,7 @@ class Solver {
     if ((rc = partial_.reserve((size_t)std::max(nitems_, 1u) * maxk * sizeof(double)))) return rc;
     if ((rc = small_.reserve((size_t)nsys_ * maxk * sizeof(double)))) return rc;
     if ((rc = small2_.reserve((size_t)nsys_ * maxk * sizeof(double)))) return rc;
+    if ((rc = small3_.reserve((size_t)nsys_ * maxk * sizeof(double)))) return rc;
     if ((rc = len_.reserve((size_t)nsys_ * sizeof(uint32_t)))) return rc;
     if (!items.empty())
       AHX_CUDA(cudaMemcpyAsync(items_.p, items.data(), items.size() * sizeof(Item),
@@ -266,17 +342,43 @@ class Solver {
   Operator& op_;
   uint32_t p_, nsys_ = 0, nitems_ = 0, maxk_ = 0;
   uint64_t total_ = 0;
-  DevBuf items_, first_, partial_, small_, small2_, len_;
+  DevBuf items_, first_, partial_, small_, small2_, small3_, len_;
+  DevBuf gm_;  // device GMRES state (GmDev arrays)
+};
+
+// CUDA graphs of GMRES steps: one executable graph per chunk of kGraphChunk
+// consecutive steps of a cycle, valid while the operator precision, the basis
+// buffer and m stay the same (tolerance and step limit are read from device
+// memory, so they may change between calls).
+constexpr uint32_t kGraphChunk = 5;
+struct GmresGraphs {
+  int prec = -1;
+  const void* vptr = nullptr;
+  uint32_t m = 0;
+  bool failed = false;  // capture is not possible on this stream: launch directly
+  std::vector<cudaGraphExec_t> exec;
+  ~GmresGraphs() { reset(); }
+  void reset() {
+    for (cudaGraphExec_t e : exec)
+      if (e) cudaGraphExecDestroy(e);
+    exec.clear();
+    prec = -1;
+    vptr = nullptr;
+    m = 0;
+  }
 };
 
 namespace {
 
 // Restarted GMRES(m) on `sv`'s systems with the operator at precision prec.
-// B, X: device, ntot x p.  active[q] selects the systems to solve.
-// Mirrors solvers/GMRES.cpp:80-181 per system.
+// B, X: device, ntot x p.  done[q] excludes systems.  Mirrors
+// solvers/GMRES.cpp:80-181 per system; the Arnoldi steps (product, two
+// classical Gram-Schmidt passes, rotations, residual estimate) run without
+// host round trips and are replayed as CUDA graphs of kGraphChunk steps; the
+// host checks progress once per chunk and restarts once per cycle.
 int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uint32_t m,
                uint32_t maxit, std::vector<uint32_t>& iters, std::vector<double>& resid,
-               std::vector<char>& done, DevBuf& vbuf, DevBuf& rbuf) {
+               std::vector<char>& done, DevBuf& vbuf, DevBuf& rbuf, GmresGraphs* graphs) {
   Operator& op = sv.op_;
   cudaStream_t st = op.stream;
   const uint32_t nsys = sv.nsys_;
@@ -284,35 +386,75 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
   const uint64_t vstride = total;
   const uint32_t* sid = sv.segid();
   int rc;
+  if ((rc = op.prepare(prec))) return rc;
   if ((rc = vbuf.reserve((size_t)(m + 1) * total * sizeof(double)))) return rc;
   if ((rc = rbuf.reserve(total * sizeof(double)))) return rc;
   double* V = vbuf.as<double>();
   double* r = rbuf.as<double>();
   const uint32_t K = sv.maxk_;  // >= m + 1
-  double* dsmall = sv.small_.as<double>();
-  double* dsmall2 = sv.small2_.as<double>();
-  std::vector<double> hbuf((size_t)nsys * K), nbuf((size_t)nsys * K);
-  auto fetch = [&](double* dev, std::vector<double>& host, uint32_t nk) -> int {
-    (void)nk;
-    AHX_CUDA(cudaMemcpyAsync(host.data(), dev, (size_t)nsys * K * sizeof(double),
-                             cudaMemcpyDeviceToHost, st));
+  double* d1 = sv.small_.as<double>();
+  double* d2 = sv.small2_.as<double>();
+  double* d3 = sv.small3_.as<double>();
+  // device state
+  const size_t nd = (size_t)nsys * ((size_t)m * K + 4 * (size_t)K + 2) + 1;  // R, cs, sn, s, y, normb, resid, tol
+  const size_t nu = (size_t)nsys * 3 + 3;                                    // flags, ylen, iters, jbase, nactive, maxit
+  if ((rc = sv.gm_.reserve(nd * sizeof(double) + nu * sizeof(uint32_t)))) return rc;
+  GmDev g;
+  {
+    double* p = sv.gm_.as<double>();
+    g.R = p;
+    p += (size_t)nsys * m * K;
+    g.cs = p;
+    p += (size_t)nsys * K;
+    g.sn = p;
+    p += (size_t)nsys * K;
+    g.s = p;
+    p += (size_t)nsys * K;
+    g.y = p;
+    p += (size_t)nsys * K;
+    g.normb = p;
+    p += nsys;
+    g.resid = p;
+    p += nsys;
+    double* ptol = p;
+    p += 1;
+    uint32_t* u = reinterpret_cast<uint32_t*>(p);
+    g.flags = u;
+    g.ylen = u + nsys;
+    g.iters = u + 2 * (size_t)nsys;
+    g.jbase = u + 3 * (size_t)nsys;
+    g.nactive = g.jbase + 1;
+    uint32_t* pmaxit = g.jbase + 2;
+    g.tol = ptol;
+    g.maxit = pmaxit;
+    AHX_CUDA(cudaMemcpyAsync(ptol, &tol, sizeof(double), cudaMemcpyHostToDevice, st));
+    AHX_CUDA(cudaMemcpyAsync(pmaxit, &maxit, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  }
+  std::vector<double> hbuf((size_t)nsys * K);
+  auto fetch = [&](const double* dev) -> int {
+    AHX_CUDA(cudaMemcpyAsync(hbuf.data(), dev, (size_t)nsys * K * sizeof(double), cudaMemcpyDeviceToHost, st));
     AHX_CUDA(cudaStreamSynchronize(st));
     return AHX_OK;
   };
   // normb
-  if ((rc = sv.dots(B, 0, 1, B, dsmall))) return rc;
-  if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+  if ((rc = sv.dots(B, 0, 1, B, d1))) return rc;
+  if ((rc = fetch(d1))) return rc;
   std::vector<double> normb(nsys);
-  for (uint32_t q = 0; q < nsys; ++q) normb[q] = std::sqrt(nbuf[(size_t)q * K]);
-  // r = b - A x
+  for (uint32_t q = 0; q < nsys; ++q) normb[q] = std::sqrt(hbuf[(size_t)q * K]);
+  AHX_CUDA(cudaMemcpyAsync(g.normb, normb.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+  // r = b - A x (no product for a zero initial guess: r = b)
+  if ((rc = sv.dots(X, 0, 1, X, d1))) return rc;
+  if ((rc = fetch(d1))) return rc;
+  bool x_zero = true;
+  for (uint32_t q = 0; q < nsys; ++q) x_zero = x_zero && hbuf[(size_t)q * K] == 0.0;
   AHX_CUDA(cudaMemcpyAsync(r, B, total * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  if ((rc = op.apply(prec, -1.0, sv.p_, X, r))) return rc;
-  if ((rc = sv.dots(r, 0, 1, r, dsmall))) return rc;
-  if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+  if (!x_zero && (rc = op.apply(prec, -1.0, sv.p_, X, r))) return rc;
+  if ((rc = sv.dots(r, 0, 1, r, d1))) return rc;
+  if ((rc = fetch(d1))) return rc;
   std::vector<double> beta(nsys);
   std::vector<double> zero_fix(nsys, 0.0);
   for (uint32_t q = 0; q < nsys; ++q) {
-    beta[q] = std::sqrt(nbuf[(size_t)q * K]);
+    beta[q] = std::sqrt(hbuf[(size_t)q * K]);
     if (done[q]) continue;
     if (normb[q] == 0.0) {
       // x = 0 (solvers/GMRES.cpp:96-103)
@@ -332,105 +474,127 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
   if (std::any_of(zero_fix.begin(), zero_fix.end(), [](double v) { return v != 0.0; })) {
     std::vector<double> f(nsys);
     for (uint32_t q = 0; q < nsys; ++q) f[q] = zero_fix[q] != 0.0 ? 0.0 : 1.0;
-    AHX_CUDA(cudaMemcpyAsync(dsmall2, f.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
-    scale_kernel<<<grid_for(total), 256, 0, st>>>(X, X, dsmall2, 1, 0, total, op.ntot, sid, op.nseg);
+    AHX_CUDA(cudaMemcpyAsync(d2, f.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(total), 256, 0, st>>>(X, X, d2, 1, 0, total, op.ntot, sid, op.nseg);
   }
-  std::vector<double> Hm((size_t)nsys * (m + 1) * m), cs((size_t)nsys * (m + 1)),
-      sn((size_t)nsys * (m + 1)), s((size_t)nsys * (m + 1));
-  std::vector<double> ycoef((size_t)nsys * K, 0.0);
-  std::vector<uint32_t> ylen(nsys, 0);
-  uint32_t j = 1;
   auto active_left = [&]() {
     for (uint32_t q = 0; q < nsys; ++q)
       if (!done[q]) return true;
     return false;
   };
-  // solve H y = s (upper triangular, column oriented as dtrsv) for system q with k columns
-  auto tri_solve = [&](uint32_t q, uint32_t k) {
-    const double* Hq = Hm.data() + (size_t)q * (m + 1) * m;
-    double* y = ycoef.data() + (size_t)q * K;
-    for (uint32_t i = 0; i < k; ++i) y[i] = s[(size_t)q * (m + 1) + i];
-    for (int jj = (int)k - 1; jj >= 0; --jj) {
-      y[jj] /= Hq[jj + (size_t)jj * (m + 1)];
-      for (int i = 0; i < jj; ++i) y[i] -= y[jj] * Hq[i + (size_t)jj * (m + 1)];
-    }
-    ylen[q] = k;
-  };
-  while (active_left() && j <= maxit) {
-    // V_0 = r / beta
-    for (uint32_t q = 0; q < nsys; ++q) nbuf[q] = done[q] ? 0.0 : beta[q] * beta[q];
-    AHX_CUDA(cudaMemcpyAsync(dsmall2, nbuf.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
-    scale_kernel<<<grid_for(total), 256, 0, st>>>(V, r, dsmall2, 1, 1, total, op.ntot, sid, op.nseg);
-    std::vector<char> cyc(nsys);
-    for (uint32_t q = 0; q < nsys; ++q) {
-      cyc[q] = !done[q];
-      s[(size_t)q * (m + 1)] = beta[q];
-      for (uint32_t i = 1; i <= m; ++i) s[(size_t)q * (m + 1) + i] = 0.0;
-      ylen[q] = 0;
-    }
-    uint32_t i = 0;
-    for (; i < m && j <= maxit; i++, j++) {
+  const unsigned sgrid = (nsys + 127) / 128;
+  // steps i0 .. i1 - 1 of a cycle, then the count of systems still running
+  auto steps = [&](uint32_t i0, uint32_t i1) -> int {
+    for (uint32_t i = i0; i < i1; ++i) {
       double* vi = V + (size_t)i * vstride;
       double* w = V + (size_t)(i + 1) * vstride;
       AHX_CUDA(cudaMemsetAsync(w, 0, total * sizeof(double), st));
-      if ((rc = op.apply(prec, 1.0, sv.p_, vi, w))) return rc;
+      int e = op.apply(prec, 1.0, sv.p_, vi, w);
+      if (e) return e;
       // CGS2: h = V^T w; w -= V h; h2 = V^T w; w -= V h2
-      if ((rc = sv.dots(V, vstride, i + 1, w, dsmall))) return rc;
-      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, dsmall, K,
-                                                              total, op.ntot, sid, op.nseg);
-      if ((rc = sv.dots(V, vstride, i + 1, w, dsmall2))) return rc;
-      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, dsmall2, K,
-                                                              total, op.ntot, sid, op.nseg);
-      std::vector<double> h1((size_t)nsys * K), h2((size_t)nsys * K);
-      if ((rc = fetch(dsmall, h1, i + 1))) return rc;
-      if ((rc = fetch(dsmall2, h2, i + 1))) return rc;
-      if ((rc = sv.dots(w, 0, 1, w, dsmall))) return rc;
-      if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+      if ((e = sv.dots(V, vstride, i + 1, w, d1))) return e;
+      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, d1, K, total, op.ntot, sid,
+                                                              op.nseg);
+      if ((e = sv.dots(V, vstride, i + 1, w, d2))) return e;
+      sub_combination_kernel<<<grid_for(total), 256, 0, st>>>(w, V, vstride, i + 1, d2, K, total, op.ntot, sid,
+                                                              op.nseg);
+      if ((e = sv.dots(w, 0, 1, w, d3))) return e;
+      arnoldi_kernel<<<sgrid, 128, 0, st>>>(g, i, m, K, d1, d2, d3, nsys);
       // w /= |w|
-      scale_kernel<<<grid_for(total), 256, 0, st>>>(w, w, dsmall, K, 1, total, op.ntot, sid, op.nseg);
-      AHX_CUDA(cudaGetLastError());
-      for (uint32_t q = 0; q < nsys; ++q) {
-        if (!cyc[q] || done[q]) continue;
-        double* Hq = Hm.data() + (size_t)q * (m + 1) * m;
-        double* col = Hq + (size_t)i * (m + 1);
-        for (uint32_t k = 0; k <= i; ++k) col[k] = h1[(size_t)q * K + k] + h2[(size_t)q * K + k];
-        col[i + 1] = std::sqrt(nbuf[(size_t)q * K]);
-        double* csq = cs.data() + (size_t)q * (m + 1);
-        double* snq = sn.data() + (size_t)q * (m + 1);
-        double* sq = s.data() + (size_t)q * (m + 1);
-        for (uint32_t k = 0; k < i; k++) appl_rot(col[k], col[k + 1], csq[k], snq[k]);
-        gen_rot(col[i], col[i + 1], csq[i], snq[i]);
-        appl_rot(col[i], col[i + 1], csq[i], snq[i]);
-        appl_rot(sq[i], sq[i + 1], csq[i], snq[i]);
-        resid[q] = std::fabs(sq[i + 1] / normb[q]);
-        iters[q] = j;
-        if (resid[q] < tol) {
-          tri_solve(q, i + 1);
-          done[q] = 1;
-        }
-      }
+      scale_kernel<<<grid_for(total), 256, 0, st>>>(w, w, d3, K, 1, total, op.ntot, sid, op.nseg);
     }
-    // systems still running: update with the i vectors of this cycle
-    for (uint32_t q = 0; q < nsys; ++q)
-      if (cyc[q] && !done[q] && i > 0) tri_solve(q, i);
-    AHX_CUDA(cudaMemcpyAsync(sv.small_.p, ycoef.data(), (size_t)nsys * K * sizeof(double),
-                             cudaMemcpyHostToDevice, st));
-    AHX_CUDA(cudaMemcpyAsync(sv.len_.p, ylen.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    add_combination_kernel<<<grid_for(total), 256, 0, st>>>(X, V, vstride, sv.len_.as<uint32_t>(),
-                                                            sv.small_.as<double>(), K, total,
-                                                            op.ntot, sid, op.nseg);
+    count_active_kernel<<<1, 256, 0, st>>>(g, nsys);
     AHX_CUDA(cudaGetLastError());
-    if (!active_left()) break;
+    return AHX_OK;
+  };
+  if (graphs && (graphs->prec != prec || graphs->vptr != V || graphs->m != m)) {
+    graphs->reset();
+    graphs->prec = prec;
+    graphs->vptr = V;
+    graphs->m = m;
+  }
+  auto run_chunk = [&](uint32_t c, uint32_t i0, uint32_t i1) -> int {
+    if (!graphs || graphs->failed) return steps(i0, i1);
+    if (graphs->exec.size() <= c) graphs->exec.resize(c + 1, nullptr);
+    if (!graphs->exec[c]) {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        graphs->failed = true;
+        return steps(i0, i1);
+      }
+      const int e = steps(i0, i1);
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      cudaGraphExec_t ex = nullptr;
+      if (e || ce != cudaSuccess || !graph || cudaGraphInstantiate(&ex, graph, 0) != cudaSuccess) {
+        // nothing ran while capturing: launch the same steps directly from now on
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        graphs->failed = true;
+        return steps(i0, i1);
+      }
+      cudaGraphDestroy(graph);
+      graphs->exec[c] = ex;
+    }
+    AHX_CUDA(cudaGraphLaunch(graphs->exec[c], st));
+    return AHX_OK;
+  };
+  uint32_t j = 1;  // global number of the next step
+  std::vector<uint32_t> flags(nsys), hiters(nsys);
+  std::vector<double> hres(nsys);
+  while (active_left() && j <= maxit) {
+    // V_0 = r / beta; a cycle of at most m steps for the running systems
+    for (uint32_t q = 0; q < nsys; ++q) hbuf[q] = done[q] ? 0.0 : beta[q] * beta[q];
+    AHX_CUDA(cudaMemcpyAsync(d2, hbuf.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(total), 256, 0, st>>>(V, r, d2, 1, 1, total, op.ntot, sid, op.nseg);
+    std::fill(hbuf.begin(), hbuf.end(), 0.0);
+    for (uint32_t q = 0; q < nsys; ++q) {
+      hbuf[(size_t)q * K] = beta[q];
+      flags[q] = done[q] ? 0u : 1u;
+    }
+    AHX_CUDA(cudaMemcpyAsync(g.s, hbuf.data(), (size_t)nsys * K * sizeof(double), cudaMemcpyHostToDevice, st));
+    AHX_CUDA(cudaMemcpyAsync(g.flags, flags.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    AHX_CUDA(cudaMemsetAsync(g.ylen, 0, nsys * sizeof(uint32_t), st));
+    const uint32_t jb = j - 1;
+    AHX_CUDA(cudaMemcpyAsync(g.jbase, &jb, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    const uint32_t icap = std::min(m, maxit - jb);  // steps this cycle may count
+    uint32_t ran = 0;
+    for (uint32_t c = 0; c * kGraphChunk < icap; ++c) {
+      const uint32_t i0 = c * kGraphChunk, i1 = std::min(m, i0 + kGraphChunk);
+      if ((rc = run_chunk(c, i0, i1))) return rc;
+      ran = std::min(i1, icap);
+      uint32_t nact = 0;
+      AHX_CUDA(cudaMemcpyAsync(&nact, g.nactive, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      AHX_CUDA(cudaStreamSynchronize(st));
+      if (nact == 0) break;
+    }
+    cycle_end_kernel<<<sgrid, 128, 0, st>>>(g, ran, m, K, nsys);
+    add_combination_kernel<<<grid_for(total), 256, 0, st>>>(X, V, vstride, g.ylen, g.y, K, total, op.ntot, sid,
+                                                            op.nseg);
+    AHX_CUDA(cudaGetLastError());
+    j = jb + ran + 1;
+    AHX_CUDA(cudaMemcpyAsync(flags.data(), g.flags, nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaMemcpyAsync(hiters.data(), g.iters, nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaMemcpyAsync(hres.data(), g.resid, nsys * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t q = 0; q < nsys; ++q) {
+      if (!(flags[q] & 1u)) continue;
+      iters[q] = hiters[q];
+      resid[q] = hres[q];
+      if (flags[q] & 2u) done[q] = 1;
+    }
+    if (!active_left() || j > maxit) break;
     // r = b - A x for the running systems
     AHX_CUDA(cudaMemcpyAsync(r, B, total * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if ((rc = op.apply(prec, -1.0, sv.p_, X, r))) return rc;
-    if ((rc = sv.dots(r, 0, 1, r, dsmall))) return rc;
-    if ((rc = fetch(dsmall, nbuf, 1))) return rc;
+    if ((rc = sv.dots(r, 0, 1, r, d1))) return rc;
+    if ((rc = fetch(d1))) return rc;
     for (uint32_t q = 0; q < nsys; ++q) {
       if (done[q]) continue;
-      beta[q] = std::sqrt(nbuf[(size_t)q * K]);
+      beta[q] = std::sqrt(hbuf[(size_t)q * K]);
       resid[q] = beta[q] / normb[q];
       if (resid[q] < tol) {
+        // the step count after the cycle, as solvers/GMRES.cpp:168-172 reports it
         done[q] = 1;
         iters[q] = j;
       }
@@ -456,8 +620,9 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
   std::vector<double> resid(nsys, 0.0);
   std::vector<char> done(nsys, 0);
   DevBuf vbuf, rbuf, rr, z;
+  GmresGraphs graphs[3];  // per operator precision
   if (prec == kFP64) {
-    rc = gmres_core(sv, kFP64, B, X, tol, m, maxit, iters, resid, done, vbuf, rbuf);
+    rc = gmres_core(sv, kFP64, B, X, tol, m, maxit, iters, resid, done, vbuf, rbuf, &graphs[kFP64]);
   } else {
     // FP64 refinement: r = b - A64 x (FP64 leaves), solve A_prec z = r by one
     // GMRES(m) cycle to an inner tolerance, x += z.
@@ -465,7 +630,9 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     if ((rc = rr.reserve(total * sizeof(double)))) return rc;
     if ((rc = z.reserve(total * sizeof(double)))) return rc;
     cudaStream_t st = op.stream;
-    const double inner_tol = prec == kFP32 ? 1e-6 : 1e-2;
+    // inner tolerance near the storage precision's product accuracy (FP32
+    // ~3e-7, BF16 factors ~4e-4): fewer outer steps, i.e. fewer FP64 products
+    const double inner_tol = prec == kFP32 ? 1e-6 : 1e-3;
     std::vector<double> normb(nsys), nb((size_t)nsys * sv.maxk_);
     if ((rc = sv.dots(B, 0, 1, B, sv.small_.as<double>()))) return rc;
     AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -479,9 +646,16 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     int inner_prec = prec;
     bool undone = false;  // the residual just recomputed follows an undo: accept it
     std::vector<double> prev(nsys, INFINITY), undo(nsys, 0.0);
+    // a zero initial guess needs no product for the first residual
+    if ((rc = sv.dots(X, 0, 1, X, sv.small_.as<double>()))) return rc;
+    AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
+    AHX_CUDA(cudaStreamSynchronize(st));
+    bool x_zero = true;
+    for (uint32_t q = 0; q < nsys; ++q) x_zero = x_zero && nb[(size_t)q * sv.maxk_] == 0.0;
     for (;;) {
       AHX_CUDA(cudaMemcpyAsync(rr.p, B, total * 8, cudaMemcpyDeviceToDevice, st));
-      if ((rc = op.apply(kFP64, -1.0, p, X, rr.as<double>()))) return rc;
+      if (!x_zero && (rc = op.apply(kFP64, -1.0, p, X, rr.as<double>()))) return rc;
+      x_zero = false;
       if ((rc = sv.dots(rr.as<double>(), 0, 1, rr.as<double>(), sv.small_.as<double>()))) return rc;
       AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
       AHX_CUDA(cudaStreamSynchronize(st));
@@ -530,7 +704,7 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
       const uint32_t budget = std::min(m, maxit - used);
       if ((rc = gmres_core(sv, inner_prec, rr.as<double>(), z.as<double>(),
                            inner_prec == kFP64 ? std::max(tol, 1e-12) : inner_tol, m, budget, it2, res2,
-                           idone, vbuf, rbuf)))
+                           idone, vbuf, rbuf, &graphs[inner_prec])))
         return rc;
       uint32_t step = 0;
       for (uint32_t q = 0; q < nsys; ++q)

@@ -246,7 +246,7 @@ def run_gpu(args):
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("mv_kernel_fp32_16rhs_c2")
+            traffic = json.load(open(prof)).get("tc_product_fp32_16rhs_sphere65536")
         except Exception:
             traffic = None
     value = ws * NRHS / (ms32 * 1e-3)
