@@ -395,6 +395,96 @@ def run_large(args):
     print(json.dumps(out))
 
 
+def run_product(args):
+    """Products only (profiling cases): `--geometry` sphere (Fibonacci) or cube (random
+    surface, seed 4), `--n` points, `--leaf`, `--rhs`, `--precision`; assembly with the
+    mean nearest-neighbour diagonal, then `--warmup` + `--steps` products Y += A X."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n = args.n
+    P = A.geometry.cube_surface(n, 4) if args.geometry == "cube" else A.geometry.fibonacci_sphere(n)
+    H = A.HMatrix(P, "bbx", bmin=args.leaf, eta=ETA, device=0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    H.set_stream(stream.cuda_stream)
+    H.matgenGeH_omp(A.mean_nn(P), EPS)
+    H.prepare(args.precision)
+    X = torch.from_numpy(np.random.default_rng(1).uniform(-1.0, 1.0, (args.rhs, n))).to(dev)
+    Y = torch.zeros_like(X)
+    for _ in range(args.warmup):
+        H.mltaGeHVec(1.0, X, Y, precision=args.precision)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        H.mltaGeHVec(1.0, X, Y, precision=args.precision)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    b = algorithmic_bytes(H, args.precision, args.rhs)
+    print(json.dumps({"workload": f"laplace-{args.geometry}-{n}-{args.rhs}rhs-{args.precision}", "ms": ms,
+                      "algorithmic_bytes": b, "achieved_gbs": b / (ms * 1e-3) / 1e9}))
+
+
+def run_predictor(args):
+    """Learned rank predictor: trains the 8-64-64-1 network on the GPU on (feature, ACA rank)
+    pairs of five assembled H-matrices (spheres, an ellipsoid, a cube surface; leaf 32, eta 0.8,
+    eps 1e-6), then assembles two held-out N = 65,536 matrices with and without rank hints."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    G = A.geometry
+    train = []
+    for n, geo in [(3000, "s"), (5000, "e"), (8000, "s"), (16384, "c"), (32768, "s")]:
+        P = G.fibonacci_sphere(n) if geo == "s" else (G.ellipsoid_surface(n, n) if geo == "e" else G.cube_surface(n, n))
+        train.append(A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA).matgenGeH_omp(A.mean_nn(P), EPS))
+    X, r = A.training_set(train, EPS)
+    M = A.RankPredictor(seed=0)
+    t0 = time.perf_counter()
+    losses = M.fit(X, r, epochs=60, batch=512, lr=3e-3)
+    t_train = time.perf_counter() - t0
+    out = {"workload": "rank-predictor", "train_pairs": int(len(r)), "train_s": t_train,
+           "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1])}
+    for name, P in [("ellipsoid-65536", G.ellipsoid_surface(65536, 5, (1.0, 0.7, 0.4))),
+                    ("sphere-65536", G.fibonacci_sphere(65536))]:
+        h = A.mean_nn(P)
+        H0 = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+        H0.matgenGeH_omp(h, EPS)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H0.matgenGeH_omp(h, EPS)
+        torch.cuda.synchronize()
+        t_plain = time.perf_counter() - t0
+        a0, st0, lv = H0.aca_ranks(), H0.assembly_stats(), H0.leaves()
+        t0 = time.perf_counter()
+        pred = M.predict(H0.features(EPS))
+        t_pred = time.perf_counter() - t0
+        adm = (lv[:, 4] == 1) & (a0 >= 0)
+        rel = np.abs(pred[adm] - a0[adm]) / np.maximum(a0[adm], 1)
+        H1 = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+        hint = np.where(lv[:, 4] == 1, pred, -1.0)
+        H1.assemble_hinted(h, EPS, hint)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H1.assemble_hinted(h, EPS, hint)
+        torch.cuda.synchronize()
+        t_hint = time.perf_counter() - t0
+        st1 = H1.assembly_stats()
+        out[name] = {"identical_ranks": bool((H1.aca_ranks() == a0).all() and (H1.ranks() == H0.ranks()).all()),
+                     "median_rel_rank_err": float(np.median(rel)), "p90_rel_rank_err": float(np.percentile(rel, 90)),
+                     "plain": {"assembly_s": t_plain, "workspace_bytes": st0[0], "retries": st0[1], "batches": st0[2]},
+                     "hinted": {"assembly_s": t_hint, "workspace_bytes": st1[0], "retries": st1[1], "batches": st1[2],
+                                "predict_s": t_pred}}
+        H0.close()
+        H1.close()
+    print(json.dumps(out))
+
+
 def run_batch(args):
     """Many uneven H-matrices in one launch: `--instances` instances (256), N log-uniform
     in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
@@ -466,11 +556,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor"],
                     help="sphere: the default product benchmark; cube-large: N = 2^20 "
                          "cube surface, 64 right-hand sides, products and GMRES; batch: "
                          "256 uneven instances, one launch per product, batched GMRES")
     ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--geometry", default="sphere", choices=["sphere", "cube"], help="product workload")
+    ap.add_argument("--leaf", type=int, default=BMIN, help="product workload")
+    ap.add_argument("--rhs", type=int, default=NRHS, help="product workload")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp64"], help="product workload")
     ap.add_argument("--n-large", type=int, default=1 << 20)
     ap.add_argument("--diag", default="mean", choices=["mean", "min"],
                     help="cube-large / batch: h = mean (configured) or minimum nearest-neighbour "
@@ -490,6 +584,10 @@ def main():
         run_large(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "product":
+        run_product(args)
+    elif args.workload == "predictor":
+        run_predictor(args)
     else:
         run_gpu(args)
 
