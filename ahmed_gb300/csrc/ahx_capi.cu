@@ -16,37 +16,10 @@ namespace ahx {
 namespace {
 thread_local std::string g_err;
 
-// Workspace budget of one ACA batch (bytes); AHX_ACA_WS_BYTES overrides.
-size_t aca_ws_budget() {
-  const char* e = std::getenv("AHX_ACA_WS_BYTES");
-  if (e && *e) return (size_t)std::strtoull(e, nullptr, 10);
-  return (size_t)4 << 30;
-}
-
-// first capacity of the ACA rank workspace per leaf; AHX_ACA_KCAP overrides
-uint32_t aca_kcap_default() {
-  const char* e = std::getenv("AHX_ACA_KCAP");
-  if (e && *e) return std::max<uint32_t>(1u, (uint32_t)std::strtoul(e, nullptr, 10));
-  return 48u;
-}
 // leaves with more rows or columns than this use the CTA-per-leaf kernel; the
 // rest run one warp per leaf (warp reductions; the FP64 pipe is the limit)
 constexpr uint32_t kLargeLeaf = 4096;
 
-template <class T>
-int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
-  if (v.empty()) return AHX_OK;
-  int rc = b.reserve(v.size() * sizeof(T));
-  if (rc) return rc;
-  AHX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-  return AHX_OK;
-}
-
-uint32_t maxk_of(uint32_t n1, uint32_t n2, uint32_t rankmax) {
-  // unsigned arithmetic as in Include/apprx.h:143-144
-  uint32_t maxk = (uint32_t)(n1 * n2) / (n1 + n2) + 4u;
-  return maxk > rankmax ? rankmax : maxk;
-}
 
 // Append-only growable FP64 arena.
 int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {

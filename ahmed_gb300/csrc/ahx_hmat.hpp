@@ -2,7 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -50,6 +52,35 @@ struct ProdCopy {
     nleaves = nvunits = nrunits = grid = t_rows = ntreduce = 0;
   }
 };
+
+// Workspace budget of one ACA batch (bytes); AHX_ACA_WS_BYTES overrides.
+inline size_t aca_ws_budget() {
+  const char* e = std::getenv("AHX_ACA_WS_BYTES");
+  if (e && *e) return (size_t)std::strtoull(e, nullptr, 10);
+  return (size_t)4 << 30;
+}
+
+// first capacity of the ACA rank workspace per leaf; AHX_ACA_KCAP overrides
+inline uint32_t aca_kcap_default() {
+  const char* e = std::getenv("AHX_ACA_KCAP");
+  if (e && *e) return std::max<uint32_t>(1u, (uint32_t)std::strtoul(e, nullptr, 10));
+  return 48u;
+}
+
+// ACA rank bound of a leaf: unsigned arithmetic as in Include/apprx.h:143-144
+inline uint32_t maxk_of(uint32_t n1, uint32_t n2, uint32_t rankmax) {
+  uint32_t maxk = (uint32_t)(n1 * n2) / (n1 + n2) + 4u;
+  return maxk > rankmax ? rankmax : maxk;
+}
+
+template <class T>
+int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+  if (v.empty()) return AHX_OK;
+  int rc = b.reserve(v.size() * sizeof(T));
+  if (rc) return rc;
+  AHX_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return AHX_OK;
+}
 
 // Builds the streams of a mixed precision from FP64 leaves (offsets into arena64).
 int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,

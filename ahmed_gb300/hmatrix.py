@@ -165,6 +165,15 @@ class HMatrix:
         check(lib().ahx_hmat_assembly_stats(self._h, ptr(out)))
         return tuple(int(v) for v in out)
 
+    def helmholtz_aca_ranks(self, wavenumber, h, eps, rankmax=2**32 - 1, rank_hint=None):
+        """Complex ACA ranks of the Helmholtz matrix exp(ikr)/(4 pi r) per leaf
+        (-1 inadmissible, -2 ACA failed); bounding-box trees."""
+        out = np.zeros(self.nleaves, np.int32)
+        hint = None if rank_hint is None else np.ascontiguousarray(rank_hint, dtype=np.float32)
+        check(lib().ahx_helm_aca_ranks(self._h, float(wavenumber), float(h), float(eps),
+                                       min(int(rankmax), 2**32 - 1), ptr(hint), ptr(out)))
+        return out
+
     def features(self, eps, wavenumber=0.0):
         out = np.zeros((self.nleaves, 8), np.float32)
         check(lib().ahx_hmat_features(self._h, float(wavenumber), float(eps), ptr(out)))

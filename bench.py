@@ -485,6 +485,69 @@ def run_predictor(args):
     print(json.dumps(out))
 
 
+def run_helmholtz(args):
+    """Rank predictor on the Helmholtz kernel exp(ikr)/(4 pi r) (diagonal exp(ikh)/(4 pi h)):
+    (feature, complex-ACA rank) pairs from Fibonacci spheres at N = 16,384 / 65,536 / 131,072
+    with wavenumbers k ~ U[1, 20] (numpy PCG64 seed 7), eps 1e-6, leaf 32, eta 0.8; the MLP is
+    trained on the GPU; then complex ACA with and without predicted ranks on held-out
+    matrices (random sphere points, N = 65,536, k = 3.7 and 16.2)."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    G = A.geometry
+    rng = np.random.default_rng(7)
+    Xs, ys = [], []
+    t0 = time.perf_counter()
+    for n, nk in [(16384, 12), (65536, 5), (131072, 3)]:
+        P = G.fibonacci_sphere(n)
+        h = A.mean_nn(P)
+        H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+        lv = H.leaves()
+        for k in rng.uniform(1.0, 20.0, nk):
+            r = H.helmholtz_aca_ranks(k, h, EPS)
+            sel = (lv[:, 4] == 1) & (r >= 0)
+            Xs.append(H.features(EPS, wavenumber=k)[sel])
+            ys.append(r[sel])
+        H.close()
+    t_data = time.perf_counter() - t0
+    X, y = np.concatenate(Xs), np.concatenate(ys)
+    M = A.RankPredictor(seed=0)
+    t0 = time.perf_counter()
+    losses = M.fit(X, y, epochs=30, batch=1024, lr=2e-3)
+    t_train = time.perf_counter() - t0
+    out = {"workload": "helmholtz-rank-predictor", "train_pairs": int(len(y)), "pairs_s": t_data,
+           "train_s": t_train, "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1])}
+    P = G.sphere_surface(65536, 17)
+    h = A.mean_nn(P)
+    H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+    lv = H.leaves()
+    for k in (3.7, 16.2):
+        H.helmholtz_aca_ranks(k, h, EPS)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r0 = H.helmholtz_aca_ranks(k, h, EPS)
+        t_plain = time.perf_counter() - t0
+        st0 = H.assembly_stats()
+        t0 = time.perf_counter()
+        pred = M.predict(H.features(EPS, wavenumber=k))
+        t_pred = time.perf_counter() - t0
+        hint = np.where(lv[:, 4] == 1, pred, -1.0)
+        t0 = time.perf_counter()
+        r1 = H.helmholtz_aca_ranks(k, h, EPS, rank_hint=hint)
+        t_hint = time.perf_counter() - t0
+        st1 = H.assembly_stats()
+        adm = (lv[:, 4] == 1) & (r0 >= 0)
+        rel = np.abs(pred[adm] - r0[adm]) / np.maximum(r0[adm], 1)
+        out[f"k{k:g}"] = {"identical_ranks": bool((r0 == r1).all()), "mean_rank": float(r0[adm].mean()),
+                          "median_rel_rank_err": float(np.median(rel)), "p90_rel_rank_err": float(np.percentile(rel, 90)),
+                          "plain": {"aca_s": t_plain, "workspace_bytes": st0[0], "retries": st0[1], "batches": st0[2]},
+                          "hinted": {"aca_s": t_hint, "predict_s": t_pred, "workspace_bytes": st1[0],
+                                     "retries": st1[1], "batches": st1[2]}}
+    H.close()
+    print(json.dumps(out))
+
+
 def run_batch(args):
     """Many uneven H-matrices in one launch: `--instances` instances (256), N log-uniform
     in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
@@ -556,7 +619,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz"],
                     help="sphere: the default product benchmark; cube-large: N = 2^20 "
                          "cube surface, 64 right-hand sides, products and GMRES; batch: "
                          "256 uneven instances, one launch per product, batched GMRES")
@@ -588,6 +651,8 @@ def main():
         run_product(args)
     elif args.workload == "predictor":
         run_predictor(args)
+    elif args.workload == "helmholtz":
+        run_helmholtz(args)
     else:
         run_gpu(args)
 

@@ -90,6 +90,15 @@ int ahx_hmat_assembly_stats(const ahx_hmat* H, uint64_t* out3);
  * log diam1, log diam2, log centre distance, min diam / distance, log n1,
  * log n2, wavenumber * max diam, -log10(eps) (diam: Include/cluster.h:194) */
 int ahx_hmat_features(const ahx_hmat* H, double wavenumber, double eps, float* out);
+
+/* Helmholtz exp(i k r) / (4 pi r) (diagonal exp(i k h) / (4 pi h)): complex
+ * ACA of every admissible leaf with the reference's ACA<dcomp> stopping rule
+ * (Include/ACA.h:217-350), ranks[l] = rank (-1 inadmissible, -2 ACA failed).
+ * rank_hint (may be NULL; negative: none) sizes the workspaces as in
+ * ahx_assemble_hinted; ahx_hmat_assembly_stats reports the batches.
+ * Bounding-box trees (ACA start row 0). */
+int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax,
+                       const float* rank_hint, int32_t* ranks);
 /* per leaf: rank after recompression, -1 for dense leaves (mblock::isLrM/rank) */
 int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks);
 /* per leaf: ACA rank before recompression, -1 for dense */

@@ -194,6 +194,7 @@ def ref():
         L.ref_entry.restype = dbl
         L.ref_entry.argtypes = [vp, u32, u32]
         L.ref_free.argtypes = [vp]
+        L.ref_helm_ranks.argtypes = [vp, dbl, dbl, dbl, u32, vp]
         _ref = L
     return _ref
 
@@ -228,6 +229,12 @@ class RefH:
 
     def assemble(self, eps, rankmax=2**32 - 1, nthreads=0):
         ref().ref_assemble(self._H, eps, rankmax, nthreads)
+
+    def helmholtz_aca_ranks(self, wavenumber, h, eps, rankmax=2**32 - 1):
+        """Complex ACA ranks of the Helmholtz matrix per leaf (-1 inadmissible, -2 failed)."""
+        out = np.zeros(self.nleaves, np.int32)
+        ref().ref_helm_ranks(self._H, wavenumber, h, eps, rankmax, _p(out))
+        return out
 
     def ranks(self):
         out = np.zeros(self.nleaves, np.int32)

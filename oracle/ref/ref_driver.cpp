@@ -57,6 +57,31 @@ struct LaplaceGen {
   }
 };
 
+// Helmholtz single-layer collocation generator (complex): exp(i k r) / (4 pi r),
+// exp(i k h) / (4 pi h) on the diagonal.
+struct HelmGen {
+  const Pt* dofs;
+  const unsigned* op_perm;
+  double h, k;
+  dcomp entry(unsigned i, unsigned j) const {
+    const unsigned a = op_perm[i], b = op_perm[j];
+    double r = h;
+    if (a != b) {
+      const double dx = dofs[a].c[0] - dofs[b].c[0];
+      const double dy = dofs[a].c[1] - dofs[b].c[1];
+      const double dz = dofs[a].c[2] - dofs[b].c[2];
+      r = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    const double s = 1.0 / (4.0 * M_PI * r);
+    return dcomp(cos(k * r) * s, sin(k * r) * s);
+  }
+  void cmpbl(unsigned b1, unsigned n1, unsigned b2, unsigned n2, dcomp* data) const {
+    for (unsigned j = 0; j < n2; ++j)
+      for (unsigned i = 0; i < n1; ++i) data[i + j * n1] = entry(b1 + i, b2 + j);
+  }
+  double scale(unsigned b1, unsigned, unsigned b2, unsigned) const { return abs(entry(b1, b2)); }
+};
+
 struct RefH {
   unsigned n = 0, kind = 0;
   std::vector<Pt> dofs;
@@ -238,6 +263,29 @@ unsigned ref_cg(void* p, double* b, double* x, double* eps, unsigned* nsteps) {
 
 // one generator entry in permuted order (for dense checks)
 double ref_entry(void* p, unsigned i, unsigned j) { return ((RefH*)p)->gen.entry(i, j); }
+
+// ACA ranks of the Helmholtz matrix (bounding-box trees: start row 0), the
+// reference's complex ::ACA (Include/ACA.h:217-350 with T = dcomp) per
+// admissible leaf: out[l] = k on success, -2 when ACA fails, -1 inadmissible.
+void ref_helm_ranks(void* p, double wavenumber, double h, double eps, unsigned rankmax, int* out) {
+  RefH* H = (RefH*)p;
+  HelmGen gen{H->dofs.data(), H->op_perm.data(), h, wavenumber};
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long l = 0; l < (long)H->nblcks; ++l) {
+    blcluster* bl = H->leaves[l];
+    out[l] = -1;
+    const unsigned n1 = bl->getn1(), n2 = bl->getn2();
+    unsigned maxk = n1 * n2 / (n1 + n2) + 4;
+    if (maxk > rankmax) maxk = rankmax;
+    if (!bl->isadm() || !maxk) continue;
+    unsigned k = 0;
+    dcomp *U, *V;
+    const bool succ = ::ACA(gen, bl->getb1(), n1, bl->getb2(), n2, eps, maxk, 0u, k, U, V);
+    delete[] V;
+    delete[] U;
+    out[l] = succ ? (int)k : -2;
+  }
+}
 
 void ref_free(void* p) {
   RefH* H = (RefH*)p;

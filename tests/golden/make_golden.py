@@ -4,7 +4,8 @@ Runs only where the AHMED sources are available and oracle/ref/build_ref.sh
 has produced oracle/_ref/libahmed_ref.so.  The outputs (small .npz files next
 to this script) are committed; the tests read them on any host.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py            (Laplace cases)
+        python tests/golden/make_golden.py helmholtz  (complex ACA ranks)
 """
 import os
 import sys
@@ -82,5 +83,32 @@ def main():
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+# Helmholtz exp(ikr)/(4 pi r): ranks of the reference's complex ACA per leaf
+HELM_CASES = {
+    "helm_fib4096": (lambda: G.fibonacci_sphere(4096), 32),
+    "helm_ell3000": (lambda: G.ellipsoid_surface(3000, 9), 32),
+}
+HELM_K = (1.0, 5.0, 15.0)
+
+
+def helmholtz():
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    for name, (gen, bmin) in HELM_CASES.items():
+        P = gen()
+        h = O.mean_nn(P)
+        R = O.RefH(P, O.TREE_BBX, bmin, ETA, h)
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+               "eps": np.float64(EPS), "leaves": R.leaves(), "wavenumbers": np.array(HELM_K)}
+        for k in HELM_K:
+            out[f"ranks_k{k:g}"] = R.helmholtz_aca_ranks(k, h, EPS)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
+        helmholtz()
+    else:
+        main()
