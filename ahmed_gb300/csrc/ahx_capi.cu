@@ -252,14 +252,16 @@ int prepare_product(ahx_hmat* H, int prec) {
 }
 
 int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,
-                        const double* arena64, uint64_t n, int device, cudaStream_t s) {
+                        const double* arena64, uint64_t n, int device, cudaStream_t s, uint32_t pmax,
+                        uint32_t unit_bytes) {
   const bool bf = prec == kBF16FP32;
-  const uint32_t pmax = bf ? 64u : 16u;
+  if (!bf || pmax == 0) pmax = bf ? 64u : 16u;  // FP32 storage: 16 per pass
+  if (unit_bytes == 0 || unit_bytes > kTcSlotData) unit_bytes = kTcSlotData;
   int sms = 0;
   AHX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const uint32_t grid = (uint32_t)std::max(sms, 1);
   TcLayout L;
-  build_tc_layout(leaves, bf, pmax, grid * kTcGroups, L);
+  build_tc_layout(leaves, bf, pmax, grid * kTcGroups, L, unit_bytes);
   AHX_CUDA(tc_init_attributes());
   int rc;
   if ((rc = pc.vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;
@@ -307,6 +309,7 @@ int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& lea
   pc.grid = grid;
   pc.t_rows = L.t_rows;
   pc.pmax = pmax;
+  pc.unit_bytes = unit_bytes;
   pc.bytes = L.payload_bytes;
   return AHX_OK;
 }
@@ -591,6 +594,95 @@ int ahx_hmat_assembly_stats(const ahx_hmat* H, uint64_t* out) {
   out[0] = H->stat_ws_bytes;
   out[1] = H->stat_retries;
   out[2] = H->stat_batches;
+  return AHX_OK;
+}
+
+// Autotuner for the mixed-precision streams: for each candidate bucketing (the
+// right-hand-side width the units are sized for: 64 / 32 / 16 with BF16
+// factors, 16 with FP32 storage; the unit byte cap: 11, 8.25 or 5.5 KB) it
+// builds the streams, times 3 products with p right-hand sides after one
+// warm-up (CUDA events on the handle's stream) and keeps the fastest.
+// out4 = {chosen width, chosen unit cap, best time in ns, candidates timed}.
+int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4) {
+  if (!H || p == 0 || (precision != AHX_FP32 && precision != AHX_BF16_FP32)) {
+    set_error("ahx_hmat_autotune: invalid argument (mixed precisions only)");
+    return AHX_ERR_ARG;
+  }
+  if (!H->assembled) {
+    set_error("not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  const int prec = precision == AHX_FP32 ? kFP32 : kBF16FP32;
+  const auto& Ls = H->tree.leaves;
+  std::vector<PlanLeaf> pls;
+  for (uint32_t l = 0; l < (uint32_t)Ls.size(); ++l)
+    if (H->rank[l] != 0) pls.push_back(PlanLeaf{Ls[l].b1, Ls[l].n1, Ls[l].b2, Ls[l].n2, H->rank[l], H->off[l]});
+  const uint64_t n = H->tree.n;
+  DevBuf X, Y;
+  if ((rc = X.reserve(n * p * sizeof(double))) || (rc = Y.reserve(n * p * sizeof(double)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(X.p, 0, n * p * sizeof(double), H->stream));
+  AHX_CUDA(cudaMemsetAsync(Y.p, 0, n * p * sizeof(double), H->stream));
+  std::vector<uint32_t> widths = prec == kBF16FP32 ? std::vector<uint32_t>{64u, 32u, 16u} : std::vector<uint32_t>{16u};
+  const uint32_t units[3] = {kTcSlotData, (kTcSlotData * 3 / 4) & ~15u, (kTcSlotData / 2) & ~15u};
+  cudaEvent_t e0, e1;
+  AHX_CUDA(cudaEventCreate(&e0));
+  AHX_CUDA(cudaEventCreate(&e1));
+  float best = INFINITY;
+  uint32_t bw = widths[0], bu = units[0], count = 0;
+  for (uint32_t w : widths) {
+    for (uint32_t u : units) {
+      ProdCopy cand;
+      if ((rc = build_mixed_streams(cand, prec, pls, H->arena64.as<double>(), n, H->device, H->stream, w, u))) {
+        cand.release_all();
+        break;
+      }
+      const TcPlan pl = mixed_plan(cand, n);
+      cudaError_t ce = launch_matvec_tc(prec, pl, 1.0, p, X.as<double>(), n, Y.as<double>(), n, H->stream);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, H->stream);
+      for (int r = 0; r < 3 && ce == cudaSuccess; ++r)
+        ce = launch_matvec_tc(prec, pl, 1.0, p, X.as<double>(), n, Y.as<double>(), n, H->stream);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e1, H->stream);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      const int se = check_stream_error(cand, H->stream);
+      cand.release_all();
+      if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(ce, "autotune");
+      }
+      if (se) {
+        rc = se;
+        break;
+      }
+      ++count;
+      if (ms < best) {
+        best = ms;
+        bw = w;
+        bu = u;
+      }
+    }
+    if (rc) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  X.release();
+  Y.release();
+  if (rc) return rc;
+  ProdCopy& pc = H->prod[prec];
+  pc.release_all();
+  if ((rc = build_mixed_streams(pc, prec, pls, H->arena64.as<double>(), n, H->device, H->stream, bw, bu)))
+    return rc;
+  pc.valid = true;
+  if (out4) {
+    out4[0] = bw;
+    out4[1] = bu;
+    out4[2] = (uint32_t)std::min(best / 3.f * 1e6f, 4e9f);
+    out4[3] = count;
+  }
   return AHX_OK;
 }
 

@@ -43,6 +43,7 @@ struct ProdCopy {
   // mixed-precision fragment streams (FP32 / BF16 products, tensor cores)
   DevBuf vstream, rstream, vunits, runits, sides, vranges, rranges, treduce, xb, xf, yr, t, err;
   uint32_t nvunits = 0, nrunits = 0, grid = 0, t_rows = 0, ntreduce = 0, pmax = 16;
+  uint32_t unit_bytes = 0;  // unit cap the streams were built with
   void release_all() {
     for (DevBuf* b : {&lr, &dn, &leaves, &order, &vstream, &rstream, &vunits, &runits, &sides, &vranges,
                       &rranges, &treduce, &xb, &xf, &yr, &t, &err})
@@ -83,8 +84,10 @@ int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 }
 
 // Builds the streams of a mixed precision from FP64 leaves (offsets into arena64).
+// pmax / unit_bytes 0: the defaults (64 for BF16 factors, 16 for FP32; kTcSlotData)
 int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& leaves,
-                        const double* arena64, uint64_t n, int device, cudaStream_t s);
+                        const double* arena64, uint64_t n, int device, cudaStream_t s, uint32_t pmax = 0,
+                        uint32_t unit_bytes = 0);
 TcPlan mixed_plan(const ProdCopy& pc, uint64_t n);
 // Reports (and clears) a timeout raised by a streaming kernel.
 int check_stream_error(ProdCopy& pc, cudaStream_t s);

@@ -151,9 +151,10 @@ struct TcLayout {
 
 // lr_bf16: low-rank factors in BF16 (else FP32); pmax: right-hand sides the
 // units are sized for; nparts: consumer groups of one sweep launch
-// (grid * kTcGroups), each given a contiguous unit range
+// (grid * kTcGroups), each given a contiguous unit range; unit_bytes: cap of
+// one unit's fragments + A rows (<= kTcSlotData)
 void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t pmax, uint32_t nparts,
-                     TcLayout& L);
+                     TcLayout& L, uint32_t unit_bytes = kTcSlotData);
 
 struct TcPlan {
   const TcVUnit* vunits = nullptr;

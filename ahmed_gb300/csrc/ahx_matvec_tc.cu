@@ -783,8 +783,9 @@ void balance_ranges(const std::vector<uint64_t>& bytes, uint32_t grid, std::vect
 }
 
 void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t pmax, uint32_t nparts,
-                     TcLayout& L) {
+                     TcLayout& L, uint32_t unit_bytes) {
   L = TcLayout();
+  const uint32_t cap = std::min(unit_bytes, kTcSlotData);
   const uint32_t es = lr_bf16 ? 2u : 4u;
   const uint32_t s_t = (pmax + 8) * es;  // T rows and the V sweep's X rows (factor type)
   const uint32_t s_x = (pmax + 8) * 4;   // FP32 X rows of dense leaves
@@ -816,7 +817,7 @@ void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t
     for (uint32_t c0 = 0; c0 < kc; c0 += 64) {
       const uint32_t nc = std::min(64u, kc - c0), nt = (nc + 7) / 8;
       const uint32_t rowb = nt * 8 * es + s_t;
-      const uint32_t chunk = std::max(16u, (kTcSlotData / rowb) & ~15u);
+      const uint32_t chunk = std::max(16u, (cap / rowb) & ~15u);
       VGroup G{L.vunits.size(), 0, tb + c0, nc};
       for (uint32_t j0 = 0; j0 < n2; j0 += chunk) {
         const uint32_t jn = std::min(chunk, n2 - j0), kp = round8(jn);
@@ -926,7 +927,7 @@ void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t
           else break;
           const uint32_t nbytes = round8(na1 - a0) * cb0 + round8(nc1g1 - c0g1) * cb1;
           const uint32_t ne = entries(a0, na1, st0) + entries(c0g1, nc1g1, st1);
-          if ((a1 > a0 || c1g1 > c0g1) && (nbytes > kTcSlotData || ne > 32)) break;
+          if ((a1 > a0 || c1g1 > c0g1) && (nbytes > cap || ne > 32)) break;
           a1 = na1;
           c1g1 = nc1g1;
         }

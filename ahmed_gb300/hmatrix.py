@@ -165,6 +165,13 @@ class HMatrix:
         check(lib().ahx_hmat_assembly_stats(self._h, ptr(out)))
         return tuple(int(v) for v in out)
 
+    def autotune(self, precision, p):
+        """Choose the mixed product's stream bucketing for p right-hand sides by timing
+        candidates; returns (width, unit_bytes, best_ns, candidates)."""
+        out = np.zeros(4, np.uint32)
+        check(lib().ahx_hmat_autotune(self._h, _prec(precision), int(p), ptr(out)))
+        return tuple(int(v) for v in out)
+
     def helmholtz_aca_ranks(self, wavenumber, h, eps, rankmax=2**32 - 1, rank_hint=None):
         """Complex ACA ranks of the Helmholtz matrix exp(ikr)/(4 pi r) per leaf
         (-1 inadmissible, -2 ACA failed); bounding-box trees."""

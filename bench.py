@@ -213,6 +213,7 @@ def run_gpu(args):
 
     H.prepare("fp64")
     H.prepare("fp32")
+    tuned = H.autotune("fp32", NRHS) if args.autotune else None
     ms64 = timed("fp64", max(2, args.steps // 4), args.warmup)
     with ClockSampler(local) as cs:
         ms32 = timed("fp32", args.steps, args.warmup)
@@ -261,7 +262,9 @@ def run_gpu(args):
                        fp64_arena_bytes=int(H.storage_bytes("fp64")),
                        plain_fp64_value=ws * NRHS / (ms64 * 1e-3), plain_fp64_ms=ms64,
                        mixed_over_plain=ms64 / ms32, fp32_max_rel_err_per_rhs=err32,
-                       assembly_s=t_asm),
+                       assembly_s=t_asm,
+                       autotuned=(None if tuned is None else
+                                  {"rhs_width": tuned[0], "unit_bytes": tuned[1], "candidates": tuned[3]})),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes": bytes32,
@@ -336,6 +339,8 @@ def run_large(args):
     ex = _sample_rows_exact(P, op, x1[None, :], rows, h)[:, 0]
     out["assembly_rel_err_sampled_rows"] = float(np.linalg.norm(y1.cpu().numpy()[rows] - ex) / np.linalg.norm(ex))
     H.prepare("bf16")
+    if args.autotune:
+        out["autotuned"] = dict(zip(("rhs_width", "unit_bytes", "best_ns", "candidates"), H.autotune("bf16", p)))
     out["bf16_arena_bytes"] = int(H.storage_bytes("bf16"))
     X = torch.from_numpy(np.random.default_rng(5).uniform(-1.0, 1.0, (p, n))).to(dev)
     Y = torch.zeros_like(X)
@@ -617,6 +622,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ahx", choices=["ahx", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--autotune", type=int, default=1, help="1: tune the stream bucketing before timing")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
     ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz"],

@@ -91,6 +91,13 @@ int ahx_hmat_assembly_stats(const ahx_hmat* H, uint64_t* out3);
  * log n2, wavenumber * max diam, -log10(eps) (diam: Include/cluster.h:194) */
 int ahx_hmat_features(const ahx_hmat* H, double wavenumber, double eps, float* out);
 
+/* Autotuner of the mixed-precision product (AHX_FP32 or AHX_BF16_FP32): times
+ * candidate stream bucketings (right-hand-side width the units are sized for,
+ * unit byte cap) on p right-hand sides and keeps the fastest for this matrix.
+ * out4 (may be NULL): chosen width, chosen unit bytes, best ns per product,
+ * candidates timed. */
+int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4);
+
 /* Helmholtz exp(i k r) / (4 pi r) (diagonal exp(i k h) / (4 pi h)): complex
  * ACA of every admissible leaf with the reference's ACA<dcomp> stopping rule
  * (Include/ACA.h:217-350), ranks[l] = rank (-1 inadmissible, -2 ACA failed).

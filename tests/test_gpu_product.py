@@ -133,3 +133,21 @@ def test_mixed_precision_rhs_counts(prec, tol, p):
     errs = [_relerr(Ym[r] - Y0[r], Y64[r] - Y0[r]) for r in range(p)]
     assert max(errs) <= tol, errs
     H.close()
+
+
+@pytest.mark.parametrize("prec,p", [("fp32", 16), ("bf16", 40)])
+def test_autotune_keeps_results(prec, p):
+    """The autotuner only re-buckets the streams: products before and after agree to
+    rounding, and the chosen configuration is one of the candidates."""
+    P = A.geometry.cube_surface(12000, 3)
+    H = A.HMatrix(P, "bbx", bmin=32, eta=0.8).matgenGeH_omp(A.mean_nn(P), 1e-6)
+    X = np.random.default_rng(p).uniform(-1, 1, (p, H.n))
+    Y0 = H.mltaGeHVec(1.0, X, np.zeros((p, H.n)), precision=prec)
+    width, unit, ns, count = H.autotune(prec, p)
+    assert count == (9 if prec == "bf16" else 3) and ns > 0
+    assert width in ((16, 32, 64) if prec == "bf16" else (16,))
+    Y1 = H.mltaGeHVec(1.0, X, np.zeros((p, H.n)), precision=prec)
+    tol = 1e-6 if prec == "fp32" else 1e-2
+    for r in range(p):
+        assert _relerr(Y1[r], Y0[r]) <= tol
+    H.close()
