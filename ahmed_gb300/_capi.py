@@ -58,6 +58,7 @@ SIGNATURES = [
     ("ahx_hmat_assembly_stats", _i32, [_vp, _vp]),
     ("ahx_hmat_features", _i32, [_vp, _dbl, _dbl, _vp]),
     ("ahx_hmat_autotune", _i32, [_vp, _i32, _u32, _vp]),
+    ("ahx_matvec_transposed", _i32, [_vp, _dbl, _u32, _vp, _u64, _vp, _u64]),
     ("ahx_helm_aca_ranks", _i32, [_vp, _dbl, _dbl, _dbl, _u32, _vp, _vp]),
     ("ahx_mlp_nparams", _u32, []),
     ("ahx_mlp_create", _i32, [_i32, _u64, _vp]),

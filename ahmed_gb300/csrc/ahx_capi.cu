@@ -352,7 +352,11 @@ int check_stream_error(ProdCopy& pc, cudaStream_t s) {
 }
 
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
-                   double* Y, uint64_t ldY) {
+                   double* Y, uint64_t ldY, bool transposed) {
+  if (transposed && prec != kFP64) {
+    set_error("transposed products use the FP64 leaves");
+    return AHX_ERR_ARG;
+  }
   int rc = prepare_product(H, prec);
   if (rc) return rc;
   ProdCopy& pc = H->prod[prec];
@@ -373,6 +377,7 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   a.ldX = ldX;
   a.Y = Y;
   a.ldY = ldY;
+  a.transposed = transposed ? 1u : 0u;
   AHX_CUDA(launch_matvec(prec, a, H->stream));
   return AHX_OK;
 }
@@ -787,8 +792,9 @@ int ahx_hmat_prepare(ahx_hmat* H, int precision) {
   return prepare_product(H, precision);
 }
 
-int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX,
-               double* Y, uint64_t ldY) {
+namespace {
+int matvec_any(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+               uint64_t ldY, bool transposed) {
   if (!H || !X || !Y || ldX < H->tree.n || ldY < H->tree.n) {
     set_error("ahx_matvec: invalid argument");
     return AHX_ERR_ARG;
@@ -819,7 +825,7 @@ int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X
     Yd = H->stage_y.as<double>();
     ly = n;
   }
-  if ((rc = product_device(H, precision, d, p, Xd, lx, Yd, ly))) return rc;
+  if ((rc = product_device(H, precision, d, p, Xd, lx, Yd, ly, transposed))) return rc;
   if (!yd) {
     AHX_CUDA(cudaMemcpy2DAsync(Y, ldY * sizeof(double), Yd, n * sizeof(double), n * sizeof(double),
                                p, cudaMemcpyDeviceToHost, H->stream));
@@ -829,6 +835,17 @@ int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X
     if (precision != kFP64) return check_stream_error(H->prod[precision], H->stream);
   }
   return AHX_OK;
+}
+}  // namespace
+
+int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+               uint64_t ldY) {
+  return matvec_any(H, precision, d, p, X, ldX, Y, ldY, false);
+}
+
+int ahx_matvec_transposed(ahx_hmat* H, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+                          uint64_t ldY) {
+  return matvec_any(H, AHX_FP64, d, p, X, ldX, Y, ldY, true);
 }
 
 }  // extern "C"

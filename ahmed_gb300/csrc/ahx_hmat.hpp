@@ -121,7 +121,8 @@ namespace ahx {
 int prepare_product(ahx_hmat* H, int prec);
 int ensure_device(ahx_hmat* H);
 // Y += d A X on device pointers
+// Y += d A X (transposed: Y += d A^T X, plain FP64 leaves only)
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
-                   double* Y, uint64_t ldY);
+                   double* Y, uint64_t ldY, bool transposed = false);
 bool is_device_ptr(const void* p);
 }  // namespace ahx

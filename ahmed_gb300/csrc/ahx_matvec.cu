@@ -40,14 +40,58 @@ __device__ __forceinline__ void stage_x(A (*Xs)[PG + 1], const MvArgs& a, uint32
   }
 }
 
-template <typename SL, typename SD, typename A, int PG>
+// TR: the transposed product Y += d A^T X (mltaGeHtVec / mltaGeHhVec for real
+// leaves, H/mltaGeHVec.cpp:62-150): a low-rank leaf U V^T acts as V U^T (the
+// roles of the factors and of the row / column ranges swap); a dense leaf D
+// acts as D^T, one warp per column of D.
+template <typename SL, typename SD, typename A, int PG, bool TR>
 __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
   __shared__ A Xs[kCh][PG + 1];
   __shared__ A Ts[kKt][PG];
   __shared__ A red[kThreads];
-  const MvLeaf L = a.leaves[a.order[blockIdx.x]];
+  MvLeaf L = a.leaves[a.order[blockIdx.x]];
   const uint32_t tid = threadIdx.x;
   const double d = a.d;
+  uint64_t voff = L.off + (uint64_t)L.n1 * (L.rank > 0 ? (uint32_t)L.rank : 0u);  // V of U V^T
+  if (TR && L.rank > 0) {
+    const uint64_t uo = voff;
+    voff = L.off;
+    L.off = uo;
+    const uint32_t b = L.b1, n = L.n1;
+    L.b1 = L.b2;
+    L.n1 = L.n2;
+    L.b2 = b;
+    L.n2 = n;
+  }
+  if (TR && L.rank < 0) {
+    // Y[b2 + j] += d sum_i D[i + j n1] X[b1 + i]
+    const SD* Ad = L.dense_in_lr_arena ? reinterpret_cast<const SD*>(reinterpret_cast<const SL*>(a.arena_lr) + L.off)
+                                       : reinterpret_cast<const SD*>(a.arena_dn) + L.off;
+    const uint32_t warp = tid >> 5, lane = tid & 31;
+    for (uint32_t r0 = 0; r0 < a.p; r0 += PG) {
+      const uint32_t pg = min((uint32_t)PG, a.p - r0);
+      for (uint32_t j = warp; j < L.n2; j += kThreads / 32) {
+        A acc[PG];
+#pragma unroll
+        for (int r = 0; r < PG; ++r) acc[r] = 0;
+        const SD* col = Ad + (uint64_t)j * L.n1;
+        for (uint32_t i = lane; i < L.n1; i += 32) {
+          const A av = ldcvt<SD, A>(col + i);
+#pragma unroll
+          for (int r = 0; r < PG; ++r)
+            if ((uint32_t)r < pg) acc[r] = fma(av, (A)a.X[(uint64_t)(r0 + r) * a.ldX + L.b1 + i], acc[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < PG; ++r) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+        }
+        if (lane == 0)
+          for (uint32_t r = 0; r < pg; ++r) atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b2 + j, d * (double)acc[r]);
+      }
+    }
+    return;
+  }
   for (uint32_t r0 = 0; r0 < a.p; r0 += PG) {
     const uint32_t pg = min((uint32_t)PG, a.p - r0);
     if (L.rank < 0) {
@@ -80,7 +124,7 @@ __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
     } else if (L.rank > 0) {
       const uint32_t k = (uint32_t)L.rank;
       const SL* U = reinterpret_cast<const SL*>(a.arena_lr) + L.off;
-      const SL* V = U + (uint64_t)L.n1 * k;
+      const SL* V = reinterpret_cast<const SL*>(a.arena_lr) + voff;
       for (uint32_t lb = 0; lb < k; lb += kKt) {
         const uint32_t kn = min((uint32_t)kKt, k - lb);
         const uint32_t nout = kn * PG;
@@ -156,15 +200,15 @@ __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
   }
 }
 
-template <typename SL, typename SD, typename A>
+template <typename SL, typename SD, typename A, bool TR>
 cudaError_t launch_typed(const MvArgs& a, cudaStream_t s) {
   if (a.nleaves == 0 || a.p == 0) return cudaSuccess;
   const uint32_t grid = a.nleaves;
-  if (a.p == 1) mv_kernel<SL, SD, A, 1><<<grid, kThreads, 0, s>>>(a);
-  else if (a.p == 2) mv_kernel<SL, SD, A, 2><<<grid, kThreads, 0, s>>>(a);
-  else if (a.p <= 4) mv_kernel<SL, SD, A, 4><<<grid, kThreads, 0, s>>>(a);
-  else if (a.p <= 8) mv_kernel<SL, SD, A, 8><<<grid, kThreads, 0, s>>>(a);
-  else mv_kernel<SL, SD, A, 16><<<grid, kThreads, 0, s>>>(a);
+  if (a.p == 1) mv_kernel<SL, SD, A, 1, TR><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p == 2) mv_kernel<SL, SD, A, 2, TR><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p <= 4) mv_kernel<SL, SD, A, 4, TR><<<grid, kThreads, 0, s>>>(a);
+  else if (a.p <= 8) mv_kernel<SL, SD, A, 8, TR><<<grid, kThreads, 0, s>>>(a);
+  else mv_kernel<SL, SD, A, 16, TR><<<grid, kThreads, 0, s>>>(a);
   count_product_launches(1);
   return cudaGetLastError();
 }
@@ -174,7 +218,8 @@ cudaError_t launch_typed(const MvArgs& a, cudaStream_t s) {
 // the plain (FP64) form; the mixed forms run the tensor-core sweeps
 cudaError_t launch_matvec(int prec, const MvArgs& a, cudaStream_t s) {
   if (prec != kFP64) return cudaErrorInvalidValue;
-  return launch_typed<double, double, double>(a, s);
+  return a.transposed ? launch_typed<double, double, double, true>(a, s)
+                      : launch_typed<double, double, double, false>(a, s);
 }
 
 }  // namespace ahx

@@ -36,6 +36,7 @@ struct MvArgs {
   uint64_t ldX;
   double* Y;
   uint64_t ldY;
+  uint32_t transposed = 0;  // 1: Y += d A^T X (H/mltaGeHVec.cpp:62-150)
 };
 
 cudaError_t launch_matvec(int prec, const MvArgs& a, cudaStream_t s);

@@ -229,6 +229,19 @@ class HMatrix:
         p, ld = _ncols(x, self.n)
         return self.mltaGeHGeM(d, p, x, ld, y, ld, precision)
 
+    def mltaGeHtGeM(self, d, p, X, ldX, Y, ldY):
+        """Y += d A^T X (FP64 leaves; for real leaves also A^H: mltaGeHhGeM)."""
+        self._follow_torch(X, Y)
+        check(lib().ahx_matvec_transposed(self._h, float(d), int(p), ptr(X), int(ldX), ptr(Y), int(ldY)))
+        return Y
+
+    def mltaGeHtVec(self, d, x, y):
+        p, ld = _ncols(x, self.n)
+        return self.mltaGeHtGeM(d, p, x, ld, y, ld)
+
+    mltaGeHhVec = mltaGeHtVec
+    mltaGeHhGeM = mltaGeHtGeM
+
     # -- solvers ----------------------------------------------------------
     def GMRes(self, b, x, eps, m, nsteps, precision="fp64"):
         """Restarted GMRES(m); b, x of shape (n,) or (p, n).  Returns (status, eps[], nsteps[])."""

@@ -130,6 +130,11 @@ int ahx_hmat_prepare(ahx_hmat* H, int precision);
  *   mltaGeHGeM(d, bl, A, p, X, ldX, Y, ldY)        H/mltaGeHVec.cpp:573-577 */
 int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X, uint64_t ldX,
                double* Y, uint64_t ldY);
+/* Y += d A^T X with the FP64 leaves (mltaGeHtVec / mltaGeHtGeM, and for real
+ * leaves mltaGeHhVec / mltaGeHhGeM: H/mltaGeHVec.cpp:62-150).  X, Y: n x p,
+ * column-major, host or device. */
+int ahx_matvec_transposed(ahx_hmat* H, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+                          uint64_t ldY);
 
 /* Restarted GMRES(m) for p right-hand sides (each with its own Krylov space),
  * right-preconditioner free.  Replaces GMRes(A, b, x, eps, m, nsteps)

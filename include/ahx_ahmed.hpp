@@ -207,6 +207,18 @@ inline bool mltaGeHGeM(double d, blcluster* bl, mblock<double>**, unsigned p, do
   return true;
 }
 
+// H/mltaGeHVec.cpp:579-589 (mltaGeHhVec_/mltaGeHhGeM_ :62-105): y += d A^H x, Y += d A^H X (A^T for double)
+inline bool mltaGeHhVec(double d, blcluster* bl, mblock<double>**, double* x, double* y) {
+  check(ahx_matvec_transposed(bl->handle(), d, 1, x, bl->getn1(), y, bl->getn1()));
+  return true;
+}
+
+inline bool mltaGeHhGeM(double d, blcluster* bl, mblock<double>**, unsigned p, double* X,
+                        unsigned ldX, double* Y, unsigned ldY) {
+  check(ahx_matvec_transposed(bl->handle(), d, p, X, ldX, Y, ldY));
+  return true;
+}
+
 // Include/matrix.h:20-32
 template <class T>
 struct Matrix {

@@ -151,3 +151,34 @@ def test_autotune_keeps_results(prec, p):
     for r in range(p):
         assert _relerr(Y1[r], Y0[r]) <= tol
     H.close()
+
+
+@pytest.mark.parametrize("kind", ["bbx", "pca"])
+def test_transposed_product(oracle_pair, kind):
+    """y += d A^T x (mltaGeHtGeM): <A^T x, z> = <x, A z> for random x, z, several RHS."""
+    _, H = oracle_pair[kind]
+    n, p = H.n, 5
+    rng = np.random.default_rng(11)
+    X = rng.uniform(-1, 1, (p, n))
+    Z = rng.uniform(-1, 1, (p, n))
+    AtX = H.mltaGeHtGeM(-0.5, p, X, n, np.zeros((p, n)), n)
+    AZ = H.mltaGeHVec(-0.5, Z, np.zeros((p, n)))
+    for r in range(p):
+        lhs, rhs = AtX[r] @ Z[r], X[r] @ AZ[r]
+        assert abs(lhs - rhs) <= 1e-12 * np.linalg.norm(AtX[r]) * np.linalg.norm(Z[r])
+    # against the dense transpose of the assembled leaves on a small case
+    lv = H.leaves()
+    ranks = H.ranks()
+    A = np.zeros((n, n))
+    for l in range(len(lv)):
+        b1, n1, b2, n2 = (int(v) for v in lv[l][:4])
+        data = H.leaf_data(l)
+        if ranks[l] < 0:
+            A[b1:b1 + n1, b2:b2 + n2] = data.reshape(n2, n1).T
+        elif ranks[l] > 0:
+            k = int(ranks[l])
+            U = data[:n1 * k].reshape(k, n1).T
+            V = data[n1 * k:].reshape(k, n2).T
+            A[b1:b1 + n1, b2:b2 + n2] = U @ V.T
+    ref = -0.5 * (A.T @ X.T).T
+    assert np.linalg.norm(AtX - ref) <= 1e-12 * np.linalg.norm(ref)
