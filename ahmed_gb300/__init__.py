@@ -10,11 +10,14 @@ from .hmatrix import (  # noqa: F401
     GMRes,
     HBatch,
     HMatrix,
+    loadmbls,
     matgenGeH_omp,
+    mbls_header,
     mean_nn,
     min_nn,
     mltaGeHGeM,
     mltaGeHVec,
+    savembls,
 )
 from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, lib  # noqa: F401
 from .rank_predictor import RankPredictor, training_set  # noqa: F401

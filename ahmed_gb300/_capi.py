@@ -59,6 +59,11 @@ SIGNATURES = [
     ("ahx_hmat_features", _i32, [_vp, _dbl, _dbl, _vp]),
     ("ahx_hmat_autotune", _i32, [_vp, _i32, _u32, _vp]),
     ("ahx_matvec_transposed", _i32, [_vp, _dbl, _u32, _vp, _u64, _vp, _u64]),
+    ("ahx_mbls_header", _i32, [C.c_char_p, _vp, _vp, _vp]),
+    ("ahx_hmat_save", _i32, [_vp, _dbl, _u32, C.c_char_p]),
+    ("ahx_hmat_load", _i32, [_vp, C.c_char_p, _vp, _vp]),
+    ("ahx_hmat_save_stream", _i32, [_vp, _dbl, _u32, _vp, _vp]),
+    ("ahx_hmat_load_stream", _i32, [_vp, _vp, _vp, _vp, _vp]),
     ("ahx_helm_aca_ranks", _i32, [_vp, _dbl, _dbl, _dbl, _u32, _vp, _vp]),
     ("ahx_mlp_nparams", _u32, []),
     ("ahx_mlp_create", _i32, [_i32, _u64, _vp]),

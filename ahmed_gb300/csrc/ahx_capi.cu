@@ -20,37 +20,6 @@ thread_local std::string g_err;
 // rest run one warp per leaf (warp reductions; the FP64 pipe is the limit)
 constexpr uint32_t kLargeLeaf = 4096;
 
-
-// Append-only growable FP64 arena.
-int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
-  const uint64_t need = (H->arena64_elems + count) * sizeof(double);
-  if (need > H->arena64.bytes) {
-    size_t nb = std::max<size_t>(need, H->arena64.bytes * 2);
-    void* np = nullptr;
-    cudaError_t e = cudaMalloc(&np, nb);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      nb = need;
-      e = cudaMalloc(&np, nb);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        set_error("device allocation of the leaf arena failed");
-        return AHX_ERR_NOMEM;
-      }
-    }
-    if (H->arena64_elems)
-      AHX_CUDA(cudaMemcpyAsync(np, H->arena64.p, H->arena64_elems * sizeof(double),
-                               cudaMemcpyDeviceToDevice, H->stream));
-    AHX_CUDA(cudaStreamSynchronize(H->stream));
-    if (H->arena64.p) cudaFree(H->arena64.p);
-    H->arena64.p = np;
-    H->arena64.bytes = nb;
-  }
-  off = H->arena64_elems;
-  H->arena64_elems += count;
-  return AHX_OK;
-}
-
 // Runs ACA + recompression for `tasks` in workspace-bounded batches, appends the
 // factors to the arena; failed leaves go to `dense`, capacity overflows to `retry`.
 int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
@@ -155,11 +124,41 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
   return AHX_OK;
 }
 
+}  // namespace
+
+// Append-only growable FP64 arena.
+int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
+  const uint64_t need = (H->arena64_elems + count) * sizeof(double);
+  if (need > H->arena64.bytes) {
+    size_t nb = std::max<size_t>(need, H->arena64.bytes * 2);
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, nb);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      nb = need;
+      e = cudaMalloc(&np, nb);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation of the leaf arena failed");
+        return AHX_ERR_NOMEM;
+      }
+    }
+    if (H->arena64_elems)
+      AHX_CUDA(cudaMemcpyAsync(np, H->arena64.p, H->arena64_elems * sizeof(double),
+                               cudaMemcpyDeviceToDevice, H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    if (H->arena64.p) cudaFree(H->arena64.p);
+    H->arena64.p = np;
+    H->arena64.bytes = nb;
+  }
+  off = H->arena64_elems;
+  H->arena64_elems += count;
+  return AHX_OK;
+}
+
 void invalidate_products(ahx_hmat* H) {
   for (auto& pc : H->prod) pc.release_all();
 }
-
-}  // namespace
 
 void set_error(const std::string& msg) { g_err = msg; }
 

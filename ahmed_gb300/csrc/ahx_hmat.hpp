@@ -120,6 +120,10 @@ struct ahx_hmat {
 namespace ahx {
 int prepare_product(ahx_hmat* H, int prec);
 int ensure_device(ahx_hmat* H);
+// Reserves count doubles at the end of the FP64 leaf arena (grows it, stream-ordered).
+int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off);
+// Drops every precision's product copy (after the leaves change).
+void invalidate_products(ahx_hmat* H);
 // Y += d A X on device pointers
 // Y += d A X (transposed: Y += d A^T X, plain FP64 leaves only)
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,

@@ -7,6 +7,7 @@ H/mltaGeHVec.cpp:567-577), ``GMRes`` (solvers/GMRES.cpp:80) and ``CG``
 """
 import atexit
 import ctypes as C
+import os
 import weakref
 
 import numpy as np
@@ -68,6 +69,7 @@ class HMatrix:
             raise ValueError("points must have shape (n, 3)")
         self.n = pts.shape[0]
         self.points = pts
+        self.eta, self.bmin = float(eta), int(bmin)
         kind = TREES[tree] if isinstance(tree, str) else int(tree)
         h = C.c_void_p()
         check(lib().ahx_hmat_create(ptr(pts), self.n, kind, bmin, float(eta) ** 2, device,
@@ -210,6 +212,22 @@ class HMatrix:
         check(lib().ahx_hmat_set_leaves(self._h, ptr(ranks), ptr(data), ptr(offsets)))
         self.eps = self.eps or 0.0
 
+    # -- persistent leaves (savembls / loadmbls, Include/H.h:47-103) ---------
+    def save(self, path, eta=None, bmin=None):
+        """Writes the leaves in the reference's savembls layout; eta and bmin
+        default to the ones this tree was built with."""
+        eta = self.eta if eta is None else float(eta)
+        bmin = self.bmin if bmin is None else int(bmin)
+        check(lib().ahx_hmat_save(self._h, eta, bmin, os.fsencode(path)))
+
+    def load(self, path):
+        """Reads leaves written by savembls (the reference's or save()) into
+        this tree; returns the file's (eta, bmin)."""
+        eta, bmin = C.c_double(), C.c_uint32()
+        check(lib().ahx_hmat_load(self._h, os.fsencode(path), C.byref(eta), C.byref(bmin)))
+        self.eps = self.eps or 0.0
+        return eta.value, bmin.value
+
     def storage_bytes(self, precision="fp64"):
         return lib().ahx_hmat_storage_bytes(self._h, _prec(precision))
 
@@ -334,3 +352,21 @@ def GMRes(H, b, x, eps, m, nsteps, precision="fp64"):
 
 def CG(H, b, x, eps, nsteps):
     return H.CG(b, x, eps, nsteps)
+
+
+def mbls_header(path):
+    """(eta, bmin, nleaves) of a savembls file (host only)."""
+    eta, bmin, n = C.c_double(), C.c_uint32(), C.c_uint32()
+    check(lib().ahx_mbls_header(os.fsencode(path), C.byref(eta), C.byref(bmin), C.byref(n)))
+    return eta.value, bmin.value, n.value
+
+
+def savembls(eta, bmin, H, path):
+    """Include/H.h:89-103: the leaves of H with the caller's eta and bmin."""
+    H.save(path, eta, bmin)
+
+
+def loadmbls(path, H):
+    """Include/H.h:60-73 into the tree H (built with the file's eta and bmin,
+    see mbls_header); returns (eta, bmin)."""
+    return H.load(path)

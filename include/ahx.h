@@ -136,6 +136,24 @@ int ahx_matvec(ahx_hmat* H, int precision, double d, uint32_t p, const double* X
 int ahx_matvec_transposed(ahx_hmat* H, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
                           uint64_t ldY);
 
+/* Persistent leaves in the reference's file layout (native byte order):
+ *   double eta, uint32 bmin, uint32 nleaves; per leaf in leaf order uint8 present,
+ *   then uint32 n1, n2, status and status 0: uint32 rank + rank*(n1+n2) doubles (U, V),
+ *   status 4: n1*n2 doubles column-major (1 / 5: packed upper triangle, load only).
+ * Replaces savembls  Include/H.h:76-103 with mblock::save Include/mblock.h:737-773
+ *          loadmbls  Include/H.h:47-74  with mblock::load Include/mblock.h:775-806.
+ * eta and bmin are stored for the caller (the reference stores what it is given).
+ * Loading needs the handle of the same tree (points, kind, bmin, eta): every
+ * leaf's n1 x n2 is checked; a block marked absent loads as a zero block; on
+ * failure the handle is left unassembled.  ahx_mbls_header reads eta, bmin and
+ * the leaf count (host only) so the tree can be built first. */
+typedef int64_t (*ahx_io_fn)(void* ctx, void* buf, uint64_t bytes); /* bytes moved, <0 error */
+int ahx_mbls_header(const char* path, double* eta, uint32_t* bmin, uint32_t* nleaves);
+int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path);
+int ahx_hmat_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin);
+int ahx_hmat_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx);
+int ahx_hmat_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin);
+
 /* Restarted GMRES(m) for p right-hand sides (each with its own Krylov space),
  * right-preconditioner free.  Replaces GMRes(A, b, x, eps, m, nsteps)
  * solvers/GMRES.cpp:80-181.  B, X column-major n x p (host or device), X holds

@@ -11,6 +11,7 @@
 //   matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);                // Include/matgen_omp.h:197
 //   mltaGeHVec(1.0, bl, A, x, y);                                      // H/mltaGeHVec.cpp:567
 //   GMRes(Op, b, x, eps, m, nsteps);                                   // solvers/GMRES.cpp:80
+//   savembls(eta, bmin, bl, A, os); loadmbls(eta, bmin, A, is);        // Include/H.h:60-103
 //   freembls(bl, A);                                                   // Include/H.h:42
 //
 // compiles against this header by replacing the AHMED includes with it and
@@ -23,8 +24,11 @@
 #ifndef AHX_AHMED_HPP
 #define AHX_AHMED_HPP
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <iterator>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -140,23 +144,37 @@ template <class T>
 class mblock {
  public:
   mblock(const blcluster* bl, unsigned idx) : bl_(bl), idx_(idx) {}
-  unsigned getn1() const { return bl_->leaf(idx_)[1]; }
-  unsigned getn2() const { return bl_->leaf(idx_)[3]; }
-  bool isLrM() const { return bl_->rank_of(idx_) >= 0; }
+  // a leaf read by loadmbls, not yet uploaded into a block-cluster tree
+  mblock(std::shared_ptr<std::string> file, unsigned idx) : bl_(nullptr), idx_(idx), file_(file) {}
+  bool pending() const { return !bl_; }
+  const std::shared_ptr<std::string>& file() const { return file_; }
+  void attach(const blcluster* bl) {
+    bl_ = bl;
+    file_.reset();
+  }
+  unsigned getn1() const { return bound()->leaf(idx_)[1]; }
+  unsigned getn2() const { return bound()->leaf(idx_)[3]; }
+  bool isLrM() const { return bound()->rank_of(idx_) >= 0; }
   bool isGeM() const { return !isLrM(); }
-  unsigned rank() const { return (unsigned)bl_->rank_of(idx_); }
+  unsigned rank() const { return (unsigned)bound()->rank_of(idx_); }
   T* getdata() {
     if (data_.empty()) {
-      data_.resize(ahx_hmat_leaf_size(bl_->handle(), idx_));
-      if (!data_.empty()) check(ahx_hmat_get_leaf(bl_->handle(), idx_, data_.data()));
+      data_.resize(ahx_hmat_leaf_size(bound()->handle(), idx_));
+      if (!data_.empty()) check(ahx_hmat_get_leaf(bound()->handle(), idx_, data_.data()));
     }
     return data_.data();
   }
 
  private:
+  const blcluster* bound() const {
+    if (!bl_)
+      throw std::logic_error("ahx_ahmed: leaves from loadmbls are bound to a tree by bind_mbls or the first product");
+    return bl_;
+  }
   const blcluster* bl_;
   unsigned idx_;
   std::vector<T> data_;
+  std::shared_ptr<std::string> file_;
 };
 
 template <class T>
@@ -195,26 +213,79 @@ void matgenGeH_sqntl(MATGEN_T& MatGen, blcluster* root, blcluster* bl, bool recm
   matgenGeH_omp(MatGen, (unsigned)bl->nleaves(), bl, eps, rankmax, A);
 }
 
+// Include/H.h:89-103: the leaves of bl in the reference's file layout
+template <class T>
+void savembls(const double eta, const unsigned bmin, blcluster* bl, mblock<T>**&, std::ofstream& os) {
+  auto put = [](void* ctx, void* buf, uint64_t bytes) -> int64_t {
+    std::ostream& o = *static_cast<std::ostream*>(ctx);
+    o.write(static_cast<const char*>(buf), (std::streamsize)bytes);
+    return o ? (int64_t)bytes : -1;
+  };
+  check(ahx_hmat_save_stream(bl->handle(), eta, bmin, put, &os));
+}
+
+// Include/H.h:60-73 ("loadmbls does not need allocmbls"): eta and bmin come
+// back at once; the leaves wait in host memory until the block-cluster tree
+// built with them is given to bind_mbls or to the first product with A.
+template <class T>
+void loadmbls(double& eta, unsigned& bmin, mblock<T>**& A, std::ifstream& is) {
+  if (!is) throw std::runtime_error("ahx_ahmed: InputStream not found");
+  auto file = std::make_shared<std::string>(std::istreambuf_iterator<char>(is),
+                                            std::istreambuf_iterator<char>());
+  uint32_t n = 0, b = 0;
+  if (file->size() < 16) throw std::runtime_error("ahx_ahmed: loadmbls: truncated header");
+  std::memcpy(&eta, file->data(), 8);
+  std::memcpy(&b, file->data() + 8, 4);
+  std::memcpy(&n, file->data() + 12, 4);
+  bmin = b;
+  A = new mblock<T>*[n];
+  for (uint32_t i = 0; i < n; ++i) A[i] = new mblock<T>(file, i);
+}
+
+// Uploads leaves read by loadmbls into bl (no-op for leaves already bound).
+template <class T>
+void bind_mbls(blcluster* bl, mblock<T>** A) {
+  if (!A || !bl->nleaves() || !A[0] || !A[0]->pending()) return;
+  struct Src {
+    const std::string* s;
+    size_t pos;
+  } src{A[0]->file().get(), 0};
+  auto get = [](void* ctx, void* buf, uint64_t bytes) -> int64_t {
+    Src& c = *static_cast<Src*>(ctx);
+    const size_t m = std::min<size_t>(bytes, c.s->size() - c.pos);
+    std::memcpy(buf, c.s->data() + c.pos, m);
+    c.pos += m;
+    return (int64_t)m;
+  };
+  check(ahx_hmat_load_stream(bl->handle(), get, &src, nullptr, nullptr));
+  bl->refresh_ranks();
+  for (unsigned long i = 0; i < bl->nleaves(); ++i) A[i]->attach(bl);
+}
+
 // H/mltaGeHVec.cpp:567-577: y += d A x, Y += d A X (permuted ordering)
-inline bool mltaGeHVec(double d, blcluster* bl, mblock<double>**, double* x, double* y) {
+inline bool mltaGeHVec(double d, blcluster* bl, mblock<double>** A, double* x, double* y) {
+  bind_mbls(bl, A);
   check(ahx_matvec(bl->handle(), AHX_FP64, d, 1, x, bl->getn1(), y, bl->getn1()));
   return true;
 }
 
-inline bool mltaGeHGeM(double d, blcluster* bl, mblock<double>**, unsigned p, double* X,
+inline bool mltaGeHGeM(double d, blcluster* bl, mblock<double>** A, unsigned p, double* X,
                        unsigned ldX, double* Y, unsigned ldY) {
+  bind_mbls(bl, A);
   check(ahx_matvec(bl->handle(), AHX_FP64, d, p, X, ldX, Y, ldY));
   return true;
 }
 
 // H/mltaGeHVec.cpp:579-589 (mltaGeHhVec_/mltaGeHhGeM_ :62-105): y += d A^H x, Y += d A^H X (A^T for double)
-inline bool mltaGeHhVec(double d, blcluster* bl, mblock<double>**, double* x, double* y) {
+inline bool mltaGeHhVec(double d, blcluster* bl, mblock<double>** A, double* x, double* y) {
+  bind_mbls(bl, A);
   check(ahx_matvec_transposed(bl->handle(), d, 1, x, bl->getn1(), y, bl->getn1()));
   return true;
 }
 
-inline bool mltaGeHhGeM(double d, blcluster* bl, mblock<double>**, unsigned p, double* X,
+inline bool mltaGeHhGeM(double d, blcluster* bl, mblock<double>** A, unsigned p, double* X,
                         unsigned ldX, double* Y, unsigned ldY) {
+  bind_mbls(bl, A);
   check(ahx_matvec_transposed(bl->handle(), d, p, X, ldX, Y, ldY));
   return true;
 }

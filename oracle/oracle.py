@@ -195,6 +195,8 @@ def ref():
         L.ref_entry.argtypes = [vp, u32, u32]
         L.ref_free.argtypes = [vp]
         L.ref_helm_ranks.argtypes = [vp, dbl, dbl, dbl, u32, vp]
+        L.ref_save.restype = i32
+        L.ref_save.argtypes = [vp, dbl, u32, C.c_char_p]
         _ref = L
     return _ref
 
@@ -246,6 +248,11 @@ class RefH:
         out = np.zeros(cnt, np.float64)
         ref().ref_leaf_data(self._H, l, _p(out))
         return out
+
+    def savembls(self, eta, bmin, path):
+        """The reference's own savembls of the assembled leaves."""
+        if ref().ref_save(self._H, eta, bmin, os.fsencode(path)) != 0:
+            raise RuntimeError("ref_save failed")
 
     def matvec(self, X, Y, d=1.0):
         X = np.ascontiguousarray(X, dtype=np.float64)

@@ -12,9 +12,11 @@
 //   ::ACA + mblock::cpyLrM_cmpr        Include/ACA.h:217-350, Include/mblock.h:822-826
 //   mltaGeHVec / mltaGeHGeM            H/mltaGeHVec.cpp:567-577
 //   GMRes / CG                         solvers/GMRES.cpp:80-181, solvers/CG.cpp:31-113
+//   savembls                           Include/H.h:89-103, Include/mblock.h:737-773
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <iostream>
 #include <sstream>
 #include <vector>
@@ -285,6 +287,17 @@ void ref_helm_ranks(void* p, double wavenumber, double h, double eps, unsigned r
     delete[] U;
     out[l] = succ ? (int)k : -2;
   }
+}
+
+// The reference's savembls (Include/H.h:89-103, mblock::save Include/mblock.h:737-773)
+// of the assembled leaves; returns 0 on success.
+int ref_save(void* p, double eta, unsigned bmin, const char* path) {
+  RefH* H = (RefH*)p;
+  if (!H->A) return 1;
+  std::ofstream os(path, std::ios::binary);
+  if (!os) return 1;
+  savembls(eta, bmin, H->root_bl, H->A, os);
+  return os.good() ? 0 : 1;
 }
 
 void ref_free(void* p) {

@@ -1,5 +1,6 @@
 // The reference's hot-path call sequence (cluster tree, block-cluster tree,
-// allocmbls, matgenGeH_omp, mltaGeHVec, mltaGeHhVec, GMRes, freembls) compiled against
+// allocmbls, matgenGeH_omp, mltaGeHVec, mltaGeHhVec, savembls, loadmbls, GMRes, freembls)
+// compiled against
 // include/ahx_ahmed.hpp.  Checks the product against the dense matrix and
 // GMRES on the diagonal-2/(4 pi h) variant; exit status 0 on success.
 #include <cmath>
@@ -83,6 +84,32 @@ int main(int argc, char** argv) {
   const double err = std::sqrt(num / den), errt = std::sqrt(numt / den);
   std::printf("low-rank leaves %u, product error vs dense %.3e, adjoint %.3e\n", lowrank, err,
               errt);
+  bool io_ok = false;
+  {  // savembls -> loadmbls (Include/H.h:60-103) -> product on a tree built from the file
+    {
+      std::ofstream os("dropin_sphere.mbls", std::ios::binary);
+      savembls(eta, bmin, bl, A, os);
+    }
+    double eta_f = 0.0;
+    unsigned bmin_f = 0, nb = 0;
+    mblock<double>** B = nullptr;
+    std::ifstream is("dropin_sphere.mbls", std::ios::binary);
+    loadmbls(eta_f, bmin_f, B, is);
+    bemblcluster<dof, dof>* bl3 = new bemblcluster<dof, dof>(0, 0, N, N);
+    bl3->subdivide(cl, cl, eta_f * eta_f, nb);
+    std::vector<double> y3(N, 0.0);
+    mltaGeHVec(1.0, bl3, B, x.data(), y3.data());
+    double d3 = 0.0, n3 = 0.0;
+    for (unsigned i = 0; i < N; ++i) {
+      d3 += (y3[i] - y[i]) * (y3[i] - y[i]);
+      n3 += y[i] * y[i];
+    }
+    io_ok = eta_f == eta && bmin_f == bmin && nb == nblcks && B[0]->getn1() == A[0]->getn1() &&
+            std::sqrt(d3 / n3) < 1e-14;
+    std::printf("savembls/loadmbls round trip %s\n", io_ok ? "ok" : "FAILED");
+    freembls(bl3, B);
+    delete bl3;
+  }
   freembls(bl, A);
   delete bl;
 
@@ -102,5 +129,5 @@ int main(int argc, char** argv) {
   freembls(bl2, A);
   delete bl2;
   delete cl;
-  return (err < 2e-6 && errt < 2e-6 && ret == 0 && geps < 1e-8) ? 0 : 1;
+  return (err < 2e-6 && errt < 2e-6 && io_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
 }

@@ -6,6 +6,7 @@ to this script) are committed; the tests read them on any host.
 
 Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py helmholtz  (complex ACA ranks)
+        python tests/golden/make_golden.py mbls       (savembls file hashes)
 """
 import os
 import sys
@@ -107,8 +108,41 @@ def helmholtz():
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+def mbls():
+    """SHA-256 of the reference's own savembls file for sph360 (both trees):
+    pins the byte layout without committing the file (the leaf data it holds
+    are sph360.npz's *_data)."""
+    import hashlib
+    import json
+    import tempfile
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    P = G.sphere_surface(360, 11)
+    bmin = 12
+    h = O.mean_nn(P)
+    out = {"case": "sph360", "eta": ETA, "bmin": bmin}
+    gold = np.load(os.path.join(HERE, "sph360.npz"))
+    for kind, kname in ((O.TREE_BBX, "bbx"), (O.TREE_PCA, "pca")):
+        R = O.RefH(P, kind, bmin, ETA, h)
+        R.assemble(EPS, nthreads=1)
+        chunks = [R.leaf_data(l) for l in range(R.nleaves)]
+        if not np.array_equal(np.concatenate(chunks), gold[f"{kname}_data"]):
+            sys.exit("reference leaves differ from sph360.npz")
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "A.mbls")
+            R.savembls(ETA, bmin, path)
+            raw = open(path, "rb").read()
+        out[kname] = {"sha256": hashlib.sha256(raw).hexdigest(), "bytes": len(raw)}
+    path = os.path.join(HERE, "mbls_sph360.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print(f"wrote {path}")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
+    elif len(sys.argv) > 1 and sys.argv[1] == "mbls":
+        mbls()
     else:
         main()

@@ -25,6 +25,7 @@ def test_dropin_compiles_and_builds_trees_on_host(tmp_path):
 @pytest.mark.gpu
 def test_dropin_runs_on_gpu(tmp_path):
     exe = _build(tmp_path)
-    out = subprocess.run([exe, "2048"], capture_output=True, text=True, timeout=300)
+    out = subprocess.run([exe, "2048"], capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
     assert out.returncode == 0, out.stdout + out.stderr
     assert "GMRes ret 0" in out.stdout
+    assert "savembls/loadmbls round trip ok" in out.stdout
