@@ -19,5 +19,5 @@ from .hmatrix import (  # noqa: F401
     mltaGeHVec,
     savembls,
 )
-from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, lib  # noqa: F401
+from ._capi import BF16_FP32, DF64, FP32, FP64, TREE_BBX, TREE_PCA, lib  # noqa: F401
 from .rank_predictor import RankPredictor, training_set  # noqa: F401

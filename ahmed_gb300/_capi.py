@@ -21,6 +21,7 @@ TREE_PCA = 1
 FP64 = 0
 FP32 = 1
 BF16_FP32 = 2
+DF64 = 3
 
 # (name, restype, argtypes) of every exported entry point of include/ahx.h
 _vp, _u32, _u64, _i32, _dbl = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_double

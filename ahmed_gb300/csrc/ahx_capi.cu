@@ -162,6 +162,29 @@ void invalidate_products(ahx_hmat* H) {
 
 void set_error(const std::string& msg) { g_err = msg; }
 
+int prepare_df_x(ProdCopy& pc, uint64_t n, uint32_t p) {
+  return pc.xb.reserve(std::max<uint64_t>(n * p, 1) * 8);
+}
+
+int run_df(const MvLeaf* leaves, const uint32_t* order, uint32_t nleaves, ProdCopy& pc, uint64_t n, double d,
+           uint32_t p, const double* X, uint64_t ldX, double* Y, uint64_t ldY, cudaStream_t s) {
+  int rc = prepare_df_x(pc, n, p);
+  if (rc) return rc;
+  AHX_CUDA(launch_split_df(X, ldX, n, p, d, pc.xb.p, s));
+  DfArgs a;
+  a.leaves = leaves;
+  a.order = order;
+  a.nleaves = nleaves;
+  a.arena = pc.lr.as<float2>();
+  a.X = pc.xb.as<float2>();
+  a.ldX = n;
+  a.p = p;
+  a.Y = Y;
+  a.ldY = ldY;
+  AHX_CUDA(launch_matvec_df(a, s));
+  return AHX_OK;
+}
+
 int cuda_fail(cudaError_t e, const char* where) {
   g_err = std::string(where) + ": " + cudaGetErrorString(e);
   cudaGetLastError();
@@ -196,7 +219,7 @@ bool is_device_ptr(const void* ptr) {
 }
 
 int prepare_product(ahx_hmat* H, int prec) {
-  if (prec < 0 || prec > 2) {
+  if (prec < 0 || prec >= kNumPrecisions) {
     set_error("unknown precision");
     return AHX_ERR_ARG;
   }
@@ -205,6 +228,17 @@ int prepare_product(ahx_hmat* H, int prec) {
   const auto& Ls = H->tree.leaves;
   const uint32_t nl = (uint32_t)Ls.size();
   int rc;
+  if (prec == kDF64) {
+    // the FP64 leaf table, the arena split into (hi, lo) float pairs
+    if ((rc = prepare_product(H, kFP64))) return rc;
+    if ((rc = pc.lr.reserve(std::max<uint64_t>(H->arena64_elems, 1) * 8))) return rc;
+    AHX_CUDA(launch_split_df(H->arena64.as<double>(), H->arena64_elems, H->arena64_elems, 1, 1.0, pc.lr.p,
+                             H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    pc.bytes = H->arena64_elems * 8;
+    pc.valid = true;
+    return AHX_OK;
+  }
   if (prec != kFP64) {
     std::vector<PlanLeaf> pls;
     pls.reserve(nl);
@@ -359,6 +393,12 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   int rc = prepare_product(H, prec);
   if (rc) return rc;
   ProdCopy& pc = H->prod[prec];
+  if (prec == kDF64) {
+    if ((rc = prepare_df_x(pc, H->tree.n, p))) return rc;
+    const ProdCopy& f = H->prod[kFP64];
+    return run_df(f.leaves.as<MvLeaf>(), f.order.as<uint32_t>(), f.nleaves, pc, H->tree.n, d, p, X, ldX, Y,
+                  ldY, H->stream);
+  }
   if (prec != kFP64) {
     const TcPlan pl = mixed_plan(pc, H->tree.n);
     AHX_CUDA(launch_matvec_tc(prec, pl, d, p, X, ldX, Y, ldY, H->stream));

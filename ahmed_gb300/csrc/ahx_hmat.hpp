@@ -107,7 +107,7 @@ struct ahx_hmat {
   std::vector<uint64_t> off;  // element offset of each leaf in arena64
   ahx::DevBuf arena64;
   uint64_t arena64_elems = 0;
-  ahx::ProdCopy prod[3];
+  ahx::ProdCopy prod[ahx::kNumPrecisions];
   // staging buffers for host vectors
   ahx::DevBuf stage_x, stage_y;
   ahx::DevBuf scratch;  // solver scratch
@@ -119,6 +119,11 @@ struct ahx_hmat {
 
 namespace ahx {
 int prepare_product(ahx_hmat* H, int prec);
+// kDF64 product scratch for p right-hand sides (the split X), ahead of graph capture
+int prepare_df_x(ahx::ProdCopy& pc, uint64_t n, uint32_t p);
+// Y += d A X in double-float over a leaf table and pc.lr (the split FP64 arena)
+int run_df(const ahx::MvLeaf* leaves, const uint32_t* order, uint32_t nleaves, ahx::ProdCopy& pc, uint64_t n,
+           double d, uint32_t p, const double* X, uint64_t ldX, double* Y, uint64_t ldY, cudaStream_t s);
 int ensure_device(ahx_hmat* H);
 // Reserves count doubles at the end of the FP64 leaf arena (grows it, stream-ordered).
 int arena_append(ahx_hmat* H, uint64_t count, uint64_t& off);

@@ -13,7 +13,9 @@ enum Precision : int {
   kFP64 = 0,      // plain form: every leaf in FP64
   kFP32 = 1,      // all leaves in FP32, FP32 accumulation
   kBF16FP32 = 2,  // low-rank factors in BF16, dense leaves in FP32, FP32 accumulation
+  kDF64 = 3,      // FP64 leaves as float pairs, double-float arithmetic (FP64-class)
 };
+constexpr int kNumPrecisions = 4;
 
 // One leaf of the product, with absolute row/column offsets into the
 // (possibly concatenated) vectors and an element offset into its arena.
@@ -40,6 +42,25 @@ struct MvArgs {
 };
 
 cudaError_t launch_matvec(int prec, const MvArgs& a, cudaStream_t s);
+
+// Double-float product Y += A X (ahx_matvec_df.cu): arena = the FP64 arena's
+// elements as (hi, lo) float pairs at the same offsets; X = d X split the same
+// way, column-major with leading dimension ldX.
+struct DfArgs {
+  const MvLeaf* leaves;
+  const uint32_t* order;
+  uint32_t nleaves;
+  const float2* arena;
+  const float2* X;
+  uint64_t ldX;
+  uint32_t p;
+  double* Y;
+  uint64_t ldY;
+};
+cudaError_t launch_matvec_df(const DfArgs& a, cudaStream_t s);
+// dst[r + c rows] = (hi, lo) of scale * src[r + c ld], r < rows, c < cols
+cudaError_t launch_split_df(const double* src, uint64_t ld, uint64_t rows, uint32_t cols, double scale,
+                            void* dst, cudaStream_t s);
 
 // Host description of one leaf for plan building: its data in the FP64 arena.
 struct PlanLeaf {

@@ -16,6 +16,7 @@
 // kernels per pass.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -256,8 +257,17 @@ struct Operator {
   virtual ~Operator() { seg_id.release(); }
   // Y += d A X in storage precision prec
   virtual int apply(int prec, double d, uint32_t p, const double* X, double* Y) = 0;
+  // leaf bytes one product at precision prec reads (0: unknown)
+  virtual uint64_t product_bytes(int prec) const {
+    (void)prec;
+    return 0;
+  }
   // everything apply(prec, ...) allocates, done ahead (graph capture allows no allocation)
-  virtual int prepare(int prec) { (void)prec; return AHX_OK; }
+  virtual int prepare(int prec, uint32_t p) {
+    (void)prec;
+    (void)p;
+    return AHX_OK;
+  }
   int init_segments() {
     if (nseg <= 1) return AHX_OK;
     std::vector<uint32_t> id(ntot);
@@ -281,7 +291,12 @@ struct HmatOp : Operator {
   int apply(int prec, double d, uint32_t p, const double* X, double* Y) override {
     return product_device(H, prec, d, p, X, ntot, Y, ntot);
   }
-  int prepare(int prec) override { return prepare_product(H, prec); }
+  uint64_t product_bytes(int prec) const override { return H->prod[prec].bytes; }
+  int prepare(int prec, uint32_t p) override {
+    int rc = prepare_product(H, prec);
+    if (rc || prec != kDF64) return rc;
+    return prepare_df_x(H->prod[kDF64], ntot, p);
+  }
 };
 
 // Reduction plan + device scratch for a family of systems.
@@ -350,11 +365,16 @@ class Solver {
 // consecutive steps of a cycle, valid while the operator precision, the basis
 // buffer and m stay the same (tolerance and step limit are read from device
 // memory, so they may change between calls).
+// A chunk ends in a host check of the running systems, so a cycle may run up to
+// chunk - 1 steps past the last system's convergence: steps whose product reads
+// more leaf data than kLongStepBytes (a millisecond or more) run one per chunk.
 constexpr uint32_t kGraphChunk = 5;
+constexpr uint64_t kLongStepBytes = 256ull << 20;
 struct GmresGraphs {
   int prec = -1;
   const void* vptr = nullptr;
   uint32_t m = 0;
+  uint32_t chunk = 0;
   bool failed = false;  // capture is not possible on this stream: launch directly
   std::vector<cudaGraphExec_t> exec;
   ~GmresGraphs() { reset(); }
@@ -365,6 +385,7 @@ struct GmresGraphs {
     prec = -1;
     vptr = nullptr;
     m = 0;
+    chunk = 0;
   }
 };
 
@@ -386,7 +407,7 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
   const uint64_t vstride = total;
   const uint32_t* sid = sv.segid();
   int rc;
-  if ((rc = op.prepare(prec))) return rc;
+  if ((rc = op.prepare(prec, sv.p_))) return rc;
   if ((rc = vbuf.reserve((size_t)(m + 1) * total * sizeof(double)))) return rc;
   if ((rc = rbuf.reserve(total * sizeof(double)))) return rc;
   double* V = vbuf.as<double>();
@@ -507,11 +528,13 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
     AHX_CUDA(cudaGetLastError());
     return AHX_OK;
   };
-  if (graphs && (graphs->prec != prec || graphs->vptr != V || graphs->m != m)) {
+  const uint32_t chunk = op.product_bytes(prec) > kLongStepBytes ? 1u : kGraphChunk;
+  if (graphs && (graphs->prec != prec || graphs->vptr != V || graphs->m != m || graphs->chunk != chunk)) {
     graphs->reset();
     graphs->prec = prec;
     graphs->vptr = V;
     graphs->m = m;
+    graphs->chunk = chunk;
   }
   auto run_chunk = [&](uint32_t c, uint32_t i0, uint32_t i1) -> int {
     if (!graphs || graphs->failed) return steps(i0, i1);
@@ -559,8 +582,8 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
     AHX_CUDA(cudaMemcpyAsync(g.jbase, &jb, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     const uint32_t icap = std::min(m, maxit - jb);  // steps this cycle may count
     uint32_t ran = 0;
-    for (uint32_t c = 0; c * kGraphChunk < icap; ++c) {
-      const uint32_t i0 = c * kGraphChunk, i1 = std::min(m, i0 + kGraphChunk);
+    for (uint32_t c = 0; c * chunk < icap; ++c) {
+      const uint32_t i0 = c * chunk, i1 = std::min(m, i0 + chunk);
       if ((rc = run_chunk(c, i0, i1))) return rc;
       ran = std::min(i1, icap);
       uint32_t nact = 0;
@@ -606,6 +629,43 @@ int gmres_core(Solver& sv, int prec, const double* B, double* X, double tol, uin
 
 // GMRES with the storage precision `prec`: FP64 runs gmres_core directly; the
 // mixed forms run FP64 iterative refinement around inner GMRES cycles.
+// AHX_TRACE=1: per outer refinement step, the residual product and inner
+// solve times (CUDA events on the solver stream) on stderr.
+struct StepTrace {
+  bool on = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  explicit StepTrace(cudaStream_t s) : st(s) {
+    const char* e = std::getenv("AHX_TRACE");
+    on = e && *e && *e != '0';
+    if (on)
+      for (auto& x : ev) on = on && cudaEventCreate(&x) == cudaSuccess;
+  }
+  ~StepTrace() {
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+  }
+  void mark(int i) {
+    if (on) cudaEventRecord(ev[i], st);
+  }
+  // after mark(2): residual = ev0..ev1, inner solve = ev1..ev2
+  void report(int step, int rprec, int iprec, uint32_t its, double res) {
+    if (!on) return;
+    float a = 0.f, b = 0.f;
+    cudaEventSynchronize(ev[2]);
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&b, ev[1], ev[2]);
+    std::fprintf(stderr, "ahx gmres refine step %d: residual[prec %d] %.3f ms (max rel %.3e), inner[prec %d] %u its %.3f ms\n",
+                 step, rprec, a, res, iprec, its, b);
+  }
+  cudaStream_t st;
+};
+
+// Precision of the refinement's outer residual: kDF64 (default) or kFP64.
+int refine_residual_precision() {
+  const char* e = std::getenv("AHX_REFINE_RESIDUAL");
+  return (e && std::string(e) == "fp64") ? kFP64 : kDF64;
+}
+
 int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X, double tol,
                  uint32_t m, uint32_t maxit, uint32_t* iters_out, double* resid_out, int& status) {
   if (m == 0) {
@@ -620,8 +680,8 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
   std::vector<double> resid(nsys, 0.0);
   std::vector<char> done(nsys, 0);
   DevBuf vbuf, rbuf, rr, z;
-  GmresGraphs graphs[3];  // per operator precision
-  if (prec == kFP64) {
+  GmresGraphs graphs[kNumPrecisions];  // per operator precision
+  if (prec == kFP64 || prec == kDF64) {
     rc = gmres_core(sv, kFP64, B, X, tol, m, maxit, iters, resid, done, vbuf, rbuf, &graphs[kFP64]);
   } else {
     // FP64 refinement: r = b - A64 x (FP64 leaves), solve A_prec z = r by one
@@ -630,6 +690,10 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     if ((rc = rr.reserve(total * sizeof(double)))) return rc;
     if ((rc = z.reserve(total * sizeof(double)))) return rc;
     cudaStream_t st = op.stream;
+    // the outer residual in FP64-class arithmetic: double-float on the FP32
+    // pipes unless AHX_REFINE_RESIDUAL=fp64 asks for the FP64 product
+    const int resid_prec = refine_residual_precision();
+    if ((rc = op.prepare(resid_prec, p))) return rc;
     // inner tolerance near the storage precision's product accuracy (FP32
     // ~3e-7, BF16 factors ~4e-4): fewer outer steps, i.e. fewer FP64 products
     const double inner_tol = prec == kFP32 ? 1e-6 : 1e-3;
@@ -652,11 +716,15 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     AHX_CUDA(cudaStreamSynchronize(st));
     bool x_zero = true;
     for (uint32_t q = 0; q < nsys; ++q) x_zero = x_zero && nb[(size_t)q * sv.maxk_] == 0.0;
+    StepTrace trace(st);
+    int outer = 0;
     for (;;) {
+      trace.mark(0);
       AHX_CUDA(cudaMemcpyAsync(rr.p, B, total * 8, cudaMemcpyDeviceToDevice, st));
-      if (!x_zero && (rc = op.apply(kFP64, -1.0, p, X, rr.as<double>()))) return rc;
+      if (!x_zero && (rc = op.apply(resid_prec, -1.0, p, X, rr.as<double>()))) return rc;
       x_zero = false;
       if ((rc = sv.dots(rr.as<double>(), 0, 1, rr.as<double>(), sv.small_.as<double>()))) return rc;
+      trace.mark(1);
       AHX_CUDA(cudaMemcpyAsync(nb.data(), sv.small_.p, nb.size() * 8, cudaMemcpyDeviceToHost, st));
       AHX_CUDA(cudaStreamSynchronize(st));
       bool worse = false;
@@ -674,7 +742,7 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
         AHX_CUDA(cudaMemcpyAsync(sv.small2_.p, undo.data(), nsys * 8, cudaMemcpyHostToDevice, st));
         axpy_sys_kernel<<<grid_for(total), 256, 0, st>>>(X, X, z.as<double>(), sv.small2_.as<double>(), total,
                                                          op.ntot, sv.segid(), op.nseg);
-        inner_prec = kFP64;
+        inner_prec = resid_prec;
         undone = true;
         continue;
       }
@@ -703,7 +771,7 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
       std::vector<double> res2(nsys, 0.0);
       const uint32_t budget = std::min(m, maxit - used);
       if ((rc = gmres_core(sv, inner_prec, rr.as<double>(), z.as<double>(),
-                           inner_prec == kFP64 ? std::max(tol, 1e-12) : inner_tol, m, budget, it2, res2,
+                           inner_prec == resid_prec ? std::max(tol, 1e-12) : inner_tol, m, budget, it2, res2,
                            idone, vbuf, rbuf, &graphs[inner_prec])))
         return rc;
       uint32_t step = 0;
@@ -713,6 +781,12 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
           step = std::max(step, it2[q]);
         }
       used += std::max(step, 1u);
+      trace.mark(2);
+      {
+        double rmax = 0.0;
+        for (uint32_t q = 0; q < nsys; ++q) rmax = std::max(rmax, prev[q]);
+        trace.report(++outer, resid_prec, inner_prec, step, rmax);
+      }
       // x += z
       std::vector<double> ones(nsys, 1.0);
       AHX_CUDA(cudaMemcpyAsync(sv.small2_.p, ones.data(), nsys * 8, cudaMemcpyHostToDevice, st));
@@ -855,8 +929,9 @@ struct ahx_batch : ahx::Operator {
   struct Tab {
     ahx::DevBuf leaves, order, lr, dn;
     uint32_t nleaves = 0;
+    uint64_t elems = 0;  // FP64 arena elements (kFP64 table)
     ahx::ProdCopy plan;  // mixed-precision plan over the concatenated leaves
-  } tab[3];
+  } tab[ahx::kNumPrecisions];
   ahx::DevBuf stx, sty;
 
   // FP64: concatenated leaf table and arena; mixed precisions: streams built
@@ -864,6 +939,19 @@ struct ahx_batch : ahx::Operator {
   int build_tab(int pr) {
     using namespace ahx;
     Tab& T = tab[pr];
+    if (pr == kDF64) {
+      // the concatenated FP64 arena split into (hi, lo) float pairs
+      Tab& F = tab[kFP64];
+      const uint64_t elems = F.elems;
+      int rc = T.plan.lr.reserve(std::max<uint64_t>(elems, 1) * 8);
+      if (rc) return rc;
+      AHX_CUDA(launch_split_df(F.lr.as<double>(), elems, elems, 1, 1.0, T.plan.lr.p, stream));
+      AHX_CUDA(cudaStreamSynchronize(stream));
+      T.nleaves = F.nleaves;
+      T.plan.bytes = elems * 8;
+      T.plan.valid = true;
+      return AHX_OK;
+    }
     if (pr != kFP64) {
       Tab& F = tab[kFP64];
       std::vector<MvLeaf> lv(F.nleaves);
@@ -913,12 +1001,29 @@ struct ahx_batch : ahx::Operator {
     }
     AHX_CUDA(cudaStreamSynchronize(stream));
     T.nleaves = (uint32_t)all.size();
+    T.elems = elems;
     return AHX_OK;
+  }
+
+  int prepare(int pr, uint32_t p) override {
+    if (pr != ahx::kDF64) return AHX_OK;
+    int rc;
+    if (!tab[pr].plan.valid && (rc = build_tab(pr))) return rc;
+    return ahx::prepare_df_x(tab[pr].plan, ntot, p);
+  }
+
+  uint64_t product_bytes(int pr) const override {
+    return pr == ahx::kFP64 ? tab[pr].elems * sizeof(double) : tab[pr].plan.bytes;
   }
 
   int apply(int pr, double d, uint32_t p, const double* X, double* Y) override {
     using namespace ahx;
     Tab& T = tab[pr];
+    if (pr == kDF64) {
+      const Tab& F = tab[kFP64];
+      return run_df(F.leaves.as<MvLeaf>(), F.order.as<uint32_t>(), F.nleaves, T.plan, ntot, d, p, X, ntot, Y,
+                    ntot, stream);
+    }
     if (pr != kFP64) {
       const TcPlan pl = mixed_plan(T.plan, ntot);
       AHX_CUDA(launch_matvec_tc(pr, pl, d, p, X, ntot, Y, ntot, stream));
@@ -949,7 +1054,7 @@ int ahx_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t 
               uint64_t ldX, double tol, uint32_t m, uint32_t maxit, uint32_t* iters,
               double* resid) {
   if (!H || !B || !X || p == 0 || ldB < H->tree.n || ldX < H->tree.n || precision < 0 ||
-      precision > 2) {
+      precision >= kNumPrecisions) {
     set_error("ahx_gmres: invalid argument");
     return AHX_ERR_ARG;
   }
@@ -1008,7 +1113,7 @@ int ahx_cg(ahx_hmat* H, uint32_t p, const double* B, uint64_t ldB, double* X, ui
 }
 
 int ahx_batch_create(ahx_hmat* const* mats, uint32_t count, int precision, ahx_batch** out) {
-  if (!mats || !out || count == 0 || precision < 0 || precision > 2) {
+  if (!mats || !out || count == 0 || precision < 0 || precision >= kNumPrecisions) {
     set_error("ahx_batch_create: invalid argument");
     return AHX_ERR_ARG;
   }

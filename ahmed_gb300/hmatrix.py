@@ -13,9 +13,9 @@ import weakref
 import numpy as np
 
 from . import _capi
-from ._capi import BF16_FP32, FP32, FP64, TREE_BBX, TREE_PCA, check, lib, ptr
+from ._capi import BF16_FP32, DF64, FP32, FP64, TREE_BBX, TREE_PCA, check, lib, ptr
 
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16_FP32}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16_FP32, "df64": DF64}
 TREES = {"bbx": TREE_BBX, "pca": TREE_PCA}
 
 

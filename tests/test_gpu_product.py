@@ -182,3 +182,28 @@ def test_transposed_product(oracle_pair, kind):
             A[b1:b1 + n1, b2:b2 + n2] = U @ V.T
     ref = -0.5 * (A.T @ X.T).T
     assert np.linalg.norm(AtX - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("p", [1, 5, 16, 17, 64])
+@pytest.mark.parametrize("kind", ["bbx", "pca"])
+def test_df64_product_matches_fp64(oracle_pair, kind, p):
+    """Double-float product (FP64 leaves as float pairs, FP32 pipes) within 1e-13
+    of the FP64 product per right-hand side, d = -0.75 applied exactly."""
+    _, H = oracle_pair[kind]
+    n = H.n
+    X = np.random.default_rng(11 + p).uniform(-1, 1, (p, n))
+    Y0 = np.random.default_rng(12).uniform(-1, 1, (p, n))
+    Y64 = H.mltaGeHVec(-0.75, X, Y0.copy())
+    Ydf = H.mltaGeHVec(-0.75, X, Y0.copy(), precision="df64")
+    for r in range(p):
+        assert _relerr(Ydf[r] - Y0[r], Y64[r] - Y0[r]) <= 1e-13
+
+
+def test_df64_product_on_reference_leaves(golden):
+    """The reference's leaves (sph360, PCA tree): within 1e-12 of its mltaGeHVec."""
+    g = golden("sph360")
+    offs, data = g["pca_offsets"], g["pca_data"]
+    chunks = [data[offs[l]:offs[l + 1]] for l in range(len(offs) - 1)]
+    H = _with_leaves(g, "pca", g["pca_ranks"], chunks)
+    y = H.mltaGeHVec(1.0, g["x"], np.zeros(H.n), precision="df64")
+    assert _relerr(y, g["pca_y"]) <= TOL_FP64

@@ -78,8 +78,11 @@ def test_gmres_multi_rhs_equals_single(pair):
         assert _relerr(X[r], x1) <= 1e-10
 
 
+@pytest.mark.parametrize("resid", ["df64", "fp64"])
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
-def test_gmres_mixed_with_fp64_refinement(pair, prec):
+def test_gmres_mixed_with_fp64_refinement(pair, prec, resid, monkeypatch):
+    """Outer residual in double-float (default) or with the FP64 product."""
+    monkeypatch.setenv("AHX_REFINE_RESIDUAL", resid)
     _, d = pair
     _, H = d["spd"]
     b = np.random.default_rng(5).standard_normal(H.n)
@@ -88,6 +91,18 @@ def test_gmres_mixed_with_fp64_refinement(pair, prec):
     assert ret == 0, (eps, its)
     r = b - H.mltaGeHVec(1.0, x, np.zeros(H.n))
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-8
+
+
+def test_gmres_df64_matches_fp64(pair):
+    """GMRES on the double-float product follows the FP64 one (same steps)."""
+    g, d = pair
+    _, H = d["spd"]
+    b = g["gmres_b"]
+    x64, xdf = np.zeros(H.n), np.zeros(H.n)
+    r1, e1, i1 = H.GMRes(b, x64, 1e-8, 30, 300)
+    r2, e2, i2 = H.GMRes(b, xdf, 1e-8, 30, 300, precision="df64")
+    assert r1 == r2 == 0 and abs(int(i1[0]) - int(i2[0])) <= 1
+    assert _relerr(xdf, x64) <= 1e-7
 
 
 def test_gmres_zero_rhs_and_initial_guess(pair):
@@ -126,7 +141,7 @@ def test_batch_product_and_gmres_match_instances():
         H = A.HMatrix(P, "bbx")
         H.matgenGeH_omp(A.mean_nn(P), 1e-6)
         mats.append(H)
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "df64"):
         B = A.HBatch(mats, precision=prec)
         assert B.n == sum(m.n for m in mats)
         x = np.random.default_rng(7).uniform(-1, 1, B.n)
@@ -134,7 +149,7 @@ def test_batch_product_and_gmres_match_instances():
         for i, H in enumerate(mats):
             o0, o1 = B.offsets[i], B.offsets[i + 1]
             yi = H.mltaGeHVec(1.0, x[o0:o1], np.zeros(H.n), precision=prec)
-            assert _relerr(y[o0:o1], yi) <= (1e-12 if prec == "fp64" else 1e-6)
+            assert _relerr(y[o0:o1], yi) <= (1e-6 if prec == "fp32" else 1e-12)
     # batched GMRES = per-instance GMRES, on well-conditioned instances (Fibonacci
     # spheres, diagonal 2/(4 pi h)) so that rounding differences of the atomically
     # summed products are not amplified
