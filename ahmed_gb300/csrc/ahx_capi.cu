@@ -295,6 +295,20 @@ int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& lea
   const uint32_t grid = (uint32_t)std::max(sms, 1);
   TcLayout L;
   build_tc_layout(leaves, bf, pmax, grid * kTcGroups, L, unit_bytes);
+  {
+    // every unit (fragments + its A rows) must fit one ring slot
+    const uint64_t s_t = (uint64_t)(pmax + 8) * (bf ? 2 : 4), s_x = (uint64_t)(pmax + 8) * 4;
+    for (const TcVUnit& u : L.vunits)
+      if (u.bytes + u.kp * s_t > kTcSlotData) {
+        set_error("mixed product layout: a V unit exceeds the ring slot");
+        return AHX_ERR_ARG;
+      }
+    for (const TcRowUnit& u : L.runits)
+      if (u.bytes + u.kp0 * s_t + u.kp1 * s_x > kTcSlotData) {
+        set_error("mixed product layout: a rows unit exceeds the ring slot");
+        return AHX_ERR_ARG;
+      }
+  }
   AHX_CUDA(tc_init_attributes());
   int rc;
   if ((rc = pc.vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;

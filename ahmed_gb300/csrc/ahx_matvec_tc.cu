@@ -17,6 +17,7 @@
 // queued, and all warps return.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <map>
 #include <numeric>
 #include <type_traits>
@@ -279,6 +280,77 @@ __device__ __forceinline__ void bf16_group(const unsigned char* frag, const unsi
 }
 
 // ---------------------------------------------------------------------------
+// Narrow form (one right-hand side): the same fragment-ordered streams read by
+// FP32 FMAs instead of mma.sync, so a single-vector product does 1/16 of the
+// arithmetic of a 16-wide pass.  X and T rows have the stride kSN (elements)
+// and only column 0 is read; lane (g, t) of a fragment holds column 8 n + g of
+// the k-block's rows listed at frag_pos, and the four lanes t of one g sum
+// their partial dot products at the end.
+constexpr uint32_t kSN = 8;
+
+__device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// FP32 B words (k-blocks of 8: b.x = B[8 kb + t][.], b.y = B[8 kb + t + 4][.]), FP32 A rows
+template <int NT>
+__device__ __forceinline__ void narrow_f32(const unsigned char* frag, const float* side, uint32_t kp, uint32_t nt,
+                                           uint32_t n0, float (&acc)[NT], uint32_t lane) {
+  const uint32_t t = lane & 3;
+  const uint2* fb = reinterpret_cast<const uint2*>(frag) + n0 * 32 + lane;
+  for (uint32_t kb = 0; kb < (kp >> 3); ++kb) {
+    const float a0 = side[(kb * 8 + t) * kSN], a1 = side[(kb * 8 + t + 4) * kSN];
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      if (n0 + n < nt) {
+        const uint2 b = fb[(kb * nt + n) * 32];
+        acc[n] = fmaf(a1, __uint_as_float(b.y), fmaf(a0, __uint_as_float(b.x), acc[n]));
+      }
+  }
+}
+
+// BF16 B words (k-blocks of 16: b.x = B[16 kb + 2t, + 1][.], b.y = B[16 kb + 2t + 8, + 9][.];
+// a last block of 8 when kp % 16 == 8), BF16 A rows
+template <int NT>
+__device__ __forceinline__ void narrow_bf16(const unsigned char* frag, const __nv_bfloat16* side, uint32_t kp,
+                                            uint32_t nt, uint32_t n0, float (&acc)[NT], uint32_t lane) {
+  const uint32_t t = lane & 3;
+  const uint16_t* sh = reinterpret_cast<const uint16_t*>(side);
+  const uint32_t kfull = kp >> 4;
+  const uint2* fb = reinterpret_cast<const uint2*>(frag) + n0 * 32 + lane;
+  for (uint32_t kb = 0; kb < kfull; ++kb) {
+    const uint32_t k = kb * 16 + 2 * t;
+    const float a0 = bf_lo(sh[k * kSN]), a1 = bf_lo(sh[(k + 1) * kSN]);
+    const float a2 = bf_lo(sh[(k + 8) * kSN]), a3 = bf_lo(sh[(k + 9) * kSN]);
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      if (n0 + n < nt) {
+        const uint2 b = fb[(kb * nt + n) * 32];
+        float c = fmaf(a0, bf_lo(b.x), acc[n]);
+        c = fmaf(a1, bf_hi(b.x), c);
+        c = fmaf(a2, bf_lo(b.y), c);
+        acc[n] = fmaf(a3, bf_hi(b.y), c);
+      }
+  }
+  if (kp & 8) {
+    const uint32_t* ft = reinterpret_cast<const uint32_t*>(frag + (size_t)kfull * nt * 256) + n0 * 32 + lane;
+    const uint32_t k = kfull * 16 + 2 * t;
+    const float a0 = bf_lo(sh[k * kSN]), a1 = bf_lo(sh[(k + 1) * kSN]);
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      if (n0 + n < nt) {
+        const uint32_t b = ft[n * 32];
+        acc[n] = fmaf(a1, bf_hi(b), fmaf(a0, bf_lo(b), acc[n]));
+      }
+  }
+}
+
+// lane 4 g (t = 0) receives the sum over t of column g's partial sums
+__device__ __forceinline__ float narrow_sum(float v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v + __shfl_xor_sync(0xffffffffu, v, 2);
+}
+
+// ---------------------------------------------------------------------------
 // Rings.  Group g of the CTA owns kR slots; slot s has a "full" mbarrier
 // (count 1: the producer's arrive.expect_tx; the bulk copies complete its
 // transaction count) and an "empty" mbarrier (count WPU: one arrive per
@@ -420,13 +492,13 @@ __device__ void consume(const Ring& R, const uint32_t* ranges, uint32_t g, uint3
 static_assert(sizeof(TcVUnit) == kTcHead && sizeof(TcRowUnit) == kTcHead, "descriptor = slot head");
 
 // ---- V sweep: T rows (T^T = X^T V per column cluster)
-template <int P, bool BF>
+template <int P, bool BF, bool NARROW = false>
 __global__ void __launch_bounds__((Cfg<P, false>::kThreads), 1) __maxnreg__((Cfg<P, false>::kRegs))
     tc_v_kernel(TcPlan pl) {
   using TT = typename std::conditional<BF, __nv_bfloat16, float>::type;
   using C = Cfg<P, false>;
   constexpr int MTW = C::MTW;
-  constexpr uint32_t SX = (P + 8) * sizeof(TT);  // X row bytes (V's type)
+  constexpr uint32_t SX = (NARROW ? kSN : P + 8) * sizeof(TT);  // X row bytes (V's type)
   const Ring R = ring_init<C::kEmpty>();
   const uint32_t warp = threadIdx.x >> 5;
   if (warp >= (uint32_t)C::kConsumers) {
@@ -449,6 +521,28 @@ __global__ void __launch_bounds__((Cfg<P, false>::kThreads), 1) __maxnreg__((Cfg
   const uint32_t g = warp / C::W, h = warp % C::W;
   const uint32_t lane = threadIdx.x & 31, j = (lane >> 2) & 3, q = lane >> 4, t = lane & 3;
   TT* T = reinterpret_cast<TT*>(pl.t);
+  if constexpr (NARROW) {
+    // the two consumers split each unit's n-tiles (4 each); T rows of stride kSN
+    const uint32_t n0 = h * 4;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    consume<C::SEQ, TcVUnit>(R, pl.vranges, g, 0, pl.err, [&](const TcVUnit& U, const unsigned char* data, uint32_t) {
+      if (U.flags & 1u) acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+      const uint32_t nt = (U.ncols + 7u) >> 3;
+      if (n0 >= nt) return;
+      if constexpr (BF) narrow_bf16<4>(data, reinterpret_cast<const __nv_bfloat16*>(data + U.bytes), U.kp, nt, n0, acc, lane);
+      else narrow_f32<4>(data, reinterpret_cast<const float*>(data + U.bytes), U.kp, nt, n0, acc, lane);
+      if (U.flags & 2u) {
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+          if (n0 + n < nt) {
+            const float v = narrow_sum(acc[n]);
+            const uint32_t col = 8 * (n0 + n) + (lane >> 2);
+            if (t == 0 && col < U.ncols) T[(uint64_t)(U.trow + col) * kSN] = (TT)v;
+          }
+      }
+    });
+    return;
+  }
   Accs<MTW, !BF> acc;
   acc.zero();
   const uint32_t mt0 = C::MSPLIT ? h * MTW : 0, n0 = C::NSPLIT ? h * C::NTW : 0;
@@ -488,30 +582,33 @@ __global__ void __launch_bounds__((Cfg<P, false>::kThreads), 1) __maxnreg__((Cfg
   });
 }
 
-template <int P, bool BF>
+// NARROW: T rows of stride kSN, column 0 only
+template <int P, bool BF, bool NARROW = false>
 __global__ void tc_treduce_kernel(const TcTReduce* __restrict__ items, uint32_t n, void* tv) {
   using TT = typename std::conditional<BF, __nv_bfloat16, float>::type;
+  constexpr uint32_t W = NARROW ? 1 : P, S = NARROW ? kSN : P + 8;
   TT* T = reinterpret_cast<TT*>(tv);
   const uint32_t it = blockIdx.x;
   if (it >= n) return;
   const TcTReduce R = items[it];
-  for (uint32_t e = threadIdx.x; e < R.ncols * P; e += blockDim.x) {
-    const uint32_t c = e / P, p = e % P;
-    float s = (float)T[(uint64_t)(R.dst + c) * (P + 8) + p];
-    for (uint32_t k = 0; k < R.nsrc; ++k) s += (float)T[(uint64_t)(R.src + k * R.ncols + c) * (P + 8) + p];
-    T[(uint64_t)(R.dst + c) * (P + 8) + p] = (TT)s;
+  for (uint32_t e = threadIdx.x; e < R.ncols * W; e += blockDim.x) {
+    const uint32_t c = e / W, p = e % W;
+    float s = (float)T[(uint64_t)(R.dst + c) * S + p];
+    for (uint32_t k = 0; k < R.nsrc; ++k) s += (float)T[(uint64_t)(R.src + k * R.ncols + c) * S + p];
+    T[(uint64_t)(R.dst + c) * S + p] = (TT)s;
   }
 }
 
 // ---- rows sweep: Yr[row0 + n][p] += sum over the tile's groups
-template <int P, bool BF>
+template <int P, bool BF, bool NARROW = false>
 __global__ void __launch_bounds__((Cfg<P, true>::kThreads), 1) __maxnreg__((Cfg<P, true>::kRegs))
     tc_rows_kernel(TcPlan pl) {
   using TT = typename std::conditional<BF, __nv_bfloat16, float>::type;
   using C = Cfg<P, true>;
   constexpr int MTW = C::MTW;
-  constexpr uint32_t S0 = (P + 8) * sizeof(TT);  // T row bytes
-  constexpr uint32_t S1 = (P + 8) * 4;           // FP32 X row bytes
+  constexpr uint32_t SE = NARROW ? kSN : P + 8;  // row stride (elements) of T and X rows
+  constexpr uint32_t S0 = SE * sizeof(TT);       // T row bytes
+  constexpr uint32_t S1 = SE * 4;                // FP32 X row bytes
   constexpr uint32_t ES0 = sizeof(TT);
   const Ring R = ring_init<C::kEmpty>();
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -573,6 +670,41 @@ __global__ void __launch_bounds__((Cfg<P, true>::kThreads), 1) __maxnreg__((Cfg<
   const uint32_t g = warp / C::W, h = warp % C::W;
   const uint32_t mt0 = C::MSPLIT ? h * MTW : 0;
   const uint32_t j = (lane >> 2) & 3, q = lane >> 4, t = lane & 3;
+  if constexpr (NARROW) {
+    // each consumer takes every other unit (whole tiles); Yr has one float per row
+    float acc[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) acc[n] = 0.f;
+    uint32_t cur_row0 = 0, cur_nr = 0;
+    auto flush = [&]() {
+      const uint32_t nt = (cur_nr + 7u) >> 3;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        if ((uint32_t)n < nt) {
+          const float v = narrow_sum(acc[n]);
+          const uint32_t row = 8 * n + (lane >> 2);
+          if (t == 0 && row < cur_nr) atomicAdd(pl.yr + cur_row0 + row, v);
+        }
+        acc[n] = 0.f;
+      }
+    };
+    consume<C::SEQ, TcRowUnit>(R, pl.rranges, g, h, pl.err, [&](const TcRowUnit& U, const unsigned char* data, uint32_t) {
+      if (cur_nr && (U.row0 != cur_row0 || U.nr != cur_nr)) flush();
+      cur_row0 = U.row0;
+      cur_nr = U.nr;
+      const uint32_t nt = (U.nr + 7u) >> 3;
+      const unsigned char* side0 = data + U.bytes;
+      if (U.kp0) {
+        if constexpr (BF) narrow_bf16<8>(data, reinterpret_cast<const __nv_bfloat16*>(side0), U.kp0, nt, 0, acc, lane);
+        else narrow_f32<8>(data, reinterpret_cast<const float*>(side0), U.kp0, nt, 0, acc, lane);
+      }
+      if (U.kp1)
+        narrow_f32<8>(data + (size_t)U.kp0 * nt * 8 * sizeof(TT), reinterpret_cast<const float*>(side0 + (size_t)U.kp0 * S0),
+                      U.kp1, nt, 0, acc, lane);
+    });
+    if (cur_nr) flush();
+    return;
+  }
   Accs<MTW, !BF> acc;
   acc.zero();
   // consecutive units of one tile accumulate; a change of tile (or the end)
@@ -665,6 +797,33 @@ __global__ void tc_yr_kernel(const float* __restrict__ yr, uint64_t n, uint32_t 
   }
 }
 
+// narrow X rows (stride kSN): column 0 = X[r0 * ldX + i] (TF32-rounded FP32 and
+// BF16 when BF), the rest zero
+template <bool BF>
+__global__ void tc_xr_narrow_kernel(const double* __restrict__ X, uint64_t n, float* __restrict__ xf,
+                                    __nv_bfloat16* __restrict__ xb) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const float v = (float)X[i];
+    float4* of = reinterpret_cast<float4*>(xf + i * kSN);
+    of[0] = make_float4(BF ? __uint_as_float(to_tf32(v)) : v, 0.f, 0.f, 0.f);
+    of[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (BF) {
+      __nv_bfloat162 b[4];
+      b[0] = __floats2bfloat162_rn(v, 0.f);
+      b[1] = b[2] = b[3] = __floats2bfloat162_rn(0.f, 0.f);
+      *reinterpret_cast<uint4*>(xb + i * kSN) = *reinterpret_cast<uint4*>(b);
+    }
+  }
+}
+
+// Y[i] += d * Yr[i] (narrow Yr: one float per row)
+__global__ void tc_yr_narrow_kernel(const float* __restrict__ yr, uint64_t n, double d, double* __restrict__ Y) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    Y[i] += d * (double)yr[i];
+}
+
 // byte position of B[k][n] in fragment order (see TcFragTask)
 __host__ __device__ __forceinline__ uint64_t frag_pos(uint32_t k, uint32_t n, uint32_t kp, uint32_t nt, uint32_t dtype) {
   const uint32_t g = n & 7, ntile = n >> 3;
@@ -709,11 +868,28 @@ unsigned grid_rows(uint64_t n) { return (unsigned)std::min<uint64_t>((n + 255) /
 
 std::atomic<uint64_t> g_product_launches{0};
 
-template <int P, bool BF>
+template <int P, bool BF, bool NARROW = false>
 cudaError_t set_attributes() {
-  cudaError_t e = cudaFuncSetAttribute(tc_v_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  cudaError_t e =
+      cudaFuncSetAttribute(tc_v_kernel<P, BF, NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(tc_rows_kernel<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  return cudaFuncSetAttribute(tc_rows_kernel<P, BF, NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+}
+
+// one right-hand side (column r0 of X and Y): the narrow sweeps
+template <bool BF>
+cudaError_t run_tc_narrow(const TcPlan& pl, double d, uint32_t r0, const double* X, uint64_t ldX, double* Y,
+                          uint64_t ldY, cudaStream_t s) {
+  tc_xr_narrow_kernel<BF><<<grid_rows(pl.n), 256, 0, s>>>(X + (uint64_t)r0 * ldX, pl.n, pl.xf,
+                                                         reinterpret_cast<__nv_bfloat16*>(pl.xb));
+  g_product_launches += 2 + (pl.nvunits ? 1 : 0) + (pl.ntreduce ? 1 : 0) + (pl.nrunits ? 1 : 0);
+  cudaError_t e = cudaMemsetAsync(pl.yr, 0, pl.n * sizeof(float), s);
+  if (e != cudaSuccess) return e;
+  if (pl.nvunits) tc_v_kernel<16, BF, true><<<pl.grid, Cfg<16, false>::kThreads, kSmem, s>>>(pl);
+  if (pl.ntreduce) tc_treduce_kernel<16, BF, true><<<pl.ntreduce, 128, 0, s>>>(pl.treduce, pl.ntreduce, pl.t);
+  if (pl.nrunits) tc_rows_kernel<16, BF, true><<<pl.grid, Cfg<16, true>::kThreads, kSmem, s>>>(pl);
+  tc_yr_narrow_kernel<<<grid_rows(pl.n), 256, 0, s>>>(pl.yr, pl.n, d, Y + (uint64_t)r0 * ldY);
+  return cudaGetLastError();
 }
 
 template <int P, bool BF>
@@ -731,15 +907,26 @@ cudaError_t run_tc_group(const TcPlan& pl, double d, uint32_t r0, uint32_t pg, c
   return cudaGetLastError();
 }
 
+// AHX_NARROW=0 runs single-vector products through the 16-wide sweeps
+bool narrow_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("AHX_NARROW");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <bool BF>
 cudaError_t run_tc(const TcPlan& pl, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
                    uint64_t ldY, cudaStream_t s) {
   for (uint32_t r0 = 0; r0 < p; r0 += pl.pmax) {
     const uint32_t pg = std::min(pl.pmax, p - r0);
     cudaError_t e;
-    // FP32 storage runs 16 right-hand sides per pass (its 3-pass products
-    // would make wider passes tensor-bound); BF16 up to 64
-    if (!BF || pg <= 16) e = run_tc_group<16, BF>(pl, d, r0, pg, X, ldX, Y, ldY, s);
+    // one right-hand side: FP32 FMAs on the fragments (narrow sweeps); FP32
+    // storage runs 16 right-hand sides per pass (its 3-pass products would make
+    // wider passes tensor-bound); BF16 up to 64
+    if (pg == 1 && narrow_enabled()) e = run_tc_narrow<BF>(pl, d, r0, X, ldX, Y, ldY, s);
+    else if (!BF || pg <= 16) e = run_tc_group<16, BF>(pl, d, r0, pg, X, ldX, Y, ldY, s);
     else if (pg <= 32) e = run_tc_group<32, true>(pl, d, r0, pg, X, ldX, Y, ldY, s);
     else e = run_tc_group<64, true>(pl, d, r0, pg, X, ldX, Y, ldY, s);
     if (e != cudaSuccess) return e;
@@ -765,6 +952,8 @@ cudaError_t tc_init_attributes() {
   if ((e = set_attributes<16, false>()) != cudaSuccess) return e;
   if ((e = set_attributes<16, true>()) != cudaSuccess) return e;
   if ((e = set_attributes<32, true>()) != cudaSuccess) return e;
+  if ((e = set_attributes<16, false, true>()) != cudaSuccess) return e;
+  if ((e = set_attributes<16, true, true>()) != cudaSuccess) return e;
   return set_attributes<64, true>();
 }
 void count_product_launches(uint64_t n) { g_product_launches += n; }
@@ -817,7 +1006,8 @@ void build_tc_layout(const std::vector<PlanLeaf>& leaves, bool lr_bf16, uint32_t
     for (uint32_t c0 = 0; c0 < kc; c0 += 64) {
       const uint32_t nc = std::min(64u, kc - c0), nt = (nc + 7) / 8;
       const uint32_t rowb = nt * 8 * es + s_t;
-      const uint32_t chunk = std::max(16u, (cap / rowb) & ~15u);
+      const uint32_t q = cap / rowb;  // rows per unit: multiples of 16, or of 8 for small caps
+      const uint32_t chunk = q >= 16 ? q & ~15u : std::max(8u, q & ~7u);
       VGroup G{L.vunits.size(), 0, tb + c0, nc};
       for (uint32_t j0 = 0; j0 < n2; j0 += chunk) {
         const uint32_t jn = std::min(chunk, n2 - j0), kp = round8(jn);

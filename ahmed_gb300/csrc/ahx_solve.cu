@@ -959,7 +959,9 @@ struct ahx_batch : ahx::Operator {
       std::vector<PlanLeaf> pls;
       pls.reserve(lv.size());
       for (const MvLeaf& m : lv) pls.push_back(PlanLeaf{m.b1, m.n1, m.b2, m.n2, m.rank, m.off});
-      return build_mixed_streams(T.plan, pr, pls, F.lr.as<double>(), ntot, device, stream);
+      const int rc = build_mixed_streams(T.plan, pr, pls, F.lr.as<double>(), ntot, device, stream);
+      if (rc == AHX_OK) T.plan.valid = true;
+      return rc;
     }
     std::vector<MvLeaf> all;
     std::vector<uint64_t> cost;
@@ -1191,6 +1193,15 @@ int ahx_batch_destroy(ahx_batch* b) {
 }
 
 uint64_t ahx_batch_n(const ahx_batch* b) { return b ? b->ntot : 0; }
+
+int ahx_batch_prepare(ahx_batch* b, int precision) {
+  if (!b || precision < 0 || precision >= kNumPrecisions) return AHX_ERR_ARG;
+  AHX_CUDA(cudaSetDevice(b->device));
+  if (precision == kFP64) return AHX_OK;
+  if (precision == kDF64) return b->prepare(kDF64, 1);
+  if (b->tab[precision].plan.valid) return AHX_OK;
+  return b->build_tab(precision);
+}
 
 int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double* Y) {
   if (!b || !X || !Y) return AHX_ERR_ARG;

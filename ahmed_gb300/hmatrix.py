@@ -317,6 +317,11 @@ class HBatch:
 
             torch.cuda.synchronize()
 
+    def prepare(self, precision):
+        """Builds the product copy of a precision ahead of use ("df64": the
+        refinement's outer residual)."""
+        check(lib().ahx_batch_prepare(self._h, _prec(precision)))
+
     def matvec(self, d, X, Y, p=1):
         self._torch_sync(X, Y)
         check(lib().ahx_batch_matvec(self._h, float(d), int(p), ptr(X), ptr(Y)))

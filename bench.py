@@ -592,6 +592,8 @@ def run_batch(args):
     peak, _ = _peaks()
     for prec in ("bf16", "fp64"):
         Bt = A.HBatch(mats, precision=prec)
+        if prec != "fp64":
+            Bt.prepare("df64")   # refinement residual copy, built with the streams (setup)
         x = torch.from_numpy(np.random.default_rng(4).uniform(-1, 1, ntot)).to(dev)
         y = torch.zeros_like(x)
         for _ in range(3):

@@ -184,6 +184,9 @@ int ahx_batch_create(ahx_hmat* const* mats, uint32_t count, int precision, ahx_b
 int ahx_batch_destroy(ahx_batch* b);
 uint64_t ahx_batch_n(const ahx_batch* b);
 int ahx_batch_matvec(ahx_batch* b, double d, uint32_t p, const double* X, double* Y);
+/* builds the batch's product copy of a precision ahead of use (e.g. AHX_DF64, the
+ * refinement's outer residual, before a timed or captured solve) */
+int ahx_batch_prepare(ahx_batch* b, int precision);
 /* batched GMRES(m): one right-hand side per instance (b: concatenated), FP64
  * refinement around the batch's storage precision; iters/resid per instance. */
 int ahx_batch_gmres(ahx_batch* b, const double* B, double* X, double tol, uint32_t m,

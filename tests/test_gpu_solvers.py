@@ -143,6 +143,7 @@ def test_batch_product_and_gmres_match_instances():
         mats.append(H)
     for prec in ("fp64", "fp32", "df64"):
         B = A.HBatch(mats, precision=prec)
+        B.prepare("df64")   # the refinement copy next to the batch's own precision
         assert B.n == sum(m.n for m in mats)
         x = np.random.default_rng(7).uniform(-1, 1, B.n)
         y = B.matvec(1.0, x, np.zeros(B.n))
