@@ -32,6 +32,8 @@ SIGNATURES = [
     ("ahx_min_nn", _dbl, [_vp, _u32]),
     ("ahx_kernel_launches", _u64, []),
     ("ahx_hmat_create", _i32, [_vp, _u32, _i32, _u32, _dbl, _i32, _vp, _vp]),
+    ("ahx_hmat_create_sym", _i32, [_vp, _u32, _i32, _u32, _dbl, _i32, _vp, _vp]),
+    ("ahx_hmat_symmetric", _i32, [_vp]),
     ("ahx_hmat_destroy", _i32, [_vp]),
     ("ahx_hmat_set_stream", _i32, [_vp, _vp]),
     ("ahx_hmat_stream", _vp, [_vp]),

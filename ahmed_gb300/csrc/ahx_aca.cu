@@ -290,6 +290,117 @@ __device__ int aca(const Grp& g, const Blk& B, uint32_t i0, uint32_t kmax, uint3
   return outcome;
 }
 
+// ACAr_step (ACA.h:579-655), the simplified cross of the symmetric assembly:
+// rows are skipped only for a small pivot, the pivot column is searched over
+// all columns, and the next row is the largest unused entry of the new column.
+template <int G, class Grp>
+__device__ bool acar_step(const Grp& g, const Blk& B, uint32_t& i0, uint32_t k, uint32_t& no, double& nrmlsk2,
+                          double scale) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  double* const pu = B.U + (size_t)k * n1;
+  double* const pv = B.V + (size_t)k * n2;
+  ArgMax am;
+  for (;;) {
+    g.sync();
+    const uint32_t gi = B.b1 + i0;
+    const double xi = B.P.x[gi], yi = B.P.y[gi], zi = B.P.z[gi];
+    am = ArgMax{0.0, 0xffffffffu, 0.0};
+    for (uint32_t j = g.rank; j < n2; j += G) {
+      double v = lap_entry_aca(B.P, gi, B.b2 + j, xi, yi, zi, B.diag);
+      for (uint32_t l = 0; l < k; ++l) v = fma(-B.U[(size_t)l * n1 + i0], B.V[(size_t)l * n2 + j], v);
+      pv[j] = v;
+      const double a = fabs(v);
+      if (gt_nonneg(a, am.v)) am = ArgMax{a, j, v};
+    }
+    am = g.argmax(am);
+    if (!(am.v < 1e-14 * scale)) break;
+    if (owns(g, i0, G)) B.Z[i0] = -1;
+    if (++no >= n1) return false;
+    g.sync();
+    i0 = nexti<G>(g, B.Z, n1, i0);
+  }
+  const uint32_t j0 = am.idx;
+  const double sqrtpiv = sqrt(am.v);
+  const double sca = sqrtpiv / am.sv;
+  double nrmv2 = 0.0;
+  for (uint32_t j = g.rank; j < n2; j += G) {
+    const double e = pv[j] * sca;
+    pv[j] = e;
+    nrmv2 += e * e;
+  }
+  const uint32_t gj = B.b2 + j0;
+  const double xj = B.P.x[gj], yj = B.P.y[gj], zj = B.P.z[gj];
+  for (uint32_t i = g.rank; i < n1; i += G) {
+    double u = lap_entry_aca(B.P, gj, B.b1 + i, xj, yj, zj, B.diag);
+    for (uint32_t l = 0; l < k; ++l) u = fma(-B.V[(size_t)l * n2 + j0], B.U[(size_t)l * n1 + i], u);
+    pu[i] = u;
+  }
+  if (owns(g, i0, G)) B.Z[i0] = -1;
+  ++no;
+  const double dsca = 1.0 / sqrtpiv;
+  double nrmu2 = 0.0;
+  ArgMax nm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t i = g.rank; i < n1; i += G) {
+    const double e = pu[i] * dsca;
+    pu[i] = e;
+    const double ea = fabs(e);
+    nrmu2 += ea * ea;
+    if (B.Z[i] >= 0 && gt_nonneg(ea, nm.v)) nm = ArgMax{ea, i, e};
+  }
+  g.sum2(nrmu2, nrmv2);
+  nm = g.argmax(nm);
+  if (nm.v > 0.0) i0 = nm.idx;
+  nrmlsk2 = nrmu2 * nrmv2;
+  return true;
+}
+
+// ACAr driver (ACA.h:657-720): crosses until the last one is below eps of the
+// approximation's norm, no more than n2 rows used, or kmax crosses.
+template <int G, class Grp>
+__device__ int acar(const Grp& g, const Blk& B, uint32_t i0, uint32_t kmax, uint32_t kcap, double eps,
+                    uint32_t& kout) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  for (uint32_t i = g.rank; i < n1; i += G) B.Z[i] = 0;
+  double scale;
+  {
+    const uint32_t a = B.b1, b = B.b2;
+    scale = fabs(lap_entry(B.P, a, b, B.P.x[a], B.P.y[a], B.P.z[a], B.diag));
+  }
+  uint32_t k = 0, no = 0;
+  double nrmlsk2 = 0.0, nrms2 = 0.0;
+  int outcome = -1;
+  do {
+    if (k >= kcap) {
+      outcome = kAcaOverflow;
+      break;
+    }
+    if (!acar_step<G>(g, B, i0, k, no, nrmlsk2, scale)) {
+      nrmlsk2 = 0.0;
+      break;
+    }
+    double sum = 0.0;
+    const double* uk = B.U + (size_t)k * n1;
+    const double* vk = B.V + (size_t)k * n2;
+    for (uint32_t l = 0; l < k; ++l) {
+      double du = 0.0, dv = 0.0;
+      for (uint32_t i = g.rank; i < n1; i += G) du += B.U[(size_t)l * n1 + i] * uk[i];
+      for (uint32_t j = g.rank; j < n2; j += G) dv += B.V[(size_t)l * n2 + j] * vk[j];
+      g.sum2(du, dv);
+      sum += du * dv;
+    }
+    nrms2 += 2.0 * sum + nrmlsk2;
+    ++k;
+    scale = sqrt(nrmlsk2 / (double)(uint32_t)(n1 * n2));
+  } while (no < n2 && k < kmax && nrmlsk2 >= eps * eps * nrms2);
+  if (outcome < 0) {
+    const double epsa = sqrt(nrmlsk2 / nrms2);
+    outcome = epsa >= eps ? kAcaFail : kAcaOk;  // NaN (0/0) stays a success, as in the reference
+  }
+  kout = k;
+  g.sync();
+  return outcome;
+}
+
 // In-place Householder QR of A (m x k, column-major) by the group; tau[k].
 template <int G, class Grp>
 __device__ void group_qr(const Grp& g, uint32_t m, uint32_t k, double* A, double* tau) {
@@ -548,7 +659,8 @@ __device__ void aca_task(const Grp& g, const AcaParams& p, uint32_t ti, double* 
   B.Z = p.zs + t.zs;
   B.S = B.Z + t.n1;
   uint32_t k = 0;
-  const int st = aca<G>(g, B, t.i0, t.kmax, t.kcap, p.eps, k);
+  const int st = p.variant == kAcaVariantSym ? acar<G>(g, B, t.i0, t.kmax, t.kcap, p.eps, k)
+                                             : aca<G>(g, B, t.i0, t.kmax, t.kcap, p.eps, k);
   uint32_t kt = 0;
   if (st == kAcaOk && k > 0) {
     // small ranks: k x k work arrays in shared memory; larger: in the workspace
@@ -598,6 +710,24 @@ __global__ void dense_fill_kernel(PointsSoA P, double diag, const DenseTask* __r
   }
 }
 
+// Mirror images of upper blocks: V U^T (the factors swapped) or D^T.
+__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, double* __restrict__ arena) {
+  const MirrorTask t = tasks[blockIdx.x];
+  const double* src = arena + t.src;
+  double* dst = arena + t.dst;
+  if (t.rank > 0) {
+    const uint64_t nu = (uint64_t)t.n1 * t.rank, nv = (uint64_t)t.n2 * t.rank;
+    for (uint64_t e = threadIdx.x; e < nv; e += blockDim.x) dst[e] = src[nu + e];
+    for (uint64_t e = threadIdx.x; e < nu; e += blockDim.x) dst[nv + e] = src[e];
+  } else {
+    const uint64_t cnt = (uint64_t)t.n1 * t.n2;
+    for (uint64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const uint32_t j = (uint32_t)(e % t.n2), i = (uint32_t)(e / t.n2);  // D^T(j, i) = D(i, j)
+      dst[e] = src[i + (uint64_t)j * t.n1];
+    }
+  }
+}
+
 __global__ void copy_factors_kernel(const CopyTask* __restrict__ tasks, const double* __restrict__ ws,
                                     double* __restrict__ arena) {
   const CopyTask t = tasks[blockIdx.x];
@@ -634,6 +764,12 @@ cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask
                               uint32_t ntasks, double* arena, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   dense_fill_kernel<<<ntasks, 256, 0, s>>>(pts, diag, tasks, arena);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mirror(const MirrorTask* tasks, uint32_t ntasks, double* arena, cudaStream_t s) {
+  if (ntasks == 0) return cudaSuccess;
+  mirror_kernel<<<ntasks, 256, 0, s>>>(tasks, arena);
   return cudaGetLastError();
 }
 

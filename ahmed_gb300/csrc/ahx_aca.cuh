@@ -21,6 +21,10 @@ struct AcaTask {
 
 enum AcaStatus : int32_t { kAcaFail = 0, kAcaOk = 1, kAcaOverflow = 2 };
 
+// ACA of the general assembly (Include/ACA.h:217-350) or ACAr of the symmetric one
+// (Include/ACA.h:657-720, Include/apprx.h:86-132)
+enum AcaVariant : int32_t { kAcaVariantGeneral = 0, kAcaVariantSym = 1 };
+
 struct AcaResult {
   int32_t status;
   uint32_t k_aca;  // rank returned by ACA (before recompression)
@@ -41,6 +45,7 @@ struct AcaParams {
   double* ws;
   int* zs;
   AcaResult* res;
+  int32_t variant = kAcaVariantGeneral;
 };
 
 // Launchers (ahx_aca.cu)
@@ -54,6 +59,17 @@ struct DenseTask {
 };
 cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask* tasks,
                               uint32_t ntasks, double* arena, cudaStream_t s);
+
+// Mirror image of an upper block of a symmetric H-matrix into the same arena:
+// rank > 0: U (n1 x rank), V (n2 x rank) at src -> V, U at dst (the leaf V U^T);
+// rank < 0: the n1 x n2 block at src -> its transpose (n2 x n1) at dst.
+struct MirrorTask {
+  uint64_t src, dst;
+  uint32_t n1, n2;
+  int32_t rank;
+  uint32_t pad;
+};
+cudaError_t launch_mirror(const MirrorTask* tasks, uint32_t ntasks, double* arena, cudaStream_t s);
 
 // Copy recompressed factors (Un, Vn, kt columns) from the workspace into the arena.
 struct CopyTask {

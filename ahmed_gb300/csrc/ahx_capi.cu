@@ -63,6 +63,7 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
     p.pts = PointsSoA{pts, pts + H->tree.n, pts + 2 * (size_t)H->tree.n};
     p.diag = diag;
     p.eps = eps;
+    p.variant = H->tree.sym ? kAcaVariantSym : kAcaVariantGeneral;
     p.ws = ws.as<double>();
     p.zs = zs.as<int>();
     p.tasks = dtasks.as<AcaTask>();
@@ -218,6 +219,71 @@ bool is_device_ptr(const void* ptr) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The leaves a product reads as a general H-matrix.  A symmetric tree stores the
+// diagonal and upper blocks only; its blocks below the diagonal are the mirror
+// images (V U^T, D^T) of the upper ones, written into `tmp` after a copy of the
+// leaf arena.  `arena` is the arena the returned offsets refer to.
+int full_leaves(ahx_hmat* H, std::vector<PlanLeaf>& pls, DevBuf& tmp, const double*& arena) {
+  const auto& Ls = H->tree.leaves;
+  const uint32_t nl = (uint32_t)Ls.size();
+  pls.clear();
+  for (uint32_t l = 0; l < nl; ++l)
+    if (H->rank[l] != 0) pls.push_back(PlanLeaf{Ls[l].b1, Ls[l].n1, Ls[l].b2, Ls[l].n2, H->rank[l], H->off[l]});
+  arena = H->arena64.as<double>();
+  if (!H->tree.sym) return AHX_OK;
+  std::vector<MirrorTask> mt;
+  uint64_t end = H->arena64_elems;
+  for (uint32_t l = 0; l < nl; ++l) {
+    const Leaf& L = Ls[l];
+    const int32_t r = H->rank[l];
+    if (r == 0 || L.b1 == L.b2) continue;
+    const uint64_t cnt = r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
+    mt.push_back(MirrorTask{H->off[l], end, L.n1, L.n2, r, 0u});
+    pls.push_back(PlanLeaf{L.b2, L.n2, L.b1, L.n1, r, end});
+    end += cnt;
+  }
+  int rc = tmp.reserve(std::max<uint64_t>(end, 1) * sizeof(double));
+  if (rc) return rc;
+  if (H->arena64_elems)
+    AHX_CUDA(cudaMemcpyAsync(tmp.p, H->arena64.p, H->arena64_elems * sizeof(double), cudaMemcpyDeviceToDevice,
+                             H->stream));
+  DevBuf dmt;
+  if ((rc = upload(dmt, mt, H->stream))) return rc;
+  AHX_CUDA(launch_mirror(dmt.as<MirrorTask>(), (uint32_t)mt.size(), tmp.as<double>(), H->stream));
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  dmt.release();
+  arena = tmp.as<double>();
+  return AHX_OK;
+}
+
+// Leaf table of the FP64-class products (descending cost order).  transposed:
+// the off-diagonal blocks of a symmetric tree, applied as their transposes.
+int upload_leaf_table(ahx_hmat* H, const std::vector<PlanLeaf>& pls, DevBuf& leaves, DevBuf& order, uint32_t& n) {
+  std::vector<MvLeaf> mv;
+  std::vector<uint64_t> cost;
+  mv.reserve(pls.size());
+  for (const PlanLeaf& q : pls) {
+    MvLeaf m;
+    m.b1 = q.b1;
+    m.n1 = q.n1;
+    m.b2 = q.b2;
+    m.n2 = q.n2;
+    m.rank = q.rank;
+    m.dense_in_lr_arena = 1;
+    m.off = q.off;
+    mv.push_back(m);
+    cost.push_back(q.rank < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)q.rank * (q.n1 + q.n2));
+  }
+  std::vector<uint32_t> ord(mv.size());
+  std::iota(ord.begin(), ord.end(), 0u);
+  std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  int rc;
+  if ((rc = upload(leaves, mv, H->stream))) return rc;
+  if ((rc = upload(order, ord, H->stream))) return rc;
+  n = (uint32_t)mv.size();
+  return AHX_OK;
+}
+
 int prepare_product(ahx_hmat* H, int prec) {
   if (prec < 0 || prec >= kNumPrecisions) {
     set_error("unknown precision");
@@ -229,55 +295,49 @@ int prepare_product(ahx_hmat* H, int prec) {
   const uint32_t nl = (uint32_t)Ls.size();
   int rc;
   if (prec == kDF64) {
-    // the FP64 leaf table, the arena split into (hi, lo) float pairs
+    // the FP64 leaves split into (hi, lo) float pairs; a symmetric tree's mirror
+    // images are materialised, with their own leaf table
     if ((rc = prepare_product(H, kFP64))) return rc;
-    if ((rc = pc.lr.reserve(std::max<uint64_t>(H->arena64_elems, 1) * 8))) return rc;
-    AHX_CUDA(launch_split_df(H->arena64.as<double>(), H->arena64_elems, H->arena64_elems, 1, 1.0, pc.lr.p,
-                             H->stream));
+    std::vector<PlanLeaf> pls;
+    DevBuf tmp;
+    const double* src = nullptr;
+    if ((rc = full_leaves(H, pls, tmp, src))) return rc;
+    uint64_t elems = H->arena64_elems;
+    for (const PlanLeaf& q : pls)
+      elems = std::max<uint64_t>(elems, q.off + (q.rank < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)q.rank * (q.n1 + q.n2)));
+    if ((rc = pc.lr.reserve(std::max<uint64_t>(elems, 1) * 8))) return rc;
+    AHX_CUDA(launch_split_df(src, elems, elems, 1, 1.0, pc.lr.p, H->stream));
+    if (H->tree.sym && (rc = upload_leaf_table(H, pls, pc.leaves, pc.order, pc.nleaves))) return rc;
     AHX_CUDA(cudaStreamSynchronize(H->stream));
-    pc.bytes = H->arena64_elems * 8;
+    tmp.release();
+    pc.bytes = elems * 8;
     pc.valid = true;
     return AHX_OK;
   }
   if (prec != kFP64) {
     std::vector<PlanLeaf> pls;
-    pls.reserve(nl);
-    for (uint32_t l = 0; l < nl; ++l) {
-      const Leaf& L = Ls[l];
-      if (H->rank[l] == 0) continue;
-      pls.push_back(PlanLeaf{L.b1, L.n1, L.b2, L.n2, H->rank[l], H->off[l]});
-    }
-    if ((rc = build_mixed_streams(pc, prec, pls, H->arena64.as<double>(), H->tree.n, H->device,
-                                  H->stream)))
-      return rc;
+    DevBuf tmp;
+    const double* src = nullptr;
+    if ((rc = full_leaves(H, pls, tmp, src))) return rc;
+    rc = build_mixed_streams(pc, prec, pls, src, H->tree.n, H->device, H->stream);
+    tmp.release();
+    if (rc) return rc;
     pc.valid = true;
     return AHX_OK;
   }
-  std::vector<MvLeaf> mv;
-  std::vector<uint64_t> cost;
-  mv.reserve(nl);
+  // every stored leaf; for a symmetric tree the off-diagonal ones again, applied
+  // transposed (H/mltaGeHVec.cpp:421-446)
+  std::vector<PlanLeaf> all, upper;
   for (uint32_t l = 0; l < nl; ++l) {
     const Leaf& L = Ls[l];
-    const int32_t r = H->rank[l];
-    if (r == 0) continue;
-    MvLeaf m;
-    m.b1 = L.b1;
-    m.n1 = L.n1;
-    m.b2 = L.b2;
-    m.n2 = L.n2;
-    m.rank = r;
-    m.dense_in_lr_arena = 1;
-    m.off = H->off[l];
-    mv.push_back(m);
-    cost.push_back(r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2));
+    if (H->rank[l] == 0) continue;
+    const PlanLeaf q{L.b1, L.n1, L.b2, L.n2, H->rank[l], H->off[l]};
+    all.push_back(q);
+    if (H->tree.sym && L.b1 != L.b2) upper.push_back(q);
   }
-  std::vector<uint32_t> order(mv.size());
-  std::iota(order.begin(), order.end(), 0u);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
-  if ((rc = upload(pc.leaves, mv, H->stream))) return rc;
-  if ((rc = upload(pc.order, order, H->stream))) return rc;
-  pc.nleaves = (uint32_t)mv.size();
+  if ((rc = upload_leaf_table(H, all, pc.leaves, pc.order, pc.nleaves))) return rc;
+  pc.ntleaves = 0;
+  if (!upper.empty() && (rc = upload_leaf_table(H, upper, pc.tleaves, pc.torder, pc.ntleaves))) return rc;
   pc.bytes = H->arena64_elems * sizeof(double);
   AHX_CUDA(cudaStreamSynchronize(H->stream));
   pc.valid = true;
@@ -400,6 +460,7 @@ int check_stream_error(ProdCopy& pc, cudaStream_t s) {
 
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
                    double* Y, uint64_t ldY, bool transposed) {
+  if (transposed && H->tree.sym) transposed = false;  // A^T = A
   if (transposed && prec != kFP64) {
     set_error("transposed products use the FP64 leaves");
     return AHX_ERR_ARG;
@@ -409,7 +470,7 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   ProdCopy& pc = H->prod[prec];
   if (prec == kDF64) {
     if ((rc = prepare_df_x(pc, H->tree.n, p))) return rc;
-    const ProdCopy& f = H->prod[kFP64];
+    const ProdCopy& f = H->tree.sym ? pc : H->prod[kFP64];
     return run_df(f.leaves.as<MvLeaf>(), f.order.as<uint32_t>(), f.nleaves, pc, H->tree.n, d, p, X, ldX, Y,
                   ldY, H->stream);
   }
@@ -432,6 +493,14 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
   a.ldY = ldY;
   a.transposed = transposed ? 1u : 0u;
   AHX_CUDA(launch_matvec(prec, a, H->stream));
+  if (pc.ntleaves) {
+    // symmetric tree: the blocks below the diagonal are the upper ones transposed
+    a.leaves = pc.tleaves.as<MvLeaf>();
+    a.order = pc.torder.as<uint32_t>();
+    a.nleaves = pc.ntleaves;
+    a.transposed = 1u;
+    AHX_CUDA(launch_matvec(prec, a, H->stream));
+  }
   return AHX_OK;
 }
 
@@ -479,8 +548,8 @@ double ahx_min_nn(const double* pts, uint32_t n) {
   return mn;
 }
 
-int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
-                    int device, void* stream, ahx_hmat** out) {
+static int create_impl(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2, int device,
+                       void* stream, ahx_hmat** out, bool sym) {
   if (!out || !pts || n == 0 || bmin == 0 || (tree_kind != AHX_TREE_BBX && tree_kind != AHX_TREE_PCA) ||
       !(eta2 >= 0.0) || device < 0) {
     set_error("ahx_hmat_create: invalid argument");
@@ -495,10 +564,22 @@ int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin,
   H->device = device;
   H->stream = (cudaStream_t)stream;
   // trees are host work; the device is touched on the first device call
-  build_tree(H->tree, pts, n, tree_kind, bmin, eta2);
+  build_tree(H->tree, pts, n, tree_kind, bmin, eta2, sym);
   *out = H;
   return AHX_OK;
 }
+
+int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
+                    int device, void* stream, ahx_hmat** out) {
+  return create_impl(pts, n, tree_kind, bmin, eta2, device, stream, out, false);
+}
+
+int ahx_hmat_create_sym(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
+                        int device, void* stream, ahx_hmat** out) {
+  return create_impl(pts, n, tree_kind, bmin, eta2, device, stream, out, true);
+}
+
+int ahx_hmat_symmetric(const ahx_hmat* H) { return H && H->tree.sym ? 1 : 0; }
 
 int ahx_hmat_destroy(ahx_hmat* H) {
   if (!H) return AHX_OK;
@@ -673,10 +754,10 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4) {
   int rc = ensure_device(H);
   if (rc) return rc;
   const int prec = precision == AHX_FP32 ? kFP32 : kBF16FP32;
-  const auto& Ls = H->tree.leaves;
   std::vector<PlanLeaf> pls;
-  for (uint32_t l = 0; l < (uint32_t)Ls.size(); ++l)
-    if (H->rank[l] != 0) pls.push_back(PlanLeaf{Ls[l].b1, Ls[l].n1, Ls[l].b2, Ls[l].n2, H->rank[l], H->off[l]});
+  DevBuf full;
+  const double* src = nullptr;
+  if ((rc = full_leaves(H, pls, full, src))) return rc;
   const uint64_t n = H->tree.n;
   DevBuf X, Y;
   if ((rc = X.reserve(n * p * sizeof(double))) || (rc = Y.reserve(n * p * sizeof(double)))) return rc;
@@ -692,7 +773,7 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4) {
   for (uint32_t w : widths) {
     for (uint32_t u : units) {
       ProdCopy cand;
-      if ((rc = build_mixed_streams(cand, prec, pls, H->arena64.as<double>(), n, H->device, H->stream, w, u))) {
+      if ((rc = build_mixed_streams(cand, prec, pls, src, n, H->device, H->stream, w, u))) {
         cand.release_all();
         break;
       }
@@ -729,11 +810,15 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4) {
   cudaEventDestroy(e1);
   X.release();
   Y.release();
-  if (rc) return rc;
+  if (rc) {
+    full.release();
+    return rc;
+  }
   ProdCopy& pc = H->prod[prec];
   pc.release_all();
-  if ((rc = build_mixed_streams(pc, prec, pls, H->arena64.as<double>(), n, H->device, H->stream, bw, bu)))
-    return rc;
+  rc = build_mixed_streams(pc, prec, pls, src, n, H->device, H->stream, bw, bu);
+  full.release();
+  if (rc) return rc;
   pc.valid = true;
   if (out4) {
     out4[0] = bw;
@@ -771,10 +856,18 @@ int ahx_hmat_aca_ranks(const ahx_hmat* H, int32_t* ranks) {
   return AHX_OK;
 }
 
+// a dense diagonal leaf of a symmetric tree is Hermitian (mblock::setHeM): its data
+// is the packed upper triangle (Include/apprx.h:122-126)
+static bool packed_leaf(const ahx_hmat* H, uint32_t l) {
+  const Leaf& L = H->tree.leaves[l];
+  return H->tree.sym && L.b1 == L.b2 && H->rank[l] < 0;
+}
+
 uint64_t ahx_hmat_leaf_size(const ahx_hmat* H, uint32_t l) {
   if (!H || !H->assembled || l >= H->tree.leaves.size()) return 0;
   const Leaf& L = H->tree.leaves[l];
   const int32_t r = H->rank[l];
+  if (packed_leaf(H, l)) return (uint64_t)L.n1 * (L.n1 + 1) / 2;
   return r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
 }
 
@@ -787,6 +880,16 @@ int ahx_hmat_get_leaf(const ahx_hmat* H, uint32_t l, double* out) {
   const uint64_t cnt = ahx_hmat_leaf_size(H, l);
   if (!cnt) return AHX_OK;
   AHX_CUDA(cudaSetDevice(H->device));
+  if (packed_leaf(H, l)) {
+    const uint32_t n1 = H->tree.leaves[l].n1;
+    std::vector<double> full((uint64_t)n1 * n1);
+    AHX_CUDA(cudaMemcpyAsync(full.data(), H->arena64.as<double>() + H->off[l], full.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    for (uint32_t j = 0; j < n1; ++j)
+      for (uint32_t i = 0; i <= j; ++i) out[i + (uint64_t)j * (j + 1) / 2] = full[i + (uint64_t)j * n1];
+    return AHX_OK;
+  }
   AHX_CUDA(cudaMemcpyAsync(out, H->arena64.as<double>() + H->off[l], cnt * sizeof(double),
                            cudaMemcpyDeviceToHost, H->stream));
   AHX_CUDA(cudaStreamSynchronize(H->stream));
@@ -798,13 +901,48 @@ int ahx_hmat_set_leaves(ahx_hmat* H, const int32_t* ranks, const double* data,
   if (!H || !ranks || !offsets) return AHX_ERR_ARG;
   const auto& Ls = H->tree.leaves;
   const uint32_t nl = (uint32_t)Ls.size();
+  // dense diagonal leaves of a symmetric tree may come packed (mblock HeM data)
+  std::vector<uint64_t> expand;
   for (uint32_t l = 0; l < nl; ++l) {
     const uint64_t want = ranks[l] < 0 ? (uint64_t)Ls[l].n1 * Ls[l].n2
                                        : (uint64_t)ranks[l] * (Ls[l].n1 + Ls[l].n2);
-    if (offsets[l + 1] < offsets[l] || offsets[l + 1] - offsets[l] != want) {
+    const uint64_t got = offsets[l + 1] >= offsets[l] ? offsets[l + 1] - offsets[l] : ~0ull;
+    const bool packed = H->tree.sym && ranks[l] < 0 && Ls[l].b1 == Ls[l].b2 && Ls[l].n1 > 1 &&
+                        got == (uint64_t)Ls[l].n1 * (Ls[l].n1 + 1) / 2;
+    if (packed) {
+      expand.push_back(l);
+    } else if (got != want) {
       set_error("ahx_hmat_set_leaves: offsets do not match the leaf sizes");
       return AHX_ERR_ARG;
     }
+  }
+  if (!expand.empty()) {
+    std::vector<double> full;
+    std::vector<uint64_t> offs(nl + 1, 0);
+    for (uint32_t l = 0; l < nl; ++l) {
+      const uint64_t want = ranks[l] < 0 ? (uint64_t)Ls[l].n1 * Ls[l].n2
+                                         : (uint64_t)ranks[l] * (Ls[l].n1 + Ls[l].n2);
+      offs[l + 1] = offs[l] + want;
+    }
+    full.resize(offs[nl]);
+    size_t e = 0;
+    for (uint32_t l = 0; l < nl; ++l) {
+      const double* src = data + offsets[l];
+      double* dst = full.data() + offs[l];
+      if (e < expand.size() && expand[e] == l) {
+        ++e;
+        const uint32_t n1 = Ls[l].n1;
+        for (uint32_t j = 0; j < n1; ++j)
+          for (uint32_t i = 0; i <= j; ++i) {
+            const double v = src[i + (uint64_t)j * (j + 1) / 2];
+            dst[i + (uint64_t)j * n1] = v;
+            dst[j + (uint64_t)i * n1] = v;
+          }
+      } else {
+        std::copy(src, src + (offs[l + 1] - offs[l]), dst);
+      }
+    }
+    return ahx_hmat_set_leaves(H, ranks, full.data(), offs.data());
   }
   int rc = ensure_device(H);
   if (rc) return rc;

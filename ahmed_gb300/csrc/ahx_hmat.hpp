@@ -39,18 +39,20 @@ struct ProdCopy {
   DevBuf lr, dn;           // FP64 product: arena (lr) when it is not the handle's own
   DevBuf leaves, order;    // FP64 product: MvLeaf[nleaves], uint32 launch order
   uint32_t nleaves = 0;
+  DevBuf tleaves, torder;  // symmetric tree, FP64: the off-diagonal leaves applied transposed
+  uint32_t ntleaves = 0;
   uint64_t bytes = 0;      // stored leaf bytes of this precision
   // mixed-precision fragment streams (FP32 / BF16 products, tensor cores)
   DevBuf vstream, rstream, vunits, runits, sides, vranges, rranges, treduce, xb, xf, yr, t, err;
   uint32_t nvunits = 0, nrunits = 0, grid = 0, t_rows = 0, ntreduce = 0, pmax = 16;
   uint32_t unit_bytes = 0;  // unit cap the streams were built with
   void release_all() {
-    for (DevBuf* b : {&lr, &dn, &leaves, &order, &vstream, &rstream, &vunits, &runits, &sides, &vranges,
-                      &rranges, &treduce, &xb, &xf, &yr, &t, &err})
+    for (DevBuf* b : {&lr, &dn, &leaves, &order, &tleaves, &torder, &vstream, &rstream, &vunits, &runits, &sides,
+                      &vranges, &rranges, &treduce, &xb, &xf, &yr, &t, &err})
       b->release();
     valid = false;
     bytes = 0;
-    nleaves = nvunits = nrunits = grid = t_rows = ntreduce = 0;
+    nleaves = ntleaves = nvunits = nrunits = grid = t_rows = ntreduce = 0;
   }
 };
 

@@ -195,10 +195,15 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
       if (r >= 0) {
         w.put_val<uint32_t>(kStatusLowRank);
         w.put_val<uint32_t>((uint32_t)r);
+        w.put(data + pos, cnt * sizeof(double));
+      } else if (H->tree.sym && L.b1 == L.b2) {
+        // Hermitian diagonal block of a symmetric tree: packed upper triangle
+        w.put_val<uint32_t>(kStatusHerm);
+        for (uint32_t j = 0; j < L.n1; ++j) w.put(data + pos + (uint64_t)j * L.n1, (uint64_t)(j + 1) * sizeof(double));
       } else {
         w.put_val<uint32_t>(kStatusDense);
+        w.put(data + pos, cnt * sizeof(double));
       }
-      w.put(data + pos, cnt * sizeof(double));
       pos += cnt;
     }
     return AHX_OK;

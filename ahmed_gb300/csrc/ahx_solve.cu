@@ -1125,6 +1125,10 @@ int ahx_batch_create(ahx_hmat* const* mats, uint32_t count, int precision, ahx_b
       set_error("ahx_batch_create: every instance must be assembled");
       return AHX_ERR_STATE;
     }
+    if (mats[i]->tree.sym) {
+      set_error("ahx_batch_create: symmetric instances are not batched");
+      return AHX_ERR_ARG;
+    }
     if (mats[i]->device != mats[0]->device) {
       set_error("ahx_batch_create: instances on different devices");
       return AHX_ERR_ARG;

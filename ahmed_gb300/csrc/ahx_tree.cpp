@@ -226,6 +226,20 @@ struct Builder {
     T.leaves.push_back(L);
   }
 
+  // cluster/blcluster.cpp:90-113: diagonal blocks recurse symmetrically, the
+  // blocks above them are general subtrees, the blocks below are absent
+  void subdivide_sym(int32_t ia) {
+    const ClusterNode& a = T.nodes[ia];
+    if (a.son[0] >= 0) {
+      const int32_t s0 = a.son[0], s1 = a.son[1];
+      subdivide_sym(s0);
+      subdivide(s0, s1);
+      subdivide_sym(s1);
+    } else {
+      push_leaf(ia, ia, false);
+    }
+  }
+
   // cluster/blcluster.cpp:40-66
   void subdivide(int32_t ia, int32_t ib) {
     if (isadm(T.nodes[ia], T.nodes[ib])) {
@@ -247,8 +261,9 @@ struct Builder {
 
 }  // namespace
 
-void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin, double eta2) {
+void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin, double eta2, bool sym) {
   T.n = n;
+  T.sym = sym;
   T.kind = kind;
   T.bmin = bmin;
   T.eta2 = eta2;
@@ -268,7 +283,8 @@ void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin,
     B.pca_init(T.nodes[root]);
     B.pca_tree(root);
   }
-  B.subdivide(root, root);
+  if (sym) B.subdivide_sym(root);
+  else B.subdivide(root, root);
 }
 
 void leaf_features(const Tree& T, const Leaf& L, double wavenumber, double eps, float out[8]) {

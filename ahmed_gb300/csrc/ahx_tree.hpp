@@ -39,6 +39,7 @@ struct Tree {
   int kind = kTreeBbx;
   uint32_t bmin = 0;
   double eta2 = 0.0;
+  bool sym = false;                 // symmetric (HeH) block tree
   std::vector<double> pts;          // original order, xyz interleaved
   std::vector<uint32_t> op_perm;    // permuted -> original
   std::vector<uint32_t> po_perm;    // original -> permuted
@@ -48,7 +49,9 @@ struct Tree {
 
 // Builds the cluster tree over `pts` (3*n doubles, original order) and the
 // block-cluster tree with the admissibility parameter eta2 (= eta^2).
-void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin, double eta2);
+// sym: the symmetric block tree (blcluster::subdivide_sym): diagonal and upper blocks only
+void build_tree(Tree& T, const double* pts, uint32_t n, int kind, uint32_t bmin, double eta2,
+                bool sym = false);
 
 // Mean nearest-neighbour distance (exact; uniform-grid search; deterministic
 // sum order); *min_out (if given) receives the smallest one.

@@ -63,7 +63,9 @@ def _ncols(a, n):
 class HMatrix:
     """Cluster tree, block-cluster tree and (after assembly) device leaves."""
 
-    def __init__(self, points, tree="bbx", bmin=32, eta=0.8, device=0, stream=None):
+    def __init__(self, points, tree="bbx", bmin=32, eta=0.8, device=0, stream=None, symmetric=False):
+        """symmetric: the symmetric block tree (subdivide_sym) with the HeH assembly
+        (matgenHeH_omp) and products (mltaHeHVec): upper blocks stored once."""
         pts = np.ascontiguousarray(points, dtype=np.float64)
         if pts.ndim != 2 or pts.shape[1] != 3:
             raise ValueError("points must have shape (n, 3)")
@@ -72,8 +74,10 @@ class HMatrix:
         self.eta, self.bmin = float(eta), int(bmin)
         kind = TREES[tree] if isinstance(tree, str) else int(tree)
         h = C.c_void_p()
-        check(lib().ahx_hmat_create(ptr(pts), self.n, kind, bmin, float(eta) ** 2, device,
-                                    C.c_void_p(stream) if stream else None, C.byref(h)))
+        create = lib().ahx_hmat_create_sym if symmetric else lib().ahx_hmat_create
+        check(create(ptr(pts), self.n, kind, bmin, float(eta) ** 2, device,
+                     C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.symmetric = bool(symmetric)
         self._h = h
         self.h = None
         self.eps = None
@@ -151,6 +155,8 @@ class HMatrix:
         return self
 
     assemble = matgenGeH_omp
+    # symmetric handles assemble with the HeH rules (Include/matgen_omp.h:96-101)
+    matgenHeH_omp = matgenGeH_omp
 
     def assemble_hinted(self, h, eps, rank_hint, rankmax=2**32 - 1):
         """Assembly whose ACA workspace is sized by per-leaf rank hints (negative: none)."""
@@ -252,6 +258,13 @@ class HMatrix:
         self._follow_torch(X, Y)
         check(lib().ahx_matvec_transposed(self._h, float(d), int(p), ptr(X), int(ldX), ptr(Y), int(ldY)))
         return Y
+
+    # symmetric handles: the same products (H/mltaGeHVec.cpp:421-475)
+    def mltaHeHVec(self, d, x, y, precision="fp64"):
+        return self.mltaGeHVec(d, x, y, precision)
+
+    def mltaHeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
+        return self.mltaGeHGeM(d, p, X, ldX, Y, ldY, precision)
 
     def mltaGeHtVec(self, d, x, y):
         p, ld = _ncols(x, self.n)

@@ -63,6 +63,18 @@ uint64_t ahx_kernel_launches(void);
  * (a private stream is created). */
 int ahx_hmat_create(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
                     int device, void* stream, ahx_hmat** out);
+/* The same trees with the symmetric block tree: diagonal and upper blocks only
+ * (blcluster::subdivide_sym, cluster/blcluster.cpp:90-113).  Its assembly is
+ * matgenHeH_omp (Include/matgen_omp.h:96-101: ACAr for admissible blocks,
+ * Include/ACA.h:657-720; Hermitian dense diagonal blocks, Include/apprx.h:86-132)
+ * and its products are mltaHeHVec / mltaHeHGeM (H/mltaGeHVec.cpp:421-475:
+ * upper blocks applied as A and A^T).  ahx_hmat_get_leaf returns the packed
+ * upper triangle of a dense diagonal leaf (mblock HeM data); ahx_hmat_set_leaves
+ * takes it packed or full.  Symmetric handles are not batched. */
+int ahx_hmat_create_sym(const double* pts, uint32_t n, int tree_kind, uint32_t bmin, double eta2,
+                        int device, void* stream, ahx_hmat** out);
+/* 1 for a symmetric handle, else 0 */
+int ahx_hmat_symmetric(const ahx_hmat* H);
 int ahx_hmat_destroy(ahx_hmat* H);
 int ahx_hmat_set_stream(ahx_hmat* H, void* stream);
 void* ahx_hmat_stream(const ahx_hmat* H);

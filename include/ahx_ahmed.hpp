@@ -111,6 +111,19 @@ class blcluster {
     check(ahx_hmat_leaves(h_, leaves_.data()));
   }
 
+  // Include/blcluster.h:388 (cluster/blcluster.cpp:90-113): the symmetric block
+  // tree, diagonal and upper blocks (assembled by matgenHeH_omp, applied by mltaHeHVec)
+  template <class CL>
+  void subdivide_sym(CL* cl, double eta2, unsigned& nblcks, unsigned maxdepth = 0) {
+    if (maxdepth != 0) throw std::invalid_argument("ahx_ahmed: maxdepth 0");
+    std::shared_ptr<Geometry> g = cl->geometry();
+    check(ahx_hmat_create_sym(g->pts.data(), n_, g->kind, g->bmin, eta2, 0, nullptr, &h_));
+    check(ahx_hmat_perm(h_, g->op_perm, g->po_perm));
+    nblcks = ahx_hmat_nleaves(h_);
+    leaves_.resize(7 * (size_t)nblcks);
+    check(ahx_hmat_leaves(h_, leaves_.data()));
+  }
+
   unsigned long nleaves() const { return ahx_hmat_nleaves(h_); }
   unsigned long nadmleaves() const {
     unsigned long c = 0;
@@ -156,6 +169,10 @@ class mblock {
   unsigned getn2() const { return bound()->leaf(idx_)[3]; }
   bool isLrM() const { return bound()->rank_of(idx_) >= 0; }
   bool isGeM() const { return !isLrM(); }
+  // dense diagonal block of a symmetric tree: packed upper triangle (Include/mblock.h:314)
+  bool isHeM() const {
+    return isGeM() && ahx_hmat_symmetric(bound()->handle()) && bound()->leaf(idx_)[0] == bound()->leaf(idx_)[2];
+  }
   unsigned rank() const { return (unsigned)bound()->rank_of(idx_); }
   T* getdata() {
     if (data_.empty()) {
@@ -203,6 +220,16 @@ void matgenGeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps,
     delete A[i];
     A[i] = new mblock<T>(bl, i);
   }
+}
+
+// Include/matgen_omp.h:96-101: HeH assembly of a symmetric block tree (ACAr,
+// Hermitian diagonal blocks)
+template <class T, class MATGEN_T>
+void matgenHeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps, unsigned rankmax,
+                   mblock<T>** A) {
+  if (!ahx_hmat_symmetric(bl->handle()))
+    throw std::invalid_argument("ahx_ahmed: matgenHeH_omp needs a tree from subdivide_sym");
+  matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);
 }
 
 // Include/matgen_sqntl.h:88-102 (recmpr = false)
@@ -274,6 +301,17 @@ inline bool mltaGeHGeM(double d, blcluster* bl, mblock<double>** A, unsigned p, 
   bind_mbls(bl, A);
   check(ahx_matvec(bl->handle(), AHX_FP64, d, p, X, ldX, Y, ldY));
   return true;
+}
+
+// H/mltaGeHVec.cpp:654-662 (mltaHeHVec_/mltaHeHGeM_ :421-475): y += d A x for a
+// symmetric tree (its upper blocks applied as A and A^T)
+inline void mltaHeHVec(double d, blcluster* bl, mblock<double>** A, double* x, double* y) {
+  mltaGeHVec(d, bl, A, x, y);
+}
+
+inline void mltaHeHGeM(double d, blcluster* bl, mblock<double>** A, unsigned p, double* X, unsigned ldX,
+                       double* Y, unsigned ldY) {
+  mltaGeHGeM(d, bl, A, p, X, ldX, Y, ldY);
 }
 
 // H/mltaGeHVec.cpp:579-589 (mltaGeHhVec_/mltaGeHhGeM_ :62-105): y += d A^H x, Y += d A^H X (A^T for double)

@@ -178,6 +178,8 @@ def ref():
         vp, u32, i32, dbl = C.c_void_p, C.c_uint, C.c_int, C.c_double
         L.ref_build.restype = vp
         L.ref_build.argtypes = [vp, u32, i32, u32, dbl, dbl]
+        L.ref_build_sym.restype = vp
+        L.ref_build_sym.argtypes = [vp, u32, i32, u32, dbl, dbl]
         L.ref_nleaves.restype = u32
         L.ref_nleaves.argtypes = [vp]
         L.ref_perm.argtypes = [vp, vp, vp]
@@ -204,10 +206,12 @@ def ref():
 class RefH:
     """The reference library's own H-matrix (x86 container only)."""
 
-    def __init__(self, pts, kind, bmin, eta, h):
+    def __init__(self, pts, kind, bmin, eta, h, sym=False):
+        """sym: the symmetric block tree (subdivide_sym), HeH assembly and product."""
         self.pts = np.ascontiguousarray(pts, dtype=np.float64)
         self.n = self.pts.shape[0]
-        self._H = ref().ref_build(_p(self.pts), self.n, kind, bmin, eta * eta, h)
+        build = ref().ref_build_sym if sym else ref().ref_build
+        self._H = build(_p(self.pts), self.n, kind, bmin, eta * eta, h)
 
     def __del__(self):
         if getattr(self, "_H", None) and _ref is not None:

@@ -13,6 +13,9 @@
 //   mltaGeHVec / mltaGeHGeM            H/mltaGeHVec.cpp:567-577
 //   GMRes / CG                         solvers/GMRES.cpp:80-181, solvers/CG.cpp:31-113
 //   savembls                           Include/H.h:89-103, Include/mblock.h:737-773
+//   subdivide_sym / matgenHeH_omp / ACAr / mltaHeHVec  cluster/blcluster.cpp:90-113,
+//     Include/matgen_omp.h:96-101, Include/apprx.h:86-132, Include/ACA.h:579-720,
+//     H/mltaGeHVec.cpp:421-475
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -57,6 +60,11 @@ struct LaplaceGen {
   double scale(unsigned b1, unsigned, unsigned b2, unsigned) const {
     return fabs(entry(b1, b2));
   }
+  // packed upper triangle of the diagonal block, column by column (blas::hemva "U")
+  void cmpblsym(unsigned b1, unsigned n1, double* data) const {
+    for (unsigned j = 0; j < n1; ++j)
+      for (unsigned i = 0; i <= j; ++i) data[i + j * (j + 1) / 2] = entry(b1 + i, b1 + j);
+  }
 };
 
 // Helmholtz single-layer collocation generator (complex): exp(i k r) / (4 pi r),
@@ -94,15 +102,46 @@ struct RefH {
   std::vector<blcluster*> leaves;
   mblock<double>** A = nullptr;
   LaplaceGen gen;
+  bool sym = false;  // symmetric block tree (subdivide_sym), HeH leaves
 };
 
 struct HMatrixOp : public Matrix<double> {
   RefH* H;
   explicit HMatrixOp(RefH* h) : Matrix<double>(h->n, h->n), H(h) {}
   void amux(double d, double* x, double* y) const {
-    mltaGeHVec(d, H->root_bl, H->A, x, y);
+    if (H->sym) mltaHeHVec(d, H->root_bl, H->A, x, y);
+    else mltaGeHVec(d, H->root_bl, H->A, x, y);
   }
 };
+
+// apprx_sym (Include/apprx.h:86-132) with the ACA start row 0 of bounding-box trees
+template <class MATGEN_T>
+static void apprx_sym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* bl, double eps,
+                          unsigned rankmax) {
+  unsigned n1 = bl->getn1(), n2 = bl->getn2();
+  unsigned b1 = bl->getb1(), b2 = bl->getb2();
+  unsigned maxk = n1 * n2 / (n1 + n2) + 4;
+  if (maxk > rankmax) maxk = rankmax;
+  mbl = new mblock<double>(n1, n2);
+  bool succ = false;
+  if (bl->isadm() && maxk) {
+    unsigned k;
+    double *U, *V;
+    succ = ::ACAr(MatGen, b1, n1, b2, n2, eps, maxk, 0u, k, U, V);
+    if (succ) mbl->cpyLrM_cmpr(k, U, n1, V, n2, eps, k);
+    delete[] V;
+    delete[] U;
+  }
+  if (!succ) {
+    if (bl->isdbl()) {
+      mbl->setHeM();
+      MatGen.cmpblsym(b1, n1, mbl->getdata());
+    } else {
+      mbl->setGeM();
+      MatGen.cmpbl(b1, n1, b2, n2, mbl->getdata());
+    }
+  }
+}
 
 // ACA start row for bounding-box trees (they carry no centroid index): row 0.
 template <class MATGEN_T>
@@ -130,8 +169,10 @@ static void apprx_unsym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* b
 
 extern "C" {
 
-// kind 0: cluster3d_bbx tree + blcluster_geo; kind 1: bemcluster (PCA) + bemblcluster
-void* ref_build(const double* pts, unsigned n, int kind, unsigned bmin, double eta2, double h) {
+// kind 0: cluster3d_bbx tree + blcluster_geo; kind 1: bemcluster (PCA) + bemblcluster;
+// sym: the symmetric block tree (blcluster::subdivide_sym, cluster/blcluster.cpp:90-113)
+static void* build_impl(const double* pts, unsigned n, int kind, unsigned bmin, double eta2, double h,
+                        bool sym) {
   RefH* H = new RefH;
   H->n = n;
   H->kind = kind;
@@ -146,14 +187,16 @@ void* ref_build(const double* pts, unsigned n, int kind, unsigned bmin, double e
     cl->createClusterTree(bmin, H->op_perm.data(), H->po_perm.data());
     H->root_cl = cl;
     blcluster_geo* bl = new blcluster_geo(0, 0, n, n);
-    bl->subdivide(cl, cl, eta2, H->nblcks);
+    if (sym) bl->subdivide_sym(cl, eta2, H->nblcks);
+    else bl->subdivide(cl, cl, eta2, H->nblcks);
     H->root_bl = bl;
   } else {
     bemcluster<Pt>* cl = new bemcluster<Pt>(H->dofs.data(), H->op_perm.data(), 0, n);
     cl->createClusterTree(bmin, H->op_perm.data(), H->po_perm.data());
     H->root_cl = cl;
     bemblcluster<Pt, Pt>* bl = new bemblcluster<Pt, Pt>(0, 0, n, n);
-    bl->subdivide(cl, cl, eta2, H->nblcks);
+    if (sym) bl->subdivide_sym(cl, eta2, H->nblcks);
+    else bl->subdivide(cl, cl, eta2, H->nblcks);
     H->root_bl = bl;
   }
   blcluster** list;
@@ -163,7 +206,16 @@ void* ref_build(const double* pts, unsigned n, int kind, unsigned bmin, double e
   H->gen.dofs = H->dofs.data();
   H->gen.op_perm = H->op_perm.data();
   H->gen.h = h;
+  H->sym = sym;
   return H;
+}
+
+void* ref_build(const double* pts, unsigned n, int kind, unsigned bmin, double eta2, double h) {
+  return build_impl(pts, n, kind, bmin, eta2, h, false);
+}
+
+void* ref_build_sym(const double* pts, unsigned n, int kind, unsigned bmin, double eta2, double h) {
+  return build_impl(pts, n, kind, bmin, eta2, h, true);
 }
 
 unsigned ref_nleaves(void* p) { return ((RefH*)p)->nblcks; }
@@ -194,7 +246,15 @@ void ref_assemble(void* p, double eps, unsigned rankmax, int nthreads) {
   std::streambuf* old = std::cout.rdbuf();
   std::ostringstream sink;
   std::cout.rdbuf(sink.rdbuf());   // progressbar output is not wanted
-  if (H->kind == 1) {
+  if (H->sym && H->kind == 1) {
+    matgenHeH_omp(H->gen, H->nblcks, (bemblcluster<Pt, Pt>*)H->root_bl, eps, rankmax, H->A);
+  } else if (H->sym) {
+#pragma omp parallel for schedule(dynamic)
+    for (int l = 0; l < (int)H->nblcks; ++l) {
+      blcluster* b = H->leaves[l];
+      apprx_sym_bbx(H->gen, H->A[b->getidx()], b, eps, rankmax);
+    }
+  } else if (H->kind == 1) {
     matgenGeH_omp(H->gen, H->nblcks, (bemblcluster<Pt, Pt>*)H->root_bl, eps, rankmax, H->A);
   } else {
 #pragma omp parallel for schedule(dynamic)
@@ -221,6 +281,7 @@ unsigned long ref_leaf_data(void* p, unsigned l, double* out) {
   blcluster* b = H->leaves[l];
   mblock<double>* m = H->A[b->getidx()];
   unsigned long cnt = m->isLrM() ? (unsigned long)m->rank() * (b->getn1() + b->getn2())
+                    : m->isHeM() ? (unsigned long)b->getn1() * (b->getn1() + 1) / 2
                                  : (unsigned long)b->getn1() * b->getn2();
   if (out && cnt) memcpy(out, m->getdata(), cnt * sizeof(double));
   return cnt;
@@ -229,8 +290,14 @@ unsigned long ref_leaf_data(void* p, unsigned l, double* out) {
 // Y += d A X   (p columns, leading dimension n)
 void ref_matvec(void* p, double d, unsigned nrhs, double* X, double* Y) {
   RefH* H = (RefH*)p;
-  if (nrhs == 1) mltaGeHVec(d, H->root_bl, H->A, X, Y);
-  else mltaGeHGeM(d, H->root_bl, H->A, nrhs, X, H->n, Y, H->n);
+  if (H->sym) {
+    if (nrhs == 1) mltaHeHVec(d, H->root_bl, H->A, X, Y);
+    else mltaHeHGeM(d, H->root_bl, H->A, nrhs, X, H->n, Y, H->n);
+  } else if (nrhs == 1) {
+    mltaGeHVec(d, H->root_bl, H->A, X, Y);
+  } else {
+    mltaGeHGeM(d, H->root_bl, H->A, nrhs, X, H->n, Y, H->n);
+  }
 }
 
 unsigned ref_gmres(void* p, double* b, double* x, double* eps, unsigned m, unsigned* nsteps) {

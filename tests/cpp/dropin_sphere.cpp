@@ -1,6 +1,6 @@
 // The reference's hot-path call sequence (cluster tree, block-cluster tree,
-// allocmbls, matgenGeH_omp, mltaGeHVec, mltaGeHhVec, savembls, loadmbls, GMRes, freembls)
-// compiled against
+// allocmbls, matgenGeH_omp, mltaGeHVec, mltaGeHhVec, subdivide_sym, matgenHeH_omp,
+// mltaHeHVec, savembls, loadmbls, GMRes, freembls) compiled against
 // include/ahx_ahmed.hpp.  Checks the product against the dense matrix and
 // GMRES on the diagonal-2/(4 pi h) variant; exit status 0 on success.
 #include <cmath>
@@ -84,6 +84,28 @@ int main(int argc, char** argv) {
   const double err = std::sqrt(num / den), errt = std::sqrt(numt / den);
   std::printf("low-rank leaves %u, product error vs dense %.3e, adjoint %.3e\n", lowrank, err,
               errt);
+  bool sym_ok = false;
+  {  // the symmetric block tree, HeH assembly and product (Include/matgen_omp.h:96-101)
+    unsigned nb = 0;
+    bemblcluster<dof, dof>* bls = new bemblcluster<dof, dof>(0, 0, N, N);
+    bls->subdivide_sym(cl, eta * eta, nb);
+    mblock<double>** S;
+    allocmbls(bls, S);
+    matgenHeH_omp(gen, nb, bls, eps, 1000000, S);
+    std::vector<double> ys(N, 0.0);
+    mltaHeHVec(1.0, bls, S, x.data(), ys.data());
+    double ds = 0.0, ns = 0.0;
+    for (unsigned i = 0; i < N; ++i) {
+      ds += (ys[i] - y[i]) * (ys[i] - y[i]);
+      ns += y[i] * y[i];
+    }
+    unsigned hem = 0;
+    for (unsigned l = 0; l < nb; ++l) hem += S[l]->isHeM();
+    sym_ok = nb < nblcks && hem > 0 && std::sqrt(ds / ns) < 2e-6;
+    std::printf("symmetric: %u leaves (%u Hermitian), product vs general %.3e\n", nb, hem, std::sqrt(ds / ns));
+    freembls(bls, S);
+    delete bls;
+  }
   bool io_ok = false;
   {  // savembls -> loadmbls (Include/H.h:60-103) -> product on a tree built from the file
     {
@@ -129,5 +151,5 @@ int main(int argc, char** argv) {
   freembls(bl2, A);
   delete bl2;
   delete cl;
-  return (err < 2e-6 && errt < 2e-6 && io_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
+  return (err < 2e-6 && errt < 2e-6 && io_ok && sym_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
 }

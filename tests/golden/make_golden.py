@@ -7,6 +7,7 @@ to this script) are committed; the tests read them on any host.
 Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py helmholtz  (complex ACA ranks)
         python tests/golden/make_golden.py mbls       (savembls file hashes)
+        python tests/golden/make_golden.py sym        (symmetric trees, HeH assembly/product)
 """
 import os
 import sys
@@ -139,10 +140,52 @@ def mbls():
     print(f"wrote {path}")
 
 
+# symmetric block trees (subdivide_sym) with the HeH assembly (ACAr, Hermitian
+# diagonal blocks) and product (mltaHeHVec / mltaHeHGeM)
+SYM_CASES = {"sym_fib4096": ("fib4096", False), "sym_sph360": ("sph360", True)}
+
+
+def sym():
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    for name, (base, full) in SYM_CASES.items():
+        gen, bmin = CASES[base]
+        P = gen()
+        h = O.mean_nn(P)
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+               "eps": np.float64(EPS)}
+        n = P.shape[0]
+        rng = np.random.default_rng(0)
+        x = rng.uniform(-1.0, 1.0, n)
+        X = rng.uniform(-1.0, 1.0, (4, n))
+        for kind, kname in ((O.TREE_BBX, "bbx"), (O.TREE_PCA, "pca")):
+            R = O.RefH(P, kind, bmin, ETA, h, sym=True)
+            out[f"{kname}_leaves"] = R.leaves()
+            R.assemble(EPS, nthreads=1)
+            out[f"{kname}_ranks"] = R.ranks()
+            out[f"{kname}_y"] = R.matvec(x, np.zeros(n))
+            Y = np.zeros((4, n))
+            R.matvec(X, Y, d=-0.5)
+            out[f"{kname}_Y4"] = Y
+            if full and kind == O.TREE_PCA:  # (sph360's bbx tree has dense leaves only)
+                chunks = [R.leaf_data(l) for l in range(R.nleaves)]
+                offs = np.zeros(R.nleaves + 1, np.uint64)
+                offs[1:] = np.cumsum([c.size for c in chunks])
+                out[f"{kname}_data"] = np.concatenate(chunks) if chunks else np.zeros(0)
+                out[f"{kname}_offsets"] = offs
+        out["x"] = x
+        out["X4"] = X
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
     elif len(sys.argv) > 1 and sys.argv[1] == "mbls":
         mbls()
+    elif len(sys.argv) > 1 and sys.argv[1] == "sym":
+        sym()
     else:
         main()
