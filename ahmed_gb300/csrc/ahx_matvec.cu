@@ -64,30 +64,37 @@ __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
     L.n2 = n;
   }
   if (TR && L.rank < 0) {
-    // Y[b2 + j] += d sum_i D[i + j n1] X[b1 + i]
+    // Y[b2 + j] += d sum_i D[i + j n1] X[b1 + i]: one output column j of D per
+    // thread, the X rows of D's row range staged in shared memory (as the plain
+    // path stages the column range); a thread reads its column of D in order
     const SD* Ad = L.dense_in_lr_arena ? reinterpret_cast<const SD*>(reinterpret_cast<const SL*>(a.arena_lr) + L.off)
                                        : reinterpret_cast<const SD*>(a.arena_dn) + L.off;
-    const uint32_t warp = tid >> 5, lane = tid & 31;
     for (uint32_t r0 = 0; r0 < a.p; r0 += PG) {
       const uint32_t pg = min((uint32_t)PG, a.p - r0);
-      for (uint32_t j = warp; j < L.n2; j += kThreads / 32) {
+      for (uint32_t jb = 0; jb < L.n2; jb += kThreads) {
+        const uint32_t j = jb + tid;
         A acc[PG];
 #pragma unroll
         for (int r = 0; r < PG; ++r) acc[r] = 0;
-        const SD* col = Ad + (uint64_t)j * L.n1;
-        for (uint32_t i = lane; i < L.n1; i += 32) {
-          const A av = ldcvt<SD, A>(col + i);
+        for (uint32_t ib = 0; ib < L.n1; ib += kCh) {
+          const uint32_t in = min((uint32_t)kCh, L.n1 - ib);
+          __syncthreads();
+          stage_x<A, PG>(Xs, a, r0, pg, L.b1, ib, in);
+          __syncthreads();
+          if (j < L.n2) {
+            const SD* col = Ad + (uint64_t)j * L.n1 + ib;
+            for (uint32_t i = 0; i < in; ++i) {
+              const A av = ldcvt<SD, A>(col + i);
+#pragma unroll
+              for (int r = 0; r < PG; ++r) acc[r] = fma(av, Xs[i][r], acc[r]);
+            }
+          }
+        }
+        if (j < L.n2) {
 #pragma unroll
           for (int r = 0; r < PG; ++r)
-            if ((uint32_t)r < pg) acc[r] = fma(av, (A)a.X[(uint64_t)(r0 + r) * a.ldX + L.b1 + i], acc[r]);
+            if ((uint32_t)r < pg) atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b2 + j, d * (double)acc[r]);
         }
-#pragma unroll
-        for (int r = 0; r < PG; ++r) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-        }
-        if (lane == 0)
-          for (uint32_t r = 0; r < pg; ++r) atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b2 + j, d * (double)acc[r]);
       }
     }
     return;
@@ -117,9 +124,11 @@ __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
             }
           }
         }
-        if (i < L.n1)
-          for (uint32_t r = 0; r < pg; ++r)
-            atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
+        if (i < L.n1) {
+#pragma unroll
+          for (int r = 0; r < PG; ++r)
+            if ((uint32_t)r < pg) atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
+        }
       }
     } else if (L.rank > 0) {
       const uint32_t k = (uint32_t)L.rank;
@@ -190,8 +199,9 @@ __global__ void __launch_bounds__(kThreads) mv_kernel(MvArgs a) {
 #pragma unroll
               for (int r = 0; r < PG; ++r) acc[r] = fma(uv, Ts[l][r], acc[r]);
             }
-            for (uint32_t r = 0; r < pg; ++r)
-              atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
+#pragma unroll
+            for (int r = 0; r < PG; ++r)
+              if ((uint32_t)r < pg) atomicAdd(a.Y + (uint64_t)(r0 + r) * a.ldY + L.b1 + i, d * (double)acc[r]);
           }
         }
         __syncthreads();

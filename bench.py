@@ -412,11 +412,14 @@ def run_product(args):
     dev = torch.device("cuda", 0)
     n = args.n
     P = A.geometry.cube_surface(n, 4) if args.geometry == "cube" else A.geometry.fibonacci_sphere(n)
-    H = A.HMatrix(P, "bbx", bmin=args.leaf, eta=ETA, device=0)
+    H = A.HMatrix(P, "bbx", bmin=args.leaf, eta=ETA, device=0, symmetric=args.symmetric)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     H.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
     H.matgenGeH_omp(A.mean_nn(P), EPS)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
     H.prepare(args.precision)
     X = torch.from_numpy(np.random.default_rng(1).uniform(-1.0, 1.0, (args.rhs, n))).to(dev)
     Y = torch.zeros_like(X)
@@ -432,8 +435,10 @@ def run_product(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     b = algorithmic_bytes(H, args.precision, args.rhs)
-    print(json.dumps({"workload": f"laplace-{args.geometry}-{n}-{args.rhs}rhs-{args.precision}", "ms": ms,
-                      "algorithmic_bytes": b, "achieved_gbs": b / (ms * 1e-3) / 1e9}))
+    sym = "-sym" if args.symmetric else ""
+    print(json.dumps({"workload": f"laplace-{args.geometry}-{n}-{args.rhs}rhs-{args.precision}{sym}", "ms": ms,
+                      "algorithmic_bytes": b, "achieved_gbs": b / (ms * 1e-3) / 1e9, "assembly_s": t_asm,
+                      "fp64_leaf_bytes": int(H.storage_bytes("fp64"))}))
 
 
 def run_predictor(args):
@@ -636,6 +641,8 @@ def main():
     ap.add_argument("--geometry", default="sphere", choices=["sphere", "cube"], help="product workload")
     ap.add_argument("--leaf", type=int, default=BMIN, help="product workload")
     ap.add_argument("--rhs", type=int, default=NRHS, help="product workload")
+    ap.add_argument("--symmetric", action="store_true",
+                    help="product workload: symmetric block tree, HeH assembly (upper blocks once)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp64", "df64"], help="product workload")
     ap.add_argument("--n-large", type=int, default=1 << 20)
     ap.add_argument("--diag", default="mean", choices=["mean", "min"],
