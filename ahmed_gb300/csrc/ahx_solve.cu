@@ -1086,6 +1086,46 @@ int ahx_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t 
   return status;
 }
 
+// spctrlnrm (Include/matrix.h:50-75): it_num power steps on A^T A from x = 1
+// (FP64 products; A^T by the transposed product), the square root of the last norm.
+int ahx_spctrlnrm(ahx_hmat* H, uint32_t it_num, double* out) {
+  if (!H || !out) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("ahx_spctrlnrm: H-matrix not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  HmatOp op(H);
+  Solver sv(op, 1);
+  if ((rc = sv.init(2))) return rc;
+  const uint64_t n = H->tree.n;
+  DevBuf xb, yb;
+  if ((rc = xb.reserve(n * 8)) || (rc = yb.reserve(n * 8))) return rc;
+  double* x = xb.as<double>();
+  double* y = yb.as<double>();
+  cudaStream_t st = H->stream;
+  const std::vector<double> ones(n, 1.0);
+  AHX_CUDA(cudaMemcpyAsync(x, ones.data(), n * 8, cudaMemcpyHostToDevice, st));
+  double* d2 = sv.small_.as<double>();
+  double dd = 0.0;
+  for (uint32_t it = 0; it < it_num; ++it) {
+    AHX_CUDA(cudaMemsetAsync(y, 0, n * 8, st));
+    if ((rc = product_device(H, kFP64, 1.0, 1, x, n, y, n, false))) return rc;
+    AHX_CUDA(cudaMemsetAsync(x, 0, n * 8, st));
+    if ((rc = product_device(H, kFP64, 1.0, 1, y, n, x, n, true))) return rc;
+    if ((rc = sv.dots(x, 0, 1, x, d2))) return rc;
+    scale_kernel<<<grid_for(n), 256, 0, st>>>(x, x, d2, sv.maxk_, 1, n, n, nullptr, 1);  // x /= |x|
+    AHX_CUDA(cudaGetLastError());
+  }
+  if (it_num) AHX_CUDA(cudaMemcpyAsync(&dd, d2, 8, cudaMemcpyDeviceToHost, st));
+  AHX_CUDA(cudaStreamSynchronize(st));
+  xb.release();
+  yb.release();
+  *out = std::sqrt(std::sqrt(dd));
+  return AHX_OK;
+}
+
 int ahx_cg(ahx_hmat* H, uint32_t p, const double* B, uint64_t ldB, double* X, uint64_t ldX,
            double tol, uint32_t maxit, uint32_t* iters, double* resid) {
   if (!H || !B || !X || p == 0 || ldB < H->tree.n || ldX < H->tree.n) {

@@ -284,6 +284,13 @@ class HMatrix:
                                      float(eps), int(m), int(nsteps), ptr(iters), ptr(res)))
         return (0 if code == _capi.AHX_OK else 1), res, iters
 
+    def spctrlnrm(self, it_num=10):
+        """Include/matrix.h:50-75: sqrt of the largest eigenvalue of A^T A by it_num
+        power steps from x = 1 (FP64 leaves)."""
+        out = C.c_double()
+        check(lib().ahx_spctrlnrm(self._h, int(it_num), C.byref(out)))
+        return out.value
+
     def CG(self, b, x, eps, nsteps):
         p, ld = _ncols(b, self.n)
         self._follow_torch(b, x)

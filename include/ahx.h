@@ -183,6 +183,10 @@ int ahx_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t 
               uint64_t ldX, double tol, uint32_t m, uint32_t maxit, uint32_t* iters,
               double* resid);
 
+/* Spectral norm sqrt(lambda_max(A^T A)) by it_num power steps from x = 1 with the
+ * FP64 leaves; replaces spctrlnrm(A, it_num) Include/matrix.h:50-75. */
+int ahx_spctrlnrm(ahx_hmat* H, uint32_t it_num, double* out);
+
 /* Conjugate gradients for p right-hand sides; replaces CG(A, b, x, eps, nsteps)
  * solvers/CG.cpp:31-113 (FP64 product). */
 int ahx_cg(ahx_hmat* H, uint32_t p, const double* B, uint64_t ldB, double* X, uint64_t ldX,

@@ -25,6 +25,7 @@
 #define AHX_AHMED_HPP
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
@@ -345,7 +346,32 @@ struct HMatrixOperator : public Matrix<double> {
   blcluster* bl;
   explicit HMatrixOperator(blcluster* b) : Matrix<double>(b->getn1(), b->getn1()), bl(b) {}
   void amux(double d, double* x, double* y) const override { mltaGeHVec(d, bl, nullptr, x, y); }
+  void atmux(double d, double* x, double* y) const override { mltaGeHhVec(d, bl, nullptr, x, y); }
 };
+
+// Include/matrix.h:50-75: sqrt of the largest eigenvalue of A^H A by it_num power steps;
+// on the GPU for the H-matrix operator, else with the operator's own amux / atmux
+template <class T>
+double spctrlnrm(Matrix<T>& A, const unsigned it_num = 10) {
+  if (HMatrixOperator* h = dynamic_cast<HMatrixOperator*>(&A)) {
+    double v = 0.0;
+    check(ahx_spctrlnrm(h->bl->handle(), it_num, &v));
+    return v;
+  }
+  std::vector<T> x(A.n, (T)1), y(A.m);
+  double d = 0.0;
+  for (unsigned i = 0; i < it_num; ++i) {
+    std::fill(y.begin(), y.end(), (T)0);
+    A.amux((T)1, x.data(), y.data());
+    std::fill(x.begin(), x.end(), (T)0);
+    A.atmux((T)1, y.data(), x.data());
+    d = 0.0;
+    for (const T& v : x) d += (double)(v * v);
+    d = std::sqrt(d);
+    for (T& v : x) v = (T)(v / d);
+  }
+  return std::sqrt(d);
+}
 
 // solvers/GMRES.cpp:80: returns 0 converged, 1 not; eps and nsteps updated
 inline unsigned GMRes(const Matrix<double>& A, double* const b, double* const x, double& eps,

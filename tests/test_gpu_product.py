@@ -207,3 +207,34 @@ def test_df64_product_on_reference_leaves(golden):
     H = _with_leaves(g, "pca", g["pca_ranks"], chunks)
     y = H.mltaGeHVec(1.0, g["x"], np.zeros(H.n), precision="df64")
     assert _relerr(y, g["pca_y"]) <= TOL_FP64
+
+
+def _dense_of(H):
+    """The assembled H-matrix as a dense array (from its leaves)."""
+    n = H.n
+    lv, ranks = H.leaves(), H.ranks()
+    A = np.zeros((n, n))
+    for l in range(len(lv)):
+        b1, n1, b2, n2 = (int(v) for v in lv[l][:4])
+        data = H.leaf_data(l)
+        if ranks[l] < 0:
+            A[b1:b1 + n1, b2:b2 + n2] = data.reshape(n2, n1).T
+        elif ranks[l] > 0:
+            k = int(ranks[l])
+            A[b1:b1 + n1, b2:b2 + n2] = data[:n1 * k].reshape(k, n1).T @ data[n1 * k:].reshape(k, n2)
+    return A
+
+
+def test_spctrlnrm_matches_power_iteration(oracle_pair):
+    """spctrlnrm (Include/matrix.h:50-75) equals the same 10 power steps on the
+    dense form of the assembled leaves (numpy, FP64)."""
+    _, H = oracle_pair["bbx"]
+    A = _dense_of(H)
+    x = np.ones(H.n)
+    for _ in range(10):
+        x = A.T @ (A @ x)
+        d = np.linalg.norm(x)
+        x = x / d
+    ref = np.sqrt(d)
+    assert abs(H.spctrlnrm(10) - ref) / ref <= 1e-12
+    assert abs(np.linalg.norm(A, 2) - ref) / ref <= 1e-3   # 10 steps: near the true norm
