@@ -65,6 +65,7 @@ SIGNATURES = [
     ("ahx_mbls_header", _i32, [C.c_char_p, _vp, _vp, _vp]),
     ("ahx_batch_prepare", _i32, [_vp, _i32]),
     ("ahx_spctrlnrm", _i32, [_vp, _u32, _vp]),
+    ("ahx_agglomerate", _i32, [_vp, _dbl, _u32, _vp]),
     ("ahx_hmat_save", _i32, [_vp, _dbl, _u32, C.c_char_p]),
     ("ahx_hmat_load", _i32, [_vp, C.c_char_p, _vp, _vp]),
     ("ahx_hmat_save_stream", _i32, [_vp, _dbl, _u32, _vp, _vp]),

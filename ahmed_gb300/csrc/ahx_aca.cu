@@ -679,6 +679,59 @@ __device__ void aca_task(const Grp& g, const AcaParams& p, uint32_t ti, double* 
   if (g.rank == 0) p.res[ti] = AcaResult{st, k, kt, 0u};
 }
 
+// Agglomeration (H/agglH.cpp:14-107): the concatenated factors of sibling
+// low-rank blocks (gathered into the task's workspace, zero elsewhere)
+// recompressed to the parent's rank with the relative threshold of
+// mblock::unify_cols / unify_rows (H/mblock_D.cpp:662-862).
+template <int G, class Grp>
+__device__ void merge_task(const Grp& g, const MergeParams& p, uint32_t ti, double* smem) {
+  const MergeTask t = p.tasks[ti];
+  const uint32_t m = t.m, n = t.n, kc = t.k;
+  double* U = p.ws + t.ws;
+  double* V = U + (size_t)m * kc;
+  double* Un = V + (size_t)n * kc;
+  double* Vn = Un + (size_t)m * kc;
+  double* Rg = Vn + (size_t)n * kc;
+  double* Vsg = Rg + (size_t)kc * kc;
+  double* sigg = Vsg + (size_t)kc * kc;
+  double* taug = sigg + kc;
+  uint32_t kt = 0;
+  if (kc > 0) {
+    const bool sm = kc <= (uint32_t)KSM;
+    double* R = sm ? smem : Rg;
+    double* Vs = sm ? smem + KSM * LDS : Vsg;
+    double* sig = sm ? smem + 2 * KSM * LDS : sigg;
+    double* tau = sm ? smem + 2 * KSM * LDS + KSM : taug;
+    int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : p.zs + t.zs;
+    g.sync();
+    kt = recompress<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau, perm);
+  }
+  if (g.rank == 0) p.res[ti] = AcaResult{kAcaOk, kc, kt, 0u};
+}
+
+__global__ void __launch_bounds__(32 * kSmallWarps) merge_small_kernel(MergeParams p) {
+  extern __shared__ double smem_all[];
+  const uint32_t w = threadIdx.x >> 5;
+  const uint32_t task = blockIdx.x * kSmallWarps + w;
+  if (task >= p.ntasks) return;
+  Group<32> g(threadIdx.x & 31);
+  merge_task<32>(g, p, task, smem_all + (size_t)w * kSmemPerGroup);
+}
+
+__global__ void copy2d_kernel(const Seg2D* __restrict__ segs, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+  const Seg2D s = segs[blockIdx.x];
+  if (s.src == kSegIdentity) {
+    for (uint32_t c = threadIdx.x; c < s.ncols; c += blockDim.x) dst[s.dst + (uint64_t)c * s.ld_dst + c] = 1.0;
+    return;
+  }
+  const uint64_t cnt = (uint64_t)s.nrows * s.ncols;
+  for (uint64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const uint64_t c = e / s.nrows, r = e - c * s.nrows;
+    dst[s.dst + c * s.ld_dst + r] = src[s.src + e];
+  }
+}
+
 __global__ void __launch_bounds__(32 * kSmallWarps) aca_small_kernel(AcaParams p) {
   extern __shared__ double smem_all[];
   const uint32_t w = threadIdx.x >> 5;
@@ -696,6 +749,14 @@ __global__ void __launch_bounds__(kLargeThreads) aca_large_kernel(AcaParams p) {
   if (task >= p.ntasks) return;
   Group<kLargeThreads> g(threadIdx.x, smem_all + kSmemPerGroup);
   aca_task<kLargeThreads>(g, p, task, smem_all);
+}
+
+__global__ void __launch_bounds__(kLargeThreads) merge_large_kernel(MergeParams p) {
+  extern __shared__ double smem_all[];
+  const uint32_t task = blockIdx.x;
+  if (task >= p.ntasks) return;
+  Group<kLargeThreads> g(threadIdx.x, smem_all + kSmemPerGroup);
+  merge_task<kLargeThreads>(g, p, task, smem_all);
 }
 
 __global__ void dense_fill_kernel(PointsSoA P, double diag, const DenseTask* __restrict__ tasks,
@@ -764,6 +825,28 @@ cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask
                               uint32_t ntasks, double* arena, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   dense_fill_kernel<<<ntasks, 256, 0, s>>>(pts, diag, tasks, arena);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_merge(const MergeParams& p, bool large, cudaStream_t s) {
+  if (p.ntasks == 0) return cudaSuccess;
+  if (!large) {
+    const size_t smem = sizeof(double) * kSmemPerGroup * kSmallWarps;
+    cudaError_t e = cudaFuncSetAttribute(merge_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    merge_small_kernel<<<(p.ntasks + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, smem, s>>>(p);
+  } else {
+    const size_t smem = sizeof(double) * (kSmemPerGroup + 3 * (kLargeThreads / 32) + 8);
+    cudaError_t e = cudaFuncSetAttribute(merge_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    merge_large_kernel<<<p.ntasks, kLargeThreads, smem, s>>>(p);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy2d(const Seg2D* segs, uint32_t nsegs, const double* src, double* dst, cudaStream_t s) {
+  if (nsegs == 0) return cudaSuccess;
+  copy2d_kernel<<<nsegs, 256, 0, s>>>(segs, src, dst);
   return cudaGetLastError();
 }
 

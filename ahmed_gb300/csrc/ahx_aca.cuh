@@ -71,6 +71,32 @@ struct MirrorTask {
 };
 cudaError_t launch_mirror(const MirrorTask* tasks, uint32_t ntasks, double* arena, cudaStream_t s);
 
+// Agglomeration: recompression of merged sibling blocks.  Workspace at `ws`
+// (doubles, aca_ws_doubles(m, n, k)): U (m x k) and V (n x k) hold the gathered
+// factors; Un, Vn receive the result; `zs` (ints): m + n scratch.
+struct MergeTask {
+  uint32_t m, n, k, pad;
+  uint64_t ws, zs;
+};
+struct MergeParams {
+  const MergeTask* tasks;
+  uint32_t ntasks;
+  double* ws;
+  int* zs;
+  double eps;
+  AcaResult* res;  // k_aca = k, kt = recompressed rank
+};
+// large: one CTA per task (m or n above 4096), else one warp
+cudaError_t launch_merge(const MergeParams& p, bool large, cudaStream_t s);
+// dst[s.dst + c * ld_dst + r] = src[s.src + c * nrows + r], r < nrows, c < ncols;
+// src == kSegIdentity: ones on the diagonal (r == c) of the zeroed destination
+constexpr uint64_t kSegIdentity = ~0ull;
+struct Seg2D {
+  uint64_t src, dst;
+  uint32_t nrows, ncols, ld_dst, pad;
+};
+cudaError_t launch_copy2d(const Seg2D* segs, uint32_t nsegs, const double* src, double* dst, cudaStream_t s);
+
 // Copy recompressed factors (Un, Vn, kt columns) from the workspace into the arena.
 struct CopyTask {
   uint64_t src_u, src_v;  // workspace offsets (doubles)

@@ -1,0 +1,337 @@
+// Agglomeration of an assembled H-matrix: agglH (H/agglH.cpp:111-272), the
+// recmpr branch of matgenGeH_sqntl (Include/matgen_sqntl.h:32-55, 88-102).
+//
+// Bottom up, a block that is not diagonal and whose sons are all leaves is
+// replaced by one low-rank leaf when the recompressed union of its sons
+// (unify_sons_, H/agglH.cpp:14-107: relative threshold eps, at most max_rank)
+// stores no more than the sons did.  The block tree is rebuilt from the
+// cluster tree; the candidates of one height are merged as one batch on the
+// GPU (factors gathered into workspaces, QR + SVD recompression per block);
+// the merged leaf takes its first son's index and the indices are then
+// compacted like fill_gaps_ (H/agglH.cpp:185-211).  The leaf arena is
+// rewritten in leaf order.
+//
+// A dense son D enters the union in factored form D I^T (its columns as U, an
+// identity as V), so that every union is one QR + SVD recompression of
+// [U_cat][V_cat]^T; the reference forms the dense block and takes its SVD
+// (mblock::unify_cols, H/mblock_D.cpp:804-860) with the same truncation rule.
+// The reference unifies the sons pairwise (columns, then rows) and truncates
+// after each step; this one-shot union truncates once.
+#include <algorithm>
+#include <vector>
+
+#include "ahx_aca.cuh"
+#include "ahx_hmat.hpp"
+
+namespace ahx {
+namespace {
+
+struct BNode {
+  uint32_t b1, n1, b2, n2;
+  int32_t rc, cc;
+  int32_t son[4];  // row-major 2 x 2 (son[2 i + j]); -1: absent
+  int32_t leaf;    // leaf index while a leaf, else -1
+  bool dbl;        // diagonal block (never merged)
+  bool decided;    // tried (merged or kept)
+};
+
+struct TreeBuilder {
+  const Tree& T;
+  std::vector<BNode> nodes;
+  uint32_t next_leaf = 0;
+  bool failed = false;  // the leaves are not those of the cluster tree's block tree
+
+  int32_t add(int32_t ia, int32_t ib) {
+    const ClusterNode& a = T.nodes[ia];
+    const ClusterNode& b = T.nodes[ib];
+    BNode n{};
+    n.b1 = a.nbeg;
+    n.n1 = a.nend - a.nbeg;
+    n.b2 = b.nbeg;
+    n.n2 = b.nend - b.nbeg;
+    n.rc = ia;
+    n.cc = ib;
+    n.son[0] = n.son[1] = n.son[2] = n.son[3] = -1;
+    n.leaf = -1;
+    n.dbl = n.b1 == n.b2;
+    n.decided = false;
+    nodes.push_back(n);
+    return (int32_t)nodes.size() - 1;
+  }
+  // the recursion of Tree's own builder: its leaves come out in leaf order
+  int32_t general(int32_t ia, int32_t ib) {
+    const int32_t id = add(ia, ib);
+    const uint32_t l = next_leaf;
+    if (l < T.leaves.size() && T.leaves[l].row_cl == ia && T.leaves[l].col_cl == ib) {
+      nodes[id].leaf = (int32_t)next_leaf++;
+      return id;
+    }
+    const ClusterNode& a = T.nodes[ia];
+    const ClusterNode& b = T.nodes[ib];
+    if (failed || a.son[0] < 0 || b.son[0] < 0) {
+      failed = true;
+      return id;
+    }
+    const int32_t as[2] = {a.son[0], a.son[1]}, bs[2] = {b.son[0], b.son[1]};
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) {
+        const int32_t s = general(as[i], bs[j]);
+        nodes[id].son[2 * i + j] = s;
+      }
+    return id;
+  }
+  int32_t sym(int32_t ia) {
+    const int32_t id = add(ia, ia);
+    const uint32_t l = next_leaf;
+    if (l < T.leaves.size() && T.leaves[l].row_cl == ia && T.leaves[l].col_cl == ia) {
+      nodes[id].leaf = (int32_t)next_leaf++;
+      return id;
+    }
+    const ClusterNode& a = T.nodes[ia];
+    if (failed || a.son[0] < 0) {
+      failed = true;
+      return id;
+    }
+    const int32_t s0 = sym(a.son[0]);
+    nodes[id].son[0] = s0;
+    const int32_t s1 = general(a.son[0], a.son[1]);
+    nodes[id].son[1] = s1;
+    const int32_t s3 = sym(a.son[1]);
+    nodes[id].son[3] = s3;
+    return id;
+  }
+};
+
+}  // namespace
+}  // namespace ahx
+
+using namespace ahx;
+
+extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged) {
+  if (!H || !(eps >= 0.0)) return AHX_ERR_ARG;
+  if (!H->assembled) {
+    set_error("ahx_agglomerate: H-matrix not assembled");
+    return AHX_ERR_STATE;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  Tree& T = H->tree;
+  if (T.nodes.empty() || T.leaves.empty()) return AHX_OK;
+  // the block tree of the current leaves (the root is the node of cluster 0 with itself)
+  TreeBuilder B{T};
+  const int32_t root = T.sym ? B.sym(0) : B.general(0, 0);
+  if (B.failed || B.next_leaf != T.leaves.size()) {
+    set_error("ahx_agglomerate: the leaves do not form the block tree (agglomerate once per assembly)");
+    return AHX_ERR_STATE;
+  }
+  std::vector<BNode>& N = B.nodes;
+  const uint32_t nl0 = (uint32_t)T.leaves.size();
+  // leaf state, indexed by the reference's leaf index (idx)
+  std::vector<int32_t> rank(H->rank);
+  std::vector<uint64_t> off(H->off);
+  std::vector<int32_t> leaf_node(nl0, -1);
+  for (int32_t i = 0; i < (int32_t)N.size(); ++i)
+    if (N[i].leaf >= 0) leaf_node[N[i].leaf] = i;
+  auto size_of = [&](int32_t leaf) -> uint64_t {
+    const BNode& q = N[leaf_node[leaf]];
+    const int32_t r = rank[leaf];
+    return r < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)r * (q.n1 + q.n2);
+  };
+  uint32_t merged = 0;
+  DevBuf ws, zs, dtasks, dres, dsegs, dcopy;
+  const size_t budget = aca_ws_budget();
+  for (;;) {
+    // candidates of this height: undecided, not diagonal, all sons leaves
+    std::vector<int32_t> cand;
+    for (int32_t i = 0; i < (int32_t)N.size(); ++i) {
+      BNode& q = N[i];
+      if (q.leaf >= 0 || q.decided || q.dbl) continue;
+      bool all_leaves = true;
+      for (int s = 0; s < 4; ++s)
+        if (q.son[s] < 0 || N[q.son[s]].leaf < 0) all_leaves = false;
+      if (all_leaves) cand.push_back(i);
+    }
+    if (cand.empty()) break;
+    // batches under the workspace budget, small (warp) and large (CTA) blocks apart
+    for (int large = 0; large < 2; ++large) {
+      std::vector<int32_t> todo;
+      for (int32_t c : cand)
+        if ((std::max(N[c].n1, N[c].n2) > 4096u) == (large == 1)) todo.push_back(c);
+      size_t at = 0;
+      while (at < todo.size()) {
+        std::vector<MergeTask> tasks;
+        std::vector<Seg2D> segs;
+        std::vector<int32_t> which;
+        uint64_t wsz = 0, zsz = 0;
+        for (; at < todo.size(); ++at) {
+          const BNode& q = N[todo[at]];
+          uint32_t k = 0;  // union columns: the ranks, and the widths of dense sons
+          for (int s = 0; s < 4; ++s) {
+            const BNode& c = N[q.son[s]];
+            k += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
+          }
+          const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u));
+          if (!tasks.empty() && (wsz + need) * sizeof(double) > budget) break;
+          MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
+          // U = [U00 U01 0 0; 0 0 U10 U11], V = [V00 0 V10 0; 0 V01 0 V11]; a dense
+          // son contributes (D, I)
+          uint32_t col = 0;
+          for (int s = 0; s < 4; ++s) {
+            const BNode& c = N[q.son[s]];
+            const bool dense = rank[c.leaf] < 0;
+            const uint32_t kc = dense ? c.n2 : (uint32_t)rank[c.leaf];
+            if (kc == 0) continue;
+            const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
+            const uint64_t o = off[c.leaf];
+            const uint64_t vdst = wsz + (uint64_t)q.n1 * k + (uint64_t)col * q.n2 + co;
+            segs.push_back(Seg2D{o, wsz + (uint64_t)col * q.n1 + ro, c.n1, kc, q.n1, 0u});
+            if (dense) segs.push_back(Seg2D{kSegIdentity, vdst, kc, kc, q.n2, 0u});
+            else segs.push_back(Seg2D{o + (uint64_t)c.n1 * kc, vdst, c.n2, kc, q.n2, 0u});
+            col += kc;
+          }
+          tasks.push_back(t);
+          which.push_back(todo[at]);
+          wsz += need;
+          zsz += q.n1 + q.n2 + 1;
+        }
+        if ((rc = ws.reserve(std::max<uint64_t>(wsz, 1) * sizeof(double)))) return rc;
+        if ((rc = zs.reserve(std::max<uint64_t>(zsz, 1) * sizeof(int)))) return rc;
+        AHX_CUDA(cudaMemsetAsync(ws.p, 0, wsz * sizeof(double), H->stream));
+        if ((rc = upload(dsegs, segs, H->stream))) return rc;
+        AHX_CUDA(launch_copy2d(dsegs.as<Seg2D>(), (uint32_t)segs.size(), H->arena64.as<double>(), ws.as<double>(),
+                               H->stream));
+        if ((rc = upload(dtasks, tasks, H->stream))) return rc;
+        if ((rc = dres.reserve(tasks.size() * sizeof(AcaResult)))) return rc;
+        MergeParams p;
+        p.tasks = dtasks.as<MergeTask>();
+        p.ntasks = (uint32_t)tasks.size();
+        p.ws = ws.as<double>();
+        p.zs = zs.as<int>();
+        p.eps = eps;
+        p.res = dres.as<AcaResult>();
+        AHX_CUDA(launch_merge(p, large == 1, H->stream));
+        std::vector<AcaResult> res(tasks.size());
+        AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, res.size() * sizeof(AcaResult), cudaMemcpyDeviceToHost,
+                                 H->stream));
+        AHX_CUDA(cudaStreamSynchronize(H->stream));
+        std::vector<CopyTask> copies;
+        for (size_t q = 0; q < tasks.size(); ++q) {
+          BNode& nd = N[which[q]];
+          nd.decided = true;
+          const uint32_t kt = std::min(res[q].kt, max_rank);
+          uint64_t pre = 0;
+          for (int s = 0; s < 4; ++s) pre += size_of(N[nd.son[s]].leaf);
+          const uint64_t post = (uint64_t)kt * (nd.n1 + nd.n2);
+          if (pre < post) continue;  // H/agglH.cpp:86: merge when it does not cost more
+          // the merged block takes its first son's index; the other sons' are freed
+          const int32_t first = N[nd.son[0]].leaf;
+          uint64_t dst = 0;
+          if (post && (rc = arena_append(H, post, dst))) return rc;
+          if (post) {
+            const MergeTask& t = tasks[q];
+            const uint64_t un = t.ws + (uint64_t)(t.m + t.n) * t.k;  // Un follows U and V
+            copies.push_back(CopyTask{un, un + (uint64_t)t.m * t.k, dst, t.m, t.n, kt, 0u});
+          }
+          rank[first] = (int32_t)kt;
+          off[first] = dst;
+          leaf_node[first] = which[q];
+          nd.leaf = first;
+          ++merged;
+        }
+        if (!copies.empty()) {
+          if ((rc = upload(dcopy, copies, H->stream))) return rc;
+          AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), ws.as<double>(),
+                                       H->arena64.as<double>(), H->stream));
+          AHX_CUDA(cudaStreamSynchronize(H->stream));
+        }
+      }
+    }
+  }
+  for (DevBuf* b : {&ws, &zs, &dtasks, &dres, &dsegs, &dcopy}) b->release();
+  if (nmerged) *nmerged = merged;
+  if (!merged) return AHX_OK;
+  // fill_gaps_ (H/agglH.cpp:185-211): in DFS order, leaves whose index is past the new
+  // count move to the lowest free index
+  std::vector<int32_t> dfs;  // leaf indices of the final tree in DFS order
+  {
+    std::vector<int32_t> stack{root};
+    while (!stack.empty()) {
+      const int32_t i = stack.back();
+      stack.pop_back();
+      const BNode& q = N[i];
+      if (q.leaf >= 0) {
+        dfs.push_back(q.leaf);
+        continue;
+      }
+      for (int s = 3; s >= 0; --s)
+        if (q.son[s] >= 0) stack.push_back(q.son[s]);
+    }
+  }
+  const uint32_t nnew = (uint32_t)dfs.size();
+  std::vector<uint8_t> taken(nl0, 0);
+  for (int32_t l : dfs)
+    if ((uint32_t)l < nnew) taken[l] = 1;
+  std::vector<int32_t> final_idx(nl0, -1);
+  uint32_t gap = 0;
+  for (int32_t l : dfs) {
+    if ((uint32_t)l < nnew) {
+      final_idx[l] = l;
+    } else {
+      while (taken[gap]) ++gap;
+      taken[gap] = 1;
+      final_idx[l] = (int32_t)gap;
+    }
+  }
+  // new leaf list in index order; the arena rewritten in that order
+  std::vector<Leaf> leaves(nnew);
+  std::vector<int32_t> nrank(nnew);
+  std::vector<uint64_t> noff(nnew);
+  std::vector<CopyTask> moves;
+  uint64_t total = 0;
+  std::vector<int32_t> at_idx(nnew, -1);
+  for (int32_t l : dfs) at_idx[final_idx[l]] = l;
+  for (uint32_t k = 0; k < nnew; ++k) {
+    const int32_t l = at_idx[k];
+    const BNode& q = N[leaf_node[l]];
+    Leaf L{};
+    if ((uint32_t)l < nl0 && leaf_node[l] >= 0 && N[leaf_node[l]].son[0] < 0) {
+      L = T.leaves[l];  // an original leaf
+    } else {
+      L.b1 = q.b1;
+      L.n1 = q.n1;
+      L.b2 = q.b2;
+      L.n2 = q.n2;
+      L.adm = 0;  // the merged block keeps its (inadmissible) tree flag
+      L.i0 = 0;
+      L.row_cl = q.rc;
+      L.col_cl = q.cc;
+    }
+    L.idx = k;
+    leaves[k] = L;
+    nrank[k] = rank[l];
+    const uint64_t cnt = rank[l] < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)rank[l] * (q.n1 + q.n2);
+    noff[k] = total;
+    if (cnt) {
+      // dense: n1 x n2 as "U" with kt = n2 columns and an empty "V"
+      if (rank[l] < 0) moves.push_back(CopyTask{off[l], off[l], total, q.n1, 0u, q.n2, 0u});
+      else moves.push_back(CopyTask{off[l], off[l] + (uint64_t)q.n1 * rank[l], total, q.n1, q.n2, (uint32_t)rank[l], 0u});
+    }
+    total += cnt;
+  }
+  DevBuf fresh, dm;
+  if ((rc = fresh.reserve(std::max<uint64_t>(total, 1) * sizeof(double)))) return rc;
+  if ((rc = upload(dm, moves, H->stream))) return rc;
+  AHX_CUDA(launch_copy_factors(dm.as<CopyTask>(), (uint32_t)moves.size(), H->arena64.as<double>(),
+                               fresh.as<double>(), H->stream));
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  dm.release();
+  H->arena64.release();
+  H->arena64 = fresh;
+  H->arena64_elems = total;
+  invalidate_products(H);
+  T.leaves = leaves;
+  H->rank = nrank;
+  H->aca_rank = nrank;
+  H->off = noff;
+  return AHX_OK;
+}

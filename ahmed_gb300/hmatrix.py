@@ -284,6 +284,21 @@ class HMatrix:
                                      float(eps), int(m), int(nsteps), ptr(iters), ptr(res)))
         return (0 if code == _capi.AHX_OK else 1), res, iters
 
+    def agglH(self, eps=None, max_rank=2**32 - 1):
+        """Agglomeration (H/agglH.cpp:111-272): merges sibling low-rank leaves whose
+        recompressed union stores no more; returns the number of merged blocks."""
+        eps = self.eps if eps is None else float(eps)
+        n = C.c_uint32()
+        check(lib().ahx_agglomerate(self._h, eps, min(int(max_rank), 2**32 - 1), C.byref(n)))
+        return n.value
+
+    def matgenGeH_sqntl(self, h=None, recmpr=False, eps=1e-6, rankmax=2**32 - 1):
+        """Include/matgen_sqntl.h:88-102: the assembly, then (recmpr) agglomeration."""
+        self.matgenGeH_omp(h, eps, rankmax)
+        if recmpr:
+            self.agglH(eps, rankmax)
+        return self
+
     def spctrlnrm(self, it_num=10):
         """Include/matrix.h:50-75: sqrt of the largest eigenvalue of A^T A by it_num
         power steps from x = 1 (FP64 leaves)."""

@@ -121,6 +121,13 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4);
  * Bounding-box trees (ACA start row 0). */
 int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax,
                        const float* rank_hint, int32_t* ranks);
+/* Agglomeration (agglH, H/agglH.cpp:111-272; the recmpr branch of matgenGeH_sqntl,
+ * Include/matgen_sqntl.h:32-55): bottom up, a non-diagonal block whose sons are all
+ * low-rank leaves becomes one low-rank leaf when the recompressed union (relative
+ * threshold eps, rank <= max_rank; unify_sons_, H/agglH.cpp:14-107) stores no more;
+ * leaf indices are then compacted as fill_gaps does.  Unions with dense sons are not
+ * formed.  Once per assembly.  nmerged (may be NULL): blocks merged. */
+int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged);
 /* per leaf: rank after recompression, -1 for dense leaves (mblock::isLrM/rank) */
 int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks);
 /* per leaf: ACA rank before recompression, -1 for dense */

@@ -140,6 +140,12 @@ class blcluster {
     ranks_.resize(ahx_hmat_nleaves(h_));
     check(ahx_hmat_ranks(h_, ranks_.data()));
   }
+  // leaves and ranks again (after an agglomeration changed the leaves)
+  void refresh() {
+    leaves_.resize(7 * (size_t)ahx_hmat_nleaves(h_));
+    check(ahx_hmat_leaves(h_, leaves_.data()));
+    refresh_ranks();
+  }
   int rank_of(unsigned l) const { return ranks_.at(l); }
 
  private:
@@ -233,12 +239,26 @@ void matgenHeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps,
   matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);
 }
 
-// Include/matgen_sqntl.h:88-102 (recmpr = false)
+// H/agglH.cpp:253-272: agglomeration of the assembled leaves (unions of low-rank sons)
+template <class T>
+void agglH(blcluster* bl, mblock<T>**& A, double eps, unsigned max_rank) {
+  const unsigned before = (unsigned)bl->nleaves();
+  check(ahx_agglomerate(bl->handle(), eps, max_rank, nullptr));
+  bl->refresh();
+  for (unsigned i = 0; i < before; ++i) delete A[i];
+  delete[] A;
+  const unsigned n = (unsigned)bl->nleaves();
+  A = new mblock<T>*[n];
+  for (unsigned i = 0; i < n; ++i) A[i] = new mblock<T>(bl, i);
+}
+
+// Include/matgen_sqntl.h:88-102: the assembly; recmpr agglomerates afterwards
 template <class T, class MATGEN_T>
 void matgenGeH_sqntl(MATGEN_T& MatGen, blcluster* root, blcluster* bl, bool recmpr, double eps,
-                     unsigned rankmax, mblock<T>** A) {
-  if (recmpr || root != bl) throw std::invalid_argument("ahx_ahmed: recmpr and sub-blocks not built");
+                     unsigned rankmax, mblock<T>**& A) {
+  if (root != bl) throw std::invalid_argument("ahx_ahmed: sub-blocks not built");
   matgenGeH_omp(MatGen, (unsigned)bl->nleaves(), bl, eps, rankmax, A);
+  if (recmpr) agglH(bl, A, eps, rankmax);
 }
 
 // Include/H.h:89-103: the leaves of bl in the reference's file layout

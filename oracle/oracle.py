@@ -197,6 +197,7 @@ def ref():
         L.ref_entry.argtypes = [vp, u32, u32]
         L.ref_free.argtypes = [vp]
         L.ref_helm_ranks.argtypes = [vp, dbl, dbl, dbl, u32, vp]
+        L.ref_agglomerate.argtypes = [vp, dbl, u32]
         L.ref_save.restype = i32
         L.ref_save.argtypes = [vp, dbl, u32, C.c_char_p]
         _ref = L
@@ -252,6 +253,10 @@ class RefH:
         out = np.zeros(cnt, np.float64)
         ref().ref_leaf_data(self._H, l, _p(out))
         return out
+
+    def agglomerate(self, eps, rankmax=2**32 - 1):
+        """The reference's agglH of the assembled leaves."""
+        ref().ref_agglomerate(self._H, eps, rankmax)
 
     def savembls(self, eta, bmin, path):
         """The reference's own savembls of the assembled leaves."""

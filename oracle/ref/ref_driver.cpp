@@ -356,6 +356,18 @@ void ref_helm_ranks(void* p, double wavenumber, double h, double eps, unsigned r
   }
 }
 
+// The reference's agglomeration agglH (H/agglH.cpp:253-272) of the assembled
+// leaves; the leaf list is rebuilt in DFS order (indices as agglH left them).
+void ref_agglomerate(void* p, double eps, unsigned rankmax) {
+  RefH* H = (RefH*)p;
+  agglH(H->root_bl, H->A, eps, rankmax, (contBasis<double>*)NULL);
+  blcluster** list;
+  H->nblcks = H->root_bl->nleaves();
+  gen_BlSequence(H->root_bl, list);
+  H->leaves.assign(list, list + H->nblcks);
+  delete[] list;
+}
+
 // The reference's savembls (Include/H.h:89-103, mblock::save Include/mblock.h:737-773)
 // of the assembled leaves; returns 0 on success.
 int ref_save(void* p, double eta, unsigned bmin, const char* path) {

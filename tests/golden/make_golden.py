@@ -8,6 +8,7 @@ Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py helmholtz  (complex ACA ranks)
         python tests/golden/make_golden.py mbls       (savembls file hashes)
         python tests/golden/make_golden.py sym        (symmetric trees, HeH assembly/product)
+        python tests/golden/make_golden.py aggl       (agglomeration, agglH)
 """
 import os
 import sys
@@ -180,6 +181,35 @@ def sym():
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+def aggl():
+    """The reference's agglomeration (agglH) after its assembly: leaves in index
+    order, their ranks, the stored doubles and y = A x."""
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    for base in ("fib4096", "cube3000"):
+        gen, bmin = CASES[base]
+        P = gen()
+        h = O.mean_nn(P)
+        n = P.shape[0]
+        x = np.random.default_rng(0).uniform(-1.0, 1.0, n)
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+               "eps": np.float64(EPS), "x": x}
+        for kind, kname in ((O.TREE_BBX, "bbx"), (O.TREE_PCA, "pca")):
+            R = O.RefH(P, kind, bmin, ETA, h)
+            R.assemble(EPS, nthreads=1)
+            R.agglomerate(EPS)
+            L = R.leaves()
+            r = R.ranks()
+            order = np.argsort(L[:, 5])
+            out[f"{kname}_leaves"] = L[order]
+            out[f"{kname}_ranks"] = r[order]
+            out[f"{kname}_stored"] = np.int64(sum(R.leaf_data(l).size for l in range(R.nleaves)))
+            out[f"{kname}_y"] = R.matvec(x, np.zeros(n))
+        path = os.path.join(HERE, f"aggl_{base}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
@@ -187,5 +217,7 @@ if __name__ == "__main__":
         mbls()
     elif len(sys.argv) > 1 and sys.argv[1] == "sym":
         sym()
+    elif len(sys.argv) > 1 and sys.argv[1] == "aggl":
+        aggl()
     else:
         main()
