@@ -532,14 +532,78 @@ __device__ void jacobi_warp16(uint32_t m, uint32_t n, double* R, double* Vs, uin
   __syncwarp();
 }
 
+// One-sided Jacobi (Hestenes) on the columns of R (mmin x nmin, column-major with
+// stride ld), rotations accumulated in Vs: the column pairs of a round-robin
+// tournament (circle method) rotate in parallel, one warp per pair, so that a
+// whole CTA works on one wide SVD.  Same rotation formulas and stopping rule as
+// the serial sweeps; the pair order differs.
+__device__ void jacobi_cta(uint32_t mmin, uint32_t nmin, double* R, double* Vs, uint32_t ld) {
+  __shared__ int rotated;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const uint32_t np = (nmin + 1) & ~1u;  // players: a dummy one when nmin is odd
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    __syncthreads();
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (uint32_t r = 0; r + 1 < np; ++r) {
+      for (uint32_t k = warp; k < np / 2; k += nw) {
+        const uint32_t pa = k, pb = np - 1 - k;
+        const uint32_t a = pa == 0 ? 0 : (pa - 1 + r) % (np - 1) + 1;
+        const uint32_t b = pb == 0 ? 0 : (pb - 1 + r) % (np - 1) + 1;
+        const uint32_t p = min(a, b), q = max(a, b);
+        if (q >= nmin) continue;  // the dummy's pair
+        double* cp = R + (size_t)p * ld;
+        double* cq = R + (size_t)q * ld;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (uint32_t i = lane; i < mmin; i += 32) {
+          const double x = cp[i], y = cq[i];
+          al += x * x;
+          be += y * y;
+          ga += x * y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, o);
+          be += __shfl_xor_sync(0xffffffffu, be, o);
+          ga += __shfl_xor_sync(0xffffffffu, ga, o);
+        }
+        if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+        if (lane == 0) rotated = 1;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double s = c * t;
+        for (uint32_t i = lane; i < mmin; i += 32) {
+          const double x = cp[i], y = cq[i];
+          cp[i] = c * x - s * y;
+          cq[i] = s * x + c * y;
+        }
+        double* vp = Vs + (size_t)p * ld;
+        double* vq = Vs + (size_t)q * ld;
+        for (uint32_t i = lane; i < nmin; i += 32) {
+          const double x = vp[i], y = vq[i];
+          vp[i] = c * x - s * y;
+          vq[i] = s * x + c * y;
+        }
+      }
+      __syncthreads();
+    }
+    if (!rotated) break;
+  }
+  __syncthreads();
+}
+
 // addtrll (H/mblock_D.cpp:356-465) for a fresh low-rank block: recompress U V^T
 // of rank k to kt <= k columns (relative threshold delta, absolute 1e-64).
 // Results in Un (n1 x kt) and Vn (n2 x kt).
 template <int G, class Grp>
 __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t k, double* U,
                                double* V, double* Un, double* Vn, double delta, double* R,
-                               double* Vs, uint32_t ld, double* sig, double* tau, int* perm) {
+                               double* Vs, uint32_t ld, double* sig, double* tau, int* perm, bool cm = false) {
   if (k == 0) return 0;
+  // R and Vs: row-major with a padded stride in shared memory, column-major (the
+  // Jacobi sweeps read columns) in the global workspace
+  auto ix = [&](uint32_t i, uint32_t j) -> size_t { return cm ? (size_t)j * ld + i : (size_t)i * ld + j; };
   const uint32_t mmin = min(n1, k), nmin = min(n2, k), amin = min(mmin, nmin);
   double* tau1 = tau;
   double* tau2 = tau + k;
@@ -552,7 +616,7 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
     for (uint32_t j = 0; j < nmin; ++j) {
       double d = 0.0;
       for (uint32_t l = max(i, j); l < k; ++l) d += U[i + (size_t)l * n1] * V[j + (size_t)l * n2];
-      R[i * ld + j] = d;
+      R[ix(i, j)] = d;
       fro += d * d;
     }
   }
@@ -560,13 +624,16 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   const double thresh = delta * sqrt(fro) / (double)sqrtf((float)mmin * (float)nmin);
   for (uint32_t i = g.rank; i < mmin; i += G)
     for (uint32_t j = 0; j < nmin; ++j)
-      if (fabs(R[i * ld + j]) < thresh) R[i * ld + j] = 0.0;
+      if (fabs(R[ix(i, j)]) < thresh) R[ix(i, j)] = 0.0;
   for (uint32_t i = g.rank; i < nmin; i += G)
-    for (uint32_t j = 0; j < nmin; ++j) Vs[i * ld + j] = (i == j) ? 1.0 : 0.0;
+    for (uint32_t j = 0; j < nmin; ++j) Vs[ix(i, j)] = (i == j) ? 1.0 : 0.0;
   // one-sided Jacobi on the columns of R (Hestenes), rotations accumulated in Vs
-  if (G == 32 && mmin <= 16 && nmin <= 16) {
+  if (G == 32 && !cm && mmin <= 16 && nmin <= 16) {
     g.sync();
     jacobi_warp16(mmin, nmin, R, Vs, ld);
+  } else if (G > 32 && cm) {
+    g.sync();
+    jacobi_cta(mmin, nmin, R, Vs, ld);
   } else
   for (int sweep = 0; sweep < 40; ++sweep) {
     bool rotated = false;
@@ -574,7 +641,7 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
       for (uint32_t q = p + 1; q < nmin; ++q) {
         double al = 0.0, be = 0.0, ga = 0.0;
         for (uint32_t i = g.rank; i < mmin; i += G) {
-          const double x = R[i * ld + p], y = R[i * ld + q];
+          const double x = R[ix(i, p)], y = R[ix(i, q)];
           al += x * x;
           be += y * y;
           ga += x * y;
@@ -587,14 +654,14 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
         const double c = 1.0 / sqrt(1.0 + t * t);
         const double s = c * t;
         for (uint32_t i = g.rank; i < mmin; i += G) {
-          const double x = R[i * ld + p], y = R[i * ld + q];
-          R[i * ld + p] = c * x - s * y;
-          R[i * ld + q] = s * x + c * y;
+          const double x = R[ix(i, p)], y = R[ix(i, q)];
+          R[ix(i, p)] = c * x - s * y;
+          R[ix(i, q)] = s * x + c * y;
         }
         for (uint32_t i = g.rank; i < nmin; i += G) {
-          const double x = Vs[i * ld + p], y = Vs[i * ld + q];
-          Vs[i * ld + p] = c * x - s * y;
-          Vs[i * ld + q] = s * x + c * y;
+          const double x = Vs[ix(i, p)], y = Vs[ix(i, q)];
+          Vs[ix(i, p)] = c * x - s * y;
+          Vs[ix(i, q)] = s * x + c * y;
         }
       }
     }
@@ -603,7 +670,7 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   g.sync();
   for (uint32_t j = 0; j < nmin; ++j) {
     double s = 0.0;
-    for (uint32_t i = g.rank; i < mmin; i += G) s += R[i * ld + j] * R[i * ld + j];
+    for (uint32_t i = g.rank; i < mmin; i += G) s += R[ix(i, j)] * R[ix(i, j)];
     s = g.sum(s);
     if (g.rank == 0) sig[j] = sqrt(s);
   }
@@ -628,8 +695,8 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   // Un = Q1 [R(:, perm[:kt]); 0],  Vn = Q2 [Vs(:, perm[:kt]); 0]
   for (uint32_t j = 0; j < kt; ++j) {
     const int pj = perm[j];
-    for (uint32_t i = g.rank; i < n1; i += G) Un[i + (size_t)j * n1] = i < mmin ? R[i * ld + pj] : 0.0;
-    for (uint32_t i = g.rank; i < n2; i += G) Vn[i + (size_t)j * n2] = i < nmin ? Vs[i * ld + pj] : 0.0;
+    for (uint32_t i = g.rank; i < n1; i += G) Un[i + (size_t)j * n1] = i < mmin ? R[ix(i, pj)] : 0.0;
+    for (uint32_t i = g.rank; i < n2; i += G) Vn[i + (size_t)j * n2] = i < nmin ? Vs[ix(i, pj)] : 0.0;
   }
   group_apply_q<G>(g, n1, mmin, U, tau1, kt, Un);
   group_apply_q<G>(g, n2, nmin, V, tau2, kt, Vn);
@@ -674,7 +741,7 @@ __device__ void aca_task(const Grp& g, const AcaParams& p, uint32_t ti, double* 
     int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : B.Z;
     g.sync();
     kt = recompress<G>(g, t.n1, t.n2, k, B.U, B.V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau,
-                       perm);
+                       perm, !sm);
   }
   if (g.rank == 0) p.res[ti] = AcaResult{st, k, kt, 0u};
 }
@@ -704,18 +771,18 @@ __device__ void merge_task(const Grp& g, const MergeParams& p, uint32_t ti, doub
     double* tau = sm ? smem + 2 * KSM * LDS + KSM : taug;
     int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : p.zs + t.zs;
     g.sync();
-    kt = recompress<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau, perm);
+    kt = recompress<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau, perm, !sm);
   }
   if (g.rank == 0) p.res[ti] = AcaResult{kAcaOk, kc, kt, 0u};
 }
 
-__global__ void __launch_bounds__(32 * kSmallWarps) merge_small_kernel(MergeParams p) {
+// one warp per CTA: consecutive (similarly costly) unions go to different SMs
+__global__ void __launch_bounds__(32) merge_small_kernel(MergeParams p) {
   extern __shared__ double smem_all[];
-  const uint32_t w = threadIdx.x >> 5;
-  const uint32_t task = blockIdx.x * kSmallWarps + w;
+  const uint32_t task = blockIdx.x;
   if (task >= p.ntasks) return;
   Group<32> g(threadIdx.x & 31);
-  merge_task<32>(g, p, task, smem_all + (size_t)w * kSmemPerGroup);
+  merge_task<32>(g, p, task, smem_all);
 }
 
 __global__ void copy2d_kernel(const Seg2D* __restrict__ segs, const double* __restrict__ src,
@@ -831,10 +898,10 @@ cudaError_t launch_dense_fill(const PointsSoA& pts, double diag, const DenseTask
 cudaError_t launch_merge(const MergeParams& p, bool large, cudaStream_t s) {
   if (p.ntasks == 0) return cudaSuccess;
   if (!large) {
-    const size_t smem = sizeof(double) * kSmemPerGroup * kSmallWarps;
+    const size_t smem = sizeof(double) * kSmemPerGroup;
     cudaError_t e = cudaFuncSetAttribute(merge_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    merge_small_kernel<<<(p.ntasks + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, smem, s>>>(p);
+    merge_small_kernel<<<p.ntasks, 32, smem, s>>>(p);
   } else {
     const size_t smem = sizeof(double) * (kSmemPerGroup + 3 * (kLargeThreads / 32) + 8);
     cudaError_t e = cudaFuncSetAttribute(merge_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -16,8 +16,12 @@
 // [U_cat][V_cat]^T; the reference forms the dense block and takes its SVD
 // (mblock::unify_cols, H/mblock_D.cpp:804-860) with the same truncation rule.
 // The reference unifies the sons pairwise (columns, then rows) and truncates
-// after each step; this one-shot union truncates once.
+// after each step; this one-shot union truncates once.  Unions wider than
+// kMaxUnion columns are not formed.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "ahx_aca.cuh"
@@ -25,6 +29,8 @@
 
 namespace ahx {
 namespace {
+
+constexpr uint32_t kMaxUnion = 1024;
 
 struct BNode {
   uint32_t b1, n1, b2, n2;
@@ -140,23 +146,58 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
   uint32_t merged = 0;
   DevBuf ws, zs, dtasks, dres, dsegs, dcopy;
   const size_t budget = aca_ws_budget();
+  const char* tr = std::getenv("AHX_TRACE");
+  const bool trace = tr && *tr && *tr != '0';
+  int round = 0;
   for (;;) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint32_t merged0 = merged;
     // candidates of this height: undecided, not diagonal, all sons leaves
     std::vector<int32_t> cand;
     for (int32_t i = 0; i < (int32_t)N.size(); ++i) {
       BNode& q = N[i];
       if (q.leaf >= 0 || q.decided || q.dbl) continue;
       bool all_leaves = true;
-      for (int s = 0; s < 4; ++s)
-        if (q.son[s] < 0 || N[q.son[s]].leaf < 0) all_leaves = false;
-      if (all_leaves) cand.push_back(i);
+      uint32_t w = 0;
+      for (int s = 0; s < 4; ++s) {
+        if (q.son[s] < 0 || N[q.son[s]].leaf < 0) {
+          all_leaves = false;
+          break;
+        }
+        const BNode& c = N[q.son[s]];
+        w += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
+      }
+      if (!all_leaves) continue;
+      if (w > kMaxUnion) {
+        q.decided = true;
+        continue;
+      }
+      cand.push_back(i);
     }
     if (cand.empty()) break;
-    // batches under the workspace budget, small (warp) and large (CTA) blocks apart
+    uint64_t kmax_round = 0;
+    // union widths (columns of the factored union)
+    auto width = [&](int32_t c) -> uint32_t {
+      uint32_t k = 0;
+      for (int s = 0; s < 4; ++s) {
+        const BNode& x = N[N[c].son[s]];
+        k += rank[x.leaf] < 0 ? x.n2 : (uint32_t)rank[x.leaf];
+      }
+      return k;
+    };
+    // batches under the workspace budget: one warp per union, one CTA for unions
+    // wider than 64 columns (the SVD's column pairs in parallel) or blocks over 4096
+    // rows; the costliest first so that they spread over the SMs
+    std::vector<uint64_t> cost(N.size(), 0);
+    for (int32_t c : cand) {
+      const uint64_t w = width(c);
+      cost[c] = w * w * (N[c].n1 + N[c].n2);
+    }
+    std::vector<int32_t> parts[2];
+    for (int32_t c : cand) parts[(width(c) > 64u || std::max(N[c].n1, N[c].n2) > 4096u) ? 1 : 0].push_back(c);
     for (int large = 0; large < 2; ++large) {
-      std::vector<int32_t> todo;
-      for (int32_t c : cand)
-        if ((std::max(N[c].n1, N[c].n2) > 4096u) == (large == 1)) todo.push_back(c);
+      std::vector<int32_t>& todo = parts[large];
+      std::stable_sort(todo.begin(), todo.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
       size_t at = 0;
       while (at < todo.size()) {
         std::vector<MergeTask> tasks;
@@ -170,6 +211,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
             const BNode& c = N[q.son[s]];
             k += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
           }
+          kmax_round = std::max<uint64_t>(kmax_round, k);
           const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u));
           if (!tasks.empty() && (wsz + need) * sizeof(double) > budget) break;
           MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
@@ -246,8 +288,15 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
         }
       }
     }
+    if (trace) {
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      std::fprintf(stderr, "ahx agglomerate round %d: %zu unions tried, %u merged, widest union %llu, %.1f ms\n",
+                   round, cand.size(), merged - merged0, (unsigned long long)kmax_round, ms);
+    }
+    ++round;
   }
   for (DevBuf* b : {&ws, &zs, &dtasks, &dres, &dsegs, &dcopy}) b->release();
+  (void)round;
   if (nmerged) *nmerged = merged;
   if (!merged) return AHX_OK;
   // fill_gaps_ (H/agglH.cpp:185-211): in DFS order, leaves whose index is past the new
