@@ -23,6 +23,9 @@ constexpr int kThreads = 128;
 constexpr int kCh = 128;  // X rows per staged chunk
 constexpr int kKt = 32;   // low-rank columns per pass
 constexpr int kNorm = 32; // terms between renormalisations of an accumulator
+// loads in flight per thread in the streaming loops: deeper for narrow passes
+template <int PG>
+constexpr int kPF = PG <= 2 ? 4 : 1;
 
 
 struct dfloat {
@@ -131,13 +134,20 @@ __global__ void __launch_bounds__(kThreads, 8) mv_df_kernel(DfArgs a) {
             const float2* col = D + i + (uint64_t)jb * L.n1;
             for (uint32_t j0 = 0; j0 < jn; j0 += kNorm) {
               const uint32_t je = min(j0 + kNorm, jn);
-              dfloat av = ld(col + (uint64_t)j0 * L.n1);
+              // the next PF columns' elements in flight (PF = 4 for narrow passes:
+              // few operations per element, so more loads must overlap)
+              dfloat buf[kPF<PG>];
+#pragma unroll
+              for (int u = 0; u < kPF<PG>; ++u)
+                buf[u] = j0 + u < je ? ld(col + (uint64_t)(j0 + u) * L.n1) : dfloat{0.f, 0.f};
               for (uint32_t j = j0; j < je; ++j) {
-                const uint32_t jp = j + 1 < je ? j + 1 : j;
-                const dfloat nx = ld(col + (uint64_t)jp * L.n1);
+                const dfloat av = buf[0];
+#pragma unroll
+                for (int u = 0; u + 1 < kPF<PG>; ++u) buf[u] = buf[u + 1];
+                const uint32_t jf = j + kPF<PG>;
+                buf[kPF<PG> - 1] = jf < je ? ld(col + (uint64_t)jf * L.n1) : dfloat{0.f, 0.f};
 #pragma unroll
                 for (int r = 0; r < PG; ++r) df_madd(acc[r], av, Xs[j][r]);
-                av = nx;
               }
 #pragma unroll
               for (int r = 0; r < PG; ++r) df_norm(acc[r]);
@@ -169,8 +179,16 @@ __global__ void __launch_bounds__(kThreads, 8) mv_df_kernel(DfArgs a) {
           if (l < kn) {
             for (uint32_t j0 = js; j0 < jn; j0 += kNorm * S) {
               const uint32_t je = min(j0 + kNorm * S, jn);
+              dfloat buf[kPF<PG>];
+#pragma unroll
+              for (int u = 0; u < kPF<PG>; ++u)
+                buf[u] = j0 + u * S < je ? ld(vc + jb + j0 + u * S) : dfloat{0.f, 0.f};
               for (uint32_t j = j0; j < je; j += S) {
-                const dfloat vv = ld(vc + jb + j);
+                const dfloat vv = buf[0];
+#pragma unroll
+                for (int u = 0; u + 1 < kPF<PG>; ++u) buf[u] = buf[u + 1];
+                const uint32_t jf = j + kPF<PG> * S;
+                buf[kPF<PG> - 1] = jf < je ? ld(vc + jb + jf) : dfloat{0.f, 0.f};
 #pragma unroll
                 for (int r = 0; r < PG; ++r) df_madd(acc[r], vv, Xs[j][r]);
               }
