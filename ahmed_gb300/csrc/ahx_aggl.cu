@@ -144,7 +144,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
     return r < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)r * (q.n1 + q.n2);
   };
   uint32_t merged = 0;
-  DevBuf ws, zs, dtasks, dres, dsegs, dcopy;
+  ScopedBuf ws, zs, dtasks, dres, dsegs, dcopy;
   const size_t budget = aca_ws_budget();
   const char* tr = std::getenv("AHX_TRACE");
   const bool trace = tr && *tr && *tr != '0';
@@ -295,7 +295,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
     }
     ++round;
   }
-  for (DevBuf* b : {&ws, &zs, &dtasks, &dres, &dsegs, &dcopy}) b->release();
+  for (ScopedBuf* b : {&ws, &zs, &dtasks, &dres, &dsegs, &dcopy}) b->release();
   (void)round;
   if (nmerged) *nmerged = merged;
   if (!merged) return AHX_OK;
@@ -367,13 +367,22 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
     }
     total += cnt;
   }
-  DevBuf fresh, dm;
+  DevBuf fresh;
+  ScopedBuf dm;
   if ((rc = fresh.reserve(std::max<uint64_t>(total, 1) * sizeof(double)))) return rc;
-  if ((rc = upload(dm, moves, H->stream))) return rc;
-  AHX_CUDA(launch_copy_factors(dm.as<CopyTask>(), (uint32_t)moves.size(), H->arena64.as<double>(),
-                               fresh.as<double>(), H->stream));
-  AHX_CUDA(cudaStreamSynchronize(H->stream));
-  dm.release();
+  if ((rc = upload(dm, moves, H->stream))) {
+    fresh.release();
+    return rc;
+  }
+  {
+    cudaError_t e = launch_copy_factors(dm.as<CopyTask>(), (uint32_t)moves.size(), H->arena64.as<double>(),
+                                        fresh.as<double>(), H->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+    if (e != cudaSuccess) {
+      fresh.release();
+      return cuda_fail(e, "agglomerate: arena compaction");
+    }
+  }
   H->arena64.release();
   H->arena64 = fresh;
   H->arena64_elems = total;

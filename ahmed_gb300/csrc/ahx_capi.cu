@@ -247,7 +247,7 @@ int full_leaves(ahx_hmat* H, std::vector<PlanLeaf>& pls, DevBuf& tmp, const doub
   if (H->arena64_elems)
     AHX_CUDA(cudaMemcpyAsync(tmp.p, H->arena64.p, H->arena64_elems * sizeof(double), cudaMemcpyDeviceToDevice,
                              H->stream));
-  DevBuf dmt;
+  ScopedBuf dmt;
   if ((rc = upload(dmt, mt, H->stream))) return rc;
   AHX_CUDA(launch_mirror(dmt.as<MirrorTask>(), (uint32_t)mt.size(), tmp.as<double>(), H->stream));
   AHX_CUDA(cudaStreamSynchronize(H->stream));
@@ -299,7 +299,7 @@ int prepare_product(ahx_hmat* H, int prec) {
     // images are materialised, with their own leaf table
     if ((rc = prepare_product(H, kFP64))) return rc;
     std::vector<PlanLeaf> pls;
-    DevBuf tmp;
+    ScopedBuf tmp;
     const double* src = nullptr;
     if ((rc = full_leaves(H, pls, tmp, src))) return rc;
     uint64_t elems = H->arena64_elems;
@@ -316,7 +316,7 @@ int prepare_product(ahx_hmat* H, int prec) {
   }
   if (prec != kFP64) {
     std::vector<PlanLeaf> pls;
-    DevBuf tmp;
+    ScopedBuf tmp;
     const double* src = nullptr;
     if ((rc = full_leaves(H, pls, tmp, src))) return rc;
     rc = build_mixed_streams(pc, prec, pls, src, H->tree.n, H->device, H->stream);
@@ -755,7 +755,7 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4) {
   if (rc) return rc;
   const int prec = precision == AHX_FP32 ? kFP32 : kBF16FP32;
   std::vector<PlanLeaf> pls;
-  DevBuf full;
+  ScopedBuf full;
   const double* src = nullptr;
   if ((rc = full_leaves(H, pls, full, src))) return rc;
   const uint64_t n = H->tree.n;

@@ -33,6 +33,14 @@ struct DevBuf {
   T* as() const { return static_cast<T*>(p); }
 };
 
+// A temporary device buffer released when the scope ends (error paths included).
+struct ScopedBuf : DevBuf {
+  ScopedBuf() = default;
+  ScopedBuf(const ScopedBuf&) = delete;
+  ScopedBuf& operator=(const ScopedBuf&) = delete;
+  ~ScopedBuf() { release(); }
+};
+
 // The product's view of one storage precision.
 struct ProdCopy {
   bool valid = false;

@@ -1100,7 +1100,7 @@ int ahx_spctrlnrm(ahx_hmat* H, uint32_t it_num, double* out) {
   Solver sv(op, 1);
   if ((rc = sv.init(2))) return rc;
   const uint64_t n = H->tree.n;
-  DevBuf xb, yb;
+  ScopedBuf xb, yb;
   if ((rc = xb.reserve(n * 8)) || (rc = yb.reserve(n * 8))) return rc;
   double* x = xb.as<double>();
   double* y = yb.as<double>();
