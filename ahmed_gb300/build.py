@@ -19,7 +19,7 @@ CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp"]
 
 CU_SOURCES = ["ahx_aca.cu", "ahx_matvec.cu", "ahx_matvec_tc.cu", "ahx_matvec_df.cu", "ahx_capi.cu", "ahx_solve.cu",
               "ahx_mlp.cu", "ahx_aca_helm.cu", "ahx_io.cu",
-              "ahx_aggl.cu"]
+              "ahx_aggl.cu", "ahx_matvec_z.cu", "ahx_solve_z.cu"]
 CXX_SOURCES = ["ahx_tree.cpp"]
 
 

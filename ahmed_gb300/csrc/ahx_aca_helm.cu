@@ -1,11 +1,14 @@
-// Complex ACA ranks of the Helmholtz single-layer matrix exp(i k r) / (4 pi r)
-// (diagonal exp(i k h) / (4 pi h)): the reference's ACA with T = dcomp
-// (Include/ACA.h:46-350; complex arithmetic of Include/cmplx.h:80-245: own
-// complex type, |z| = sqrt(re^2 + im^2), a / z = a / |z|^2 * conj(z), scpr =
-// sum conj(x) y), one warp per admissible leaf, every leaf with the
-// reference's stopping rule and counters.  The factors are not kept: the
-// entry point reports the rank per leaf (training data and verification of
-// the rank predictor on oscillatory kernels).
+// Helmholtz single-layer matrix exp(i k r) / (4 pi r) (diagonal exp(i k h) /
+// (4 pi h)) on the GPU: the reference's ACA with T = dcomp (Include/ACA.h:46-350;
+// complex arithmetic of Include/cmplx.h:80-245: |z| = sqrt(re^2 + im^2), a / z
+// = a / |z|^2 * conj(z), scpr = sum conj(x) y), one warp per admissible leaf,
+// every leaf with the reference's stopping rule and counters.
+//   ahx_helm_aca_ranks: the ACA rank per leaf only (training data and
+//     verification of the rank predictor on oscillatory kernels);
+//   ahx_helm_assemble: the complex H-matrix (apprx_unsym, Include/apprx.h:136-172,
+//     with T = dcomp): ACA, recompression as mblock<dcomp>::addtrll
+//     (H/mblock_Z.cpp:200-300), dense leaves where ACA fails or the block is
+//     inadmissible; leaves in the mblock<dcomp> layout in a complex arena.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -320,6 +323,298 @@ __device__ int aca(const G32& g, const HBlk& B, uint32_t i0, uint32_t kmax, uint
   return outcome;
 }
 
+// ---------------------------------------------------------------------------
+// Recompression of a complex low-rank block U V^H (mblock<dcomp>::addtrll,
+// H/mblock_Z.cpp:200-300: QR of U and V, SVD of R1 R2^H after dropping entries
+// below delta |R|_F / sqrt(mmin nmin), truncation at delta sigma_0, Q applied),
+// by one warp.  The row i of every column belongs to lane i % 32.
+
+__device__ __forceinline__ Cx cmul(Cx a, Cx b) { return Cx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+// conj(a) b
+__device__ __forceinline__ Cx cmulc(Cx a, Cx b) { return Cx{a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re}; }
+__device__ __forceinline__ Cx cinv(Cx a) {
+  const double s = 1.0 / (a.re * a.re + a.im * a.im);
+  return Cx{a.re * s, -a.im * s};
+}
+
+// Householder QR of A (m x k, column-major) in LAPACK's zgeqrf form:
+// H_c = I - tau_c v_c v_c^H with v_c(c) = 1, a real diagonal beta in R.
+__device__ void zqr(const G32& g, uint32_t m, uint32_t k, Cx* A, Cx* tau) {
+  const uint32_t kk = min(m, k);
+  for (uint32_t c = 0; c < kk; ++c) {
+    Cx* a = A + (size_t)c * m;
+    double xn2 = 0.0, ar = 0.0, ai = 0.0;
+    for (uint32_t i = g.rank; i < m; i += 32) {
+      const Cx v = a[i];
+      if (i > c) xn2 += v.re * v.re + v.im * v.im;
+      else if (i == c) {
+        ar = v.re;
+        ai = v.im;
+      }
+    }
+    G32::sum3(xn2, ar, ai);
+    if (xn2 == 0.0 && ai == 0.0) {
+      if (g.rank == 0) tau[c] = Cx{0.0, 0.0};
+      continue;
+    }
+    const double nrm = sqrt(ar * ar + ai * ai + xn2);
+    const double beta = ar >= 0.0 ? -nrm : nrm;
+    const Cx t{(beta - ar) / beta, -ai / beta};
+    const Cx sc = cinv(Cx{ar - beta, ai});
+    if (g.rank == 0) tau[c] = t;
+    for (uint32_t i = g.rank; i < m; i += 32) {
+      if (i > c) a[i] = cmul(a[i], sc);
+      else if (i == c) a[i] = Cx{beta, 0.0};
+    }
+    // the remaining columns: b -= conj(tau) v (v^H b)
+    const Cx tc = cconj(t);
+    for (uint32_t q = c + 1; q < k; ++q) {
+      Cx* b = A + (size_t)q * m;
+      double sr = 0.0, si = 0.0;
+      for (uint32_t i = g.rank; i < m; i += 32) {
+        if (i > c) {
+          const Cx z = cmulc(a[i], b[i]);
+          sr += z.re;
+          si += z.im;
+        } else if (i == c) {
+          sr += b[i].re;
+          si += b[i].im;
+        }
+      }
+      G32::sum2(sr, si);
+      const Cx f = cmul(tc, Cx{sr, si});
+      for (uint32_t i = g.rank; i < m; i += 32) {
+        if (i > c) {
+          const Cx z = cmul(f, a[i]);
+          b[i].re -= z.re;
+          b[i].im -= z.im;
+        } else if (i == c) {
+          b[i].re -= f.re;
+          b[i].im -= f.im;
+        }
+      }
+    }
+  }
+}
+
+// C (m x nc, ld m) := Q C with Q = H_0 ... H_{kr-1} from zqr (tau read after a
+// warp barrier).
+__device__ void zapply_q(const G32& g, uint32_t m, uint32_t kr, const Cx* A, const Cx* tau, uint32_t nc, Cx* C) {
+  for (int c = (int)kr - 1; c >= 0; --c) {
+    const Cx t = tau[c];
+    if (t.re == 0.0 && t.im == 0.0) continue;
+    const Cx* a = A + (size_t)c * m;
+    for (uint32_t q = 0; q < nc; ++q) {
+      Cx* b = C + (size_t)q * m;
+      double sr = 0.0, si = 0.0;
+      for (uint32_t i = g.rank; i < m; i += 32) {
+        if (i > (uint32_t)c) {
+          const Cx z = cmulc(a[i], b[i]);
+          sr += z.re;
+          si += z.im;
+        } else if (i == (uint32_t)c) {
+          sr += b[i].re;
+          si += b[i].im;
+        }
+      }
+      G32::sum2(sr, si);
+      const Cx f = cmul(t, Cx{sr, si});
+      for (uint32_t i = g.rank; i < m; i += 32) {
+        if (i > (uint32_t)c) {
+          const Cx z = cmul(f, a[i]);
+          b[i].re -= z.re;
+          b[i].im -= z.im;
+        } else if (i == (uint32_t)c) {
+          b[i].re -= f.re;
+          b[i].im -= f.im;
+        }
+      }
+    }
+  }
+}
+
+// Un (n1 x kt), Vn (n2 x kt) with Un Vn^H = the truncated U V^H (rank k); R, Vs:
+// column-major with stride ld >= k; sig: k doubles; tau: 2k; perm: nmin + 1 ints.
+__device__ uint32_t zrecompress(const G32& g, uint32_t n1, uint32_t n2, uint32_t k, Cx* U, Cx* V, Cx* Un, Cx* Vn,
+                                double delta, Cx* R, Cx* Vs, uint32_t ld, double* sig, Cx* tau, int* perm) {
+  const uint32_t mmin = min(n1, k), nmin = min(n2, k), amin = min(mmin, nmin);
+  Cx* tau1 = tau;
+  Cx* tau2 = tau + k;
+  zqr(g, n1, k, U, tau1);
+  zqr(g, n2, k, V, tau2);
+  __syncwarp();
+  // R = R1 R2^H (Include/blas.h utrmmh)
+  double fro = 0.0;
+  for (uint32_t i = g.rank; i < mmin; i += 32) {
+    for (uint32_t j = 0; j < nmin; ++j) {
+      double dr = 0.0, di = 0.0;
+      for (uint32_t l = max(i, j); l < k; ++l) {
+        const Cx u = U[i + (size_t)l * n1], v = V[j + (size_t)l * n2];
+        dr += u.re * v.re + u.im * v.im;
+        di += u.im * v.re - u.re * v.im;
+      }
+      R[i + (size_t)j * ld] = Cx{dr, di};
+      fro += dr * dr + di * di;
+    }
+  }
+  fro = G32::sum(fro);
+  const double thresh = delta * sqrt(fro) / (double)sqrtf((float)mmin * (float)nmin);
+  for (uint32_t i = g.rank; i < mmin; i += 32)
+    for (uint32_t j = 0; j < nmin; ++j)
+      if (cabs(R[i + (size_t)j * ld]) < thresh) R[i + (size_t)j * ld] = Cx{0.0, 0.0};
+  for (uint32_t i = g.rank; i < nmin; i += 32)
+    for (uint32_t j = 0; j < nmin; ++j) Vs[i + (size_t)j * ld] = Cx{i == j ? 1.0 : 0.0, 0.0};
+  // one-sided Jacobi (Hestenes) on the columns of R with complex rotations
+  // [x y] <- [c x - s e y, s x + c e y], e = conj(gamma) / |gamma|, gamma = x^H y
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    bool rotated = false;
+    for (uint32_t p = 0; p + 1 < nmin; ++p) {
+      for (uint32_t q = p + 1; q < nmin; ++q) {
+        double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+        for (uint32_t i = g.rank; i < mmin; i += 32) {
+          const Cx x = R[i + (size_t)p * ld], y = R[i + (size_t)q * ld];
+          al += x.re * x.re + x.im * x.im;
+          be += y.re * y.re + y.im * y.im;
+          const Cx z = cmulc(x, y);
+          gr += z.re;
+          gi += z.im;
+        }
+        G32::sum2(al, be);
+        G32::sum2(gr, gi);
+        const double ga = sqrt(gr * gr + gi * gi);
+        if (ga == 0.0 || ga <= 1e-15 * sqrt(al * be)) continue;
+        rotated = true;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double s = c * t;
+        const Cx e{gr / ga, -gi / ga};
+        for (uint32_t i = g.rank; i < mmin; i += 32) {
+          const Cx x = R[i + (size_t)p * ld], ey = cmul(e, R[i + (size_t)q * ld]);
+          R[i + (size_t)p * ld] = Cx{c * x.re - s * ey.re, c * x.im - s * ey.im};
+          R[i + (size_t)q * ld] = Cx{s * x.re + c * ey.re, s * x.im + c * ey.im};
+        }
+        for (uint32_t i = g.rank; i < nmin; i += 32) {
+          const Cx x = Vs[i + (size_t)p * ld], ey = cmul(e, Vs[i + (size_t)q * ld]);
+          Vs[i + (size_t)p * ld] = Cx{c * x.re - s * ey.re, c * x.im - s * ey.im};
+          Vs[i + (size_t)q * ld] = Cx{s * x.re + c * ey.re, s * x.im + c * ey.im};
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  for (uint32_t j = 0; j < nmin; ++j) {
+    double sj = 0.0;
+    for (uint32_t i = g.rank; i < mmin; i += 32) sj += cabs2(R[i + (size_t)j * ld]);
+    sj = G32::sum(sj);
+    if (g.rank == 0) sig[j] = sqrt(sj);
+  }
+  __syncwarp();
+  if (g.rank == 0) {
+    for (uint32_t j = 0; j < nmin; ++j) perm[j] = (int)j;
+    for (uint32_t j = 0; j < nmin; ++j) {
+      uint32_t b = j;
+      for (uint32_t q = j + 1; q < nmin; ++q)
+        if (sig[perm[q]] > sig[perm[b]]) b = q;
+      const int t = perm[j];
+      perm[j] = perm[b];
+      perm[b] = t;
+    }
+    uint32_t kt = min(amin, k);
+    const double s0 = nmin ? sig[perm[0]] : 0.0;
+    while (kt > 0 && (sig[perm[kt - 1]] <= delta * s0 || sig[perm[kt - 1]] < 1e-64)) --kt;
+    perm[nmin] = (int)kt;
+  }
+  __syncwarp();
+  const uint32_t kt = (uint32_t)perm[nmin];
+  // Un = Q1 [R(:, perm[:kt]); 0] (R's columns are sigma_j u_j), Vn = Q2 [Vs(:, perm[:kt]); 0]
+  for (uint32_t j = 0; j < kt; ++j) {
+    const int pj = perm[j];
+    for (uint32_t i = g.rank; i < n1; i += 32) Un[i + (size_t)j * n1] = i < mmin ? R[i + (size_t)pj * ld] : Cx{0.0, 0.0};
+    for (uint32_t i = g.rank; i < n2; i += 32) Vn[i + (size_t)j * n2] = i < nmin ? Vs[i + (size_t)pj * ld] : Cx{0.0, 0.0};
+  }
+  zapply_q(g, n1, mmin, U, tau1, kt, Un);
+  zapply_q(g, n2, nmin, V, tau2, kt, Vn);
+  __syncwarp();
+  return kt;
+}
+
+// One leaf of the Helmholtz assembly.  Workspace (complex, at ws):
+//   U[n1 kcap] V[n2 kcap] Un[n1 kcap] Vn[n2 kcap] R[kcap^2] Vs[kcap^2] sig[kcap] tau[2 kcap]
+// ints at zs: Z[n1] S[n2] (later the SVD permutation).
+struct ZTask {
+  uint32_t b1, n1, b2, n2, i0, kmax, kcap, leaf;
+  uint64_t ws, zs;
+};
+
+__global__ void __launch_bounds__(32 * kWarps)
+    helm_assemble_kernel(PointsSoA P, double k, double h, double eps, const ZTask* __restrict__ tasks, uint32_t n,
+                         Cx* __restrict__ ws, int* __restrict__ zs, AcaResult* __restrict__ res) {
+  const uint32_t t = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  if (t >= n) return;
+  const ZTask T = tasks[t];
+  G32 g(threadIdx.x & 31);
+  HBlk B;
+  B.P = P;
+  B.k = k;
+  B.h = h;
+  B.b1 = T.b1;
+  B.n1 = T.n1;
+  B.b2 = T.b2;
+  B.n2 = T.n2;
+  const uint32_t kc = T.kcap;
+  B.U = ws + T.ws;
+  B.V = B.U + (size_t)T.n1 * kc;
+  B.Z = zs + T.zs;
+  B.S = B.Z + T.n1;
+  uint32_t kk = 0, kt = 0;
+  const int st = aca(g, B, T.i0, T.kmax, kc, eps, kk);
+  if (st == kAcaOk && kk > 0) {
+    Cx* Un = B.V + (size_t)T.n2 * kc;
+    Cx* Vn = Un + (size_t)T.n1 * kc;
+    Cx* R = Vn + (size_t)T.n2 * kc;
+    Cx* Vs = R + (size_t)kc * kc;
+    double* sig = reinterpret_cast<double*>(Vs + (size_t)kc * kc);
+    Cx* tau = Vs + (size_t)kc * kc + kc;
+    __syncwarp();
+    kt = zrecompress(g, T.n1, T.n2, kk, B.U, B.V, Un, Vn, eps, R, Vs, kc, sig, tau, B.Z);
+  }
+  if (g.rank == 0) res[t] = AcaResult{st, kk, kt, 0u};
+}
+
+struct ZDense {
+  uint32_t b1, n1, b2, n2;
+  uint64_t off;
+};
+
+__global__ void helm_dense_kernel(PointsSoA P, double k, double h, const ZDense* __restrict__ tasks,
+                                  Cx* __restrict__ arena) {
+  const ZDense t = tasks[blockIdx.x];
+  HBlk B;
+  B.P = P;
+  B.k = k;
+  B.h = h;
+  const uint64_t cnt = (uint64_t)t.n1 * t.n2;
+  Cx* out = arena + t.off;
+  for (uint64_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const uint32_t i = (uint32_t)(e % t.n1), j = (uint32_t)(e / t.n1);
+    out[e] = helm_entry(B, t.b1 + i, t.b2 + j);
+  }
+}
+
+struct ZCopy {
+  uint64_t src_u, src_v, dst;
+  uint32_t n1, n2, kt, pad;
+};
+
+__global__ void helm_copy_kernel(const ZCopy* __restrict__ tasks, const Cx* __restrict__ ws, Cx* __restrict__ arena) {
+  const ZCopy t = tasks[blockIdx.x];
+  const uint64_t nu = (uint64_t)t.n1 * t.kt, nv = (uint64_t)t.n2 * t.kt;
+  Cx* dst = arena + t.dst;
+  for (uint64_t e = threadIdx.x; e < nu; e += blockDim.x) dst[e] = ws[t.src_u + e];
+  for (uint64_t e = threadIdx.x; e < nv; e += blockDim.x) dst[nu + e] = ws[t.src_v + e];
+}
+
 struct HTask {
   uint32_t b1, n1, b2, n2, kmax, kcap, leaf, pad;
   uint64_t ws;  // Cx offset of U (then V) in the batch workspace
@@ -434,5 +729,227 @@ extern "C" int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, doub
     }
     tasks.swap(retry);
   }
+  return AHX_OK;
+}
+
+namespace ahx {
+namespace {
+
+// Append-only growable complex arena of the Helmholtz leaves.
+int zarena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
+  ZState& Z = H->z;
+  const uint64_t need = (Z.elems + count) * sizeof(Cx);
+  if (need > Z.arena.bytes) {
+    size_t nb = std::max<size_t>(need, Z.arena.bytes * 2);
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, nb);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      nb = need;
+      e = cudaMalloc(&np, nb);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation of the complex leaf arena failed");
+        return AHX_ERR_NOMEM;
+      }
+    }
+    if (Z.elems) {
+      const cudaError_t ce = cudaMemcpyAsync(np, Z.arena.p, Z.elems * sizeof(Cx), cudaMemcpyDeviceToDevice, H->stream);
+      if (ce != cudaSuccess) {
+        cudaFree(np);
+        return cuda_fail(ce, "cudaMemcpyAsync (complex arena)");
+      }
+    }
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    if (Z.arena.p) cudaFree(Z.arena.p);
+    Z.arena.p = np;
+    Z.arena.bytes = nb;
+  }
+  off = Z.elems;
+  Z.elems += count;
+  return AHX_OK;
+}
+
+uint64_t zws_elems(const ZTask& t) { return aca_ws_doubles(t.n1, t.n2, t.kcap); }
+
+}  // namespace
+}  // namespace ahx
+
+extern "C" int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax) {
+  if (!H || !(h > 0.0) || !(eps > 0.0) || !std::isfinite(wavenumber)) {
+    set_error("ahx_helm_assemble: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  if (H->tree.sym) {
+    set_error("ahx_helm_assemble: the Helmholtz matrix is complex symmetric, not Hermitian: use a general block tree");
+    return AHX_ERR_ARG;
+  }
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  ZState& Z = H->z;
+  Z.assembled = Z.valid32 = Z.table = false;
+  Z.elems = 0;
+  Z.k = wavenumber;
+  Z.h = h;
+  Z.eps = eps;
+  const auto& Ls = H->tree.leaves;
+  const uint32_t nl = (uint32_t)Ls.size();
+  Z.rank.assign(nl, -1);
+  Z.aca_rank.assign(nl, -1);
+  Z.off.assign(nl, 0);
+  H->stat_ws_bytes = H->stat_retries = H->stat_batches = 0;
+  std::vector<ZTask> tasks;
+  std::vector<uint32_t> dense;
+  const uint32_t kcap0 = aca_kcap_default();
+  for (uint32_t l = 0; l < nl; ++l) {
+    const Leaf& L = Ls[l];
+    const uint32_t maxk = maxk_of(L.n1, L.n2, rankmax);
+    if (L.adm && maxk) {
+      ZTask t{};
+      t.b1 = L.b1;
+      t.n1 = L.n1;
+      t.b2 = L.b2;
+      t.n2 = L.n2;
+      t.i0 = L.i0;
+      t.kmax = maxk;
+      t.kcap = std::min(maxk, kcap0);
+      t.leaf = l;
+      tasks.push_back(t);
+    } else {
+      dense.push_back(l);
+    }
+  }
+  uint64_t est = 0;
+  for (uint32_t l : dense) est += (uint64_t)Ls[l].n1 * Ls[l].n2;
+  for (const ZTask& t : tasks) est += (uint64_t)(t.n1 + t.n2) * std::min(t.kmax, 16u);
+  if (Z.arena.bytes < est * sizeof(Cx)) {
+    Z.arena.release();
+    if ((rc = Z.arena.reserve(std::max<uint64_t>(est, 1) * sizeof(Cx)))) return rc;
+  }
+  const size_t budget = aca_ws_budget();
+  const double* pts = H->pts.as<double>();
+  const PointsSoA P{pts, pts + H->tree.n, pts + 2 * (size_t)H->tree.n};
+  ScopedBuf ws, zs, dtasks, dres, dcopy;
+  while (!tasks.empty()) {
+    std::sort(tasks.begin(), tasks.end(), [](const ZTask& a, const ZTask& b) {
+      return (uint64_t)(a.n1 + a.n2) * a.kcap > (uint64_t)(b.n1 + b.n2) * b.kcap;
+    });
+    std::vector<ZTask> retry;
+    size_t i = 0;
+    while (i < tasks.size()) {
+      uint64_t wsc = 0, zsi = 0;
+      size_t j = i;
+      for (; j < tasks.size(); ++j) {
+        const uint64_t w = zws_elems(tasks[j]);
+        if (j > i && (wsc + w) * sizeof(Cx) + (zsi + tasks[j].n1 + tasks[j].n2) * 4 > budget) break;
+        tasks[j].ws = wsc;
+        tasks[j].zs = zsi;
+        wsc += w;
+        zsi += tasks[j].n1 + tasks[j].n2;
+      }
+      std::vector<ZTask> batch(tasks.begin() + i, tasks.begin() + j);
+      i = j;
+      H->stat_ws_bytes = std::max<uint64_t>(H->stat_ws_bytes, wsc * sizeof(Cx) + zsi * 4);
+      H->stat_batches++;
+      if ((rc = ws.reserve(std::max<uint64_t>(wsc, 1) * sizeof(Cx)))) return rc;
+      if ((rc = zs.reserve(std::max<uint64_t>(zsi, 1) * 4))) return rc;
+      if ((rc = upload(dtasks, batch, H->stream))) return rc;
+      if ((rc = dres.reserve(batch.size() * sizeof(AcaResult)))) return rc;
+      const uint32_t nb = (uint32_t)batch.size();
+      helm_assemble_kernel<<<(nb + kWarps - 1) / kWarps, 32 * kWarps, 0, H->stream>>>(
+          P, wavenumber, h, eps, dtasks.as<ZTask>(), nb, ws.as<Cx>(), zs.as<int>(), dres.as<AcaResult>());
+      AHX_CUDA(cudaGetLastError());
+      std::vector<AcaResult> res(nb);
+      AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, nb * sizeof(AcaResult), cudaMemcpyDeviceToHost, H->stream));
+      AHX_CUDA(cudaStreamSynchronize(H->stream));
+      std::vector<ZCopy> copies;
+      for (uint32_t q = 0; q < nb; ++q) {
+        const ZTask& t = batch[q];
+        const AcaResult& r = res[q];
+        if (r.status == kAcaOverflow) {
+          ZTask u = t;
+          u.kcap = std::min(t.kmax, std::max(t.kcap * 4, 16u));
+          retry.push_back(u);
+          H->stat_retries++;
+          continue;
+        }
+        if (r.status != kAcaOk) {
+          dense.push_back(t.leaf);
+          continue;
+        }
+        Z.aca_rank[t.leaf] = (int32_t)r.k_aca;
+        Z.rank[t.leaf] = (int32_t)r.kt;
+        if (r.kt == 0) continue;
+        uint64_t off = 0;
+        if ((rc = zarena_append(H, (uint64_t)r.kt * (t.n1 + t.n2), off))) return rc;
+        Z.off[t.leaf] = off;
+        const uint64_t un = t.ws + (uint64_t)(t.n1 + t.n2) * t.kcap;  // Un follows U and V
+        copies.push_back(ZCopy{un, un + (uint64_t)t.n1 * t.kcap, off, t.n1, t.n2, r.kt, 0u});
+      }
+      if (!copies.empty()) {
+        if ((rc = upload(dcopy, copies, H->stream))) return rc;
+        helm_copy_kernel<<<(uint32_t)copies.size(), 128, 0, H->stream>>>(dcopy.as<ZCopy>(), ws.as<Cx>(),
+                                                                          Z.arena.as<Cx>());
+        AHX_CUDA(cudaGetLastError());
+      }
+      AHX_CUDA(cudaStreamSynchronize(H->stream));
+    }
+    tasks.swap(retry);
+  }
+  // dense leaves (inadmissible and failed ACA) in leaf order
+  std::sort(dense.begin(), dense.end());
+  std::vector<ZDense> dt;
+  for (uint32_t l : dense) {
+    const Leaf& L = Ls[l];
+    uint64_t off = 0;
+    if ((rc = zarena_append(H, (uint64_t)L.n1 * L.n2, off))) return rc;
+    Z.off[l] = off;
+    Z.rank[l] = -1;
+    Z.aca_rank[l] = -1;
+    dt.push_back(ZDense{L.b1, L.n1, L.b2, L.n2, off});
+  }
+  if (!dt.empty()) {
+    ScopedBuf ddt;
+    if ((rc = upload(ddt, dt, H->stream))) return rc;
+    helm_dense_kernel<<<(uint32_t)dt.size(), 256, 0, H->stream>>>(P, wavenumber, h, ddt.as<ZDense>(), Z.arena.as<Cx>());
+    AHX_CUDA(cudaGetLastError());
+  }
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  Z.assembled = true;
+  return AHX_OK;
+}
+
+extern "C" int ahx_helm_ranks(const ahx_hmat* H, int32_t* ranks) {
+  if (!H || !ranks) return AHX_ERR_ARG;
+  if (!H->z.assembled) {
+    set_error("ahx_helm_ranks: Helmholtz leaves not assembled");
+    return AHX_ERR_STATE;
+  }
+  std::copy(H->z.rank.begin(), H->z.rank.end(), ranks);
+  return AHX_OK;
+}
+
+extern "C" uint64_t ahx_helm_leaf_size(const ahx_hmat* H, uint32_t l) {
+  if (!H || !H->z.assembled || l >= H->tree.leaves.size()) return 0;
+  const Leaf& L = H->tree.leaves[l];
+  const int32_t r = H->z.rank[l];
+  return r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
+}
+
+extern "C" int ahx_helm_get_leaf(const ahx_hmat* H, uint32_t l, double* out) {
+  if (!H || !out || l >= H->tree.leaves.size()) {
+    set_error("ahx_helm_get_leaf: invalid argument");
+    return AHX_ERR_ARG;
+  }
+  if (!H->z.assembled) {
+    set_error("ahx_helm_get_leaf: Helmholtz leaves not assembled");
+    return AHX_ERR_STATE;
+  }
+  const uint64_t cnt = ahx_helm_leaf_size(H, l);
+  if (!cnt) return AHX_OK;
+  AHX_CUDA(cudaSetDevice(H->device));
+  AHX_CUDA(cudaMemcpyAsync(out, H->z.arena.as<Cx>() + H->z.off[l], cnt * sizeof(Cx), cudaMemcpyDeviceToHost,
+                           H->stream));
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
   return AHX_OK;
 }

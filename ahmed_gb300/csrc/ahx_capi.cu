@@ -594,6 +594,7 @@ int ahx_hmat_destroy(ahx_hmat* H) {
   H->stage_x.release();
   H->stage_y.release();
   H->scratch.release();
+  H->z.release_all();
   if (H->own_stream && H->stream) cudaStreamDestroy(H->stream);
   delete H;
   return AHX_OK;

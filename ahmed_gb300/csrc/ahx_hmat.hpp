@@ -64,6 +64,30 @@ struct ProdCopy {
   }
 };
 
+// Complex (Helmholtz) leaves of a handle's block tree in the mblock<dcomp>
+// layout (low rank: U (n1 x k) then V (n2 x k), the block U V^H; dense: n1 x n2
+// column-major), complex elements interleaved (re, im).
+struct ZState {
+  bool assembled = false;
+  double k = 0.0, h = 0.0, eps = 0.0;
+  std::vector<int32_t> rank, aca_rank;  // per leaf, -1 dense
+  std::vector<uint64_t> off;            // complex element offset of each leaf
+  DevBuf arena;                         // complex128 elements
+  uint64_t elems = 0;
+  DevBuf arena32;                       // complex64 copy (AHX_FP32 storage)
+  bool valid32 = false;
+  DevBuf leaves, order;                 // product leaf table, launch order
+  uint32_t nleaves = 0;
+  bool table = false;
+  DevBuf gm;                            // GMRES workspace
+  void release_all() {
+    for (DevBuf* b : {&arena, &arena32, &leaves, &order, &gm}) b->release();
+    assembled = valid32 = table = false;
+    elems = 0;
+    nleaves = 0;
+  }
+};
+
 // Workspace budget of one ACA batch (bytes); AHX_ACA_WS_BYTES overrides.
 inline size_t aca_ws_budget() {
   const char* e = std::getenv("AHX_ACA_WS_BYTES");
@@ -118,6 +142,7 @@ struct ahx_hmat {
   ahx::DevBuf arena64;
   uint64_t arena64_elems = 0;
   ahx::ProdCopy prod[ahx::kNumPrecisions];
+  ahx::ZState z;  // Helmholtz (complex) leaves, when assembled
   // staging buffers for host vectors
   ahx::DevBuf stage_x, stage_y;
   ahx::DevBuf scratch;  // solver scratch
@@ -144,4 +169,10 @@ void invalidate_products(ahx_hmat* H);
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
                    double* Y, uint64_t ldY, bool transposed = false);
 bool is_device_ptr(const void* p);
+// Leaf table of a product in descending cost order (ahx_capi.cu)
+int upload_leaf_table(ahx_hmat* H, const std::vector<PlanLeaf>& pls, DevBuf& leaves, DevBuf& order, uint32_t& n);
+// Helmholtz leaves: Y += d op(A) X on device pointers (prec kFP64: complex128
+// leaves; kFP32: complex64 leaves, FP32 accumulation)
+int zproduct_device(ahx_hmat* H, int prec, int op, double dre, double dim, uint32_t p, const double2* X,
+                    uint64_t ldX, double2* Y, uint64_t ldY);
 }  // namespace ahx

@@ -62,6 +62,29 @@ cudaError_t launch_matvec_df(const DfArgs& a, cudaStream_t s);
 cudaError_t launch_split_df(const double* src, uint64_t ld, uint64_t rows, uint32_t cols, double scale,
                             void* dst, cudaStream_t s);
 
+// Complex product Y += d op(A) X (ahx_matvec_z.cu) over complex leaves in the
+// mblock<dcomp> layout; MvLeaf offsets count complex elements.  arena: complex128
+// (single = 0) or complex64 (single = 1, FP32 accumulation); X, Y: complex128,
+// column-major, leading dimensions in complex elements.
+enum ZOp : int { kZOpN = 0, kZOpH = 1, kZOpT = 2 };  // A, A^H, A^T
+struct ZArgs {
+  const MvLeaf* leaves;
+  const uint32_t* order;
+  uint32_t nleaves;
+  const void* arena;
+  int single;
+  double dre, dim;
+  uint32_t p;
+  const double2* X;
+  uint64_t ldX;
+  double2* Y;
+  uint64_t ldY;
+  int op;
+};
+cudaError_t launch_matvec_z(const ZArgs& a, cudaStream_t s);
+// dst[i] = (float) src[i], complex128 -> complex64
+cudaError_t launch_z_to_c64(const double2* src, uint64_t n, float2* dst, cudaStream_t s);
+
 // Host description of one leaf for plan building: its data in the FP64 arena.
 struct PlanLeaf {
   uint32_t b1, n1, b2, n2;

@@ -53,6 +53,16 @@ def _prec(p):
     return PRECISIONS[p] if isinstance(p, str) else int(p)
 
 
+def _is_complex(a):
+    """complex numpy array or torch tensor"""
+    dt = getattr(a, "dtype", None)
+    if dt is None:
+        return False
+    if isinstance(dt, np.dtype):
+        return dt.kind == "c"
+    return bool(getattr(dt, "is_complex", False))
+
+
 def _ncols(a, n):
     if a.ndim == 1:
         return 1, n
@@ -240,9 +250,45 @@ class HMatrix:
     def prepare(self, precision="fp64"):
         check(lib().ahx_hmat_prepare(self._h, _prec(precision)))
 
+    # -- Helmholtz leaves (mblock<dcomp>) ---------------------------------
+    def helmholtz_assemble(self, wavenumber, h=None, eps=1e-6, rankmax=2**32 - 1):
+        """The Helmholtz H-matrix exp(ikr)/(4 pi r) (diagonal exp(ikh)/(4 pi h)) on this
+        tree, as the reference's apprx_unsym with T = dcomp (ACA<dcomp> + addtrll).
+        Complex products and GMRes take complex128 arrays (see mltaGeHVec)."""
+        self.zh = mean_nn(self.points) if h is None else float(h)
+        self.zk = float(wavenumber)
+        check(lib().ahx_helm_assemble(self._h, self.zk, self.zh, float(eps), min(int(rankmax), 2**32 - 1)))
+        return self
+
+    def helm_ranks(self):
+        out = np.zeros(self.nleaves, np.int32)
+        check(lib().ahx_helm_ranks(self._h, ptr(out)))
+        return out
+
+    def helm_leaf_data(self, l):
+        cnt = lib().ahx_helm_leaf_size(self._h, l)
+        out = np.zeros(cnt, np.complex128)
+        if cnt:
+            check(lib().ahx_helm_get_leaf(self._h, l, ptr(out)))
+        return out
+
+    def helm_storage_bytes(self, precision="fp64"):
+        return lib().ahx_helm_storage_bytes(self._h, _prec(precision))
+
+    def _helm_product(self, op, d, p, X, ldX, Y, ldY, precision):
+        self._follow_torch(X, Y)
+        d = complex(d)
+        check(lib().ahx_helm_matvec(self._h, _prec(precision), int(op), d.real, d.imag, int(p), ptr(X),
+                                    int(ldX), ptr(Y), int(ldY)))
+        return Y
+
     # -- product ----------------------------------------------------------
     def mltaGeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
-        """Y += d A X with X, Y column-major (numpy / torch, host or CUDA)."""
+        """Y += d A X with X, Y column-major (numpy / torch, host or CUDA).  Complex
+        arrays use the Helmholtz leaves (the reference's dcomp instantiation;
+        precision "fp32": complex64 leaves)."""
+        if _is_complex(X):
+            return self._helm_product(0, d, p, X, ldX, Y, ldY, precision)
         self._follow_torch(X, Y)
         check(lib().ahx_matvec(self._h, _prec(precision), float(d), int(p), ptr(X), int(ldX),
                                ptr(Y), int(ldY)))
@@ -253,11 +299,19 @@ class HMatrix:
         p, ld = _ncols(x, self.n)
         return self.mltaGeHGeM(d, p, x, ld, y, ld, precision)
 
-    def mltaGeHtGeM(self, d, p, X, ldX, Y, ldY):
-        """Y += d A^T X (FP64 leaves; for real leaves also A^H: mltaGeHhGeM)."""
+    def mltaGeHtGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
+        """Y += d A^T X (FP64 leaves; complex arrays: the Helmholtz leaves)."""
+        if _is_complex(X):
+            return self._helm_product(2, d, p, X, ldX, Y, ldY, precision)
         self._follow_torch(X, Y)
         check(lib().ahx_matvec_transposed(self._h, float(d), int(p), ptr(X), int(ldX), ptr(Y), int(ldY)))
         return Y
+
+    def mltaGeHhGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
+        """Y += d A^H X (real leaves: A^T)."""
+        if _is_complex(X):
+            return self._helm_product(1, d, p, X, ldX, Y, ldY, precision)
+        return self.mltaGeHtGeM(d, p, X, ldX, Y, ldY)
 
     # symmetric handles: the same products (H/mltaGeHVec.cpp:421-475)
     def mltaHeHVec(self, d, x, y, precision="fp64"):
@@ -266,12 +320,13 @@ class HMatrix:
     def mltaHeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
         return self.mltaGeHGeM(d, p, X, ldX, Y, ldY, precision)
 
-    def mltaGeHtVec(self, d, x, y):
+    def mltaGeHtVec(self, d, x, y, precision="fp64"):
         p, ld = _ncols(x, self.n)
-        return self.mltaGeHtGeM(d, p, x, ld, y, ld)
+        return self.mltaGeHtGeM(d, p, x, ld, y, ld, precision)
 
-    mltaGeHhVec = mltaGeHtVec
-    mltaGeHhGeM = mltaGeHtGeM
+    def mltaGeHhVec(self, d, x, y, precision="fp64"):
+        p, ld = _ncols(x, self.n)
+        return self.mltaGeHhGeM(d, p, x, ld, y, ld, precision)
 
     # -- solvers ----------------------------------------------------------
     def GMRes(self, b, x, eps, m, nsteps, precision="fp64"):
@@ -280,8 +335,9 @@ class HMatrix:
         self._follow_torch(b, x)
         iters = np.zeros(p, np.uint32)
         res = np.zeros(p, np.float64)
-        code = check(lib().ahx_gmres(self._h, _prec(precision), p, ptr(b), ld, ptr(x), ld,
-                                     float(eps), int(m), int(nsteps), ptr(iters), ptr(res)))
+        fn = lib().ahx_helm_gmres if _is_complex(b) else lib().ahx_gmres
+        code = check(fn(self._h, _prec(precision), p, ptr(b), ld, ptr(x), ld, float(eps), int(m), int(nsteps),
+                        ptr(iters), ptr(res)))
         return (0 if code == _capi.AHX_OK else 1), res, iters
 
     def agglH(self, eps=None, max_rank=2**32 - 1):

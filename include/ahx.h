@@ -121,6 +121,35 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4);
  * Bounding-box trees (ACA start row 0). */
 int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax,
                        const float* rank_hint, int32_t* ranks);
+/* Helmholtz H-matrix on the handle's (general) block tree: the same kernel and
+ * diagonal, assembled as the reference's mblock<dcomp> leaves (apprx_unsym with
+ * T = dcomp, Include/apprx.h:136-172: ACA<dcomp> from the leaf's start row i0,
+ * recompression mblock<dcomp>::addtrll H/mblock_Z.cpp:200-300, dense leaves
+ * from the generator where ACA fails).  Independent of the real assembly of the
+ * same handle.  Complex vectors are interleaved (re, im) doubles, the layout of
+ * dcomp; leading dimensions count complex elements. */
+int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax);
+/* per leaf: rank after recompression, -1 for dense leaves */
+int ahx_helm_ranks(const ahx_hmat* H, int32_t* ranks);
+/* complex elements of leaf l (U then V, or the dense block) */
+uint64_t ahx_helm_leaf_size(const ahx_hmat* H, uint32_t l);
+/* copy leaf l (mblock<dcomp>::getdata() layout) into out (2 * size doubles) */
+int ahx_helm_get_leaf(const ahx_hmat* H, uint32_t l, double* out);
+/* bytes of the complex leaves: AHX_FP64 complex128, AHX_FP32 complex64 */
+uint64_t ahx_helm_storage_bytes(const ahx_hmat* H, int precision);
+/* Y += d op(A) X, op 0: A (mltaGeHVec / mltaGeHGeM with T = dcomp,
+ * H/mltaGeHVec.cpp:770-780), 1: A^H (mltaGeHhVec / mltaGeHhGeM, :782-792),
+ * 2: A^T (mltaGeHtVec / mltaGeHtGeM, :794-805); d = d_re + i d_im.  precision
+ * AHX_FP64: complex128 leaves; AHX_FP32: complex64 leaves, FP32 accumulation
+ * (the reference's scomp instantiation).  X, Y: n x p complex, host or device. */
+int ahx_helm_matvec(ahx_hmat* H, int precision, int op, double d_re, double d_im, uint32_t p, const double* X,
+                    uint64_t ldX, double* Y, uint64_t ldY);
+/* Restarted complex GMRES(m) per right-hand side: GMRes(const Matrix<dcomp>&, b,
+ * x, eps, m, nsteps) solvers/GMRES.cpp:246-366 (tol, maxit, iters and resid as in
+ * ahx_gmres).  AHX_FP32: FP64 iterative refinement around complex64 inner solves.
+ * B, X: n x p complex, host or device; X holds the initial guess. */
+int ahx_helm_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint64_t ldB, double* X, uint64_t ldX,
+                   double tol, uint32_t m, uint32_t maxit, uint32_t* iters, double* resid);
 /* Agglomeration (agglH, H/agglH.cpp:111-272; the recmpr branch of matgenGeH_sqntl,
  * Include/matgen_sqntl.h:32-55): bottom up, a non-diagonal block whose sons are all
  * low-rank leaves becomes one low-rank leaf when the recompressed union (relative

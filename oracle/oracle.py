@@ -200,6 +200,13 @@ def ref():
         L.ref_agglomerate.argtypes = [vp, dbl, u32]
         L.ref_save.restype = i32
         L.ref_save.argtypes = [vp, dbl, u32, C.c_char_p]
+        L.ref_helm_assemble.argtypes = [vp, dbl, dbl, dbl, u32, i32]
+        L.ref_helm_ranks_assembled.argtypes = [vp, vp]
+        L.ref_helm_leaf_data.restype = C.c_ulong
+        L.ref_helm_leaf_data.argtypes = [vp, u32, vp]
+        L.ref_helm_matvec.argtypes = [vp, i32, dbl, dbl, u32, vp, vp]
+        L.ref_helm_gmres.restype = u32
+        L.ref_helm_gmres.argtypes = [vp, vp, vp, vp, u32, vp]
         _ref = L
     return _ref
 
@@ -281,4 +288,36 @@ class RefH:
         e = C.c_double(eps)
         ns = C.c_uint(nsteps)
         r = ref().ref_cg(self._H, _p(b), _p(x), C.byref(e), C.byref(ns))
+        return r, e.value, ns.value
+
+    # --- Helmholtz (complex) H-matrix: mblock<dcomp> leaves of the same tree ---
+    def helm_assemble(self, wavenumber, h, eps, rankmax=2**32 - 1, nthreads=0):
+        ref().ref_helm_assemble(self._H, wavenumber, h, eps, rankmax, nthreads)
+
+    def helm_ranks(self):
+        """per leaf: rank after recompression, -1 dense"""
+        out = np.zeros(self.nleaves, np.int32)
+        ref().ref_helm_ranks_assembled(self._H, _p(out))
+        return out
+
+    def helm_leaf_data(self, l):
+        cnt = ref().ref_helm_leaf_data(self._H, l, None)
+        out = np.zeros(cnt, np.complex128)
+        ref().ref_helm_leaf_data(self._H, l, _p(out))
+        return out
+
+    def helm_matvec(self, X, Y, d=1.0, op=0):
+        """Y += d op(A) X; X, Y complex (p x n rows = columns of the n x p array); op 0 A, 1 A^H, 2 A^T."""
+        X = np.ascontiguousarray(X, dtype=np.complex128)
+        assert Y.dtype == np.complex128 and Y.flags.c_contiguous
+        p = 1 if X.ndim == 1 else X.shape[0]
+        d = complex(d)
+        ref().ref_helm_matvec(self._H, op, d.real, d.imag, p, _p(X), _p(Y))
+        return Y
+
+    def helm_gmres(self, b, x, eps, m, nsteps):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        e = C.c_double(eps)
+        ns = C.c_uint(nsteps)
+        r = ref().ref_helm_gmres(self._H, _p(b), _p(x), C.byref(e), m, C.byref(ns))
         return r, e.value, ns.value

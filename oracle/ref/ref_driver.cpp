@@ -103,6 +103,14 @@ struct RefH {
   mblock<double>** A = nullptr;
   LaplaceGen gen;
   bool sym = false;  // symmetric block tree (subdivide_sym), HeH leaves
+  mblock<dcomp>** Az = nullptr;  // Helmholtz leaves (mblock<dcomp>)
+};
+
+// The Helmholtz H-matrix as the reference's complex GMRes sees it.
+struct ZMatrixOp : public Matrix<dcomp> {
+  RefH* H;
+  explicit ZMatrixOp(RefH* h) : Matrix<dcomp>(h->n, h->n), H(h) {}
+  void amux(dcomp d, dcomp* x, dcomp* y) const { mltaGeHVec(d, H->root_bl, H->Az, x, y); }
 };
 
 struct HMatrixOp : public Matrix<double> {
@@ -144,18 +152,18 @@ static void apprx_sym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* bl,
 }
 
 // ACA start row for bounding-box trees (they carry no centroid index): row 0.
-template <class MATGEN_T>
-static void apprx_unsym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* bl,
+template <class T, class MATGEN_T>
+static void apprx_unsym_bbx(MATGEN_T& MatGen, mblock<T>*& mbl, blcluster* bl,
                             double eps, unsigned rankmax) {
   unsigned n1 = bl->getn1(), n2 = bl->getn2();
   unsigned b1 = bl->getb1(), b2 = bl->getb2();
   unsigned maxk = n1 * n2 / (n1 + n2) + 4;
   if (maxk > rankmax) maxk = rankmax;
-  mbl = new mblock<double>(n1, n2);
+  mbl = new mblock<T>(n1, n2);
   bool succ = false;
   if (bl->isadm() && maxk) {
     unsigned k;
-    double *U, *V;
+    T *U, *V;
     succ = ::ACA(MatGen, b1, n1, b2, n2, eps, maxk, 0u, k, U, V);
     if (succ) mbl->cpyLrM_cmpr(k, U, n1, V, n2, eps, k);
     delete[] V;
@@ -356,6 +364,80 @@ void ref_helm_ranks(void* p, double wavenumber, double h, double eps, unsigned r
   }
 }
 
+// Helmholtz H-matrix: the reference's assembly with T = dcomp (apprx_unsym,
+// Include/apprx.h:136-172: ::ACA<dcomp> then mblock<dcomp>::cpyLrM_cmpr ->
+// addtrll, H/mblock_Z.cpp:200-300; dense leaves from cmpbl).
+void ref_helm_assemble(void* p, double wavenumber, double h, double eps, unsigned rankmax, int nthreads) {
+  RefH* H = (RefH*)p;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  if (H->Az) freembls(H->nblcks, H->Az);
+  allocmbls(H->nblcks, H->Az);
+  HelmGen gen{H->dofs.data(), H->op_perm.data(), h, wavenumber};
+  std::streambuf* old = std::cout.rdbuf();
+  std::ostringstream sink;
+  std::cout.rdbuf(sink.rdbuf());
+  if (H->kind == 1) {
+    matgenGeH_omp(gen, H->nblcks, (bemblcluster<Pt, Pt>*)H->root_bl, eps, rankmax, H->Az);
+  } else {
+#pragma omp parallel for schedule(dynamic)
+    for (int l = 0; l < (int)H->nblcks; ++l) {
+      blcluster* b = H->leaves[l];
+      apprx_unsym_bbx(gen, H->Az[b->getidx()], b, eps, rankmax);
+    }
+  }
+  std::cout.rdbuf(old);
+}
+
+// per leaf of the Helmholtz matrix: rank (LrM) or -1 (dense)
+void ref_helm_ranks_assembled(void* p, int* out) {
+  RefH* H = (RefH*)p;
+  for (unsigned l = 0; l < H->nblcks; ++l) {
+    mblock<dcomp>* m = H->Az[H->leaves[l]->getidx()];
+    out[l] = m->isLrM() ? (int)m->rank() : -1;
+  }
+}
+
+// complex entries of Helmholtz leaf l (U then V, or the dense block) as
+// interleaved (re, im) doubles in out; returns the complex count
+unsigned long ref_helm_leaf_data(void* p, unsigned l, double* out) {
+  RefH* H = (RefH*)p;
+  blcluster* b = H->leaves[l];
+  mblock<dcomp>* m = H->Az[b->getidx()];
+  unsigned long cnt = m->isLrM() ? (unsigned long)m->rank() * (b->getn1() + b->getn2())
+                                 : (unsigned long)b->getn1() * b->getn2();
+  if (out && cnt) memcpy(out, m->getdata(), cnt * sizeof(dcomp));
+  return cnt;
+}
+
+// Y += d op(A) X, op 0: A (mltaGeHGeM), 1: A^H (mltaGeHhGeM), 2: A^T (mltaGeHtGeM);
+// X, Y: n x nrhs complex, interleaved doubles, leading dimension n
+void ref_helm_matvec(void* p, int op, double dre, double dim, unsigned nrhs, double* X, double* Y) {
+  RefH* H = (RefH*)p;
+  const dcomp d(dre, dim);
+  dcomp* x = (dcomp*)X;
+  dcomp* y = (dcomp*)Y;
+  if (op == 1) mltaGeHhGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
+  else if (op == 2) mltaGeHtGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
+  else if (nrhs == 1) mltaGeHVec(d, H->root_bl, H->Az, x, y);
+  else mltaGeHGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
+}
+
+// the reference's complex GMRes (solvers/GMRES.cpp:246-366) with the Helmholtz leaves
+unsigned ref_helm_gmres(void* p, double* b, double* x, double* eps, unsigned m, unsigned* nsteps) {
+  RefH* H = (RefH*)p;
+  ZMatrixOp op(H);
+  double e = *eps;
+  unsigned ns = *nsteps;
+  std::streambuf* old = std::cout.rdbuf();
+  std::ostringstream sink;
+  std::cout.rdbuf(sink.rdbuf());
+  unsigned r = GMRes(op, (dcomp*)b, (dcomp*)x, e, m, ns);
+  std::cout.rdbuf(old);
+  *eps = e;
+  *nsteps = ns;
+  return r;
+}
+
 // The reference's agglomeration agglH (H/agglH.cpp:253-272) of the assembled
 // leaves; the leaf list is rebuilt in DFS order (indices as agglH left them).
 void ref_agglomerate(void* p, double eps, unsigned rankmax) {
@@ -382,6 +464,7 @@ int ref_save(void* p, double eta, unsigned bmin, const char* path) {
 void ref_free(void* p) {
   RefH* H = (RefH*)p;
   if (H->A) freembls(H->nblcks, H->A);
+  if (H->Az) freembls(H->nblcks, H->Az);
   delete H->root_bl;
   delete H->root_cl;
   delete H;

@@ -9,6 +9,8 @@ Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py mbls       (savembls file hashes)
         python tests/golden/make_golden.py sym        (symmetric trees, HeH assembly/product)
         python tests/golden/make_golden.py aggl       (agglomeration, agglH)
+        python tests/golden/make_golden.py zhmat      (Helmholtz H-matrix: complex assembly,
+                                                       products, GMRes)
 """
 import os
 import sys
@@ -210,6 +212,68 @@ def aggl():
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+# Helmholtz H-matrices: the reference's mblock<dcomp> assembly (ACA<dcomp> +
+# addtrll of H/mblock_Z.cpp), its complex products A, A^H, A^T and its complex
+# GMRes.  GMRES cases use h = (smallest point distance) / gm_div: with the mean
+# spacing the collocation matrix is indefinite and GMRES stagnates.
+ZH_CASES = {"zh_fib4096": ("fib4096", O.TREE_BBX, 1, False, 8.0),
+            "zh_ell2500": ("ell2500", O.TREE_PCA, 2, True, 4.0)}
+ZH_K = 5.0
+ZH_D = complex(0.7, -0.3)
+
+
+def zhmat():
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    from scipy.spatial import cKDTree
+    for name, (base, kind, p, full, gm_div) in ZH_CASES.items():
+        gen, bmin = CASES[base]
+        P = gen()
+        n = P.shape[0]
+        h = O.mean_nn(P)
+        rng = np.random.default_rng(3)
+        X = rng.standard_normal((p, n)) + 1j * rng.standard_normal((p, n))
+        Y0 = rng.standard_normal((p, n)) + 1j * rng.standard_normal((p, n))
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+               "eps": np.float64(EPS), "kind": np.int32(kind), "k": np.float64(ZH_K), "d": np.complex128(ZH_D),
+               "X": X, "Y0": Y0}
+        R = O.RefH(P, kind, bmin, ETA, h)
+        out["leaves"] = R.leaves()
+        out["op_perm"] = R.perm()[0]
+        R.helm_assemble(ZH_K, h, EPS, nthreads=1)
+        out["ranks"] = R.helm_ranks()
+        for op in (0, 1, 2):
+            Y = Y0.copy()
+            R.helm_matvec(X, Y, d=ZH_D, op=op)
+            out[f"Y_op{op}"] = Y
+        if full:  # factors (U then V) of 40 low-rank leaves spread over the leaf list
+            L = out["leaves"]
+            size = (L[:, 1].astype(np.int64) + L[:, 3]) * out["ranks"]
+            lr = np.flatnonzero((out["ranks"] >= 0) & (size <= 2048))
+            pick = lr[np.linspace(0, lr.size - 1, min(40, lr.size)).astype(int)]
+            chunks = [R.helm_leaf_data(int(l)) for l in pick]
+            offs = np.zeros(pick.size + 1, np.uint64)
+            offs[1:] = np.cumsum([c.size for c in chunks])
+            out["data_leaves"] = pick.astype(np.uint32)
+            out["data"] = np.concatenate(chunks)
+            out["offsets"] = offs
+        dd, _ = cKDTree(P).query(P, 2)
+        gh = float(dd[:, 1].min()) / gm_div
+        G2 = O.RefH(P, kind, bmin, ETA, gh)
+        G2.helm_assemble(ZH_K, gh, EPS, nthreads=1)
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        x = np.zeros(n, np.complex128)
+        r, e, ns = G2.helm_gmres(b, x, 1e-8, 100, 100)
+        if r != 0:
+            sys.exit(f"{name}: the reference GMRes did not converge in one cycle")
+        out.update({"gm_h": np.float64(gh), "gm_b": b, "gm_x": x, "gm_iters": np.uint32(ns),
+                    "gm_resid": np.float64(e), "gm_m": np.uint32(100)})
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB) ranks>=0: {(out['ranks'] >= 0).sum()}"
+              f" gmres {ns} steps {e:.2e}")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
@@ -219,5 +283,7 @@ if __name__ == "__main__":
         sym()
     elif len(sys.argv) > 1 and sys.argv[1] == "aggl":
         aggl()
+    elif len(sys.argv) > 1 and sys.argv[1] == "zhmat":
+        zhmat()
     else:
         main()
