@@ -501,7 +501,8 @@ def run_helmholtz(args):
     (feature, complex-ACA rank) pairs from Fibonacci spheres at N = 16,384 / 65,536 / 131,072
     with wavenumbers k ~ U[1, 20] (numpy PCG64 seed 7), eps 1e-6, leaf 32, eta 0.8; the MLP is
     trained on the GPU; then complex ACA with and without predicted ranks on held-out
-    matrices (random sphere points, N = 65,536, k = 3.7 and 16.2)."""
+    matrices (random sphere points, N = 65,536, k = 3.7 and 16.2), and the complex
+    H-matrix of the k = 16.2 one: assembly and products with complex128 / complex64 leaves."""
     import torch
     import ahmed_gb300 as A
 
@@ -555,6 +556,42 @@ def run_helmholtz(args):
                           "plain": {"aca_s": t_plain, "workspace_bytes": st0[0], "retries": st0[1], "batches": st0[2]},
                           "hinted": {"aca_s": t_hint, "predict_s": t_pred, "workspace_bytes": st1[0],
                                      "retries": st1[1], "batches": st1[2]}}
+    # the complex H-matrix itself (mblock<dcomp> leaves) at k = 16.2: assembly and
+    # products with complex128 and complex64 leaves (CUDA events, 16 and 1 RHS)
+    dev = torch.device("cuda", 0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H.helmholtz_assemble(16.2, h, EPS)
+    torch.cuda.synchronize()
+    zr = H.helm_ranks()
+    zout = {"k": 16.2, "assembly_s": time.perf_counter() - t0, "low_rank_leaves": int((zr >= 0).sum()),
+            "mean_rank": float(zr[zr >= 0].mean()), "complex128_bytes": int(H.helm_storage_bytes("fp64")),
+            "complex64_bytes": int(H.helm_storage_bytes("fp32"))}
+    rng2 = np.random.default_rng(11)
+    for p in (16, 1):
+        X = torch.from_numpy(rng2.standard_normal((p, H.n)) + 1j * rng2.standard_normal((p, H.n))).to(dev)
+        ys = {}
+        for prec in ("fp64", "fp32"):
+            Y = torch.zeros_like(X)
+            H.mltaGeHVec(1.0, X, Y, precision=prec)  # warm-up (builds the complex64 copy)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(5):
+                H.mltaGeHVec(1.0, X, Y, precision=prec)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 5
+            Y.zero_()
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+            ys[prec] = Y.cpu().numpy()
+            leaf = H.helm_storage_bytes(prec)
+            byts = leaf + p * H.n * 16 * 3
+            zout[f"{prec}_{p}rhs"] = {"ms": ms, "algorithmic_bytes": int(byts), "achieved_gbs": byts / (ms * 1e-3) / 1e9}
+        err = np.linalg.norm(ys["fp32"] - ys["fp64"], axis=1) / np.linalg.norm(ys["fp64"], axis=1)
+        zout[f"fp32_err_{p}rhs"] = float(err.max())
+    out["complex_hmatrix"] = zout
     H.close()
     print(json.dumps(out))
 

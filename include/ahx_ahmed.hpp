@@ -19,13 +19,16 @@
 // leaves live in one libahx handle (trees on the host, bit-identical to the
 // reference's; leaves on the GPU).  mblock<T> objects are host views that
 // copy a leaf back from the device when their data is asked for.
-// MATGEN_T: the GPU generator is the Laplace collocation kernel; the
-// generator object passes h (diagonal 1/(4 pi h)) through `geth()`.
+// MATGEN_T: the GPU generators are the Laplace collocation kernel (mblock<double>
+// leaves) and the Helmholtz kernel exp(ikr)/(4 pi r) (mblock<dcomp> leaves); the
+// generator object passes h (diagonal 1/(4 pi h), resp. exp(ikh)/(4 pi h)) through
+// `geth()` and, for dcomp, the wavenumber through `getk()`.
 #ifndef AHX_AHMED_HPP
 #define AHX_AHMED_HPP
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
@@ -33,11 +36,14 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "ahx.h"
 
 namespace ahx_ahmed {
+
+using dcomp = std::complex<double>;  // the reference's dcomp (Include/cmplx.h)
 
 inline void check(int rc) {
   if (rc != AHX_OK && rc != AHX_NOT_CONVERGED)
@@ -147,12 +153,20 @@ class blcluster {
     refresh_ranks();
   }
   int rank_of(unsigned l) const { return ranks_.at(l); }
+  // per-leaf ranks of the Helmholtz (mblock<dcomp>) leaves
+  void refresh_zranks() {
+    zranks_.resize(ahx_hmat_nleaves(h_));
+    check(ahx_helm_ranks(h_, zranks_.data()));
+  }
+  int zrank_of(unsigned l) const { return zranks_.at(l); }
+  int rank_of(unsigned l, const double*) const { return rank_of(l); }
+  int rank_of(unsigned l, const dcomp*) const { return zrank_of(l); }
 
  private:
   unsigned n_;
   ahx_hmat* h_ = nullptr;
   std::vector<uint32_t> leaves_;
-  std::vector<int32_t> ranks_;
+  std::vector<int32_t> ranks_, zranks_;
 };
 
 template <class T1, class T2>
@@ -174,22 +188,27 @@ class mblock {
   }
   unsigned getn1() const { return bound()->leaf(idx_)[1]; }
   unsigned getn2() const { return bound()->leaf(idx_)[3]; }
-  bool isLrM() const { return bound()->rank_of(idx_) >= 0; }
+  bool isLrM() const { return bound()->rank_of(idx_, (const T*)nullptr) >= 0; }
   bool isGeM() const { return !isLrM(); }
   // dense diagonal block of a symmetric tree: packed upper triangle (Include/mblock.h:314)
   bool isHeM() const {
     return isGeM() && ahx_hmat_symmetric(bound()->handle()) && bound()->leaf(idx_)[0] == bound()->leaf(idx_)[2];
   }
-  unsigned rank() const { return (unsigned)bound()->rank_of(idx_); }
+  unsigned rank() const { return (unsigned)bound()->rank_of(idx_, (const T*)nullptr); }
   T* getdata() {
-    if (data_.empty()) {
-      data_.resize(ahx_hmat_leaf_size(bound()->handle(), idx_));
-      if (!data_.empty()) check(ahx_hmat_get_leaf(bound()->handle(), idx_, data_.data()));
-    }
+    if (data_.empty()) fetch(bound()->handle(), idx_, data_);
     return data_.data();
   }
 
  private:
+  static void fetch(ahx_hmat* h, unsigned l, std::vector<double>& d) {
+    d.resize(ahx_hmat_leaf_size(h, l));
+    if (!d.empty()) check(ahx_hmat_get_leaf(h, l, d.data()));
+  }
+  static void fetch(ahx_hmat* h, unsigned l, std::vector<dcomp>& d) {
+    d.resize(ahx_helm_leaf_size(h, l));
+    if (!d.empty()) check(ahx_helm_get_leaf(h, l, reinterpret_cast<double*>(d.data())));
+  }
   const blcluster* bound() const {
     if (!bl_)
       throw std::logic_error("ahx_ahmed: leaves from loadmbls are bound to a tree by bind_mbls or the first product");
@@ -217,12 +236,23 @@ void freembls(blcluster* bl, mblock<T>**& A) {
   A = nullptr;
 }
 
+template <class MATGEN_T>
+void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const double*) {
+  check(ahx_assemble(bl->handle(), MatGen.geth(), eps, rankmax));
+  bl->refresh_ranks();
+}
+// mblock<dcomp>: the Helmholtz kernel (apprx_unsym with T = dcomp)
+template <class MATGEN_T>
+void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const dcomp*) {
+  check(ahx_helm_assemble(bl->handle(), MatGen.getk(), MatGen.geth(), eps, rankmax));
+  bl->refresh_zranks();
+}
+
 // Include/matgen_omp.h:197-213: ACA assembly of every leaf (on the GPU)
 template <class T, class MATGEN_T>
 void matgenGeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps, unsigned rankmax,
                    mblock<T>** A) {
-  check(ahx_assemble(bl->handle(), MatGen.geth(), eps, rankmax));
-  bl->refresh_ranks();
+  assemble_leaves(MatGen, bl, eps, rankmax, (const T*)nullptr);
   for (unsigned i = 0; i < nblcks; ++i) {
     delete A[i];
     A[i] = new mblock<T>(bl, i);
@@ -264,6 +294,7 @@ void matgenGeH_sqntl(MATGEN_T& MatGen, blcluster* root, blcluster* bl, bool recm
 // Include/H.h:89-103: the leaves of bl in the reference's file layout
 template <class T>
 void savembls(const double eta, const unsigned bmin, blcluster* bl, mblock<T>**&, std::ofstream& os) {
+  static_assert(std::is_same<T, double>::value, "ahx_ahmed: savembls of mblock<double> leaves");
   auto put = [](void* ctx, void* buf, uint64_t bytes) -> int64_t {
     std::ostream& o = *static_cast<std::ostream*>(ctx);
     o.write(static_cast<const char*>(buf), (std::streamsize)bytes);
@@ -277,6 +308,7 @@ void savembls(const double eta, const unsigned bmin, blcluster* bl, mblock<T>**&
 // built with them is given to bind_mbls or to the first product with A.
 template <class T>
 void loadmbls(double& eta, unsigned& bmin, mblock<T>**& A, std::ifstream& is) {
+  static_assert(std::is_same<T, double>::value, "ahx_ahmed: loadmbls of mblock<double> leaves");
   if (!is) throw std::runtime_error("ahx_ahmed: InputStream not found");
   auto file = std::make_shared<std::string>(std::istreambuf_iterator<char>(is),
                                             std::istreambuf_iterator<char>());
@@ -349,6 +381,36 @@ inline bool mltaGeHhGeM(double d, blcluster* bl, mblock<double>** A, unsigned p,
   return true;
 }
 
+// H/mltaGeHVec.cpp:770-805: the dcomp products of the Helmholtz leaves,
+// op 0: A, 1: A^H, 2: A^T
+inline bool zproduct(int op, dcomp d, blcluster* bl, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+                     unsigned ldY) {
+  check(ahx_helm_matvec(bl->handle(), AHX_FP64, op, d.real(), d.imag(), p, reinterpret_cast<double*>(X), ldX,
+                        reinterpret_cast<double*>(Y), ldY));
+  return true;
+}
+inline bool mltaGeHVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp* y) {
+  return zproduct(0, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHGeM(dcomp d, blcluster* bl, mblock<dcomp>**, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+                       unsigned ldY) {
+  return zproduct(0, d, bl, p, X, ldX, Y, ldY);
+}
+inline bool mltaGeHhVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp* y) {
+  return zproduct(1, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHhGeM(dcomp d, blcluster* bl, mblock<dcomp>**, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+                        unsigned ldY) {
+  return zproduct(1, d, bl, p, X, ldX, Y, ldY);
+}
+inline bool mltaGeHtVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp* y) {
+  return zproduct(2, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHtGeM(dcomp d, blcluster* bl, mblock<dcomp>**, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+                        unsigned ldY) {
+  return zproduct(2, d, bl, p, X, ldX, Y, ldY);
+}
+
 // Include/matrix.h:20-32
 template <class T>
 struct Matrix {
@@ -401,6 +463,29 @@ inline unsigned GMRes(const Matrix<double>& A, double* const b, double* const x,
   uint32_t its = 0;
   double res = 0.0;
   const int rc = ahx_gmres(H->bl->handle(), AHX_FP64, 1, b, A.n, x, A.n, eps, m, nsteps, &its, &res);
+  check(rc);
+  eps = res;
+  nsteps = its;
+  return rc == AHX_OK ? 0u : 1u;
+}
+
+// The Helmholtz H-matrix as a Matrix<dcomp> (complex symmetric: A^T = A)
+struct ZHMatrixOperator : public Matrix<dcomp> {
+  blcluster* bl;
+  explicit ZHMatrixOperator(blcluster* b) : Matrix<dcomp>(b->getn1(), b->getn1()), bl(b) {}
+  void amux(dcomp d, dcomp* x, dcomp* y) const override { mltaGeHVec(d, bl, nullptr, x, y); }
+  void atmux(dcomp d, dcomp* x, dcomp* y) const override { mltaGeHtVec(d, bl, nullptr, x, y); }
+};
+
+// solvers/GMRES.cpp:246: complex GMRes
+inline unsigned GMRes(const Matrix<dcomp>& A, dcomp* const b, dcomp* const x, double& eps, const unsigned m,
+                      unsigned& nsteps) {
+  const ZHMatrixOperator* H = dynamic_cast<const ZHMatrixOperator*>(&A);
+  if (!H) throw std::invalid_argument("ahx_ahmed: complex GMRes runs on a ZHMatrixOperator");
+  uint32_t its = 0;
+  double res = 0.0;
+  const int rc = ahx_helm_gmres(H->bl->handle(), AHX_FP64, 1, reinterpret_cast<const double*>(b), A.n,
+                                reinterpret_cast<double*>(x), A.n, eps, m, nsteps, &its, &res);
   check(rc);
   eps = res;
   nsteps = its;

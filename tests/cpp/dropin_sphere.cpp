@@ -1,8 +1,9 @@
 // The reference's hot-path call sequence (cluster tree, block-cluster tree,
 // allocmbls, matgenGeH_omp, mltaGeHVec, mltaGeHhVec, subdivide_sym, matgenHeH_omp,
-// mltaHeHVec, savembls, loadmbls, GMRes, freembls) compiled against
-// include/ahx_ahmed.hpp.  Checks the product against the dense matrix and
-// GMRES on the diagonal-2/(4 pi h) variant; exit status 0 on success.
+// mltaHeHVec, savembls, loadmbls, GMRes, freembls; with T = double and, for the
+// Helmholtz kernel, T = dcomp) compiled against include/ahx_ahmed.hpp.  Checks
+// the products against the dense matrices and GMRES on well-conditioned
+// variants; exit status 0 on success.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -21,6 +22,12 @@ struct dof {
 struct LaplaceGen {  // the MATGEN_T of this example: K = 1/(4 pi r), diagonal 1/(4 pi h)
   double h;
   double geth() const { return h; }
+};
+
+struct HelmholtzGen {  // mblock<dcomp> leaves: exp(ikr)/(4 pi r), diagonal exp(ikh)/(4 pi h)
+  double h, k;
+  double geth() const { return h; }
+  double getk() const { return k; }
 };
 
 int main(int argc, char** argv) {
@@ -135,6 +142,61 @@ int main(int argc, char** argv) {
   freembls(bl, A);
   delete bl;
 
+  bool helm_ok = false;
+  {  // the Helmholtz matrix with T = dcomp: assembly, A / A^H products, complex GMRes
+    const double k = 5.0;
+    unsigned nz = 0;
+    bemblcluster<dof, dof>* blz = new bemblcluster<dof, dof>(0, 0, N, N);
+    blz->subdivide(cl, cl, eta * eta, nz);
+    mblock<dcomp>** Z;
+    allocmbls(blz, Z);
+    HelmholtzGen hg{h, k};
+    matgenGeH_omp(hg, nz, blz, eps, 1000000, Z);
+    unsigned zlr = 0;
+    for (unsigned l = 0; l < nz; ++l) zlr += Z[l]->isLrM();
+    std::vector<dcomp> zx(N), zy(N, 0.0), zyh(N, 0.0);
+    for (unsigned i = 0; i < N; ++i) zx[i] = dcomp(x[i], std::cos(0.1 * i));
+    mltaGeHVec(dcomp(1.0, 0.0), blz, Z, zx.data(), zy.data());
+    mltaGeHhVec(dcomp(1.0, 0.0), blz, Z, zx.data(), zyh.data());
+    double zn = 0.0, znh = 0.0, zd = 0.0, zdh = 0.0;
+    for (unsigned i = 0; i < N; ++i) {  // dense A x and A^H x (A is complex symmetric)
+      const dof& a = dofs[op_perm[i]];
+      dcomp s = 0.0, sh = 0.0;
+      for (unsigned j = 0; j < N; ++j) {
+        const dof& b = dofs[op_perm[j]];
+        const double dx = a.c[0] - b.c[0], dy = a.c[1] - b.c[1], dz = a.c[2] - b.c[2];
+        const double r = i == j ? h : std::sqrt(dx * dx + dy * dy + dz * dz);
+        const dcomp e = std::exp(dcomp(0.0, k * r)) / (4.0 * M_PI * r);
+        s += e * zx[j];
+        sh += std::conj(e) * zx[j];
+      }
+      zn += std::norm(zy[i] - s);
+      znh += std::norm(zyh[i] - sh);
+      zd += std::norm(s);
+      zdh += std::norm(sh);
+    }
+    const double zerr = std::sqrt(zn / zd), zerrh = std::sqrt(znh / zdh);
+    freembls(blz, Z);
+    delete blz;
+    // complex GMRes with the diagonal of a well-conditioned variant (h_min / 8)
+    bemblcluster<dof, dof>* blg = new bemblcluster<dof, dof>(0, 0, N, N);
+    blg->subdivide(cl, cl, eta * eta, nz);
+    allocmbls(blg, Z);
+    HelmholtzGen hg2{ahx_min_nn(pts.data(), N) / 8.0, k};
+    matgenGeH_omp(hg2, nz, blg, eps, 1000000, Z);
+    ZHMatrixOperator zop(blg);
+    std::vector<dcomp> zb(N), zs(N, 0.0);
+    for (unsigned i = 0; i < N; ++i) zb[i] = dcomp(std::sin(0.37 * i), std::cos(0.11 * i));
+    double zeps = 1e-8;
+    unsigned zsteps = 300;
+    const unsigned zret = GMRes(zop, zb.data(), zs.data(), zeps, 50, zsteps);
+    freembls(blg, Z);
+    delete blg;
+    helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8;
+    std::printf("helmholtz: %u low-rank leaves, product error %.3e, adjoint %.3e, GMRes ret %u eps %.3e steps %u\n",
+                zlr, zerr, zerrh, zret, zeps, zsteps);
+  }
+
   // GMRES on the SPD variant (diagonal 2/(4 pi h))
   bemblcluster<dof, dof>* bl2 = new bemblcluster<dof, dof>(0, 0, N, N);
   bl2->subdivide(cl, cl, eta * eta, nblcks);
@@ -151,5 +213,5 @@ int main(int argc, char** argv) {
   freembls(bl2, A);
   delete bl2;
   delete cl;
-  return (err < 2e-6 && errt < 2e-6 && io_ok && sym_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
+  return (err < 2e-6 && errt < 2e-6 && io_ok && sym_ok && helm_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
 }

@@ -30,3 +30,4 @@ def test_dropin_runs_on_gpu(tmp_path):
     assert "GMRes ret 0" in out.stdout
     assert "savembls/loadmbls round trip ok" in out.stdout
     assert "symmetric:" in out.stdout
+    assert "helmholtz:" in out.stdout
