@@ -323,6 +323,124 @@ __device__ int aca(const G32& g, const HBlk& B, uint32_t i0, uint32_t kmax, uint
   return outcome;
 }
 
+// ACAr_step (ACA.h:579-655) with T = dcomp, the cross of the symmetric assembly:
+// rows are skipped only for a small pivot, the pivot column is searched over all
+// columns, the next row is the largest unused entry of the new column.
+__device__ bool acar_step(const G32& g, const HBlk& B, uint32_t& i0, uint32_t k, uint32_t& no, double& nrmlsk2,
+                          double scale) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  Cx* const pu = B.U + (size_t)k * n1;
+  Cx* const pv = B.V + (size_t)k * n2;
+  ArgMax am;
+  for (;;) {
+    __syncwarp();
+    am = ArgMax{0.0, 0xffffffffu, 0.0};
+    for (uint32_t j = g.rank; j < n2; j += 32) {
+      Cx v = cconj(helm_entry(B, B.b1 + i0, B.b2 + j));
+      for (uint32_t l = 0; l < k; ++l) caxpy(nconj(B.U[(size_t)l * n1 + i0]), B.V[(size_t)l * n2 + j], v);
+      pv[j] = v;
+      const double a = cabs(v);
+      if (gt_nonneg(a, am.v)) am = ArgMax{a, j, 0.0};
+    }
+    am = G32::argmax(am);
+    if (!(am.v < 1e-14 * scale)) break;
+    if (i0 % 32 == g.rank) B.Z[i0] = -1;
+    if (++no >= n1) return false;
+    __syncwarp();
+    i0 = nexti(g, B.Z, n1, i0);
+  }
+  __syncwarp();
+  const uint32_t j0 = am.idx;
+  const double sqrtpiv = sqrt(am.v);
+  const Cx sca = rdiv(sqrtpiv, pv[j0]);
+  __syncwarp();
+  double nrmv2 = 0.0;
+  for (uint32_t j = g.rank; j < n2; j += 32) {
+    Cx e = pv[j];
+    cmul_eq(e, sca);
+    pv[j] = e;
+    nrmv2 += cabs2(e);
+  }
+  for (uint32_t i = g.rank; i < n1; i += 32) {
+    Cx u = helm_entry(B, B.b1 + i, B.b2 + j0);
+    for (uint32_t l = 0; l < k; ++l) caxpy(nconj(B.V[(size_t)l * n2 + j0]), B.U[(size_t)l * n1 + i], u);
+    pu[i] = u;
+  }
+  if (i0 % 32 == g.rank) B.Z[i0] = -1;
+  ++no;
+  __syncwarp();
+  const double dsca = 1.0 / sqrtpiv;
+  double nrmu2 = 0.0;
+  ArgMax nm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t i = g.rank; i < n1; i += 32) {
+    Cx e = pu[i];
+    e.re *= dsca;
+    e.im *= dsca;
+    pu[i] = e;
+    const double ea = cabs(e);
+    nrmu2 += ea * ea;
+    if (B.Z[i] >= 0 && gt_nonneg(ea, nm.v)) nm = ArgMax{ea, i, 0.0};
+  }
+  G32::sum2(nrmu2, nrmv2);
+  nm = G32::argmax(nm);
+  if (nm.v > 0.0) i0 = nm.idx;
+  nrmlsk2 = nrmu2 * nrmv2;
+  return true;
+}
+
+// ACAr (ACA.h:657-720) with T = dcomp: crosses until the last one is below eps of
+// the approximation's norm, no more than n2 rows used, or kmax crosses.
+__device__ int acar(const G32& g, const HBlk& B, uint32_t i0, uint32_t kmax, uint32_t kcap, double eps,
+                    uint32_t& kout) {
+  const uint32_t n1 = B.n1, n2 = B.n2;
+  for (uint32_t i = g.rank; i < n1; i += 32) B.Z[i] = 0;
+  double scale = cabs(helm_entry(B, B.b1, B.b2));
+  uint32_t k = 0, no = 0;
+  double nrmlsk2 = 0.0, nrms2 = 0.0;
+  int outcome = -1;
+  do {
+    if (k >= kcap) {
+      outcome = kAcaOverflow;
+      break;
+    }
+    if (!acar_step(g, B, i0, k, no, nrmlsk2, scale)) {
+      nrmlsk2 = 0.0;
+      break;
+    }
+    __syncwarp();
+    // Re sum_l scpr(U_l, U_k) scpr(V_l, V_k)
+    double sre = 0.0;
+    const Cx* uk = B.U + (size_t)k * n1;
+    const Cx* vk = B.V + (size_t)k * n2;
+    for (uint32_t l = 0; l < k; ++l) {
+      double ur = 0.0, ui = 0.0, vr = 0.0, vi = 0.0;
+      for (uint32_t i = g.rank; i < n1; i += 32) {
+        const Cx a = B.U[(size_t)l * n1 + i], b = uk[i];
+        ur += a.re * b.re + a.im * b.im;
+        ui += a.re * b.im - a.im * b.re;
+      }
+      for (uint32_t j = g.rank; j < n2; j += 32) {
+        const Cx a = B.V[(size_t)l * n2 + j], b = vk[j];
+        vr += a.re * b.re + a.im * b.im;
+        vi += a.re * b.im - a.im * b.re;
+      }
+      G32::sum2(ur, ui);
+      G32::sum2(vr, vi);
+      sre += ur * vr - ui * vi;
+    }
+    nrms2 += 2.0 * sre + nrmlsk2;
+    ++k;
+    scale = sqrt(nrmlsk2 / (double)(uint32_t)(n1 * n2));
+  } while (no < n2 && k < kmax && nrmlsk2 >= eps * eps * nrms2);
+  if (outcome < 0) {
+    const double epsa = sqrt(nrmlsk2 / nrms2);
+    outcome = epsa >= eps ? kAcaFail : kAcaOk;  // NaN (0/0) stays a success, as in the reference
+  }
+  kout = k;
+  __syncwarp();
+  return outcome;
+}
+
 // ---------------------------------------------------------------------------
 // Recompression of a complex low-rank block U V^H (mblock<dcomp>::addtrll,
 // H/mblock_Z.cpp:200-300: QR of U and V, SVD of R1 R2^H after dropping entries
@@ -549,7 +667,7 @@ struct ZTask {
 
 __global__ void __launch_bounds__(32 * kWarps)
     helm_assemble_kernel(PointsSoA P, double k, double h, double eps, const ZTask* __restrict__ tasks, uint32_t n,
-                         Cx* __restrict__ ws, int* __restrict__ zs, AcaResult* __restrict__ res) {
+                         Cx* __restrict__ ws, int* __restrict__ zs, AcaResult* __restrict__ res, int sym) {
   const uint32_t t = blockIdx.x * kWarps + (threadIdx.x >> 5);
   if (t >= n) return;
   const ZTask T = tasks[t];
@@ -568,7 +686,7 @@ __global__ void __launch_bounds__(32 * kWarps)
   B.Z = zs + T.zs;
   B.S = B.Z + T.n1;
   uint32_t kk = 0, kt = 0;
-  const int st = aca(g, B, T.i0, T.kmax, kc, eps, kk);
+  const int st = sym ? acar(g, B, T.i0, T.kmax, kc, eps, kk) : aca(g, B, T.i0, T.kmax, kc, eps, kk);
   if (st == kAcaOk && kk > 0) {
     Cx* Un = B.V + (size_t)T.n2 * kc;
     Cx* Vn = Un + (size_t)T.n1 * kc;
@@ -780,10 +898,6 @@ extern "C" int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, doubl
     set_error("ahx_helm_assemble: invalid argument");
     return AHX_ERR_ARG;
   }
-  if (H->tree.sym) {
-    set_error("ahx_helm_assemble: the Helmholtz matrix is complex symmetric, not Hermitian: use a general block tree");
-    return AHX_ERR_ARG;
-  }
   int rc = ensure_device(H);
   if (rc) return rc;
   ZState& Z = H->z;
@@ -857,7 +971,8 @@ extern "C" int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, doubl
       if ((rc = dres.reserve(batch.size() * sizeof(AcaResult)))) return rc;
       const uint32_t nb = (uint32_t)batch.size();
       helm_assemble_kernel<<<(nb + kWarps - 1) / kWarps, 32 * kWarps, 0, H->stream>>>(
-          P, wavenumber, h, eps, dtasks.as<ZTask>(), nb, ws.as<Cx>(), zs.as<int>(), dres.as<AcaResult>());
+          P, wavenumber, h, eps, dtasks.as<ZTask>(), nb, ws.as<Cx>(), zs.as<int>(), dres.as<AcaResult>(),
+          H->tree.sym ? 1 : 0);
       AHX_CUDA(cudaGetLastError());
       std::vector<AcaResult> res(nb);
       AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, nb * sizeof(AcaResult), cudaMemcpyDeviceToHost, H->stream));
@@ -929,10 +1044,19 @@ extern "C" int ahx_helm_ranks(const ahx_hmat* H, int32_t* ranks) {
   return AHX_OK;
 }
 
+namespace {
+// dense diagonal block of a symmetric tree: stored full, given out packed (SyM)
+bool packed_zleaf(const ahx_hmat* H, uint32_t l) {
+  const Leaf& L = H->tree.leaves[l];
+  return H->tree.sym && H->z.rank[l] < 0 && L.b1 == L.b2;
+}
+}  // namespace
+
 extern "C" uint64_t ahx_helm_leaf_size(const ahx_hmat* H, uint32_t l) {
   if (!H || !H->z.assembled || l >= H->tree.leaves.size()) return 0;
   const Leaf& L = H->tree.leaves[l];
   const int32_t r = H->z.rank[l];
+  if (packed_zleaf(H, l)) return (uint64_t)L.n1 * (L.n1 + 1) / 2;
   return r < 0 ? (uint64_t)L.n1 * L.n2 : (uint64_t)r * (L.n1 + L.n2);
 }
 
@@ -948,6 +1072,18 @@ extern "C" int ahx_helm_get_leaf(const ahx_hmat* H, uint32_t l, double* out) {
   const uint64_t cnt = ahx_helm_leaf_size(H, l);
   if (!cnt) return AHX_OK;
   AHX_CUDA(cudaSetDevice(H->device));
+  if (packed_zleaf(H, l)) {
+    // upper triangle column by column (data[i + j (j + 1) / 2] = A(i, j), i <= j)
+    const uint32_t n1 = H->tree.leaves[l].n1;
+    std::vector<Cx> full((size_t)n1 * n1);
+    AHX_CUDA(cudaMemcpyAsync(full.data(), H->z.arena.as<Cx>() + H->z.off[l], full.size() * sizeof(Cx),
+                             cudaMemcpyDeviceToHost, H->stream));
+    AHX_CUDA(cudaStreamSynchronize(H->stream));
+    Cx* o = reinterpret_cast<Cx*>(out);
+    for (uint32_t j = 0; j < n1; ++j)
+      for (uint32_t i = 0; i <= j; ++i) o[i + (size_t)j * (j + 1) / 2] = full[i + (size_t)j * n1];
+    return AHX_OK;
+  }
   AHX_CUDA(cudaMemcpyAsync(out, H->z.arena.as<Cx>() + H->z.off[l], cnt * sizeof(Cx), cudaMemcpyDeviceToHost,
                            H->stream));
   AHX_CUDA(cudaStreamSynchronize(H->stream));

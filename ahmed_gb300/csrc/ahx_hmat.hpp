@@ -78,13 +78,16 @@ struct ZState {
   bool valid32 = false;
   DevBuf leaves, order;                 // product leaf table, launch order
   uint32_t nleaves = 0;
+  DevBuf tleaves, torder;               // symmetric tree: the off-diagonal leaves, applied transposed
+  uint32_t ntleaves = 0;
   bool table = false;
   DevBuf gm;                            // GMRES workspace
+  DevBuf xc;                            // conjugated right-hand sides (adjoint of a symmetric matrix)
   void release_all() {
-    for (DevBuf* b : {&arena, &arena32, &leaves, &order, &gm}) b->release();
+    for (DevBuf* b : {&arena, &arena32, &leaves, &order, &tleaves, &torder, &gm, &xc}) b->release();
     assembled = valid32 = table = false;
     elems = 0;
-    nleaves = 0;
+    nleaves = ntleaves = 0;
   }
 };
 

@@ -113,15 +113,34 @@ __global__ void zadd_kernel(double2* Y, const double2* X, uint64_t n) {
   }
 }
 
+// Y[:, c] = conj(X[:, c]) (in place when X == Y)
+__global__ void zconj_kernel(const double2* X, uint64_t ldX, double2* Y, uint64_t ldY, uint64_t n, uint32_t p) {
+  const uint64_t total = n * p;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t c = e / n, i = e - c * n;
+    const double2 v = X[c * ldX + i];
+    Y[c * ldY + i] = make_double2(v.x, -v.y);
+  }
+}
+
+// Leaf tables of the complex products; a symmetric tree (complex symmetric
+// matrix, mltaSyHVec_ H/mltaGeHVec.cpp:490-515) adds its off-diagonal leaves a
+// second time, applied transposed.
 int build_ztable(ahx_hmat* H) {
   ZState& Z = H->z;
   if (Z.table) return AHX_OK;
   const auto& Ls = H->tree.leaves;
-  std::vector<PlanLeaf> pls;
-  for (uint32_t l = 0; l < (uint32_t)Ls.size(); ++l)
-    if (Z.rank[l] != 0) pls.push_back(PlanLeaf{Ls[l].b1, Ls[l].n1, Ls[l].b2, Ls[l].n2, Z.rank[l], Z.off[l]});
+  std::vector<PlanLeaf> pls, tls;
+  for (uint32_t l = 0; l < (uint32_t)Ls.size(); ++l) {
+    if (Z.rank[l] == 0) continue;
+    const PlanLeaf q{Ls[l].b1, Ls[l].n1, Ls[l].b2, Ls[l].n2, Z.rank[l], Z.off[l]};
+    pls.push_back(q);
+    if (H->tree.sym && Ls[l].b1 != Ls[l].b2) tls.push_back(q);
+  }
   int rc = upload_leaf_table(H, pls, Z.leaves, Z.order, Z.nleaves);
   if (rc) return rc;
+  Z.ntleaves = 0;
+  if (!tls.empty() && (rc = upload_leaf_table(H, tls, Z.tleaves, Z.torder, Z.ntleaves))) return rc;
   Z.table = true;
   return AHX_OK;
 }
@@ -324,6 +343,22 @@ int zproduct_device(ahx_hmat* H, int prec, int op, double dre, double dim, uint3
                     uint64_t ldX, double2* Y, uint64_t ldY) {
   int rc = prepare_z(H, prec);
   if (rc) return rc;
+  ZState& Z = H->z;
+  if (H->tree.sym && op == kZOpH) {
+    // complex symmetric A: A^H X = conj(A conj(X)) (mltaSyHhVec_, H/mltaGeHVec.cpp:546-555)
+    const uint64_t n = H->tree.n;
+    if ((rc = Z.xc.reserve(std::max<uint64_t>(n * p, 1) * sizeof(double2)))) return rc;
+    double2* Xc = Z.xc.as<double2>();
+    const unsigned grid = zgrid(n * p);
+    zconj_kernel<<<grid, 256, 0, H->stream>>>(X, ldX, Xc, n, n, p);
+    zconj_kernel<<<grid, 256, 0, H->stream>>>(Y, ldY, Y, ldY, n, p);
+    AHX_CUDA(cudaGetLastError());
+    if ((rc = zproduct_device(H, prec, kZOpN, dre, -dim, p, Xc, n, Y, ldY))) return rc;
+    zconj_kernel<<<grid, 256, 0, H->stream>>>(Y, ldY, Y, ldY, n, p);
+    AHX_CUDA(cudaGetLastError());
+    return AHX_OK;
+  }
+  if (H->tree.sym) op = kZOpN;  // A^T = A
   ZArgs a;
   a.leaves = H->z.leaves.as<MvLeaf>();
   a.order = H->z.order.as<uint32_t>();
@@ -339,6 +374,14 @@ int zproduct_device(ahx_hmat* H, int prec, int op, double dre, double dim, uint3
   a.ldY = ldY;
   a.op = op;
   AHX_CUDA(launch_matvec_z(a, H->stream));
+  if (Z.ntleaves) {
+    // the blocks below the diagonal: the upper ones transposed
+    a.leaves = Z.tleaves.as<MvLeaf>();
+    a.order = Z.torder.as<uint32_t>();
+    a.nleaves = Z.ntleaves;
+    a.op = kZOpT;
+    AHX_CUDA(launch_matvec_z(a, H->stream));
+  }
   return AHX_OK;
 }
 

@@ -253,12 +253,15 @@ class HMatrix:
     # -- Helmholtz leaves (mblock<dcomp>) ---------------------------------
     def helmholtz_assemble(self, wavenumber, h=None, eps=1e-6, rankmax=2**32 - 1):
         """The Helmholtz H-matrix exp(ikr)/(4 pi r) (diagonal exp(ikh)/(4 pi h)) on this
-        tree, as the reference's apprx_unsym with T = dcomp (ACA<dcomp> + addtrll).
+        tree, as the reference's apprx_unsym with T = dcomp (ACA<dcomp> + addtrll); on a
+        symmetric handle the complex symmetric form of matgenSyH_omp (ACAr<dcomp>).
         Complex products and GMRes take complex128 arrays (see mltaGeHVec)."""
         self.zh = mean_nn(self.points) if h is None else float(h)
         self.zk = float(wavenumber)
         check(lib().ahx_helm_assemble(self._h, self.zk, self.zh, float(eps), min(int(rankmax), 2**32 - 1)))
         return self
+
+    matgenSyH_omp = helmholtz_assemble
 
     def helm_ranks(self):
         out = np.zeros(self.nleaves, np.int32)
@@ -319,6 +322,10 @@ class HMatrix:
 
     def mltaHeHGeM(self, d, p, X, ldX, Y, ldY, precision="fp64"):
         return self.mltaGeHGeM(d, p, X, ldX, Y, ldY, precision)
+
+    # complex symmetric (Helmholtz leaves of a symmetric handle, H/mltaGeHVec.cpp:885-895)
+    mltaSyHVec = mltaHeHVec
+    mltaSyHGeM = mltaHeHGeM
 
     def mltaGeHtVec(self, d, x, y, precision="fp64"):
         p, ld = _ncols(x, self.n)

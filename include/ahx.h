@@ -121,13 +121,18 @@ int ahx_hmat_autotune(ahx_hmat* H, int precision, uint32_t p, uint32_t* out4);
  * Bounding-box trees (ACA start row 0). */
 int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax,
                        const float* rank_hint, int32_t* ranks);
-/* Helmholtz H-matrix on the handle's (general) block tree: the same kernel and
- * diagonal, assembled as the reference's mblock<dcomp> leaves (apprx_unsym with
- * T = dcomp, Include/apprx.h:136-172: ACA<dcomp> from the leaf's start row i0,
- * recompression mblock<dcomp>::addtrll H/mblock_Z.cpp:200-300, dense leaves
- * from the generator where ACA fails).  Independent of the real assembly of the
- * same handle.  Complex vectors are interleaved (re, im) doubles, the layout of
- * dcomp; leading dimensions count complex elements. */
+/* Helmholtz H-matrix on the handle's block tree: the same kernel and diagonal,
+ * assembled as the reference's mblock<dcomp> leaves.  General tree: apprx_unsym
+ * with T = dcomp (Include/apprx.h:136-172: ACA<dcomp> from the leaf's start row
+ * i0, recompression mblock<dcomp>::addtrll H/mblock_Z.cpp:200-300, dense leaves
+ * from the generator where ACA fails).  Symmetric tree (ahx_hmat_create_sym): the
+ * complex symmetric form of matgenSyH_omp (Include/matgen_omp.h:102-107:
+ * ACAr<dcomp>, dense diagonal blocks symmetric, mblock SyM) whose products are
+ * mltaSyHVec / mltaSyHGeM (H/mltaGeHVec.cpp:490-545, 885-895: upper blocks
+ * applied as A and A^T; A^T = A, A^H = conj(A)); ahx_helm_get_leaf gives those
+ * diagonal blocks packed (upper triangle by columns).  Independent of the real
+ * assembly of the same handle.  Complex vectors are interleaved (re, im)
+ * doubles, the layout of dcomp; leading dimensions count complex elements. */
 int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, double eps, uint32_t rankmax);
 /* per leaf: rank after recompression, -1 for dense leaves */
 int ahx_helm_ranks(const ahx_hmat* H, int32_t* ranks);

@@ -191,9 +191,9 @@ class mblock {
   bool isLrM() const { return bound()->rank_of(idx_, (const T*)nullptr) >= 0; }
   bool isGeM() const { return !isLrM(); }
   // dense diagonal block of a symmetric tree: packed upper triangle (Include/mblock.h:314)
-  bool isHeM() const {
-    return isGeM() && ahx_hmat_symmetric(bound()->handle()) && bound()->leaf(idx_)[0] == bound()->leaf(idx_)[2];
-  }
+  bool isHeM() const { return !std::is_same<T, dcomp>::value && diag_dense(); }
+  // dense diagonal block of a complex symmetric matrix: packed upper triangle (SyM)
+  bool isSyM() const { return std::is_same<T, dcomp>::value && diag_dense(); }
   unsigned rank() const { return (unsigned)bound()->rank_of(idx_, (const T*)nullptr); }
   T* getdata() {
     if (data_.empty()) fetch(bound()->handle(), idx_, data_);
@@ -201,6 +201,9 @@ class mblock {
   }
 
  private:
+  bool diag_dense() const {
+    return isGeM() && ahx_hmat_symmetric(bound()->handle()) && bound()->leaf(idx_)[0] == bound()->leaf(idx_)[2];
+  }
   static void fetch(ahx_hmat* h, unsigned l, std::vector<double>& d) {
     d.resize(ahx_hmat_leaf_size(h, l));
     if (!d.empty()) check(ahx_hmat_get_leaf(h, l, d.data()));
@@ -266,6 +269,17 @@ void matgenHeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps,
                    mblock<T>** A) {
   if (!ahx_hmat_symmetric(bl->handle()))
     throw std::invalid_argument("ahx_ahmed: matgenHeH_omp needs a tree from subdivide_sym");
+  matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);
+}
+
+// Include/matgen_omp.h:102-107: the complex symmetric assembly of a symmetric block
+// tree (ACAr<dcomp>, symmetric dense diagonal blocks)
+template <class T, class MATGEN_T>
+void matgenSyH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps, unsigned rankmax,
+                   mblock<T>** A) {
+  static_assert(std::is_same<T, dcomp>::value, "ahx_ahmed: matgenSyH_omp assembles mblock<dcomp> leaves");
+  if (!ahx_hmat_symmetric(bl->handle()))
+    throw std::invalid_argument("ahx_ahmed: matgenSyH_omp needs a tree from subdivide_sym");
   matgenGeH_omp(MatGen, nblcks, bl, eps, rankmax, A);
 }
 
@@ -409,6 +423,14 @@ inline bool mltaGeHtVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp
 inline bool mltaGeHtGeM(dcomp d, blcluster* bl, mblock<dcomp>**, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
                         unsigned ldY) {
   return zproduct(2, d, bl, p, X, ldX, Y, ldY);
+}
+
+// H/mltaGeHVec.cpp:885-895: y += d A x for a complex symmetric H-matrix (its upper
+// blocks applied as A and A^T)
+inline void mltaSyHVec(dcomp d, blcluster* bl, mblock<dcomp>** A, dcomp* x, dcomp* y) { mltaGeHVec(d, bl, A, x, y); }
+inline void mltaSyHGeM(dcomp d, blcluster* bl, mblock<dcomp>** A, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+                       unsigned ldY) {
+  mltaGeHGeM(d, bl, A, p, X, ldX, Y, ldY);
 }
 
 // Include/matrix.h:20-32

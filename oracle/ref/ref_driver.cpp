@@ -90,6 +90,11 @@ struct HelmGen {
       for (unsigned i = 0; i < n1; ++i) data[i + j * n1] = entry(b1 + i, b2 + j);
   }
   double scale(unsigned b1, unsigned, unsigned b2, unsigned) const { return abs(entry(b1, b2)); }
+  // packed upper triangle of a diagonal block, column by column (symva "U")
+  void cmpblsym(unsigned b1, unsigned n1, dcomp* data) const {
+    for (unsigned j = 0; j < n1; ++j)
+      for (unsigned i = 0; i <= j; ++i) data[i + j * (j + 1) / 2] = entry(b1 + i, b1 + j);
+  }
 };
 
 struct RefH {
@@ -110,7 +115,10 @@ struct RefH {
 struct ZMatrixOp : public Matrix<dcomp> {
   RefH* H;
   explicit ZMatrixOp(RefH* h) : Matrix<dcomp>(h->n, h->n), H(h) {}
-  void amux(dcomp d, dcomp* x, dcomp* y) const { mltaGeHVec(d, H->root_bl, H->Az, x, y); }
+  void amux(dcomp d, dcomp* x, dcomp* y) const {
+    if (H->sym) mltaSyHVec(d, H->root_bl, H->Az, x, y);
+    else mltaGeHVec(d, H->root_bl, H->Az, x, y);
+  }
 };
 
 struct HMatrixOp : public Matrix<double> {
@@ -122,19 +130,20 @@ struct HMatrixOp : public Matrix<double> {
   }
 };
 
-// apprx_sym (Include/apprx.h:86-132) with the ACA start row 0 of bounding-box trees
-template <class MATGEN_T>
-static void apprx_sym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* bl, double eps,
-                          unsigned rankmax) {
+// apprx_sym (Include/apprx.h:86-132) with the ACA start row 0 of bounding-box trees;
+// cmplx_sym: complex symmetric dense diagonal blocks (SyM) instead of Hermitian ones
+template <class T, class MATGEN_T>
+static void apprx_sym_bbx(MATGEN_T& MatGen, mblock<T>*& mbl, blcluster* bl, double eps,
+                          unsigned rankmax, bool cmplx_sym = false) {
   unsigned n1 = bl->getn1(), n2 = bl->getn2();
   unsigned b1 = bl->getb1(), b2 = bl->getb2();
   unsigned maxk = n1 * n2 / (n1 + n2) + 4;
   if (maxk > rankmax) maxk = rankmax;
-  mbl = new mblock<double>(n1, n2);
+  mbl = new mblock<T>(n1, n2);
   bool succ = false;
   if (bl->isadm() && maxk) {
     unsigned k;
-    double *U, *V;
+    T *U, *V;
     succ = ::ACAr(MatGen, b1, n1, b2, n2, eps, maxk, 0u, k, U, V);
     if (succ) mbl->cpyLrM_cmpr(k, U, n1, V, n2, eps, k);
     delete[] V;
@@ -142,7 +151,8 @@ static void apprx_sym_bbx(MATGEN_T& MatGen, mblock<double>*& mbl, blcluster* bl,
   }
   if (!succ) {
     if (bl->isdbl()) {
-      mbl->setHeM();
+      if (cmplx_sym) mbl->setSyM();
+      else mbl->setHeM();
       MatGen.cmpblsym(b1, n1, mbl->getdata());
     } else {
       mbl->setGeM();
@@ -376,7 +386,15 @@ void ref_helm_assemble(void* p, double wavenumber, double h, double eps, unsigne
   std::streambuf* old = std::cout.rdbuf();
   std::ostringstream sink;
   std::cout.rdbuf(sink.rdbuf());
-  if (H->kind == 1) {
+  if (H->sym && H->kind == 1) {
+    matgenSyH_omp(gen, H->nblcks, (bemblcluster<Pt, Pt>*)H->root_bl, eps, rankmax, H->Az);
+  } else if (H->sym) {
+#pragma omp parallel for schedule(dynamic)
+    for (int l = 0; l < (int)H->nblcks; ++l) {
+      blcluster* b = H->leaves[l];
+      apprx_sym_bbx(gen, H->Az[b->getidx()], b, eps, rankmax, true);
+    }
+  } else if (H->kind == 1) {
     matgenGeH_omp(gen, H->nblcks, (bemblcluster<Pt, Pt>*)H->root_bl, eps, rankmax, H->Az);
   } else {
 #pragma omp parallel for schedule(dynamic)
@@ -404,7 +422,8 @@ unsigned long ref_helm_leaf_data(void* p, unsigned l, double* out) {
   blcluster* b = H->leaves[l];
   mblock<dcomp>* m = H->Az[b->getidx()];
   unsigned long cnt = m->isLrM() ? (unsigned long)m->rank() * (b->getn1() + b->getn2())
-                                 : (unsigned long)b->getn1() * b->getn2();
+                   : m->isSyM() ? (unsigned long)b->getn1() * (b->getn1() + 1) / 2
+                                : (unsigned long)b->getn1() * b->getn2();
   if (out && cnt) memcpy(out, m->getdata(), cnt * sizeof(dcomp));
   return cnt;
 }
@@ -416,7 +435,11 @@ void ref_helm_matvec(void* p, int op, double dre, double dim, unsigned nrhs, dou
   const dcomp d(dre, dim);
   dcomp* x = (dcomp*)X;
   dcomp* y = (dcomp*)Y;
-  if (op == 1) mltaGeHhGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
+  if (H->sym) {  // complex symmetric: A^T = A (mltaSyHVec / mltaSyHGeM, H/mltaGeHVec.cpp:885-895)
+    if (op == 1) return;  // the adjoint is not exported for SyH matrices
+    if (nrhs == 1) mltaSyHVec(d, H->root_bl, H->Az, x, y);
+    else mltaSyHGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
+  } else if (op == 1) mltaGeHhGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
   else if (op == 2) mltaGeHtGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);
   else if (nrhs == 1) mltaGeHVec(d, H->root_bl, H->Az, x, y);
   else mltaGeHGeM(d, H->root_bl, H->Az, nrhs, x, H->n, y, H->n);

@@ -178,6 +178,24 @@ int main(int argc, char** argv) {
     const double zerr = std::sqrt(zn / zd), zerrh = std::sqrt(znh / zdh);
     freembls(blz, Z);
     delete blz;
+    // the complex symmetric form on the symmetric tree (matgenSyH_omp, mltaSyHVec)
+    bemblcluster<dof, dof>* bls = new bemblcluster<dof, dof>(0, 0, N, N);
+    unsigned ns = 0;
+    bls->subdivide_sym(cl, eta * eta, ns);
+    allocmbls(bls, Z);
+    matgenSyH_omp(hg, ns, bls, eps, 1000000, Z);
+    unsigned sym_diag = 0;
+    for (unsigned l = 0; l < ns; ++l) sym_diag += Z[l]->isSyM();
+    std::vector<dcomp> zys(N, 0.0);
+    mltaSyHVec(dcomp(1.0, 0.0), bls, Z, zx.data(), zys.data());
+    double zsd = 0.0, zsn = 0.0;
+    for (unsigned i = 0; i < N; ++i) {
+      zsd += std::norm(zys[i] - zy[i]);
+      zsn += std::norm(zy[i]);
+    }
+    const double zserr = std::sqrt(zsd / zsn);
+    freembls(bls, Z);
+    delete bls;
     // complex GMRes with the diagonal of a well-conditioned variant (h_min / 8)
     bemblcluster<dof, dof>* blg = new bemblcluster<dof, dof>(0, 0, N, N);
     blg->subdivide(cl, cl, eta * eta, nz);
@@ -192,9 +210,11 @@ int main(int argc, char** argv) {
     const unsigned zret = GMRes(zop, zb.data(), zs.data(), zeps, 50, zsteps);
     freembls(blg, Z);
     delete blg;
-    helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8;
+    helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8 && sym_diag > 0 && zserr < 5e-6;
     std::printf("helmholtz: %u low-rank leaves, product error %.3e, adjoint %.3e, GMRes ret %u eps %.3e steps %u\n",
                 zlr, zerr, zerrh, zret, zeps, zsteps);
+    std::printf("helmholtz symmetric: %u leaves (%u symmetric diagonal), product vs general %.3e\n", ns, sym_diag,
+                zserr);
   }
 
   // GMRES on the SPD variant (diagonal 2/(4 pi h))

@@ -214,10 +214,15 @@ def aggl():
 
 # Helmholtz H-matrices: the reference's mblock<dcomp> assembly (ACA<dcomp> +
 # addtrll of H/mblock_Z.cpp), its complex products A, A^H, A^T and its complex
-# GMRes.  GMRES cases use h = (smallest point distance) / gm_div: with the mean
-# spacing the collocation matrix is indefinite and GMRES stagnates.
-ZH_CASES = {"zh_fib4096": ("fib4096", O.TREE_BBX, 1, False, 8.0),
-            "zh_ell2500": ("ell2500", O.TREE_PCA, 2, True, 4.0)}
+# GMRes; zhs_*: the complex symmetric form on the symmetric block tree
+# (matgenSyH_omp: ACAr<dcomp>, packed symmetric diagonal blocks; mltaSyHVec /
+# mltaSyHGeM; A^H X = conj(A conj(X)) from the same product).  GMRES cases use
+# h = (smallest point distance) / gm_div: with the mean spacing the collocation
+# matrix is indefinite and GMRES stagnates.
+ZH_CASES = {"zh_fib4096": ("fib4096", O.TREE_BBX, 1, False, 8.0, False),
+            "zh_ell2500": ("ell2500", O.TREE_PCA, 2, True, 4.0, False),
+            "zhs_fib4096": ("fib4096", O.TREE_BBX, 2, True, 8.0, True),
+            "zhs_ell2500": ("ell2500", O.TREE_PCA, 1, True, 4.0, True)}
 ZH_K = 5.0
 ZH_D = complex(0.7, -0.3)
 
@@ -226,7 +231,7 @@ def zhmat():
     if not O.ref_available():
         sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
     from scipy.spatial import cKDTree
-    for name, (base, kind, p, full, gm_div) in ZH_CASES.items():
+    for name, (base, kind, p, full, gm_div, sym) in ZH_CASES.items():
         gen, bmin = CASES[base]
         P = gen()
         n = P.shape[0]
@@ -236,18 +241,23 @@ def zhmat():
         Y0 = rng.standard_normal((p, n)) + 1j * rng.standard_normal((p, n))
         out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
                "eps": np.float64(EPS), "kind": np.int32(kind), "k": np.float64(ZH_K), "d": np.complex128(ZH_D),
-               "X": X, "Y0": Y0}
-        R = O.RefH(P, kind, bmin, ETA, h)
+               "X": X, "Y0": Y0, "sym": np.bool_(sym)}
+        R = O.RefH(P, kind, bmin, ETA, h, sym=sym)
         out["leaves"] = R.leaves()
         out["op_perm"] = R.perm()[0]
         R.helm_assemble(ZH_K, h, EPS, nthreads=1)
         out["ranks"] = R.helm_ranks()
         for op in (0, 1, 2):
             Y = Y0.copy()
-            R.helm_matvec(X, Y, d=ZH_D, op=op)
+            if sym and op == 1:
+                T = np.zeros_like(Y0)
+                R.helm_matvec(np.ascontiguousarray(X.conj()), T, d=1.0, op=0)
+                Y += ZH_D * T.conj()
+            else:
+                R.helm_matvec(X, Y, d=ZH_D, op=op)
             out[f"Y_op{op}"] = Y
+        L = out["leaves"]
         if full:  # factors (U then V) of 40 low-rank leaves spread over the leaf list
-            L = out["leaves"]
             size = (L[:, 1].astype(np.int64) + L[:, 3]) * out["ranks"]
             lr = np.flatnonzero((out["ranks"] >= 0) & (size <= 2048))
             pick = lr[np.linspace(0, lr.size - 1, min(40, lr.size)).astype(int)]
@@ -257,9 +267,14 @@ def zhmat():
             out["data_leaves"] = pick.astype(np.uint32)
             out["data"] = np.concatenate(chunks)
             out["offsets"] = offs
+        if sym:  # packed symmetric diagonal blocks (mblock SyM data) of three dense leaves
+            dd = np.flatnonzero((out["ranks"] < 0) & (L[:, 0] == L[:, 2]))[:3]
+            out["sym_leaves"] = dd.astype(np.uint32)
+            for q, l in enumerate(dd):
+                out[f"sym_data{q}"] = R.helm_leaf_data(int(l))
         dd, _ = cKDTree(P).query(P, 2)
         gh = float(dd[:, 1].min()) / gm_div
-        G2 = O.RefH(P, kind, bmin, ETA, gh)
+        G2 = O.RefH(P, kind, bmin, ETA, gh, sym=sym)
         G2.helm_assemble(ZH_K, gh, EPS, nthreads=1)
         b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
         x = np.zeros(n, np.complex128)

@@ -31,3 +31,4 @@ def test_dropin_runs_on_gpu(tmp_path):
     assert "savembls/loadmbls round trip ok" in out.stdout
     assert "symmetric:" in out.stdout
     assert "helmholtz:" in out.stdout
+    assert "helmholtz symmetric:" in out.stdout

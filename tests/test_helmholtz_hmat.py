@@ -3,15 +3,16 @@
 Fixtures (tests/golden/make_golden.py zhmat) hold the reference's own results
 with T = dcomp: the mblock<dcomp> ranks of every leaf after ACA<dcomp> and
 addtrll, Y0 + d op(A) X for its mltaGeHGeM / mltaGeHhGeM / mltaGeHtGeM, the
-factors of 40 low-rank leaves, and the solution of its complex GMRes.  The CPU
-tests pin the fixtures to the dense complex matrix; the GPU tests compare the
-library with them."""
+factors of 40 low-rank leaves, and the solution of its complex GMRes; zhs_*:
+the complex symmetric form on the symmetric block tree (matgenSyH_omp: ACAr,
+packed symmetric diagonal blocks; mltaSyHGeM).  The CPU tests pin the fixtures
+to the dense complex matrix; the GPU tests compare the library with them."""
 import numpy as np
 import pytest
 
 import ahmed_gb300 as A
 
-CASES = ["zh_fib4096", "zh_ell2500"]
+CASES = ["zh_fib4096", "zh_ell2500", "zhs_fib4096", "zhs_ell2500"]
 TREE = {0: "bbx", 1: "pca"}
 
 
@@ -56,9 +57,15 @@ def test_fixture_leaves(golden, name):
     r = g["ranks"]
     assert np.all(r[L[:, 4] == 0] == -1)  # inadmissible leaves are dense
     assert (r >= 0).sum() > 0
+    M = dense(g, float(g["h"]))
+    for q, l in enumerate(g.get("sym_leaves", [])):  # packed upper triangles
+        b1, n1 = int(L[l, 0]), int(L[l, 1])
+        iu = np.triu_indices(n1)
+        want = M[b1:b1 + n1, b1:b1 + n1].T[np.tril_indices(n1)]  # column by column, rows <= column
+        assert rel(g[f"sym_data{q}"], want) < 1e-14
+        assert iu[0].size == g[f"sym_data{q}"].size
     if "data" not in g:
         return
-    M = dense(g, float(g["h"]))
     for q, l in enumerate(g["data_leaves"]):
         b1, n1, b2, n2 = (int(v) for v in L[l, :4])
         k = int(r[l])
@@ -72,7 +79,8 @@ def test_fixture_leaves(golden, name):
 @pytest.mark.parametrize("name", CASES)
 def test_fixture_trees_match(golden, name):
     g = golden(name)
-    H = A.HMatrix(g["points"], TREE[int(g["kind"])], bmin=int(g["bmin"]), eta=float(g["eta"]))
+    H = A.HMatrix(g["points"], TREE[int(g["kind"])], bmin=int(g["bmin"]), eta=float(g["eta"]),
+                  symmetric=bool(g["sym"]))
     np.testing.assert_array_equal(H.leaves(), g["leaves"])
     np.testing.assert_array_equal(H.perm()[0], g["op_perm"])
     H.close()
@@ -80,7 +88,8 @@ def test_fixture_trees_match(golden, name):
 
 # ---------------------------------------------------------------- GPU
 def _hmat(g, h=None):
-    H = A.HMatrix(g["points"], TREE[int(g["kind"])], bmin=int(g["bmin"]), eta=float(g["eta"]))
+    H = A.HMatrix(g["points"], TREE[int(g["kind"])], bmin=int(g["bmin"]), eta=float(g["eta"]),
+                  symmetric=bool(g["sym"]))
     H.helmholtz_assemble(float(g["k"]), float(g["h"] if h is None else h), float(g["eps"]))
     return H
 
@@ -108,6 +117,8 @@ def test_ranks_match_reference(golden, name):
         Ug, Vg = mine[:n1 * kg].reshape(kg, n1).T, mine[n1 * kg:].reshape(kg, n2).T
         want = Ur @ Vr.conj().T
         assert rel(Ug @ Vg.conj().T, want) < 1e-5, l
+    for q, l in enumerate(g.get("sym_leaves", [])):  # packed symmetric diagonal blocks
+        assert rel(H.helm_leaf_data(int(l)), g[f"sym_data{q}"]) < 1e-14
     H.close()
 
 
@@ -219,7 +230,6 @@ def test_errors(golden):
     H.helmholtz_assemble(float(g["k"]), float(g["h"]), float(g["eps"]))
     assert lib().ahx_helm_matvec(H.handle, 2, 0, 1.0, 0.0, 1, ptr(X), H.n, ptr(Y), H.n) == AHX_ERR_ARG  # bf16
     assert lib().ahx_helm_matvec(H.handle, 0, 3, 1.0, 0.0, 1, ptr(X), H.n, ptr(Y), H.n) == AHX_ERR_ARG  # op
+    assert lib().ahx_helm_assemble(H.handle, 5.0, -1.0, 1e-6, 2**32 - 1) == AHX_ERR_ARG  # h <= 0
+    assert lib().ahx_helm_assemble(H.handle, float("nan"), 1.0, 1e-6, 2**32 - 1) == AHX_ERR_ARG
     H.close()
-    S = A.HMatrix(g["points"], "pca", bmin=int(g["bmin"]), eta=float(g["eta"]), symmetric=True)
-    assert lib().ahx_helm_assemble(S.handle, 5.0, float(g["h"]), 1e-6, 2**32 - 1) == AHX_ERR_ARG
-    S.close()
