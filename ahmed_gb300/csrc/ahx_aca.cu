@@ -703,6 +703,202 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   return kt;
 }
 
+// Recompression of a wide union by a whole CTA (agglomeration).  The steps of
+// recompress up to R = R1 R2^T (QR of both factors, small entries dropped), then
+// a column-pivoted Householder QR of R that stops once the trailing columns'
+// Frobenius norm is at most 1e-2 delta max_j |R(:, j)| (<= 1e-2 delta sigma_0,
+// so no singular value moves by more than that), then one-sided Jacobi on the
+// transpose of the kept rows: rr columns instead of nmin, and the pivoted
+// triangle converges in fewer sweeps.  R = Qr T P^T, T^T Z = W S gives
+// R = (Qr Z) S (P W)^T.  Workspaces (column-major, stride ld): R (mmin x nmin,
+// later the reflectors), Tt (nmin x rr), Z (rr x rr); cn, qtau: nmin doubles;
+// cperm: nmin ints; perm: rr + 1 ints.
+template <int G, class Grp>
+__device__ uint32_t recompress_qrcp(const Grp& g, uint32_t n1, uint32_t n2, uint32_t k, double* U, double* V,
+                                    double* Un, double* Vn, double delta, double* R, double* Tt, double* Z,
+                                    uint32_t ld, double* sig, double* tau, double* cn, double* qtau, int* cperm,
+                                    int* perm) {
+  if (k == 0) return 0;
+  constexpr uint32_t NW = G / 32;
+  const uint32_t warp = g.rank >> 5, lane = g.rank & 31;
+  const uint32_t mmin = min(n1, k), nmin = min(n2, k), amin = min(mmin, nmin);
+  double* tau1 = tau;
+  double* tau2 = tau + k;
+  group_qr<G>(g, n1, k, U, tau1);
+  group_qr<G>(g, n2, k, V, tau2);
+  g.sync();
+  double fro = 0.0;
+  for (uint32_t i = g.rank; i < mmin; i += G) {
+    for (uint32_t j = 0; j < nmin; ++j) {
+      double d = 0.0;
+      for (uint32_t l = max(i, j); l < k; ++l) d += U[i + (size_t)l * n1] * V[j + (size_t)l * n2];
+      R[i + (size_t)j * ld] = d;
+      fro += d * d;
+    }
+  }
+  fro = g.sum(fro);
+  const double thresh = delta * sqrt(fro) / (double)sqrtf((float)mmin * (float)nmin);
+  for (uint32_t i = g.rank; i < mmin; i += G)
+    for (uint32_t j = 0; j < nmin; ++j)
+      if (fabs(R[i + (size_t)j * ld]) < thresh) R[i + (size_t)j * ld] = 0.0;
+  g.sync();
+  // column norms
+  for (uint32_t j = warp; j < nmin; j += NW) {
+    double s = 0.0;
+    for (uint32_t i = lane; i < mmin; i += 32) {
+      const double x = R[i + (size_t)j * ld];
+      s += x * x;
+    }
+    s = Group<32>::sum(s);
+    if (lane == 0) {
+      cn[j] = s;
+      cperm[j] = (int)j;
+    }
+  }
+  g.sync();
+  ArgMax cm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t j = g.rank; j < nmin; j += G)
+    if (gt_nonneg(cn[j], cm.v)) cm = ArgMax{cn[j], j, 0.0};
+  cm = g.argmax(cm);
+  const double tol2 = (1e-2 * delta) * (1e-2 * delta) * cm.v;
+  // column-pivoted QR, stopped at the trailing norm tol
+  uint32_t rr = amin;
+  for (uint32_t c = 0; c < amin; ++c) {
+    double tot = 0.0;
+    ArgMax am{0.0, 0xffffffffu, 0.0};
+    for (uint32_t j = c + g.rank; j < nmin; j += G) {
+      const double v = cn[j];
+      tot += v;
+      if (gt_nonneg(v, am.v)) am = ArgMax{v, j, 0.0};
+    }
+    tot = g.sum(tot);
+    am = g.argmax(am);
+    if (tot <= tol2 || am.idx >= nmin) {
+      rr = c;
+      break;
+    }
+    const uint32_t p = am.idx;
+    if (p != c) {
+      for (uint32_t i = g.rank; i < mmin; i += G) {
+        const double x = R[i + (size_t)c * ld];
+        R[i + (size_t)c * ld] = R[i + (size_t)p * ld];
+        R[i + (size_t)p * ld] = x;
+      }
+      if (g.rank == 0) {
+        const double x = cn[c];
+        cn[c] = cn[p];
+        cn[p] = x;
+        const int q = cperm[c];
+        cperm[c] = cperm[p];
+        cperm[p] = q;
+      }
+    }
+    g.sync();
+    double* a = R + (size_t)c * ld;
+    double xn2 = 0.0, alpha = 0.0;
+    for (uint32_t i = g.rank; i < mmin; i += G) {
+      if (i > c) xn2 += a[i] * a[i];
+      else if (i == c) alpha = a[i];
+    }
+    g.sum2(xn2, alpha);
+    double t = 0.0;
+    if (xn2 != 0.0) {
+      const double nrm = sqrt(alpha * alpha + xn2);
+      const double beta = alpha >= 0.0 ? -nrm : nrm;
+      t = (beta - alpha) / beta;
+      const double sc = 1.0 / (alpha - beta);
+      for (uint32_t i = g.rank; i < mmin; i += G) {
+        if (i > c) a[i] *= sc;
+        else if (i == c) a[i] = beta;
+      }
+    }
+    if (g.rank == 0) qtau[c] = t;
+    g.sync();
+    // the trailing columns: b -= t v (v^T b), then their norms below row c
+    for (uint32_t j = c + 1 + warp; j < nmin; j += NW) {
+      double* b = R + (size_t)j * ld;
+      if (t != 0.0) {
+        double s = 0.0;
+        for (uint32_t i = c + lane; i < mmin; i += 32) s += (i == c ? 1.0 : a[i]) * b[i];
+        s = Group<32>::sum(s) * t;
+        for (uint32_t i = c + lane; i < mmin; i += 32) b[i] -= s * (i == c ? 1.0 : a[i]);
+      }
+      double s2 = 0.0;
+      for (uint32_t i = c + lane; i < mmin; i += 32)
+        if (i > c) s2 += b[i] * b[i];
+      s2 = Group<32>::sum(s2);
+      if (lane == 0) cn[j] = s2;
+    }
+    g.sync();
+  }
+  // Tt = T^T (T = the first rr rows of the triangle, pivoted column order), Z = I
+  for (uint32_t e = g.rank; e < nmin * rr; e += G) {
+    const uint32_t i = e / nmin, j = e - i * nmin;
+    Tt[j + (size_t)i * ld] = j >= i ? R[i + (size_t)j * ld] : 0.0;
+  }
+  for (uint32_t e = g.rank; e < rr * rr; e += G) {
+    const uint32_t i = e % rr, j = e / rr;
+    Z[i + (size_t)j * ld] = i == j ? 1.0 : 0.0;
+  }
+  g.sync();
+  if (rr > 1) jacobi_cta(nmin, rr, Tt, Z, ld);
+  for (uint32_t j = warp; j < rr; j += NW) {
+    double s = 0.0;
+    for (uint32_t i = lane; i < nmin; i += 32) {
+      const double x = Tt[i + (size_t)j * ld];
+      s += x * x;
+    }
+    s = Group<32>::sum(s);
+    if (lane == 0) sig[j] = sqrt(s);
+  }
+  g.sync();
+  if (g.rank == 0) {
+    for (uint32_t j = 0; j < rr; ++j) perm[j] = (int)j;
+    for (uint32_t j = 0; j < rr; ++j) {
+      uint32_t b = j;
+      for (uint32_t q = j + 1; q < rr; ++q)
+        if (sig[perm[q]] > sig[perm[b]]) b = q;
+      const int t = perm[j];
+      perm[j] = perm[b];
+      perm[b] = t;
+    }
+    uint32_t kt = rr;
+    const double s0 = rr ? sig[perm[0]] : 0.0;
+    while (kt > 0 && (sig[perm[kt - 1]] <= delta * s0 || sig[perm[kt - 1]] < 1e-64)) --kt;
+    perm[rr] = (int)kt;
+  }
+  g.sync();
+  const uint32_t kt = (uint32_t)perm[rr];
+  // Un = Q1 [Qr [Z(:, p) s_p; 0]; 0],  Vn = Q2 [P W(:, p); 0]
+  for (uint32_t j = 0; j < kt; ++j) {
+    const int pj = perm[j];
+    const double sj = sig[pj];
+    for (uint32_t i = g.rank; i < n1; i += G) Un[i + (size_t)j * n1] = i < rr ? Z[i + (size_t)pj * ld] * sj : 0.0;
+    for (uint32_t i = g.rank; i < n2; i += G) {
+      if (i < nmin) Vn[(uint32_t)cperm[i] + (size_t)j * n2] = Tt[i + (size_t)pj * ld] / sj;
+      else Vn[i + (size_t)j * n2] = 0.0;
+    }
+  }
+  g.sync();
+  for (int c = (int)rr - 1; c >= 0; --c) {
+    const double t = qtau[c];
+    if (t != 0.0) {
+      const double* a = R + (size_t)c * ld;
+      for (uint32_t j = warp; j < kt; j += NW) {
+        double* b = Un + (size_t)j * n1;
+        double s = 0.0;
+        for (uint32_t i = (uint32_t)c + lane; i < mmin; i += 32) s += (i == (uint32_t)c ? 1.0 : a[i]) * b[i];
+        s = Group<32>::sum(s) * t;
+        for (uint32_t i = (uint32_t)c + lane; i < mmin; i += 32) b[i] -= s * (i == (uint32_t)c ? 1.0 : a[i]);
+      }
+    }
+    g.sync();
+  }
+  group_apply_q<G>(g, n1, mmin, U, tau1, kt, Un);
+  group_apply_q<G>(g, n2, nmin, V, tau2, kt, Vn);
+  return kt;
+}
+
 template <int G, class Grp>
 __device__ void aca_task(const Grp& g, const AcaParams& p, uint32_t ti, double* smem) {
   const AcaTask t = p.tasks[ti];
@@ -771,7 +967,16 @@ __device__ void merge_task(const Grp& g, const MergeParams& p, uint32_t ti, doub
     double* tau = sm ? smem + 2 * KSM * LDS + KSM : taug;
     int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : p.zs + t.zs;
     g.sync();
-    kt = recompress<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau, perm, !sm);
+    if (G > 32 && !sm) {
+      // a CTA on a wide union: pivoted QR first; Z, cn, qtau, cperm follow tau
+      double* Z = taug + 2 * (size_t)kc;
+      double* cn = Z + (size_t)kc * kc;
+      double* qtau = cn + kc;
+      int* cperm = reinterpret_cast<int*>(qtau + kc);
+      kt = recompress_qrcp<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, Z, kc, sig, tau, cn, qtau, cperm, perm);
+    } else {
+      kt = recompress<G>(g, m, n, kc, U, V, Un, Vn, p.eps, R, Vs, sm ? LDS : kc, sig, tau, perm, !sm);
+    }
   }
   if (g.rank == 0) p.res[ti] = AcaResult{kAcaOk, kc, kt, 0u};
 }
