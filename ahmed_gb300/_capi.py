@@ -77,6 +77,10 @@ SIGNATURES = [
     ("ahx_helm_get_leaf", _i32, [_vp, _u32, _vp]),
     ("ahx_helm_storage_bytes", _u64, [_vp, _i32]),
     ("ahx_helm_matvec", _i32, [_vp, _i32, _i32, _dbl, _dbl, _u32, _vp, _u64, _vp, _u64]),
+    ("ahx_helm_save", _i32, [_vp, _dbl, _u32, C.c_char_p]),
+    ("ahx_helm_load", _i32, [_vp, C.c_char_p, _vp, _vp]),
+    ("ahx_helm_save_stream", _i32, [_vp, _dbl, _u32, _vp, _vp]),
+    ("ahx_helm_load_stream", _i32, [_vp, _vp, _vp, _vp, _vp]),
     ("ahx_helm_gmres", _i32, [_vp, _i32, _u32, _vp, _u64, _vp, _u64, _dbl, _u32, _u32, _vp, _vp]),
     ("ahx_mlp_nparams", _u32, []),
     ("ahx_mlp_create", _i32, [_i32, _u64, _vp]),

@@ -851,7 +851,6 @@ extern "C" int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, doub
 }
 
 namespace ahx {
-namespace {
 
 // Append-only growable complex arena of the Helmholtz leaves.
 int zarena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
@@ -888,6 +887,7 @@ int zarena_append(ahx_hmat* H, uint64_t count, uint64_t& off) {
   return AHX_OK;
 }
 
+namespace {
 uint64_t zws_elems(const ZTask& t) { return aca_ws_doubles(t.n1, t.n2, t.kcap); }
 
 }  // namespace

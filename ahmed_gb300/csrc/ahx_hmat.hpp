@@ -172,6 +172,8 @@ void invalidate_products(ahx_hmat* H);
 int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X, uint64_t ldX,
                    double* Y, uint64_t ldY, bool transposed = false);
 bool is_device_ptr(const void* p);
+// Reserves count complex elements at the end of the Helmholtz leaf arena (ahx_aca_helm.cu).
+int zarena_append(ahx_hmat* H, uint64_t count, uint64_t& off);
 // Leaf table of a product in descending cost order (ahx_capi.cu)
 int upload_leaf_table(ahx_hmat* H, const std::vector<PlanLeaf>& pls, DevBuf& leaves, DevBuf& order, uint32_t& n);
 // Helmholtz leaves: Y += d op(A) X on device pointers (prec kFP64: complex128

@@ -113,13 +113,19 @@ int64_t file_read(void* ctx, void* buf, uint64_t bytes) {
   return (int64_t)std::fread(buf, 1, bytes, static_cast<std::FILE*>(ctx));
 }
 
-int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
-  if (!H->assembled) {
+// cplx: the Helmholtz leaves (mblock<dcomp>: two doubles per element; packed
+// symmetric diagonal blocks are status 5, SyM) instead of the real ones.
+int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w, bool cplx) {
+  if (!(cplx ? H->z.assembled : H->assembled)) {
     set_error("not assembled");
     return AHX_ERR_STATE;
   }
   int rc = ensure_device(H);
   if (rc) return rc;
+  const std::vector<int32_t>& Rk = cplx ? H->z.rank : H->rank;
+  const std::vector<uint64_t>& Of = cplx ? H->z.off : H->off;
+  const uint64_t ew = cplx ? 2 : 1;  // doubles per element
+  const double* arena = cplx ? H->z.arena.as<double>() : H->arena64.as<double>();
   const auto& Ls = H->tree.leaves;
   const uint32_t nl = (uint32_t)Ls.size();
   w.put_val<double>(eta);
@@ -129,7 +135,7 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
   // chunks of consecutive leaves, at most `cap` doubles each (a larger leaf gets its own)
   uint64_t total = 0, largest = 0;
   for (uint32_t l = 0; l < nl; ++l) {
-    const uint64_t c = leaf_count(Ls[l], H->rank[l]);
+    const uint64_t c = leaf_count(Ls[l], Rk[l]) * ew;
     total += c;
     largest = std::max(largest, c);
   }
@@ -140,13 +146,13 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
   {
     uint64_t fill = 0;
     for (uint32_t l = 0; l < nl; ++l) {
-      const uint64_t c = leaf_count(Ls[l], H->rank[l]);
+      const uint64_t c = leaf_count(Ls[l], Rk[l]) * ew;
       if (fill + c > cap && fill > 0) {
         first.push_back(l);
         task0.push_back((uint32_t)tasks.size());
         fill = 0;
       }
-      if (c) tasks.push_back(Gather{H->off[l], fill, c});
+      if (c) tasks.push_back(Gather{Of[l] * ew, fill, c});
       fill += c;
     }
     first.push_back(nl);
@@ -172,8 +178,7 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
     if (nt) {
       const Gather& last = tasks[task0[c + 1] - 1];
       bytes = (last.dst + last.count) * sizeof(double);
-      gather_leaves_kernel<<<nt, 256, 0, H->stream>>>(H->arena64.as<double>(),
-                                                      dtasks.b.as<Gather>() + task0[c], dst);
+      gather_leaves_kernel<<<nt, 256, 0, H->stream>>>(arena, dtasks.b.as<Gather>() + task0[c], dst);
       AHX_CUDA(cudaGetLastError());
       AHX_CUDA(cudaMemcpyAsync(host[b].p, dst, bytes, cudaMemcpyDeviceToHost, H->stream));
     }
@@ -187,8 +192,8 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
     uint64_t pos = 0;
     for (uint32_t l = first[c]; l < first[c + 1]; ++l) {
       const Leaf& L = Ls[l];
-      const int32_t r = H->rank[l];
-      const uint64_t cnt = leaf_count(L, r);
+      const int32_t r = Rk[l];
+      const uint64_t cnt = leaf_count(L, r) * ew;
       w.put_val<uint8_t>(1);
       w.put_val<uint32_t>(L.n1);
       w.put_val<uint32_t>(L.n2);
@@ -197,9 +202,11 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
         w.put_val<uint32_t>((uint32_t)r);
         w.put(data + pos, cnt * sizeof(double));
       } else if (H->tree.sym && L.b1 == L.b2) {
-        // Hermitian diagonal block of a symmetric tree: packed upper triangle
-        w.put_val<uint32_t>(kStatusHerm);
-        for (uint32_t j = 0; j < L.n1; ++j) w.put(data + pos + (uint64_t)j * L.n1, (uint64_t)(j + 1) * sizeof(double));
+        // diagonal block of a symmetric tree: packed upper triangle (Hermitian for
+        // real leaves, complex symmetric for the Helmholtz ones)
+        w.put_val<uint32_t>(cplx ? kStatusSym : kStatusHerm);
+        for (uint32_t j = 0; j < L.n1; ++j)
+          w.put(data + pos + (uint64_t)j * L.n1 * ew, (uint64_t)(j + 1) * ew * sizeof(double));
       } else {
         w.put_val<uint32_t>(kStatusDense);
         w.put(data + pos, cnt * sizeof(double));
@@ -226,6 +233,7 @@ int save_impl(ahx_hmat* H, double eta, uint32_t bmin, Writer& w) {
 // Stages leaf data in leaf order into pinned buffers and uploads them into the arena.
 struct Stager {
   ahx_hmat* H;
+  bool cplx;  // the Helmholtz arena (offsets in doubles: two per element)
   uint64_t cap;
   Pinned buf[2];
   Event ev[2];
@@ -244,8 +252,8 @@ struct Stager {
   }
   int flush() {
     if (fill) {
-      AHX_CUDA(cudaMemcpyAsync(H->arena64.as<double>() + base, buf[cur].p, fill * sizeof(double),
-                               cudaMemcpyHostToDevice, H->stream));
+      double* arena = cplx ? H->z.arena.as<double>() : H->arena64.as<double>();
+      AHX_CUDA(cudaMemcpyAsync(arena + base, buf[cur].p, fill * sizeof(double), cudaMemcpyHostToDevice, H->stream));
       AHX_CUDA(cudaEventRecord(ev[cur].e, H->stream));
       used[cur] = true;
       base += fill;
@@ -267,7 +275,7 @@ struct Stager {
   }
 };
 
-int load_impl(ahx_hmat* H, Reader& rd, double* eta_out, uint32_t* bmin_out) {
+int load_impl(ahx_hmat* H, Reader& rd, double* eta_out, uint32_t* bmin_out, bool cplx) {
   double eta = 0.0;
   uint32_t bmin = 0, nfile = 0;
   if (!rd.get(&eta, sizeof eta) || !rd.get(&bmin, sizeof bmin) || !rd.get(&nfile, sizeof nfile)) {
@@ -283,19 +291,29 @@ int load_impl(ahx_hmat* H, Reader& rd, double* eta_out, uint32_t* bmin_out) {
   }
   int rc = ensure_device(H);
   if (rc) return rc;
-  invalidate_products(H);
-  H->assembled = false;
-  H->h = H->eps = 0.0;
-  H->arena64_elems = 0;
+  const uint64_t ew = cplx ? 2 : 1;  // doubles per element
   // capacity estimate: dense inadmissible leaves plus 16 columns per admissible leaf
   uint64_t est = 0;
   for (const Leaf& L : Ls)
     est += L.adm ? (uint64_t)(L.n1 + L.n2) * 16 : (uint64_t)L.n1 * L.n2;
-  H->arena64.release();
-  if ((rc = H->arena64.reserve(std::max<uint64_t>(est, 1) * sizeof(double)))) return rc;
+  if (cplx) {
+    ZState& Z = H->z;
+    Z.assembled = Z.valid32 = Z.table = false;
+    Z.k = Z.h = Z.eps = 0.0;
+    Z.elems = 0;
+    Z.arena.release();
+    if ((rc = Z.arena.reserve(std::max<uint64_t>(est, 1) * ew * sizeof(double)))) return rc;
+  } else {
+    invalidate_products(H);
+    H->assembled = false;
+    H->h = H->eps = 0.0;
+    H->arena64_elems = 0;
+    H->arena64.release();
+    if ((rc = H->arena64.reserve(std::max<uint64_t>(est, 1) * sizeof(double)))) return rc;
+  }
   std::vector<int32_t> rank(nl, 0);
   std::vector<uint64_t> off(nl, 0);
-  Stager st{H};
+  Stager st{H, cplx};
   if ((rc = st.init(std::min(io_chunk(), std::max<uint64_t>(est, 1 << 16))))) return rc;
   std::vector<double> packed, full;
   auto fail = [&](const std::string& msg) {
@@ -329,20 +347,24 @@ int load_impl(ahx_hmat* H, Reader& rd, double* eta_out, uint32_t* bmin_out) {
     // a missing block (present = 0) is a zero block: rank 0
     const bool dense = present && status != kStatusLowRank;
     rank[l] = dense ? -1 : (int32_t)r;
-    const uint64_t cnt = dense ? (uint64_t)n1 * n2 : (uint64_t)r * (n1 + n2);
-    if ((rc = arena_append(H, cnt, off[l]))) return rc;
+    const uint64_t cnt_el = dense ? (uint64_t)n1 * n2 : (uint64_t)r * (n1 + n2);
+    const uint64_t cnt = cnt_el * ew;  // doubles
+    if ((rc = cplx ? zarena_append(H, cnt_el, off[l]) : arena_append(H, cnt_el, off[l]))) return rc;
     if (dense && status != kStatusDense) {
-      // expand the packed upper triangle (real data: Hermitian = symmetric)
-      packed.resize((uint64_t)n1 * (n1 + 1) / 2);
+      // expand the packed upper triangle: symmetric (SyM; real Hermitian), or
+      // Hermitian for complex data (the mirror conjugated)
+      const bool conj = cplx && status == kStatusHerm;
+      packed.resize((uint64_t)n1 * (n1 + 1) / 2 * ew);
       if (!rd.get(packed.data(), packed.size() * sizeof(double)))
         return fail(std::to_string(l) + ": truncated");
       full.assign(cnt, 0.0);
       for (uint32_t j = 0; j < n1; ++j)
-        for (uint32_t i = 0; i <= j; ++i) {
-          const double v = packed[i + (uint64_t)j * (j + 1) / 2];
-          full[i + (uint64_t)j * n1] = v;
-          full[j + (uint64_t)i * n1] = v;
-        }
+        for (uint32_t i = 0; i <= j; ++i)
+          for (uint64_t c = 0; c < ew; ++c) {
+            const double v = packed[(i + (uint64_t)j * (j + 1) / 2) * ew + c];
+            full[(i + (uint64_t)j * n1) * ew + c] = v;
+            if (i != j) full[(j + (uint64_t)i * n1) * ew + c] = conj && c == 1 ? -v : v;
+          }
       for (uint64_t done = 0; done < cnt;) {
         double* p;
         uint64_t got;
@@ -364,10 +386,17 @@ int load_impl(ahx_hmat* H, Reader& rd, double* eta_out, uint32_t* bmin_out) {
   }
   if ((rc = st.flush())) return rc;
   AHX_CUDA(cudaStreamSynchronize(H->stream));
-  H->rank = rank;
-  H->aca_rank = rank;
-  H->off = off;
-  H->assembled = true;
+  if (cplx) {
+    H->z.rank = rank;
+    H->z.aca_rank = rank;
+    H->z.off = off;
+    H->z.assembled = true;
+  } else {
+    H->rank = rank;
+    H->aca_rank = rank;
+    H->off = off;
+    H->assembled = true;
+  }
   if (eta_out) *eta_out = eta;
   if (bmin_out) *bmin_out = bmin;
   return AHX_OK;
@@ -402,19 +431,10 @@ int ahx_mbls_header(const char* path, double* eta, uint32_t* bmin, uint32_t* nle
   return AHX_OK;
 }
 
-int ahx_hmat_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx) {
-  if (!H || !write) return AHX_ERR_ARG;
-  Writer w{write, ctx};
-  return save_impl(H, eta, bmin, w);
-}
+}  // extern "C"
 
-int ahx_hmat_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin) {
-  if (!H || !read) return AHX_ERR_ARG;
-  Reader rd{read, ctx};
-  return load_impl(H, rd, eta, bmin);
-}
-
-int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path) {
+namespace {
+int save_path(ahx_hmat* H, double eta, uint32_t bmin, const char* path, bool cplx) {
   if (!H || !path) return AHX_ERR_ARG;
   std::FILE* f = std::fopen(path, "wb");
   if (!f) {
@@ -424,7 +444,7 @@ int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path) {
   std::vector<char> iobuf(1 << 20);
   std::setvbuf(f, iobuf.data(), _IOFBF, iobuf.size());
   Writer w{file_write, f};
-  int rc = save_impl(H, eta, bmin, w);
+  int rc = save_impl(H, eta, bmin, w, cplx);
   if (std::fclose(f) != 0 && rc == AHX_OK) {
     set_error("savembls: write failed");
     rc = AHX_ERR_ARG;
@@ -432,7 +452,7 @@ int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path) {
   return rc;
 }
 
-int ahx_hmat_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin) {
+int load_path(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin, bool cplx) {
   if (!H || !path) return AHX_ERR_ARG;
   std::FILE* f = std::fopen(path, "rb");
   if (!f) {
@@ -442,9 +462,52 @@ int ahx_hmat_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin) {
   std::vector<char> iobuf(1 << 20);
   std::setvbuf(f, iobuf.data(), _IOFBF, iobuf.size());
   Reader rd{file_read, f};
-  const int rc = load_impl(H, rd, eta, bmin);
+  const int rc = load_impl(H, rd, eta, bmin, cplx);
   std::fclose(f);
   return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int ahx_hmat_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx) {
+  if (!H || !write) return AHX_ERR_ARG;
+  Writer w{write, ctx};
+  return save_impl(H, eta, bmin, w, false);
+}
+
+int ahx_hmat_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin) {
+  if (!H || !read) return AHX_ERR_ARG;
+  Reader rd{read, ctx};
+  return load_impl(H, rd, eta, bmin, false);
+}
+
+int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path) {
+  return save_path(H, eta, bmin, path, false);
+}
+
+int ahx_hmat_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin) {
+  return load_path(H, path, eta, bmin, false);
+}
+
+int ahx_helm_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx) {
+  if (!H || !write) return AHX_ERR_ARG;
+  Writer w{write, ctx};
+  return save_impl(H, eta, bmin, w, true);
+}
+
+int ahx_helm_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin) {
+  if (!H || !read) return AHX_ERR_ARG;
+  Reader rd{read, ctx};
+  return load_impl(H, rd, eta, bmin, true);
+}
+
+int ahx_helm_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path) {
+  return save_path(H, eta, bmin, path, true);
+}
+
+int ahx_helm_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin) {
+  return load_path(H, path, eta, bmin, true);
 }
 
 }  // extern "C"

@@ -275,6 +275,18 @@ class HMatrix:
             check(lib().ahx_helm_get_leaf(self._h, l, ptr(out)))
         return out
 
+    def helm_save(self, path, eta=None, bmin=None):
+        """savembls of the Helmholtz (mblock<dcomp>) leaves in the reference's layout."""
+        eta = self.eta if eta is None else float(eta)
+        bmin = self.bmin if bmin is None else int(bmin)
+        check(lib().ahx_helm_save(self._h, eta, bmin, os.fsencode(path)))
+
+    def helm_load(self, path):
+        """loadmbls of mblock<dcomp> leaves into this tree; returns the file's (eta, bmin)."""
+        eta, bmin = C.c_double(), C.c_uint32()
+        check(lib().ahx_helm_load(self._h, os.fsencode(path), C.byref(eta), C.byref(bmin)))
+        return eta.value, bmin.value
+
     def helm_storage_bytes(self, precision="fp64"):
         return lib().ahx_helm_storage_bytes(self._h, _prec(precision))
 

@@ -209,6 +209,14 @@ int ahx_hmat_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path);
 int ahx_hmat_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin);
 int ahx_hmat_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx);
 int ahx_hmat_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin);
+/* The same for the Helmholtz leaves (savembls / loadmbls of mblock<dcomp>: every
+ * element two doubles, re and im; a symmetric tree's dense diagonal blocks are
+ * written packed with status 5, SyM).  Loading fills the handle's Helmholtz
+ * leaves; packed status-1 records load as Hermitian blocks, status 5 as symmetric. */
+int ahx_helm_save(ahx_hmat* H, double eta, uint32_t bmin, const char* path);
+int ahx_helm_load(ahx_hmat* H, const char* path, double* eta, uint32_t* bmin);
+int ahx_helm_save_stream(ahx_hmat* H, double eta, uint32_t bmin, ahx_io_fn write, void* ctx);
+int ahx_helm_load_stream(ahx_hmat* H, ahx_io_fn read, void* ctx, double* eta, uint32_t* bmin);
 
 /* Restarted GMRES(m) for p right-hand sides (each with its own Krylov space),
  * right-preconditioner free.  Replaces GMRes(A, b, x, eps, m, nsteps)

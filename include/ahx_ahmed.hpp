@@ -306,15 +306,21 @@ void matgenGeH_sqntl(MATGEN_T& MatGen, blcluster* root, blcluster* bl, bool recm
 }
 
 // Include/H.h:89-103: the leaves of bl in the reference's file layout
+inline int save_leaves(blcluster* bl, double eta, unsigned bmin, ahx_io_fn put, void* ctx, const double*) {
+  return ahx_hmat_save_stream(bl->handle(), eta, bmin, put, ctx);
+}
+inline int save_leaves(blcluster* bl, double eta, unsigned bmin, ahx_io_fn put, void* ctx, const dcomp*) {
+  return ahx_helm_save_stream(bl->handle(), eta, bmin, put, ctx);
+}
+
 template <class T>
 void savembls(const double eta, const unsigned bmin, blcluster* bl, mblock<T>**&, std::ofstream& os) {
-  static_assert(std::is_same<T, double>::value, "ahx_ahmed: savembls of mblock<double> leaves");
   auto put = [](void* ctx, void* buf, uint64_t bytes) -> int64_t {
     std::ostream& o = *static_cast<std::ostream*>(ctx);
     o.write(static_cast<const char*>(buf), (std::streamsize)bytes);
     return o ? (int64_t)bytes : -1;
   };
-  check(ahx_hmat_save_stream(bl->handle(), eta, bmin, put, &os));
+  check(save_leaves(bl, eta, bmin, put, &os, (const T*)nullptr));
 }
 
 // Include/H.h:60-73 ("loadmbls does not need allocmbls"): eta and bmin come
@@ -322,7 +328,6 @@ void savembls(const double eta, const unsigned bmin, blcluster* bl, mblock<T>**&
 // built with them is given to bind_mbls or to the first product with A.
 template <class T>
 void loadmbls(double& eta, unsigned& bmin, mblock<T>**& A, std::ifstream& is) {
-  static_assert(std::is_same<T, double>::value, "ahx_ahmed: loadmbls of mblock<double> leaves");
   if (!is) throw std::runtime_error("ahx_ahmed: InputStream not found");
   auto file = std::make_shared<std::string>(std::istreambuf_iterator<char>(is),
                                             std::istreambuf_iterator<char>());
@@ -334,6 +339,15 @@ void loadmbls(double& eta, unsigned& bmin, mblock<T>**& A, std::ifstream& is) {
   bmin = b;
   A = new mblock<T>*[n];
   for (uint32_t i = 0; i < n; ++i) A[i] = new mblock<T>(file, i);
+}
+
+inline void load_leaves(blcluster* bl, ahx_io_fn get, void* ctx, const double*) {
+  check(ahx_hmat_load_stream(bl->handle(), get, ctx, nullptr, nullptr));
+  bl->refresh_ranks();
+}
+inline void load_leaves(blcluster* bl, ahx_io_fn get, void* ctx, const dcomp*) {
+  check(ahx_helm_load_stream(bl->handle(), get, ctx, nullptr, nullptr));
+  bl->refresh_zranks();
 }
 
 // Uploads leaves read by loadmbls into bl (no-op for leaves already bound).
@@ -351,8 +365,7 @@ void bind_mbls(blcluster* bl, mblock<T>** A) {
     c.pos += m;
     return (int64_t)m;
   };
-  check(ahx_hmat_load_stream(bl->handle(), get, &src, nullptr, nullptr));
-  bl->refresh_ranks();
+  load_leaves(bl, get, &src, (const T*)nullptr);
   for (unsigned long i = 0; i < bl->nleaves(); ++i) A[i]->attach(bl);
 }
 
@@ -403,11 +416,13 @@ inline bool zproduct(int op, dcomp d, blcluster* bl, unsigned p, dcomp* X, unsig
                         reinterpret_cast<double*>(Y), ldY));
   return true;
 }
-inline bool mltaGeHVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp* y) {
+inline bool mltaGeHVec(dcomp d, blcluster* bl, mblock<dcomp>** A, dcomp* x, dcomp* y) {
+  bind_mbls(bl, A);
   return zproduct(0, d, bl, 1, x, bl->getn1(), y, bl->getn1());
 }
-inline bool mltaGeHGeM(dcomp d, blcluster* bl, mblock<dcomp>**, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
+inline bool mltaGeHGeM(dcomp d, blcluster* bl, mblock<dcomp>** A, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
                        unsigned ldY) {
+  bind_mbls(bl, A);
   return zproduct(0, d, bl, p, X, ldX, Y, ldY);
 }
 inline bool mltaGeHhVec(dcomp d, blcluster* bl, mblock<dcomp>**, dcomp* x, dcomp* y) {

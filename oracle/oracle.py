@@ -205,6 +205,8 @@ def ref():
         L.ref_helm_leaf_data.restype = C.c_ulong
         L.ref_helm_leaf_data.argtypes = [vp, u32, vp]
         L.ref_helm_matvec.argtypes = [vp, i32, dbl, dbl, u32, vp, vp]
+        L.ref_helm_save.restype = i32
+        L.ref_helm_save.argtypes = [vp, dbl, u32, C.c_char_p]
         L.ref_helm_gmres.restype = u32
         L.ref_helm_gmres.argtypes = [vp, vp, vp, vp, u32, vp]
         _ref = L
@@ -321,3 +323,8 @@ class RefH:
         ns = C.c_uint(nsteps)
         r = ref().ref_helm_gmres(self._H, _p(b), _p(x), C.byref(e), m, C.byref(ns))
         return r, e.value, ns.value
+
+    def helm_savembls(self, eta, bmin, path):
+        """The reference's own savembls of the Helmholtz (mblock<dcomp>) leaves."""
+        if ref().ref_helm_save(self._H, eta, bmin, os.fsencode(path)) != 0:
+            raise RuntimeError("ref_helm_save failed")

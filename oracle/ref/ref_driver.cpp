@@ -461,6 +461,16 @@ unsigned ref_helm_gmres(void* p, double* b, double* x, double* eps, unsigned m, 
   return r;
 }
 
+// The reference's savembls (Include/H.h:89-103) of the Helmholtz (mblock<dcomp>) leaves
+int ref_helm_save(void* p, double eta, unsigned bmin, const char* path) {
+  RefH* H = (RefH*)p;
+  if (!H->Az) return 1;
+  std::ofstream os(path, std::ios::binary);
+  if (!os) return 1;
+  savembls(eta, bmin, H->root_bl, H->Az, os);
+  return os.good() ? 0 : 1;
+}
+
 // The reference's agglomeration agglH (H/agglH.cpp:253-272) of the assembled
 // leaves; the leaf list is rebuilt in DFS order (indices as agglH left them).
 void ref_agglomerate(void* p, double eps, unsigned rankmax) {

@@ -176,6 +176,30 @@ int main(int argc, char** argv) {
       zdh += std::norm(sh);
     }
     const double zerr = std::sqrt(zn / zd), zerrh = std::sqrt(znh / zdh);
+    bool zio_ok = false;
+    {  // savembls / loadmbls of the mblock<dcomp> leaves
+      {
+        std::ofstream os("dropin_helm.mbls", std::ios::binary);
+        savembls(eta, bmin, blz, Z, os);
+      }
+      double eta_f = 0.0;
+      unsigned bmin_f = 0, nb = 0;
+      mblock<dcomp>** ZB = nullptr;
+      std::ifstream is("dropin_helm.mbls", std::ios::binary);
+      loadmbls(eta_f, bmin_f, ZB, is);
+      bemblcluster<dof, dof>* bl4 = new bemblcluster<dof, dof>(0, 0, N, N);
+      bl4->subdivide(cl, cl, eta_f * eta_f, nb);
+      std::vector<dcomp> zy4(N, 0.0);
+      mltaGeHVec(dcomp(1.0, 0.0), bl4, ZB, zx.data(), zy4.data());
+      double d4 = 0.0, n4 = 0.0;
+      for (unsigned i = 0; i < N; ++i) {
+        d4 += std::norm(zy4[i] - zy[i]);
+        n4 += std::norm(zy[i]);
+      }
+      zio_ok = nb == nz && ZB[0]->rank() == Z[0]->rank() && std::sqrt(d4 / n4) < 1e-14;
+      freembls(bl4, ZB);
+      delete bl4;
+    }
     freembls(blz, Z);
     delete blz;
     // the complex symmetric form on the symmetric tree (matgenSyH_omp, mltaSyHVec)
@@ -210,11 +234,13 @@ int main(int argc, char** argv) {
     const unsigned zret = GMRes(zop, zb.data(), zs.data(), zeps, 50, zsteps);
     freembls(blg, Z);
     delete blg;
-    helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8 && sym_diag > 0 && zserr < 5e-6;
+    helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8 && sym_diag > 0 && zserr < 5e-6 &&
+              zio_ok;
     std::printf("helmholtz: %u low-rank leaves, product error %.3e, adjoint %.3e, GMRes ret %u eps %.3e steps %u\n",
                 zlr, zerr, zerrh, zret, zeps, zsteps);
     std::printf("helmholtz symmetric: %u leaves (%u symmetric diagonal), product vs general %.3e\n", ns, sym_diag,
                 zserr);
+    std::printf("helmholtz savembls/loadmbls round trip %s\n", zio_ok ? "ok" : "FAILED");
   }
 
   // GMRES on the SPD variant (diagonal 2/(4 pi h))

@@ -11,6 +11,7 @@ Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py aggl       (agglomeration, agglH)
         python tests/golden/make_golden.py zhmat      (Helmholtz H-matrix: complex assembly,
                                                        products, GMRes)
+        python tests/golden/make_golden.py zmbls      (savembls files of mblock<dcomp> leaves)
 """
 import os
 import sys
@@ -289,6 +290,31 @@ def zhmat():
               f" gmres {ns} steps {e:.2e}")
 
 
+def zmbls():
+    """The reference's own savembls files of mblock<dcomp> leaves (Helmholtz, k = 5) on a
+    200-point sphere (PCA trees, leaf 6), general and symmetric (status 5 SyM blocks)."""
+    import tempfile
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    P = G.sphere_surface(200, 11)
+    bmin, h = 6, O.mean_nn(P)
+    out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+           "eps": np.float64(EPS), "k": np.float64(ZH_K)}
+    for sym, tag in ((False, "gen"), (True, "sym")):
+        R = O.RefH(P, O.TREE_PCA, bmin, ETA, h, sym=sym)
+        R.helm_assemble(ZH_K, h, EPS, nthreads=1)
+        out[f"{tag}_leaves"] = R.leaves()
+        out[f"{tag}_op_perm"] = R.perm()[0]
+        out[f"{tag}_ranks"] = R.helm_ranks()
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "A.mbls")
+            R.helm_savembls(ETA, bmin, path)
+            out[f"{tag}_file"] = np.frombuffer(open(path, "rb").read(), np.uint8)
+    path = os.path.join(HERE, "zmbls_sph200.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
@@ -300,5 +326,7 @@ if __name__ == "__main__":
         aggl()
     elif len(sys.argv) > 1 and sys.argv[1] == "zhmat":
         zhmat()
+    elif len(sys.argv) > 1 and sys.argv[1] == "zmbls":
+        zmbls()
     else:
         main()

@@ -42,9 +42,11 @@ def write(path, eta, bmin, leaves, ranks, data, offsets, packed=(), absent=()):
                 f.write(d.tobytes())
 
 
-def read(path):
-    """Returns (eta, bmin, records); record = None (absent) or (n1, n2, status, rank, data)."""
+def read(path, dtype=np.float64):
+    """Returns (eta, bmin, records); record = None (absent) or (n1, n2, status, rank, data).
+    dtype: the leaves' element type (np.complex128 for mblock<dcomp>)."""
     raw = open(path, "rb").read()
+    esz = np.dtype(dtype).itemsize
     eta, bmin, n = struct.unpack_from("<dII", raw, 0)
     pos = 16
     recs = []
@@ -65,7 +67,7 @@ def read(path):
             cnt = n1 * n2
         else:
             cnt = n1 * (n1 + 1) // 2
-        d = np.frombuffer(raw, np.float64, cnt, pos)
-        pos += 8 * cnt
+        d = np.frombuffer(raw, dtype, cnt, pos)
+        pos += esz * cnt
         recs.append((n1, n2, status, rank, d))
     return eta, bmin, recs

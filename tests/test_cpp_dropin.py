@@ -32,3 +32,4 @@ def test_dropin_runs_on_gpu(tmp_path):
     assert "symmetric:" in out.stdout
     assert "helmholtz:" in out.stdout
     assert "helmholtz symmetric:" in out.stdout
+    assert "helmholtz savembls/loadmbls round trip ok" in out.stdout
