@@ -703,7 +703,7 @@ __device__ uint32_t recompress(const Grp& g, uint32_t n1, uint32_t n2, uint32_t 
   return kt;
 }
 
-// Recompression of a wide union by a whole CTA (agglomeration).  The steps of
+// Recompression of a wide union (agglomeration) by a warp or a whole CTA.  The steps of
 // recompress up to R = R1 R2^T (QR of both factors, small entries dropped), then
 // a column-pivoted Householder QR of R that stops once the trailing columns'
 // Frobenius norm is at most 1e-2 delta max_j |R(:, j)| (<= 1e-2 delta sigma_0,
@@ -967,8 +967,8 @@ __device__ void merge_task(const Grp& g, const MergeParams& p, uint32_t ti, doub
     double* tau = sm ? smem + 2 * KSM * LDS + KSM : taug;
     int* perm = sm ? reinterpret_cast<int*>(smem + 2 * KSM * LDS + 3 * KSM) : p.zs + t.zs;
     g.sync();
-    if (G > 32 && !sm) {
-      // a CTA on a wide union: pivoted QR first; Z, cn, qtau, cperm follow tau
+    if (!sm) {
+      // k x k beyond shared memory: pivoted QR first; Z, cn, qtau, cperm follow tau
       double* Z = taug + 2 * (size_t)kc;
       double* cn = Z + (size_t)kc * kc;
       double* qtau = cn + kc;

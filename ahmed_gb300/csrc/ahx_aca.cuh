@@ -72,9 +72,9 @@ struct MirrorTask {
 cudaError_t launch_mirror(const MirrorTask* tasks, uint32_t ntasks, double* arena, cudaStream_t s);
 
 // Agglomeration: recompression of merged sibling blocks.  Workspace at `ws`
-// (doubles, aca_ws_doubles(m, n, k), plus merge_qrcp_doubles(k) for the tasks of
-// the one-CTA kernel): U (m x k) and V (n x k) hold the gathered factors; Un, Vn
-// receive the result; `zs` (ints): m + n + 1 scratch.
+// (doubles, aca_ws_doubles(m, n, k) + merge_qrcp_doubles(k)): U (m x k) and V
+// (n x k) hold the gathered factors; Un, Vn receive the result; `zs` (ints):
+// m + n + 1 scratch.
 inline uint64_t merge_qrcp_doubles(uint32_t k) { return (uint64_t)k * k + 3ull * k; }
 struct MergeTask {
   uint32_t m, n, k, pad;

@@ -212,7 +212,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
             k += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
           }
           kmax_round = std::max<uint64_t>(kmax_round, k);
-          const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + (large ? merge_qrcp_doubles(k) : 0);
+          const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
           if (!tasks.empty() && (wsz + need) * sizeof(double) > budget) break;
           MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
           // U = [U00 U01 0 0; 0 0 U10 U11], V = [V00 0 V10 0; 0 V01 0 V11]; a dense

@@ -596,6 +596,76 @@ def run_helmholtz(args):
     print(json.dumps(out))
 
 
+def run_zhmat(args):
+    """The Helmholtz H-matrix (mblock<dcomp> leaves) on `--n` random sphere points (seed 17),
+    k = 16.2, leaf 32, eta 0.8, eps 1e-6 (`--symmetric`: the complex symmetric form on the
+    symmetric tree): complex assembly; products with complex128 and complex64 leaves at 16
+    and 1 RHS (`--warmup` + `--steps`, CUDA events); complex GMRES(50) to 1e-8 with
+    h = smallest nearest-neighbour distance / 8, one RHS b ~ N(0,1) + i N(0,1) (seed 12),
+    complex128 leaves and complex64 leaves with FP64 refinement."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    P = A.geometry.sphere_surface(args.n, 17)
+    k = 16.2
+    H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA, symmetric=args.symmetric)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H.helmholtz_assemble(k, A.mean_nn(P), EPS)
+    torch.cuda.synchronize()
+    zr = H.helm_ranks()
+    out = {"workload": f"helmholtz-sphere-{args.n}" + ("-sym" if args.symmetric else ""), "k": k,
+           "assembly_s": time.perf_counter() - t0, "low_rank_leaves": int((zr >= 0).sum()),
+           "mean_rank": float(zr[zr >= 0].mean()) if (zr >= 0).any() else 0.0,
+           "complex128_bytes": int(H.helm_storage_bytes("fp64")), "complex64_bytes": int(H.helm_storage_bytes("fp32"))}
+    peak, _ = _peaks()
+    rng = np.random.default_rng(11)
+    for p in (16, 1):
+        X = torch.from_numpy(rng.standard_normal((p, H.n)) + 1j * rng.standard_normal((p, H.n))).to(dev)
+        ys = {}
+        for prec in ("fp64", "fp32"):
+            Y = torch.zeros_like(X)
+            for _ in range(args.warmup):
+                H.mltaGeHVec(1.0, X, Y, precision=prec)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                H.mltaGeHVec(1.0, X, Y, precision=prec)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            Y.zero_()
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+            ys[prec] = Y.cpu().numpy()
+            byts = H.helm_storage_bytes(prec) + p * H.n * 16 * 3
+            out[f"{prec}_{p}rhs"] = {"ms": ms, "algorithmic_bytes": int(byts), "achieved_gbs": byts / (ms * 1e-3) / 1e9,
+                                     "frac_of_hbm": byts / (ms * 1e-3) / 1e9 / peak}
+        err = np.linalg.norm(ys["fp32"] - ys["fp64"], axis=1) / np.linalg.norm(ys["fp64"], axis=1)
+        out[f"fp32_err_{p}rhs"] = float(err.max())
+    H.close()
+    # GMRES on the well-conditioned variant
+    gh = A.min_nn(P) / 8.0
+    G = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA, symmetric=args.symmetric)
+    G.helmholtz_assemble(k, gh, EPS)
+    b = np.random.default_rng(12).standard_normal(G.n) + 1j * np.random.default_rng(13).standard_normal(G.n)
+    for prec in ("fp64", "fp32"):
+        x = np.zeros_like(b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, res, its = G.GMRes(b, x, 1e-8, 50, 2000, precision=prec)
+        t_s = time.perf_counter() - t0
+        r = b.copy()
+        G.mltaGeHVec(-1.0, x, r)  # r = b - A x with the complex128 leaves
+        out[f"gmres_{prec}"] = {"s": t_s, "converged": st == 0, "iters": int(its[0]),
+                                "true_resid": float(np.linalg.norm(r) / np.linalg.norm(b))}
+    G.close()
+    print(json.dumps(out))
+
+
 def run_batch(args):
     """Many uneven H-matrices in one launch: `--instances` instances (256), N log-uniform
     in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
@@ -670,7 +740,8 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="1: tune the stream bucketing before timing")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz",
+                             "zhmat"],
                     help="sphere: the default product benchmark; cube-large: N = 2^20 "
                          "cube surface, 64 right-hand sides, products and GMRES; batch: "
                          "256 uneven instances, one launch per product, batched GMRES")
@@ -679,7 +750,7 @@ def main():
     ap.add_argument("--leaf", type=int, default=BMIN, help="product workload")
     ap.add_argument("--rhs", type=int, default=NRHS, help="product workload")
     ap.add_argument("--symmetric", action="store_true",
-                    help="product workload: symmetric block tree, HeH assembly (upper blocks once)")
+                    help="product / zhmat workloads: symmetric block tree (upper blocks once)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp64", "df64"], help="product workload")
     ap.add_argument("--n-large", type=int, default=1 << 20)
     ap.add_argument("--diag", default="mean", choices=["mean", "min"],
@@ -706,6 +777,8 @@ def main():
         run_predictor(args)
     elif args.workload == "helmholtz":
         run_helmholtz(args)
+    elif args.workload == "zhmat":
+        run_zhmat(args)
     else:
         run_gpu(args)
 
