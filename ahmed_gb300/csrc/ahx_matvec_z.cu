@@ -76,8 +76,8 @@ __device__ __forceinline__ void emit(const ZArgs& a, uint32_t r0, uint32_t pg, u
 template <typename S, typename R, int PG, int OP>
 __global__ void __launch_bounds__(kThreads) zmv_kernel(ZArgs a) {
   __shared__ C2<R> Xs[kCh][PG];
-  __shared__ C2<R> Ts[kThreads];  // kThreads / PG columns x PG right-hand sides
-  __shared__ C2<R> red[kThreads];
+  __shared__ C2<R> Ts[kThreads];       // kThreads / PG columns x PG right-hand sides
+  __shared__ C2<R> red[kThreads * PG];  // per-slice partial inner products
   const MvLeaf L = a.leaves[a.order[blockIdx.x]];
   const S* base = reinterpret_cast<const S*>(a.arena) + L.off;
   const uint32_t tid = threadIdx.x;
@@ -120,11 +120,13 @@ __global__ void __launch_bounds__(kThreads) zmv_kernel(ZArgs a) {
       constexpr uint32_t kKt = kThreads / PG;
       for (uint32_t lb = 0; lb < k; lb += kKt) {
         const uint32_t kn = min(kKt, k - lb);
-        const uint32_t nout = kn * PG;       // <= kThreads
-        const uint32_t ns = kThreads / nout;  // threads per output
-        const uint32_t sub = tid / nout, o = tid % nout;
-        const uint32_t l = o / PG, r = o % PG;
-        C2<R> t{(R)0, (R)0};
+        // thread = (column l, row slice sub): each factor entry is loaded once and
+        // multiplied with all PG right-hand sides; the slices are summed in order
+        const uint32_t ns = kThreads / kn;
+        const uint32_t l = tid % kn, sub = tid / kn;
+        C2<R> t[PG];
+#pragma unroll
+        for (int r = 0; r < PG; ++r) t[r] = C2<R>{(R)0, (R)0};
         for (uint32_t jb = 0; jb < nc; jb += kCh) {
           const uint32_t jn = min((uint32_t)kCh, nc - jb);
           __syncthreads();
@@ -132,16 +134,24 @@ __global__ void __launch_bounds__(kThreads) zmv_kernel(ZArgs a) {
           __syncthreads();
           if (sub < ns) {
             const S* qc = Q + (uint64_t)(lb + l) * nc + jb;
-            for (uint32_t j = sub; j < jn; j += ns) cfma(t, ldz(qc + j, kConjQ), Xs[j][r]);
+            for (uint32_t j = sub; j < jn; j += ns) {
+              const C2<R> q = ldz(qc + j, kConjQ);
+#pragma unroll
+              for (int r = 0; r < PG; ++r) cfma(t[r], q, Xs[j][r]);
+            }
           }
         }
-        red[tid] = t;
+        if (sub < ns) {
+#pragma unroll
+          for (int r = 0; r < PG; ++r) red[(sub * kn + l) * PG + r] = t[r];
+        }
         __syncthreads();
-        if (tid < nout) {
-          C2<R> s = red[tid];
+        if (tid < kn * PG) {
+          const uint32_t l2 = tid / PG, r2 = tid % PG;
+          C2<R> s = red[l2 * PG + r2];
           for (uint32_t q = 1; q < ns; ++q) {
-            s.re += red[tid + q * nout].re;
-            s.im += red[tid + q * nout].im;
+            s.re += red[(q * kn + l2) * PG + r2].re;
+            s.im += red[(q * kn + l2) * PG + r2].im;
           }
           Ts[tid] = s;  // Ts[l * PG + r]
         }
