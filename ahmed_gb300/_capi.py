@@ -81,6 +81,7 @@ SIGNATURES = [
     ("ahx_helm_load", _i32, [_vp, C.c_char_p, _vp, _vp]),
     ("ahx_helm_save_stream", _i32, [_vp, _dbl, _u32, _vp, _vp]),
     ("ahx_helm_load_stream", _i32, [_vp, _vp, _vp, _vp, _vp]),
+    ("ahx_helm_agglomerate", _i32, [_vp, _dbl, _u32, _vp]),
     ("ahx_helm_gmres", _i32, [_vp, _i32, _u32, _vp, _u64, _vp, _u64, _dbl, _u32, _u32, _vp, _vp]),
     ("ahx_mlp_nparams", _u32, []),
     ("ahx_mlp_create", _i32, [_i32, _u64, _vp]),

@@ -994,7 +994,8 @@ __global__ void copy2d_kernel(const Seg2D* __restrict__ segs, const double* __re
                               double* __restrict__ dst) {
   const Seg2D s = segs[blockIdx.x];
   if (s.src == kSegIdentity) {
-    for (uint32_t c = threadIdx.x; c < s.ncols; c += blockDim.x) dst[s.dst + (uint64_t)c * s.ld_dst + c] = 1.0;
+    for (uint32_t c = threadIdx.x; c < s.ncols; c += blockDim.x)
+      dst[s.dst + (uint64_t)c * s.ld_dst + (uint64_t)c * (1 + s.cplx)] = 1.0;
     return;
   }
   const uint64_t cnt = (uint64_t)s.nrows * s.ncols;

@@ -90,12 +90,17 @@ struct MergeParams {
 };
 // large: one CTA per task (m or n above 4096), else one warp
 cudaError_t launch_merge(const MergeParams& p, bool large, cudaStream_t s);
+// Complex unions (ahx_aca_helm.cu): the same tasks and workspace layout in complex
+// elements (MergeParams::ws holds them as interleaved doubles), one warp per union.
+cudaError_t launch_zmerge(const MergeParams& p, cudaStream_t s);
 // dst[s.dst + c * ld_dst + r] = src[s.src + c * nrows + r], r < nrows, c < ncols;
-// src == kSegIdentity: ones on the diagonal (r == c) of the zeroed destination
+// src == kSegIdentity: ones on the diagonal (r == c) of the zeroed destination,
+// at dst[s.dst + c * ld_dst + c * (1 + cplx)] (cplx = 1: the real parts of a
+// complex identity stored as interleaved doubles)
 constexpr uint64_t kSegIdentity = ~0ull;
 struct Seg2D {
   uint64_t src, dst;
-  uint32_t nrows, ncols, ld_dst, pad;
+  uint32_t nrows, ncols, ld_dst, cplx;
 };
 cudaError_t launch_copy2d(const Seg2D* segs, uint32_t nsegs, const double* src, double* dst, cudaStream_t s);
 

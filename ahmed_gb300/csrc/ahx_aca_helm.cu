@@ -657,6 +657,306 @@ __device__ uint32_t zrecompress(const G32& g, uint32_t n1, uint32_t n2, uint32_t
   return kt;
 }
 
+// Recompression of a union of complex low-rank blocks (agglomeration of mblock<dcomp>
+// leaves, H/agglH.cpp:14-107 with T = dcomp) by one warp: QR of both factors,
+// R = R1 R2^H, small entries dropped as in addtrll, then a column-pivoted
+// Householder QR of R stopped once the trailing columns' Frobenius norm is at most
+// 1e-2 delta max_j |R(:, j)|, one-sided Jacobi on Tt = T^H of the kept rows T
+// (T^H Z = W S), and R = (Qr Z S) (P W)^H.  Workspaces as the real union's
+// (complex elements): R (mmin x nmin, stride ld, then the reflectors), Tt
+// (nmin x rr), Z (rr x rr); cn: nmin doubles; qtau: nmin; cperm: nmin ints;
+// perm: rr + 1 ints.
+__device__ uint32_t zrecompress_qrcp(const G32& g, uint32_t n1, uint32_t n2, uint32_t k, Cx* U, Cx* V, Cx* Un,
+                                     Cx* Vn, double delta, Cx* R, Cx* Tt, Cx* Z, uint32_t ld, double* sig, Cx* tau,
+                                     double* cn, Cx* qtau, int* cperm, int* perm) {
+  if (k == 0) return 0;
+  const uint32_t lane = g.rank;
+  const uint32_t mmin = min(n1, k), nmin = min(n2, k), amin = min(mmin, nmin);
+  Cx* tau1 = tau;
+  Cx* tau2 = tau + k;
+  zqr(g, n1, k, U, tau1);
+  zqr(g, n2, k, V, tau2);
+  __syncwarp();
+  double fro = 0.0;
+  for (uint32_t i = lane; i < mmin; i += 32) {
+    for (uint32_t j = 0; j < nmin; ++j) {
+      double dr = 0.0, di = 0.0;
+      for (uint32_t l = max(i, j); l < k; ++l) {
+        const Cx u = U[i + (size_t)l * n1], v = V[j + (size_t)l * n2];
+        dr += u.re * v.re + u.im * v.im;
+        di += u.im * v.re - u.re * v.im;
+      }
+      R[i + (size_t)j * ld] = Cx{dr, di};
+      fro += dr * dr + di * di;
+    }
+  }
+  fro = G32::sum(fro);
+  const double thresh = delta * sqrt(fro) / (double)sqrtf((float)mmin * (float)nmin);
+  for (uint32_t i = lane; i < mmin; i += 32)
+    for (uint32_t j = 0; j < nmin; ++j)
+      if (cabs(R[i + (size_t)j * ld]) < thresh) R[i + (size_t)j * ld] = Cx{0.0, 0.0};
+  __syncwarp();
+  ArgMax cm{0.0, 0xffffffffu, 0.0};
+  for (uint32_t j = 0; j < nmin; ++j) {
+    double sj = 0.0;
+    for (uint32_t i = lane; i < mmin; i += 32) sj += cabs2(R[i + (size_t)j * ld]);
+    sj = G32::sum(sj);
+    if (lane == 0) {
+      cn[j] = sj;
+      cperm[j] = (int)j;
+    }
+    if (gt_nonneg(sj, cm.v)) cm = ArgMax{sj, j, 0.0};
+  }
+  __syncwarp();
+  const double tol2 = (1e-2 * delta) * (1e-2 * delta) * cm.v;
+  uint32_t rr = amin;
+  for (uint32_t c = 0; c < amin; ++c) {
+    double tot = 0.0;
+    ArgMax am{0.0, 0xffffffffu, 0.0};
+    for (uint32_t j = c + lane; j < nmin; j += 32) {
+      const double v = cn[j];
+      tot += v;
+      if (gt_nonneg(v, am.v)) am = ArgMax{v, j, 0.0};
+    }
+    tot = G32::sum(tot);
+    am = G32::argmax(am);
+    if (tot <= tol2 || am.idx >= nmin) {
+      rr = c;
+      break;
+    }
+    const uint32_t p = am.idx;
+    __syncwarp();
+    if (p != c) {
+      for (uint32_t i = lane; i < mmin; i += 32) {
+        const Cx x = R[i + (size_t)c * ld];
+        R[i + (size_t)c * ld] = R[i + (size_t)p * ld];
+        R[i + (size_t)p * ld] = x;
+      }
+      if (lane == 0) {
+        const double x = cn[c];
+        cn[c] = cn[p];
+        cn[p] = x;
+        const int q = cperm[c];
+        cperm[c] = cperm[p];
+        cperm[p] = q;
+      }
+    }
+    __syncwarp();
+    Cx* a = R + (size_t)c * ld;
+    double xn2 = 0.0, ar = 0.0, ai = 0.0;
+    for (uint32_t i = lane; i < mmin; i += 32) {
+      const Cx v = a[i];
+      if (i > c) xn2 += v.re * v.re + v.im * v.im;
+      else if (i == c) {
+        ar = v.re;
+        ai = v.im;
+      }
+    }
+    G32::sum3(xn2, ar, ai);
+    Cx t{0.0, 0.0};
+    if (!(xn2 == 0.0 && ai == 0.0)) {
+      const double nrm = sqrt(ar * ar + ai * ai + xn2);
+      const double beta = ar >= 0.0 ? -nrm : nrm;
+      t = Cx{(beta - ar) / beta, -ai / beta};
+      const Cx sc = cinv(Cx{ar - beta, ai});
+      for (uint32_t i = lane; i < mmin; i += 32) {
+        if (i > c) a[i] = cmul(a[i], sc);
+        else if (i == c) a[i] = Cx{beta, 0.0};
+      }
+    }
+    if (lane == 0) qtau[c] = t;
+    __syncwarp();
+    // trailing columns: b -= conj(t) v (v^H b), then their norms below row c
+    const Cx tc = cconj(t);
+    for (uint32_t j = c + 1; j < nmin; ++j) {
+      Cx* b = R + (size_t)j * ld;
+      if (t.re != 0.0 || t.im != 0.0) {
+        double sr = 0.0, si = 0.0;
+        for (uint32_t i = c + lane; i < mmin; i += 32) {
+          if (i > c) {
+            const Cx z = cmulc(a[i], b[i]);
+            sr += z.re;
+            si += z.im;
+          } else {
+            sr += b[i].re;
+            si += b[i].im;
+          }
+        }
+        G32::sum2(sr, si);
+        const Cx f = cmul(tc, Cx{sr, si});
+        for (uint32_t i = c + lane; i < mmin; i += 32) {
+          if (i > c) {
+            const Cx z = cmul(f, a[i]);
+            b[i].re -= z.re;
+            b[i].im -= z.im;
+          } else {
+            b[i].re -= f.re;
+            b[i].im -= f.im;
+          }
+        }
+      }
+      double s2 = 0.0;
+      for (uint32_t i = c + lane; i < mmin; i += 32)
+        if (i > c) s2 += cabs2(b[i]);
+      s2 = G32::sum(s2);
+      if (lane == 0) cn[j] = s2;
+    }
+    __syncwarp();
+  }
+  // Tt = T^H (nmin x rr), Z = I (rr x rr)
+  for (uint32_t e = lane; e < nmin * rr; e += 32) {
+    const uint32_t i = e / nmin, j = e - i * nmin;
+    Tt[j + (size_t)i * ld] = j >= i ? cconj(R[i + (size_t)j * ld]) : Cx{0.0, 0.0};
+  }
+  for (uint32_t e = lane; e < rr * rr; e += 32) {
+    const uint32_t i = e % rr, j = e / rr;
+    Z[i + (size_t)j * ld] = Cx{i == j ? 1.0 : 0.0, 0.0};
+  }
+  __syncwarp();
+  // one-sided Jacobi on the columns of Tt (the rotations of zrecompress)
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    bool rotated = false;
+    for (uint32_t p = 0; p + 1 < rr; ++p) {
+      for (uint32_t q = p + 1; q < rr; ++q) {
+        double al = 0.0, be = 0.0, gr = 0.0, gi = 0.0;
+        for (uint32_t i = lane; i < nmin; i += 32) {
+          const Cx x = Tt[i + (size_t)p * ld], y = Tt[i + (size_t)q * ld];
+          al += x.re * x.re + x.im * x.im;
+          be += y.re * y.re + y.im * y.im;
+          const Cx z = cmulc(x, y);
+          gr += z.re;
+          gi += z.im;
+        }
+        G32::sum2(al, be);
+        G32::sum2(gr, gi);
+        const double ga = sqrt(gr * gr + gi * gi);
+        if (ga == 0.0 || ga <= 1e-15 * sqrt(al * be)) continue;
+        rotated = true;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double cs = 1.0 / sqrt(1.0 + tt * tt);
+        const double sn = cs * tt;
+        const Cx e{gr / ga, -gi / ga};
+        for (uint32_t i = lane; i < nmin; i += 32) {
+          const Cx x = Tt[i + (size_t)p * ld], ey = cmul(e, Tt[i + (size_t)q * ld]);
+          Tt[i + (size_t)p * ld] = Cx{cs * x.re - sn * ey.re, cs * x.im - sn * ey.im};
+          Tt[i + (size_t)q * ld] = Cx{sn * x.re + cs * ey.re, sn * x.im + cs * ey.im};
+        }
+        for (uint32_t i = lane; i < rr; i += 32) {
+          const Cx x = Z[i + (size_t)p * ld], ey = cmul(e, Z[i + (size_t)q * ld]);
+          Z[i + (size_t)p * ld] = Cx{cs * x.re - sn * ey.re, cs * x.im - sn * ey.im};
+          Z[i + (size_t)q * ld] = Cx{sn * x.re + cs * ey.re, sn * x.im + cs * ey.im};
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  for (uint32_t j = 0; j < rr; ++j) {
+    double sj = 0.0;
+    for (uint32_t i = lane; i < nmin; i += 32) sj += cabs2(Tt[i + (size_t)j * ld]);
+    sj = G32::sum(sj);
+    if (lane == 0) sig[j] = sqrt(sj);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (uint32_t j = 0; j < rr; ++j) perm[j] = (int)j;
+    for (uint32_t j = 0; j < rr; ++j) {
+      uint32_t b = j;
+      for (uint32_t q = j + 1; q < rr; ++q)
+        if (sig[perm[q]] > sig[perm[b]]) b = q;
+      const int t = perm[j];
+      perm[j] = perm[b];
+      perm[b] = t;
+    }
+    uint32_t kt = rr;
+    const double s0 = rr ? sig[perm[0]] : 0.0;
+    while (kt > 0 && (sig[perm[kt - 1]] <= delta * s0 || sig[perm[kt - 1]] < 1e-64)) --kt;
+    perm[rr] = (int)kt;
+  }
+  __syncwarp();
+  const uint32_t kt = (uint32_t)perm[rr];
+  // Un = Q1 [Qr [Z(:, p) s_p; 0]; 0],  Vn = Q2 [P W(:, p); 0]
+  for (uint32_t j = 0; j < kt; ++j) {
+    const int pj = perm[j];
+    const double sj = sig[pj];
+    for (uint32_t i = lane; i < n1; i += 32) {
+      const Cx z = i < rr ? Z[i + (size_t)pj * ld] : Cx{0.0, 0.0};
+      Un[i + (size_t)j * n1] = Cx{z.re * sj, z.im * sj};
+    }
+    for (uint32_t i = lane; i < n2; i += 32) {
+      if (i < nmin) {
+        const Cx w = Tt[i + (size_t)pj * ld];
+        Vn[(uint32_t)cperm[i] + (size_t)j * n2] = Cx{w.re / sj, w.im / sj};
+      } else {
+        Vn[i + (size_t)j * n2] = Cx{0.0, 0.0};
+      }
+    }
+  }
+  __syncwarp();
+  for (int c = (int)rr - 1; c >= 0; --c) {
+    const Cx t = qtau[c];
+    if (t.re != 0.0 || t.im != 0.0) {
+      const Cx* a = R + (size_t)c * ld;
+      for (uint32_t j = 0; j < kt; ++j) {
+        Cx* b = Un + (size_t)j * n1;
+        double sr = 0.0, si = 0.0;
+        for (uint32_t i = (uint32_t)c + lane; i < mmin; i += 32) {
+          if (i > (uint32_t)c) {
+            const Cx z = cmulc(a[i], b[i]);
+            sr += z.re;
+            si += z.im;
+          } else {
+            sr += b[i].re;
+            si += b[i].im;
+          }
+        }
+        G32::sum2(sr, si);
+        const Cx f = cmul(t, Cx{sr, si});
+        for (uint32_t i = (uint32_t)c + lane; i < mmin; i += 32) {
+          if (i > (uint32_t)c) {
+            const Cx z = cmul(f, a[i]);
+            b[i].re -= z.re;
+            b[i].im -= z.im;
+          } else {
+            b[i].re -= f.re;
+            b[i].im -= f.im;
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  zapply_q(g, n1, mmin, U, tau1, kt, Un);
+  zapply_q(g, n2, nmin, V, tau2, kt, Vn);
+  __syncwarp();
+  return kt;
+}
+
+// one warp per union (CTA of one warp: consecutive unions on different SMs)
+__global__ void __launch_bounds__(32) zmerge_kernel(MergeParams p) {
+  const uint32_t ti = blockIdx.x;
+  if (ti >= p.ntasks) return;
+  G32 g(threadIdx.x & 31);
+  const MergeTask t = p.tasks[ti];
+  const uint32_t m = t.m, n = t.n, kc = t.k;
+  Cx* U = reinterpret_cast<Cx*>(p.ws) + t.ws;
+  Cx* V = U + (size_t)m * kc;
+  Cx* Un = V + (size_t)n * kc;
+  Cx* Vn = Un + (size_t)m * kc;
+  Cx* R = Vn + (size_t)n * kc;
+  Cx* Tt = R + (size_t)kc * kc;
+  double* sig = reinterpret_cast<double*>(Tt + (size_t)kc * kc);
+  Cx* tau = Tt + (size_t)kc * kc + kc;
+  Cx* Z = tau + 2 * (size_t)kc;
+  double* cn = reinterpret_cast<double*>(Z + (size_t)kc * kc);
+  Cx* qtau = Z + (size_t)kc * kc + kc;
+  int* cperm = reinterpret_cast<int*>(qtau + kc);
+  uint32_t kt = 0;
+  if (kc > 0) kt = zrecompress_qrcp(g, m, n, kc, U, V, Un, Vn, p.eps, R, Tt, Z, kc, sig, tau, cn, qtau, cperm,
+                                    p.zs + t.zs);
+  if (g.rank == 0) p.res[ti] = AcaResult{kAcaOk, kc, kt, 0u};
+}
+
 // One leaf of the Helmholtz assembly.  Workspace (complex, at ws):
 //   U[n1 kcap] V[n2 kcap] Un[n1 kcap] Vn[n2 kcap] R[kcap^2] Vs[kcap^2] sig[kcap] tau[2 kcap]
 // ints at zs: Z[n1] S[n2] (later the SVD permutation).
@@ -1089,3 +1389,11 @@ extern "C" int ahx_helm_get_leaf(const ahx_hmat* H, uint32_t l, double* out) {
   AHX_CUDA(cudaStreamSynchronize(H->stream));
   return AHX_OK;
 }
+
+namespace ahx {
+cudaError_t launch_zmerge(const MergeParams& p, cudaStream_t s) {
+  if (p.ntasks == 0) return cudaSuccess;
+  zmerge_kernel<<<p.ntasks, 32, 0, s>>>(p);
+  return cudaGetLastError();
+}
+}  // namespace ahx

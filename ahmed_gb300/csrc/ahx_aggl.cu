@@ -113,10 +113,14 @@ struct TreeBuilder {
 
 using namespace ahx;
 
-extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged) {
+namespace {
+
+// cplx: the Helmholtz (mblock<dcomp>) leaves, two doubles per element; the block
+// tree changes, so the other kind of leaves of the handle is dropped.
+int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged, bool cplx) {
   if (!H || !(eps >= 0.0)) return AHX_ERR_ARG;
-  if (!H->assembled) {
-    set_error("ahx_agglomerate: H-matrix not assembled");
+  if (!(cplx ? H->z.assembled : H->assembled)) {
+    set_error("agglomerate: H-matrix not assembled");
     return AHX_ERR_STATE;
   }
   int rc = ensure_device(H);
@@ -133,8 +137,10 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
   std::vector<BNode>& N = B.nodes;
   const uint32_t nl0 = (uint32_t)T.leaves.size();
   // leaf state, indexed by the reference's leaf index (idx)
-  std::vector<int32_t> rank(H->rank);
-  std::vector<uint64_t> off(H->off);
+  std::vector<int32_t> rank(cplx ? H->z.rank : H->rank);
+  std::vector<uint64_t> off(cplx ? H->z.off : H->off);
+  const uint64_t ew = cplx ? 2 : 1;  // doubles per element
+  auto arena = [&]() -> double* { return cplx ? H->z.arena.as<double>() : H->arena64.as<double>(); };
   std::vector<int32_t> leaf_node(nl0, -1);
   for (int32_t i = 0; i < (int32_t)N.size(); ++i)
     if (N[i].leaf >= 0) leaf_node[N[i].leaf] = i;
@@ -213,7 +219,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
           }
           kmax_round = std::max<uint64_t>(kmax_round, k);
           const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
-          if (!tasks.empty() && (wsz + need) * sizeof(double) > budget) break;
+          if (!tasks.empty() && (wsz + need) * ew * sizeof(double) > budget) break;
           MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
           // U = [U00 U01 0 0; 0 0 U10 U11], V = [V00 0 V10 0; 0 V01 0 V11]; a dense
           // son contributes (D, I)
@@ -226,9 +232,10 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
             const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
             const uint64_t o = off[c.leaf];
             const uint64_t vdst = wsz + (uint64_t)q.n1 * k + (uint64_t)col * q.n2 + co;
-            segs.push_back(Seg2D{o, wsz + (uint64_t)col * q.n1 + ro, c.n1, kc, q.n1, 0u});
-            if (dense) segs.push_back(Seg2D{kSegIdentity, vdst, kc, kc, q.n2, 0u});
-            else segs.push_back(Seg2D{o + (uint64_t)c.n1 * kc, vdst, c.n2, kc, q.n2, 0u});
+            const uint32_t e32 = (uint32_t)ew;
+            segs.push_back(Seg2D{o * ew, (wsz + (uint64_t)col * q.n1 + ro) * ew, c.n1 * e32, kc, q.n1 * e32, 0u});
+            if (dense) segs.push_back(Seg2D{kSegIdentity, vdst * ew, kc, kc, q.n2 * e32, cplx ? 1u : 0u});
+            else segs.push_back(Seg2D{(o + (uint64_t)c.n1 * kc) * ew, vdst * ew, c.n2 * e32, kc, q.n2 * e32, 0u});
             col += kc;
           }
           tasks.push_back(t);
@@ -236,12 +243,11 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
           wsz += need;
           zsz += q.n1 + q.n2 + 1;
         }
-        if ((rc = ws.reserve(std::max<uint64_t>(wsz, 1) * sizeof(double)))) return rc;
+        if ((rc = ws.reserve(std::max<uint64_t>(wsz, 1) * ew * sizeof(double)))) return rc;
         if ((rc = zs.reserve(std::max<uint64_t>(zsz, 1) * sizeof(int)))) return rc;
-        AHX_CUDA(cudaMemsetAsync(ws.p, 0, wsz * sizeof(double), H->stream));
+        AHX_CUDA(cudaMemsetAsync(ws.p, 0, wsz * ew * sizeof(double), H->stream));
         if ((rc = upload(dsegs, segs, H->stream))) return rc;
-        AHX_CUDA(launch_copy2d(dsegs.as<Seg2D>(), (uint32_t)segs.size(), H->arena64.as<double>(), ws.as<double>(),
-                               H->stream));
+        AHX_CUDA(launch_copy2d(dsegs.as<Seg2D>(), (uint32_t)segs.size(), arena(), ws.as<double>(), H->stream));
         if ((rc = upload(dtasks, tasks, H->stream))) return rc;
         if ((rc = dres.reserve(tasks.size() * sizeof(AcaResult)))) return rc;
         MergeParams p;
@@ -251,7 +257,7 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
         p.zs = zs.as<int>();
         p.eps = eps;
         p.res = dres.as<AcaResult>();
-        AHX_CUDA(launch_merge(p, large == 1, H->stream));
+        AHX_CUDA(cplx ? launch_zmerge(p, H->stream) : launch_merge(p, large == 1, H->stream));
         std::vector<AcaResult> res(tasks.size());
         AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, res.size() * sizeof(AcaResult), cudaMemcpyDeviceToHost,
                                  H->stream));
@@ -268,11 +274,12 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
           // the merged block takes its first son's index; the other sons' are freed
           const int32_t first = N[nd.son[0]].leaf;
           uint64_t dst = 0;
-          if (post && (rc = arena_append(H, post, dst))) return rc;
+          if (post && (rc = cplx ? zarena_append(H, post, dst) : arena_append(H, post, dst))) return rc;
           if (post) {
             const MergeTask& t = tasks[q];
             const uint64_t un = t.ws + (uint64_t)(t.m + t.n) * t.k;  // Un follows U and V
-            copies.push_back(CopyTask{un, un + (uint64_t)t.m * t.k, dst, t.m, t.n, kt, 0u});
+            const uint32_t e32 = (uint32_t)ew;
+            copies.push_back(CopyTask{un * ew, (un + (uint64_t)t.m * t.k) * ew, dst * ew, t.m * e32, t.n * e32, kt, 0u});
           }
           rank[first] = (int32_t)kt;
           off[first] = dst;
@@ -282,8 +289,8 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
         }
         if (!copies.empty()) {
           if ((rc = upload(dcopy, copies, H->stream))) return rc;
-          AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), ws.as<double>(),
-                                       H->arena64.as<double>(), H->stream));
+          AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), ws.as<double>(), arena(),
+                                       H->stream));
           AHX_CUDA(cudaStreamSynchronize(H->stream));
         }
       }
@@ -361,35 +368,68 @@ extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint3
     const uint64_t cnt = rank[l] < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)rank[l] * (q.n1 + q.n2);
     noff[k] = total;
     if (cnt) {
-      // dense: n1 x n2 as "U" with kt = n2 columns and an empty "V"
-      if (rank[l] < 0) moves.push_back(CopyTask{off[l], off[l], total, q.n1, 0u, q.n2, 0u});
-      else moves.push_back(CopyTask{off[l], off[l] + (uint64_t)q.n1 * rank[l], total, q.n1, q.n2, (uint32_t)rank[l], 0u});
+      // dense: n1 x n2 as "U" with kt = n2 columns and an empty "V" (doubles: ew per element)
+      const uint32_t e32 = (uint32_t)ew;
+      if (rank[l] < 0)
+        moves.push_back(CopyTask{off[l] * ew, off[l] * ew, total * ew, q.n1 * e32, 0u, q.n2, 0u});
+      else
+        moves.push_back(CopyTask{off[l] * ew, (off[l] + (uint64_t)q.n1 * rank[l]) * ew, total * ew, q.n1 * e32,
+                                 q.n2 * e32, (uint32_t)rank[l], 0u});
     }
     total += cnt;
   }
   DevBuf fresh;
   ScopedBuf dm;
-  if ((rc = fresh.reserve(std::max<uint64_t>(total, 1) * sizeof(double)))) return rc;
+  if ((rc = fresh.reserve(std::max<uint64_t>(total, 1) * ew * sizeof(double)))) return rc;
   if ((rc = upload(dm, moves, H->stream))) {
     fresh.release();
     return rc;
   }
   {
-    cudaError_t e = launch_copy_factors(dm.as<CopyTask>(), (uint32_t)moves.size(), H->arena64.as<double>(),
-                                        fresh.as<double>(), H->stream);
+    cudaError_t e = launch_copy_factors(dm.as<CopyTask>(), (uint32_t)moves.size(), arena(), fresh.as<double>(),
+                                        H->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
     if (e != cudaSuccess) {
       fresh.release();
       return cuda_fail(e, "agglomerate: arena compaction");
     }
   }
-  H->arena64.release();
-  H->arena64 = fresh;
-  H->arena64_elems = total;
-  invalidate_products(H);
   T.leaves = leaves;
-  H->rank = nrank;
-  H->aca_rank = nrank;
-  H->off = noff;
+  if (cplx) {
+    ZState& Z = H->z;
+    Z.arena.release();
+    Z.arena = fresh;
+    Z.elems = total;
+    Z.valid32 = Z.table = false;
+    Z.arena32.release();
+    Z.rank = nrank;
+    Z.aca_rank = nrank;
+    Z.off = noff;
+    // the real leaves belong to the old block tree
+    invalidate_products(H);
+    H->assembled = false;
+    H->rank.clear();
+    H->aca_rank.clear();
+    H->off.clear();
+  } else {
+    H->arena64.release();
+    H->arena64 = fresh;
+    H->arena64_elems = total;
+    invalidate_products(H);
+    H->rank = nrank;
+    H->aca_rank = nrank;
+    H->off = noff;
+    H->z.release_all();  // Helmholtz leaves of the old block tree
+  }
   return AHX_OK;
+}
+
+}  // namespace
+
+extern "C" int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged) {
+  return agglomerate_impl(H, eps, max_rank, nmerged, false);
+}
+
+extern "C" int ahx_helm_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged) {
+  return agglomerate_impl(H, eps, max_rank, nmerged, true);
 }

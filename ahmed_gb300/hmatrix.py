@@ -287,6 +287,13 @@ class HMatrix:
         check(lib().ahx_helm_load(self._h, os.fsencode(path), C.byref(eta), C.byref(bmin)))
         return eta.value, bmin.value
 
+    def helm_agglH(self, eps=1e-6, max_rank=2**32 - 1):
+        """agglH with T = dcomp (H/agglH.cpp:291-305) on the Helmholtz leaves; returns the
+        number of merged blocks.  The block tree changes: real leaves must be assembled again."""
+        n = C.c_uint32()
+        check(lib().ahx_helm_agglomerate(self._h, float(eps), min(int(max_rank), 2**32 - 1), C.byref(n)))
+        return n.value
+
     def helm_storage_bytes(self, precision="fp64"):
         return lib().ahx_helm_storage_bytes(self._h, _prec(precision))
 

@@ -162,6 +162,11 @@ int ahx_helm_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint
  * leaf indices are then compacted as fill_gaps does.  Unions with dense sons are not
  * formed.  Once per assembly.  nmerged (may be NULL): blocks merged. */
 int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged);
+/* The same for the Helmholtz leaves (agglH with T = dcomp, H/agglH.cpp:291-305).
+ * Agglomeration changes the block tree: the handle's other kind of leaves (real
+ * after this call, Helmholtz after ahx_agglomerate) is dropped and must be
+ * assembled again on the new leaves if needed. */
+int ahx_helm_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged);
 /* per leaf: rank after recompression, -1 for dense leaves (mblock::isLrM/rank) */
 int ahx_hmat_ranks(const ahx_hmat* H, int32_t* ranks);
 /* per leaf: ACA rank before recompression, -1 for dense */

@@ -147,9 +147,12 @@ class blcluster {
     check(ahx_hmat_ranks(h_, ranks_.data()));
   }
   // leaves and ranks again (after an agglomeration changed the leaves)
-  void refresh() {
+  void refresh_leaves() {
     leaves_.resize(7 * (size_t)ahx_hmat_nleaves(h_));
     check(ahx_hmat_leaves(h_, leaves_.data()));
+  }
+  void refresh() {
+    refresh_leaves();
     refresh_ranks();
   }
   int rank_of(unsigned l) const { return ranks_.at(l); }
@@ -284,11 +287,20 @@ void matgenSyH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps,
 }
 
 // H/agglH.cpp:253-272: agglomeration of the assembled leaves (unions of low-rank sons)
+inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const double*) {
+  check(ahx_agglomerate(bl->handle(), eps, max_rank, nullptr));
+  bl->refresh();
+}
+inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const dcomp*) {
+  check(ahx_helm_agglomerate(bl->handle(), eps, max_rank, nullptr));
+  bl->refresh_leaves();
+  bl->refresh_zranks();
+}
+
 template <class T>
 void agglH(blcluster* bl, mblock<T>**& A, double eps, unsigned max_rank) {
   const unsigned before = (unsigned)bl->nleaves();
-  check(ahx_agglomerate(bl->handle(), eps, max_rank, nullptr));
-  bl->refresh();
+  agglomerate_leaves(bl, eps, max_rank, (const T*)nullptr);
   for (unsigned i = 0; i < before; ++i) delete A[i];
   delete[] A;
   const unsigned n = (unsigned)bl->nleaves();

@@ -205,6 +205,7 @@ def ref():
         L.ref_helm_leaf_data.restype = C.c_ulong
         L.ref_helm_leaf_data.argtypes = [vp, u32, vp]
         L.ref_helm_matvec.argtypes = [vp, i32, dbl, dbl, u32, vp, vp]
+        L.ref_helm_agglomerate.argtypes = [vp, dbl, u32]
         L.ref_helm_save.restype = i32
         L.ref_helm_save.argtypes = [vp, dbl, u32, C.c_char_p]
         L.ref_helm_gmres.restype = u32
@@ -328,3 +329,7 @@ class RefH:
         """The reference's own savembls of the Helmholtz (mblock<dcomp>) leaves."""
         if ref().ref_helm_save(self._H, eta, bmin, os.fsencode(path)) != 0:
             raise RuntimeError("ref_helm_save failed")
+
+    def helm_agglomerate(self, eps, rankmax=2**32 - 1):
+        """The reference's agglH of the Helmholtz (mblock<dcomp>) leaves."""
+        ref().ref_helm_agglomerate(self._H, eps, rankmax)

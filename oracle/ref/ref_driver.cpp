@@ -461,6 +461,18 @@ unsigned ref_helm_gmres(void* p, double* b, double* x, double* eps, unsigned m, 
   return r;
 }
 
+// The reference's agglH with T = dcomp (H/agglH.cpp:291-305) of the Helmholtz leaves;
+// the leaf list is rebuilt in DFS order (indices as agglH left them).
+void ref_helm_agglomerate(void* p, double eps, unsigned rankmax) {
+  RefH* H = (RefH*)p;
+  agglH(H->root_bl, H->Az, eps, rankmax, (contBasis<dcomp>*)NULL);
+  blcluster** list;
+  H->nblcks = H->root_bl->nleaves();
+  gen_BlSequence(H->root_bl, list);
+  H->leaves.assign(list, list + H->nblcks);
+  delete[] list;
+}
+
 // The reference's savembls (Include/H.h:89-103) of the Helmholtz (mblock<dcomp>) leaves
 int ref_helm_save(void* p, double eta, unsigned bmin, const char* path) {
   RefH* H = (RefH*)p;

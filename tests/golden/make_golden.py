@@ -12,6 +12,7 @@ Usage:  python tests/golden/make_golden.py            (Laplace cases)
         python tests/golden/make_golden.py zhmat      (Helmholtz H-matrix: complex assembly,
                                                        products, GMRes)
         python tests/golden/make_golden.py zmbls      (savembls files of mblock<dcomp> leaves)
+        python tests/golden/make_golden.py zaggl      (agglH of mblock<dcomp> leaves)
 """
 import os
 import sys
@@ -315,6 +316,38 @@ def zmbls():
     print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+def zaggl():
+    """The reference's agglH of mblock<dcomp> leaves (Helmholtz, k = 5): leaves in index
+    order, their ranks, the stored elements and y = A x after agglomeration."""
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    for base, kind, kname in (("fib4096", O.TREE_BBX, "bbx"), ("ell2500", O.TREE_PCA, "pca")):
+        gen, bmin = CASES[base]
+        P = gen()
+        h = O.mean_nn(P)
+        n = P.shape[0]
+        rng = np.random.default_rng(8)
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        out = {"points": P, "h": np.float64(h), "bmin": np.uint32(bmin), "eta": np.float64(ETA),
+               "eps": np.float64(EPS), "k": np.float64(ZH_K), "kind": np.int32(kind), "x": x}
+        R = O.RefH(P, kind, bmin, ETA, h)
+        out["op_perm"] = R.perm()[0]
+        R.helm_assemble(ZH_K, h, EPS, nthreads=1)
+        out["nleaves_before"] = np.uint32(R.nleaves)
+        R.helm_agglomerate(EPS)
+        L = R.leaves()
+        r = R.helm_ranks()
+        order = np.argsort(L[:, 5])
+        out["leaves"] = L[order]
+        out["ranks"] = r[order]
+        out["stored"] = np.int64(sum(R.helm_leaf_data(l).size for l in range(R.nleaves)))
+        y = np.zeros(n, np.complex128)
+        out["y"] = R.helm_matvec(x, y)
+        path = os.path.join(HERE, f"zaggl_{base}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB) leaves {out['nleaves_before']} -> {R.nleaves}")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
@@ -328,5 +361,7 @@ if __name__ == "__main__":
         zhmat()
     elif len(sys.argv) > 1 and sys.argv[1] == "zmbls":
         zmbls()
+    elif len(sys.argv) > 1 and sys.argv[1] == "zaggl":
+        zaggl()
     else:
         main()
