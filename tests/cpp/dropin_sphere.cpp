@@ -200,6 +200,21 @@ int main(int argc, char** argv) {
       freembls(bl4, ZB);
       delete bl4;
     }
+    bool zaggl_ok = false;
+    {  // agglH of the mblock<dcomp> leaves (H/agglH.cpp:291)
+      const unsigned before = (unsigned)blz->nleaves();
+      agglH(blz, Z, eps, 1000000);
+      std::vector<dcomp> zy5(N, 0.0);
+      mltaGeHVec(dcomp(1.0, 0.0), blz, Z, zx.data(), zy5.data());
+      double d5 = 0.0, n5 = 0.0;
+      for (unsigned i = 0; i < N; ++i) {
+        d5 += std::norm(zy5[i] - zy[i]);
+        n5 += std::norm(zy[i]);
+      }
+      zaggl_ok = blz->nleaves() < before && std::sqrt(d5 / n5) < 1e-5;
+      std::printf("helmholtz agglH: %u -> %lu leaves, product change %.3e\n", before, blz->nleaves(),
+                  std::sqrt(d5 / n5));
+    }
     freembls(blz, Z);
     delete blz;
     // the complex symmetric form on the symmetric tree (matgenSyH_omp, mltaSyHVec)
@@ -235,7 +250,7 @@ int main(int argc, char** argv) {
     freembls(blg, Z);
     delete blg;
     helm_ok = zlr > 0 && zerr < 5e-6 && zerrh < 5e-6 && zret == 0 && zeps < 1e-8 && sym_diag > 0 && zserr < 5e-6 &&
-              zio_ok;
+              zio_ok && zaggl_ok;
     std::printf("helmholtz: %u low-rank leaves, product error %.3e, adjoint %.3e, GMRes ret %u eps %.3e steps %u\n",
                 zlr, zerr, zerrh, zret, zeps, zsteps);
     std::printf("helmholtz symmetric: %u leaves (%u symmetric diagonal), product vs general %.3e\n", ns, sym_diag,

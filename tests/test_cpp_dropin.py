@@ -33,3 +33,4 @@ def test_dropin_runs_on_gpu(tmp_path):
     assert "helmholtz:" in out.stdout
     assert "helmholtz symmetric:" in out.stdout
     assert "helmholtz savembls/loadmbls round trip ok" in out.stdout
+    assert "helmholtz agglH:" in out.stdout
