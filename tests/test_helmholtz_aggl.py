@@ -94,3 +94,31 @@ def test_real_agglomeration_drops_helmholtz_leaves(golden):
     y = H.mltaGeHVec(1.0, g["x"], np.zeros_like(g["x"]))
     assert _rel(y, g["y"]) <= 1e-5
     H.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cplx", [False, True])
+def test_symmetric_tree_agglomeration(golden, cplx):
+    """Symmetric block trees (upper blocks only): the unions stay above the diagonal,
+    the product of the agglomerated matrix stays within the assembly accuracy and the
+    storage shrinks, for real (HeH) and complex symmetric (SyH) leaves."""
+    g = golden("zaggl_fib4096")
+    H = A.HMatrix(g["points"], "bbx", bmin=int(g["bmin"]), eta=float(g["eta"]), symmetric=True)
+    x = g["x"] if cplx else g["x"].real.copy()
+    if cplx:
+        H.helmholtz_assemble(float(g["k"]), float(g["h"]), float(g["eps"]))
+        stored0 = sum(H.helm_leaf_data(l).size for l in range(H.nleaves))
+    else:
+        H.matgenGeH_omp(float(g["h"]), float(g["eps"]))
+        stored0 = sum(H.leaf_data(l).size for l in range(H.nleaves))
+    y0 = H.mltaGeHVec(1.0, x, np.zeros_like(x))
+    n0 = H.nleaves
+    merged = H.helm_agglH(float(g["eps"])) if cplx else H.agglH(float(g["eps"]))
+    assert merged > 0 and H.nleaves < n0
+    L = H.leaves()
+    assert np.all(L[:, 0] <= L[:, 2])  # upper blocks only
+    y = H.mltaGeHVec(1.0, x, np.zeros_like(x))
+    assert _rel(y, y0) <= 1e-5
+    stored = sum((H.helm_leaf_data(l) if cplx else H.leaf_data(l)).size for l in range(H.nleaves))
+    assert stored < stored0
+    H.close()
