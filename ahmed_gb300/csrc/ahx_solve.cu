@@ -661,9 +661,15 @@ struct StepTrace {
 };
 
 // Precision of the refinement's outer residual: kDF64 (default) or kFP64.
-int refine_residual_precision() {
+// The outer residual's product: double-float from two right-hand sides per system
+// on, FP64 for one (there the FP64 product is the faster one: 0.64 vs 0.71 ms on a
+// 65,536-point sphere, while two RHS take 1.12 vs 0.85 ms).  AHX_REFINE_RESIDUAL=fp64
+// or df64 forces one of them.
+int refine_residual_precision(uint32_t p) {
   const char* e = std::getenv("AHX_REFINE_RESIDUAL");
-  return (e && std::string(e) == "fp64") ? kFP64 : kDF64;
+  if (e && std::string(e) == "fp64") return kFP64;
+  if (e && std::string(e) == "df64") return kDF64;
+  return p == 1 ? kFP64 : kDF64;
 }
 
 int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X, double tol,
@@ -692,7 +698,7 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
     cudaStream_t st = op.stream;
     // the outer residual in FP64-class arithmetic: double-float on the FP32
     // pipes unless AHX_REFINE_RESIDUAL=fp64 asks for the FP64 product
-    const int resid_prec = refine_residual_precision();
+    const int resid_prec = refine_residual_precision(p);
     if ((rc = op.prepare(resid_prec, p))) return rc;
     // inner tolerance near the storage precision's product accuracy (FP32
     // ~3e-7, BF16 factors ~4e-4): fewer outer steps, i.e. fewer FP64 products

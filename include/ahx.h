@@ -36,7 +36,8 @@ extern "C" {
 #define AHX_BF16_FP32 2 /* low-rank factors BF16, dense leaves FP32, FP32 accumulation */
 #define AHX_DF64 3      /* FP64 leaves as float pairs, double-float arithmetic on the FP32
                            pipes (about 2^-44 relative; FP64-class): the refinement's outer
-                           residual (AHX_REFINE_RESIDUAL=fp64 selects the FP64 product) */
+                           residual from two right-hand sides per system on (one: the FP64
+                           product; AHX_REFINE_RESIDUAL=fp64 / df64 forces either) */
 
 typedef struct ahx_hmat ahx_hmat;
 typedef struct ahx_batch ahx_batch;
