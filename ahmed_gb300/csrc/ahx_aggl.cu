@@ -199,8 +199,14 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
       const uint64_t w = width(c);
       cost[c] = w * w * (N[c].n1 + N[c].n2);
     }
+    // a warp per union hides its loads' latency only among many unions: a round of
+    // fewer unions than warp slots runs its unions of more than 256 rows on CTAs
+    const bool few = cand.size() < 8u * 152u;
     std::vector<int32_t> parts[2];
-    for (int32_t c : cand) parts[(width(c) > 64u || std::max(N[c].n1, N[c].n2) > 4096u) ? 1 : 0].push_back(c);
+    for (int32_t c : cand) {
+      const uint32_t rows = std::max(N[c].n1, N[c].n2);
+      parts[(width(c) > 64u || rows > 4096u || (few && rows > 256u)) ? 1 : 0].push_back(c);
+    }
     for (int large = 0; large < 2; ++large) {
       std::vector<int32_t>& todo = parts[large];
       std::stable_sort(todo.begin(), todo.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });

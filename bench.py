@@ -666,6 +666,34 @@ def run_zhmat(args):
     print(json.dumps(out))
 
 
+def run_aggl(args):
+    """Agglomeration (agglH) after the assembly: Fibonacci sphere `--n` points, leaf 32,
+    eta 0.8, eps 1e-6, bounding-box tree (`--symmetric`: the symmetric one); wall clock of
+    the agglomeration, leaves and FP64 storage before / after, and the change of y = A x."""
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    P = A.geometry.fibonacci_sphere(args.n)
+    H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA, symmetric=args.symmetric)
+    H.matgenGeH_omp(A.mean_nn(P), EPS)
+    x = np.random.default_rng(0).uniform(-1.0, 1.0, H.n)
+    y0 = H.mltaGeHVec(1.0, x, np.zeros(H.n))
+    n0, s0 = H.nleaves, H.storage_bytes("fp64")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    merged = H.agglH(EPS)
+    torch.cuda.synchronize()
+    t_aggl = time.perf_counter() - t0
+    y = H.mltaGeHVec(1.0, x, np.zeros(H.n))
+    print(json.dumps({"workload": f"agglomeration-sphere-{args.n}" + ("-sym" if args.symmetric else ""),
+                      "agglomeration_s": t_aggl, "merged": int(merged), "leaves_before": int(n0),
+                      "leaves_after": int(H.nleaves), "fp64_bytes_before": int(s0),
+                      "fp64_bytes_after": int(H.storage_bytes("fp64")),
+                      "product_change": float(np.linalg.norm(y - y0) / np.linalg.norm(y0))}))
+    H.close()
+
+
 def run_batch(args):
     """Many uneven H-matrices in one launch: `--instances` instances (256), N log-uniform
     in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
@@ -741,7 +769,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
     ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz",
-                             "zhmat"],
+                             "zhmat", "aggl"],
                     help="sphere: the default product benchmark; cube-large: N = 2^20 "
                          "cube surface, 64 right-hand sides, products and GMRES; batch: "
                          "256 uneven instances, one launch per product, batched GMRES")
@@ -779,6 +807,8 @@ def main():
         run_helmholtz(args)
     elif args.workload == "zhmat":
         run_zhmat(args)
+    elif args.workload == "aggl":
+        run_aggl(args)
     else:
         run_gpu(args)
 
