@@ -149,6 +149,22 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
     const int32_t r = rank[leaf];
     return r < 0 ? (uint64_t)q.n1 * q.n2 : (uint64_t)r * (q.n1 + q.n2);
   };
+  // columns of a union's factored form: the sons' ranks and the widths of dense
+  // sons; a union of four dense sons is the parent block itself (n2 columns)
+  auto dense_sons = [&](const BNode& q) -> bool {
+    for (int s = 0; s < 4; ++s)
+      if (rank[N[q.son[s]].leaf] >= 0) return false;
+    return true;
+  };
+  auto union_width = [&](const BNode& q) -> uint32_t {
+    if (dense_sons(q)) return q.n2;
+    uint32_t k = 0;
+    for (int s = 0; s < 4; ++s) {
+      const BNode& c = N[q.son[s]];
+      k += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
+    }
+    return k;
+  };
   uint32_t merged = 0;
   ScopedBuf ws, zs, dtasks, dres, dsegs, dcopy;
   const size_t budget = aca_ws_budget();
@@ -164,17 +180,14 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
       BNode& q = N[i];
       if (q.leaf >= 0 || q.decided || q.dbl) continue;
       bool all_leaves = true;
-      uint32_t w = 0;
       for (int s = 0; s < 4; ++s) {
         if (q.son[s] < 0 || N[q.son[s]].leaf < 0) {
           all_leaves = false;
           break;
         }
-        const BNode& c = N[q.son[s]];
-        w += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
       }
       if (!all_leaves) continue;
-      if (w > kMaxUnion) {
+      if (union_width(q) > kMaxUnion) {
         q.decided = true;
         continue;
       }
@@ -183,14 +196,7 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
     if (cand.empty()) break;
     uint64_t kmax_round = 0;
     // union widths (columns of the factored union)
-    auto width = [&](int32_t c) -> uint32_t {
-      uint32_t k = 0;
-      for (int s = 0; s < 4; ++s) {
-        const BNode& x = N[N[c].son[s]];
-        k += rank[x.leaf] < 0 ? x.n2 : (uint32_t)rank[x.leaf];
-      }
-      return k;
-    };
+    auto width = [&](int32_t c) -> uint32_t { return union_width(N[c]); };
     // batches under the workspace budget: one warp per union, one CTA for unions
     // wider than 64 columns (the SVD's column pairs in parallel) or blocks over 4096
     // rows; the costliest first so that they spread over the SMs
@@ -218,19 +224,28 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
         uint64_t wsz = 0, zsz = 0;
         for (; at < todo.size(); ++at) {
           const BNode& q = N[todo[at]];
-          uint32_t k = 0;  // union columns: the ranks, and the widths of dense sons
-          for (int s = 0; s < 4; ++s) {
-            const BNode& c = N[q.son[s]];
-            k += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
-          }
+          const uint32_t k = union_width(q);
+          const bool all_dense = dense_sons(q);
           kmax_round = std::max<uint64_t>(kmax_round, k);
           const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
           if (!tasks.empty() && (wsz + need) * ew * sizeof(double) > budget) break;
           MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
           // U = [U00 U01 0 0; 0 0 U10 U11], V = [V00 0 V10 0; 0 V01 0 V11]; a dense
-          // son contributes (D, I)
+          // son contributes (D, I).  Four dense sons: U = the parent block, V = I (n2
+          // columns instead of 2 n2).
+          const uint32_t e32 = (uint32_t)ew;
+          if (all_dense) {
+            for (int s = 0; s < 4; ++s) {
+              const BNode& c = N[q.son[s]];
+              const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
+              segs.push_back(Seg2D{off[c.leaf] * ew, (wsz + (uint64_t)co * q.n1 + ro) * ew, c.n1 * e32, c.n2,
+                                   q.n1 * e32, 0u});
+            }
+            segs.push_back(Seg2D{kSegIdentity, (wsz + (uint64_t)q.n1 * k) * ew, q.n2, q.n2, q.n2 * e32,
+                                 cplx ? 1u : 0u});
+          }
           uint32_t col = 0;
-          for (int s = 0; s < 4; ++s) {
+          for (int s = 0; s < 4 && !all_dense; ++s) {
             const BNode& c = N[q.son[s]];
             const bool dense = rank[c.leaf] < 0;
             const uint32_t kc = dense ? c.n2 : (uint32_t)rank[c.leaf];
@@ -238,7 +253,6 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
             const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
             const uint64_t o = off[c.leaf];
             const uint64_t vdst = wsz + (uint64_t)q.n1 * k + (uint64_t)col * q.n2 + co;
-            const uint32_t e32 = (uint32_t)ew;
             segs.push_back(Seg2D{o * ew, (wsz + (uint64_t)col * q.n1 + ro) * ew, c.n1 * e32, kc, q.n1 * e32, 0u});
             if (dense) segs.push_back(Seg2D{kSegIdentity, vdst * ew, kc, kc, q.n2 * e32, cplx ? 1u : 0u});
             else segs.push_back(Seg2D{(o + (uint64_t)c.n1 * kc) * ew, vdst * ew, c.n2 * e32, kc, q.n2 * e32, 0u});
