@@ -62,3 +62,34 @@ def test_leaf_list_is_a_partition():
             cover[b1:b1 + n1, b2:b2 + n2] += 1
         assert (cover == 1).all()
         assert np.array_equal(lv[:, 5], np.arange(len(lv)))
+
+
+def test_helmholtz_calls_before_assembly_fail_on_the_host(tmp_path):
+    """The Helmholtz entry points check arguments and state before any device work,
+    so a handle without assembled complex leaves gets status codes, not faults."""
+    L = _capi.lib()
+    P = A.geometry.fibonacci_sphere(512)
+    H = A.HMatrix(P, "bbx", bmin=32, eta=0.8)
+    h, n = H.handle, H.n
+    X = np.zeros(n, np.complex128)
+    Y = np.zeros(n, np.complex128)
+    ptr = _capi.ptr
+    ranks = np.zeros(H.nleaves, np.int32)
+    assert L.ahx_helm_ranks(h, ptr(ranks)) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_leaf_size(h, 0) == 0
+    assert L.ahx_helm_get_leaf(h, 0, ptr(X)) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_get_leaf(h, H.nleaves, ptr(X)) == _capi.AHX_ERR_ARG
+    assert L.ahx_helm_storage_bytes(h, 0) == 0
+    assert L.ahx_helm_matvec(h, 0, 0, 1.0, 0.0, 1, ptr(X), n, ptr(Y), n) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_matvec(h, 0, 0, 1.0, 0.0, 1, ptr(X), n - 1, ptr(Y), n) == _capi.AHX_ERR_ARG
+    assert L.ahx_helm_matvec(h, 0, 7, 1.0, 0.0, 1, ptr(X), n, ptr(Y), n) == _capi.AHX_ERR_ARG
+    its = np.zeros(1, np.uint32)
+    res = np.zeros(1)
+    assert L.ahx_helm_gmres(h, 0, 1, ptr(X), n, ptr(Y), n, 1e-8, 10, 10, ptr(its), ptr(res)) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_gmres(h, 0, 1, ptr(X), n, ptr(Y), n, 1e-8, 0, 10, ptr(its), ptr(res)) == _capi.AHX_ERR_ARG
+    assert L.ahx_helm_save(h, 0.8, 32, os.fsencode(str(tmp_path / "z.mbls"))) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_agglomerate(h, 1e-6, 2**32 - 1, None) == _capi.AHX_ERR_STATE
+    assert L.ahx_helm_assemble(h, 5.0, 0.0, 1e-6, 2**32 - 1) == _capi.AHX_ERR_ARG
+    assert L.ahx_helm_assemble(h, 5.0, 0.05, -1.0, 2**32 - 1) == _capi.AHX_ERR_ARG
+    assert L.ahx_helm_load(h, os.fsencode(str(tmp_path / "missing.mbls")), None, None) == _capi.AHX_ERR_ARG
+    H.close()
