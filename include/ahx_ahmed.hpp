@@ -44,6 +44,7 @@
 namespace ahx_ahmed {
 
 using dcomp = std::complex<double>;  // the reference's dcomp (Include/cmplx.h)
+using scomp = std::complex<float>;   // the reference's scomp
 
 inline void check(int rc) {
   if (rc != AHX_OK && rc != AHX_NOT_CONVERGED)
@@ -164,6 +165,8 @@ class blcluster {
   int zrank_of(unsigned l) const { return zranks_.at(l); }
   int rank_of(unsigned l, const double*) const { return rank_of(l); }
   int rank_of(unsigned l, const dcomp*) const { return zrank_of(l); }
+  int rank_of(unsigned l, const float*) const { return rank_of(l); }
+  int rank_of(unsigned l, const scomp*) const { return zrank_of(l); }
 
  private:
   unsigned n_;
@@ -179,6 +182,8 @@ using bemblcluster = blcluster;
 // block, n1 x n2 column-major for a dense one.
 template <class T>
 class mblock {
+  static constexpr bool kComplex = std::is_same<T, dcomp>::value || std::is_same<T, scomp>::value;
+
  public:
   mblock(const blcluster* bl, unsigned idx) : bl_(bl), idx_(idx) {}
   // a leaf read by loadmbls, not yet uploaded into a block-cluster tree
@@ -194,9 +199,9 @@ class mblock {
   bool isLrM() const { return bound()->rank_of(idx_, (const T*)nullptr) >= 0; }
   bool isGeM() const { return !isLrM(); }
   // dense diagonal block of a symmetric tree: packed upper triangle (Include/mblock.h:314)
-  bool isHeM() const { return !std::is_same<T, dcomp>::value && diag_dense(); }
+  bool isHeM() const { return !kComplex && diag_dense(); }
   // dense diagonal block of a complex symmetric matrix: packed upper triangle (SyM)
-  bool isSyM() const { return std::is_same<T, dcomp>::value && diag_dense(); }
+  bool isSyM() const { return kComplex && diag_dense(); }
   unsigned rank() const { return (unsigned)bound()->rank_of(idx_, (const T*)nullptr); }
   T* getdata() {
     if (data_.empty()) fetch(bound()->handle(), idx_, data_);
@@ -210,6 +215,18 @@ class mblock {
   static void fetch(ahx_hmat* h, unsigned l, std::vector<double>& d) {
     d.resize(ahx_hmat_leaf_size(h, l));
     if (!d.empty()) check(ahx_hmat_get_leaf(h, l, d.data()));
+  }
+  // mblock<float> / mblock<scomp>: the FP64 / complex128 leaf rounded to single precision
+  static void fetch(ahx_hmat* h, unsigned l, std::vector<float>& d) {
+    std::vector<double> w;
+    fetch(h, l, w);
+    d.assign(w.begin(), w.end());
+  }
+  static void fetch(ahx_hmat* h, unsigned l, std::vector<scomp>& d) {
+    std::vector<dcomp> w;
+    fetch(h, l, w);
+    d.resize(w.size());
+    for (size_t i = 0; i < w.size(); ++i) d[i] = scomp((float)w[i].real(), (float)w[i].imag());
   }
   static void fetch(ahx_hmat* h, unsigned l, std::vector<dcomp>& d) {
     d.resize(ahx_helm_leaf_size(h, l));
@@ -248,6 +265,16 @@ void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankm
   bl->refresh_ranks();
 }
 // mblock<dcomp>: the Helmholtz kernel (apprx_unsym with T = dcomp)
+// mblock<float> / mblock<scomp>: assembled in FP64 / complex128 (the reference's
+// ACA<float> runs in single precision); the products use the FP32 / complex64 copies
+template <class MATGEN_T>
+void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const float*) {
+  assemble_leaves(MatGen, bl, eps, rankmax, (const double*)nullptr);
+}
+template <class MATGEN_T>
+void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const scomp*) {
+  assemble_leaves(MatGen, bl, eps, rankmax, (const dcomp*)nullptr);
+}
 template <class MATGEN_T>
 void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const dcomp*) {
   check(ahx_helm_assemble(bl->handle(), MatGen.getk(), MatGen.geth(), eps, rankmax));
@@ -291,10 +318,17 @@ inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, con
   check(ahx_agglomerate(bl->handle(), eps, max_rank, nullptr));
   bl->refresh();
 }
+inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const float*) {
+  agglomerate_leaves(bl, eps, max_rank, (const double*)nullptr);
+}
+inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const scomp*);
 inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const dcomp*) {
   check(ahx_helm_agglomerate(bl->handle(), eps, max_rank, nullptr));
   bl->refresh_leaves();
   bl->refresh_zranks();
+}
+inline void agglomerate_leaves(blcluster* bl, double eps, unsigned max_rank, const scomp*) {
+  agglomerate_leaves(bl, eps, max_rank, (const dcomp*)nullptr);
 }
 
 template <class T>
@@ -356,6 +390,13 @@ void loadmbls(double& eta, unsigned& bmin, mblock<T>**& A, std::ifstream& is) {
 inline void load_leaves(blcluster* bl, ahx_io_fn get, void* ctx, const double*) {
   check(ahx_hmat_load_stream(bl->handle(), get, ctx, nullptr, nullptr));
   bl->refresh_ranks();
+}
+// files of single-precision leaves (4 or 8 bytes per element) are not read
+inline void load_leaves(blcluster*, ahx_io_fn, void*, const float*) {
+  throw std::logic_error("ahx_ahmed: loadmbls of mblock<float> leaves is not supported");
+}
+inline void load_leaves(blcluster*, ahx_io_fn, void*, const scomp*) {
+  throw std::logic_error("ahx_ahmed: loadmbls of mblock<scomp> leaves is not supported");
 }
 inline void load_leaves(blcluster* bl, ahx_io_fn get, void* ctx, const dcomp*) {
   check(ahx_helm_load_stream(bl->handle(), get, ctx, nullptr, nullptr));
@@ -458,6 +499,81 @@ inline void mltaSyHVec(dcomp d, blcluster* bl, mblock<dcomp>** A, dcomp* x, dcom
 inline void mltaSyHGeM(dcomp d, blcluster* bl, mblock<dcomp>** A, unsigned p, dcomp* X, unsigned ldX, dcomp* Y,
                        unsigned ldY) {
   mltaGeHGeM(d, bl, A, p, X, ldX, Y, ldY);
+}
+
+// H/mltaGeHVec.cpp:671-691 (float) and 908-940 (scomp): the single-precision
+// instantiations, on the FP32 / complex64 copies of the leaves (FP32 accumulation);
+// the vectors pass through double precision
+inline bool sproduct(int op, double d, blcluster* bl, unsigned p, const float* X, unsigned ldX, float* Y,
+                     unsigned ldY) {
+  const unsigned n = bl->getn1();
+  std::vector<double> x((size_t)n * p), y((size_t)n * p);
+  for (unsigned c = 0; c < p; ++c)
+    for (unsigned i = 0; i < n; ++i) {
+      x[(size_t)c * n + i] = X[(size_t)c * ldX + i];
+      y[(size_t)c * n + i] = Y[(size_t)c * ldY + i];
+    }
+  if (op == 0) check(ahx_matvec(bl->handle(), AHX_FP32, d, p, x.data(), n, y.data(), n));
+  else check(ahx_matvec_transposed(bl->handle(), d, p, x.data(), n, y.data(), n));
+  for (unsigned c = 0; c < p; ++c)
+    for (unsigned i = 0; i < n; ++i) Y[(size_t)c * ldY + i] = (float)y[(size_t)c * n + i];
+  return true;
+}
+inline bool mltaGeHVec(float d, blcluster* bl, mblock<float>** A, float* x, float* y) {
+  bind_mbls(bl, A);
+  return sproduct(0, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHGeM(float d, blcluster* bl, mblock<float>** A, unsigned p, float* X, unsigned ldX, float* Y,
+                       unsigned ldY) {
+  bind_mbls(bl, A);
+  return sproduct(0, d, bl, p, X, ldX, Y, ldY);
+}
+// real leaves: A^H = A^T (the FP64 leaves)
+inline bool mltaGeHhVec(float d, blcluster* bl, mblock<float>** A, float* x, float* y) {
+  bind_mbls(bl, A);
+  return sproduct(1, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHhGeM(float d, blcluster* bl, mblock<float>** A, unsigned p, float* X, unsigned ldX, float* Y,
+                        unsigned ldY) {
+  bind_mbls(bl, A);
+  return sproduct(1, d, bl, p, X, ldX, Y, ldY);
+}
+inline bool cproduct(int op, scomp d, blcluster* bl, unsigned p, const scomp* X, unsigned ldX, scomp* Y,
+                     unsigned ldY) {
+  const unsigned n = bl->getn1();
+  std::vector<dcomp> x((size_t)n * p), y((size_t)n * p);
+  for (unsigned c = 0; c < p; ++c)
+    for (unsigned i = 0; i < n; ++i) {
+      x[(size_t)c * n + i] = dcomp(X[(size_t)c * ldX + i].real(), X[(size_t)c * ldX + i].imag());
+      y[(size_t)c * n + i] = dcomp(Y[(size_t)c * ldY + i].real(), Y[(size_t)c * ldY + i].imag());
+    }
+  check(ahx_helm_matvec(bl->handle(), AHX_FP32, op, d.real(), d.imag(), p, reinterpret_cast<double*>(x.data()), n,
+                        reinterpret_cast<double*>(y.data()), n));
+  for (unsigned c = 0; c < p; ++c)
+    for (unsigned i = 0; i < n; ++i)
+      Y[(size_t)c * ldY + i] = scomp((float)y[(size_t)c * n + i].real(), (float)y[(size_t)c * n + i].imag());
+  return true;
+}
+inline bool mltaGeHVec(scomp d, blcluster* bl, mblock<scomp>**, scomp* x, scomp* y) {
+  return cproduct(0, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHGeM(scomp d, blcluster* bl, mblock<scomp>**, unsigned p, scomp* X, unsigned ldX, scomp* Y,
+                       unsigned ldY) {
+  return cproduct(0, d, bl, p, X, ldX, Y, ldY);
+}
+inline bool mltaGeHhVec(scomp d, blcluster* bl, mblock<scomp>**, scomp* x, scomp* y) {
+  return cproduct(1, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHhGeM(scomp d, blcluster* bl, mblock<scomp>**, unsigned p, scomp* X, unsigned ldX, scomp* Y,
+                        unsigned ldY) {
+  return cproduct(1, d, bl, p, X, ldX, Y, ldY);
+}
+inline bool mltaGeHtVec(scomp d, blcluster* bl, mblock<scomp>**, scomp* x, scomp* y) {
+  return cproduct(2, d, bl, 1, x, bl->getn1(), y, bl->getn1());
+}
+inline bool mltaGeHtGeM(scomp d, blcluster* bl, mblock<scomp>**, unsigned p, scomp* X, unsigned ldX, scomp* Y,
+                        unsigned ldY) {
+  return cproduct(2, d, bl, p, X, ldX, Y, ldY);
 }
 
 // Include/matrix.h:20-32

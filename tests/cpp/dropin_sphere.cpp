@@ -139,6 +139,50 @@ int main(int argc, char** argv) {
     freembls(bl3, B);
     delete bl3;
   }
+  bool single_ok = false;
+  {  // the single-precision instantiations: mblock<float> (FP32 leaves) and mblock<scomp>
+    unsigned nb = 0;
+    bemblcluster<dof, dof>* bls = new bemblcluster<dof, dof>(0, 0, N, N);
+    bls->subdivide(cl, cl, eta * eta, nb);
+    mblock<float>** F;
+    allocmbls(bls, F);
+    matgenGeH_omp(gen, nb, bls, eps, 1000000, F);
+    std::vector<float> xf(x.begin(), x.end()), yf(N, 0.f);
+    mltaGeHVec(1.0f, bls, F, xf.data(), yf.data());
+    double df = 0.0, nf = 0.0;
+    for (unsigned i = 0; i < N; ++i) {
+      df += (yf[i] - y[i]) * (yf[i] - y[i]);
+      nf += y[i] * y[i];
+    }
+    const bool f_ok = std::sqrt(df / nf) < 2e-6 && F[0]->getdata() != nullptr;
+    freembls(bls, F);
+    mblock<scomp>** C;
+    allocmbls(bls, C);
+    HelmholtzGen hg{h, 5.0};
+    matgenGeH_omp(hg, nb, bls, eps, 1000000, C);
+    mblock<dcomp>** Cd;  // the same leaves seen in double precision
+    allocmbls(bls, Cd);
+    for (unsigned l = 0; l < nb; ++l) Cd[l] = new mblock<dcomp>(bls, l);
+    std::vector<scomp> xs(N), ys(N, 0.f);
+    std::vector<dcomp> xd(N), yd(N, 0.0);
+    for (unsigned i = 0; i < N; ++i) {
+      xs[i] = scomp((float)x[i], (float)std::cos(0.1 * i));
+      xd[i] = dcomp(xs[i].real(), xs[i].imag());
+    }
+    mltaGeHVec(scomp(1.f, 0.f), bls, C, xs.data(), ys.data());
+    mltaGeHVec(dcomp(1.0, 0.0), bls, Cd, xd.data(), yd.data());
+    double dc = 0.0, nc = 0.0;
+    for (unsigned i = 0; i < N; ++i) {
+      dc += std::norm(dcomp(ys[i].real(), ys[i].imag()) - yd[i]);
+      nc += std::norm(yd[i]);
+    }
+    single_ok = f_ok && std::sqrt(dc / nc) < 2e-5 && C[0]->isLrM() == Cd[0]->isLrM();
+    std::printf("single precision: float product error %.3e, scomp vs dcomp %.3e\n", std::sqrt(df / nf),
+                std::sqrt(dc / nc));
+    freembls(bls, Cd);
+    freembls(bls, C);
+    delete bls;
+  }
   freembls(bl, A);
   delete bl;
 
@@ -274,5 +318,5 @@ int main(int argc, char** argv) {
   freembls(bl2, A);
   delete bl2;
   delete cl;
-  return (err < 2e-6 && errt < 2e-6 && io_ok && sym_ok && helm_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
+  return (err < 2e-6 && errt < 2e-6 && io_ok && sym_ok && helm_ok && single_ok && ret == 0 && geps < 1e-8) ? 0 : 1;
 }

@@ -34,3 +34,4 @@ def test_dropin_runs_on_gpu(tmp_path):
     assert "helmholtz symmetric:" in out.stdout
     assert "helmholtz savembls/loadmbls round trip ok" in out.stdout
     assert "helmholtz agglH:" in out.stdout
+    assert "single precision:" in out.stdout
