@@ -93,3 +93,39 @@ def test_helmholtz_calls_before_assembly_fail_on_the_host(tmp_path):
     assert L.ahx_helm_assemble(h, 5.0, 0.05, -1.0, 2**32 - 1) == _capi.AHX_ERR_ARG
     assert L.ahx_helm_load(h, os.fsencode(str(tmp_path / "missing.mbls")), None, None) == _capi.AHX_ERR_ARG
     H.close()
+
+
+def test_python_mirror_dispatches_by_element_type(monkeypatch):
+    """Complex arrays go to the Helmholtz entry points (the reference's dcomp overloads),
+    real ones to the real leaves: A, A^H, A^T and GMRes (a recording stand-in for the
+    library, no device work)."""
+    from ahmed_gb300 import hmatrix as HM
+
+    P = A.geometry.fibonacci_sphere(256)
+    H = A.HMatrix(P, "bbx", bmin=32, eta=0.8)
+    calls = []
+
+    class Rec:
+        def __getattr__(self, name):
+            def f(*args):
+                calls.append((name, args[2] if name == "ahx_helm_matvec" else None))
+                return 0
+            return f
+
+    monkeypatch.setattr(HM, "lib", lambda: Rec())
+    n = H.n
+    z = np.zeros(n, np.complex128)
+    r = np.zeros(n)
+    H.mltaGeHVec(1.0, z, z.copy())
+    H.mltaGeHhVec(1.0, z, z.copy())
+    H.mltaGeHtVec(1.0, z, z.copy())
+    H.mltaSyHVec(1.0, z, z.copy())
+    H.mltaGeHVec(1.0, r, r.copy())
+    H.mltaGeHhVec(1.0, r, r.copy())
+    H.GMRes(z, z.copy(), 1e-8, 10, 10)
+    H.GMRes(r, r.copy(), 1e-8, 10, 10)
+    assert calls == [("ahx_helm_matvec", 0), ("ahx_helm_matvec", 1), ("ahx_helm_matvec", 2),
+                     ("ahx_helm_matvec", 0), ("ahx_matvec", None), ("ahx_matvec_transposed", None),
+                     ("ahx_helm_gmres", None), ("ahx_gmres", None)]
+    monkeypatch.undo()
+    H.close()
