@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 import ahmed_gb300 as A
+from ahmed_gb300 import _capi
 
 import mbls_format as F
 
@@ -115,3 +116,18 @@ def test_assemble_save_load_round_trip(golden, tag, chunk, tmp_path, monkeypatch
     assert np.linalg.norm(Y1 - Y2) <= 1e-14 * np.linalg.norm(Y1)
     H.close()
     G.close()
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_header_of_complex_file(golden, tag, tmp_path):
+    """ahx_mbls_header reads the common header of a complex file (host only), so the
+    tree can be built before the leaves are loaded."""
+    g, path = _file(golden, tag, tmp_path)
+    eta, bmin, n = A.mbls_header(path)
+    assert eta == float(g["eta"]) and bmin == int(g["bmin"]) and n == len(g[f"{tag}_leaves"])
+    # a tree with another leaf count is refused before any device work
+    H = A.HMatrix(g["points"], "bbx", bmin=int(g["bmin"]), eta=float(g["eta"]))
+    if H.nleaves != n:
+        with pytest.raises(_capi.AhxError, match="leaves"):
+            H.helm_load(path)
+    H.close()
