@@ -1164,9 +1164,16 @@ constexpr size_t kNoAllocHeader = 256;  // task slot + result slot
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-size_t noalloc_bytes(uint32_t n1, uint32_t n2, uint32_t kmax) {
-  const size_t ws = aca_ws_doubles(n1, n2, kmax) * sizeof(double);
-  return kNoAllocHeader + ws + (size_t)(n1 + n2) * sizeof(int);
+// Blocks beyond this many rows or columns, or rank bounds beyond kNoAllocMaxK,
+// are refused before any size arithmetic (they could never fit the array).
+constexpr uint32_t kNoAllocMaxDim = 1u << 20;
+constexpr uint32_t kNoAllocMaxK = 1u << 16;
+
+// bytes of scratch for a block; the ACA columns have the reference's kmax + 1
+// capacity (Include/ACA.h:231-232).  64-bit arithmetic throughout.
+uint64_t noalloc_bytes(uint32_t n1, uint32_t n2, uint32_t kmax) {
+  const uint64_t ws = aca_ws_doubles(n1, n2, kcap_limit(kmax)) * sizeof(double);
+  return kNoAllocHeader + ws + ((uint64_t)n1 + n2) * sizeof(int);
 }
 
 template <int G>
@@ -1218,9 +1225,29 @@ __global__ void __launch_bounds__(G < 64 ? 32 : G)
   }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and context:
+// a context torn down and created again (cudaDeviceReset) loads the module
+// again, so an address resolved in the old context is not reused.
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[256] = {};
+void* g_noalloc_ctx[256] = {};
+
+// the calling thread's current driver context (cuCtxGetCurrent through the
+// runtime's entry-point query, so that the library needs no -lcuda)
+void* current_context() {
+  using Fn = int (*)(void**);
+  static Fn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &f, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<Fn>(f);
+  }();
+  void* ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
 
 }  // namespace
 }  // namespace ahx
@@ -1235,7 +1262,13 @@ extern "C" int ahx_aca_block_noalloc(const double* px, const double* py, const d
     set_error("ahx_aca_block_noalloc: invalid argument");
     return AHX_ERR_ARG;
   }
-  const size_t need = noalloc_bytes(n1, n2, kmax);
+  if (n1 > kNoAllocMaxDim || n2 > kNoAllocMaxDim || kmax > kNoAllocMaxK) {
+    set_error("ahx_aca_block_noalloc: block " + std::to_string(n1) + " x " + std::to_string(n2) +
+              " with kmax " + std::to_string(kmax) + " exceeds the fixed scratch array (" +
+              std::to_string(kNoAllocScratchBytes) + " bytes)");
+    return AHX_ERR_ARG;
+  }
+  const uint64_t need = noalloc_bytes(n1, n2, kmax);
   if (need > kNoAllocScratchBytes) {
     set_error("ahx_aca_block_noalloc: block " + std::to_string(n1) + " x " + std::to_string(n2) +
               " with kmax " + std::to_string(kmax) + " needs " + std::to_string(need) +
@@ -1253,14 +1286,18 @@ extern "C" int ahx_aca_block_noalloc(const double* px, const double* py, const d
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-      // first call on this device: resolve the array's device address (the
-      // current device is the one the kernel will run on)
-      e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch);
+    void* ctx = current_context();
+    if (!g_noalloc_ptr[dev] || ctx != g_noalloc_ctx[dev]) {
+      // first call on this device (or in a new context): resolve the array's
+      // device address; the current device is the one the kernel will run on
+      void* ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
       if (e != cudaSuccess) {
         g_noalloc_ptr[dev] = nullptr;
         return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
       }
+      g_noalloc_ptr[dev] = ptr;
+      g_noalloc_ctx[dev] = current_context();
     }
     scratch = g_noalloc_ptr[dev];
   }
@@ -1271,11 +1308,11 @@ extern "C" int ahx_aca_block_noalloc(const double* px, const double* py, const d
   t.n2 = n2;
   t.i0 = i0;
   t.kmax = kmax;
-  t.kcap = kmax;
+  t.kcap = kcap_limit(kmax);  // never overflows: status is 1 or 0
   t.leaf = 0;
   const PointsSoA P{px, py, pz};
   const double diag = 1.0 / (kFourPi * h);
-  const uint64_t wsd = aca_ws_doubles(n1, n2, kmax);
+  const uint64_t wsd = aca_ws_doubles(n1, n2, t.kcap);
   cudaStream_t s = (cudaStream_t)stream;
   if (std::max(n1, n2) > 256) {
     const size_t smem = sizeof(double) * (kSmemPerGroup + 3 * (kLargeThreads / 32) + 8);

@@ -32,8 +32,10 @@ struct AcaResult {
   uint32_t pad;
 };
 
+// 64-bit throughout: n1 + n2 and kcap * kcap overflow 32 bits for large blocks
 inline uint64_t aca_ws_doubles(uint32_t n1, uint32_t n2, uint32_t kcap) {
-  return 2ull * (uint64_t)(n1 + n2) * kcap + 2ull * kcap * kcap + 3ull * kcap;
+  const uint64_t n = (uint64_t)n1 + n2, k = kcap;
+  return 2ull * n * k + 2ull * k * k + 3ull * k;
 }
 
 struct AcaParams {

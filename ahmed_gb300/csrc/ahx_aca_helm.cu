@@ -1090,9 +1090,9 @@ extern "C" int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, doub
     t.b2 = L.b2;
     t.n2 = L.n2;
     t.kmax = maxk;
-    t.kcap = std::min(maxk, aca_kcap_default());
+    t.kcap = std::min(kcap_limit(maxk), aca_kcap_default());
     if (rank_hint && rank_hint[l] >= 0.f)
-      t.kcap = std::min(maxk, std::max(8u, (uint32_t)std::ceil(rank_hint[l] * 1.25f + 4.f)));
+      t.kcap = std::min(kcap_limit(maxk), std::max(8u, (uint32_t)std::ceil(rank_hint[l] * 1.25f + 4.f)));
     t.leaf = l;
     tasks.push_back(t);
   }
@@ -1135,9 +1135,9 @@ extern "C" int ahx_helm_aca_ranks(ahx_hmat* H, double wavenumber, double h, doub
       AHX_CUDA(cudaStreamSynchronize(H->stream));
       for (uint32_t q = 0; q < nb; ++q) {
         const HTask& t = batch[q];
-        if (res[q].x == kAcaOverflow) {
+        if (res[q].x == kAcaOverflow && t.kcap < kcap_limit(t.kmax)) {
           HTask u = t;
-          u.kcap = std::min(t.kmax, std::max(t.kcap * 4, 16u));
+          u.kcap = std::min(kcap_limit(t.kmax), std::max(t.kcap * 4, 16u));
           retry.push_back(u);
           H->stat_retries++;
         } else {
@@ -1226,7 +1226,7 @@ extern "C" int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, doubl
       t.n2 = L.n2;
       t.i0 = L.i0;
       t.kmax = maxk;
-      t.kcap = std::min(maxk, kcap0);
+      t.kcap = std::min(kcap_limit(maxk), kcap0);
       t.leaf = l;
       tasks.push_back(t);
     } else {
@@ -1281,9 +1281,9 @@ extern "C" int ahx_helm_assemble(ahx_hmat* H, double wavenumber, double h, doubl
       for (uint32_t q = 0; q < nb; ++q) {
         const ZTask& t = batch[q];
         const AcaResult& r = res[q];
-        if (r.status == kAcaOverflow) {
+        if (r.status == kAcaOverflow && t.kcap < kcap_limit(t.kmax)) {
           ZTask u = t;
-          u.kcap = std::min(t.kmax, std::max(t.kcap * 4, 16u));
+          u.kcap = std::min(kcap_limit(t.kmax), std::max(t.kcap * 4, 16u));
           retry.push_back(u);
           H->stat_retries++;
           continue;

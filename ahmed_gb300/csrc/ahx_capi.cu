@@ -82,9 +82,11 @@ int run_aca(ahx_hmat* H, std::vector<AcaTask>& tasks, double diag, double eps,
     for (size_t q = 0; q < all.size(); ++q) {
       const AcaTask& t = all[q];
       const AcaResult& r = res[q];
-      if (r.status == kAcaOverflow) {
+      // an overflow at the full capacity cannot happen (kcap_limit); were it
+      // to, the leaf is treated as an ACA failure so that the loop ends
+      if (r.status == kAcaOverflow && t.kcap < kcap_limit(t.kmax)) {
         AcaTask u = t;
-        u.kcap = std::min(t.kmax, std::max(t.kcap * 4, 16u));
+        u.kcap = std::min(kcap_limit(t.kmax), std::max(t.kcap * 4, 16u));
         retry.push_back(u);
         H->stat_retries++;
         continue;
@@ -677,11 +679,11 @@ int ahx_assemble_hinted(ahx_hmat* H, double h, double eps, uint32_t rankmax,
       t.n2 = L.n2;
       t.i0 = L.i0;
       t.kmax = maxk;
-      t.kcap = std::min(maxk, kcap0);
+      t.kcap = std::min(kcap_limit(maxk), kcap0);
       if (rank_hint && rank_hint[l] >= 0.f) {
         // predicted rank plus a margin; an under-prediction only costs a retry
         const float want = rank_hint[l] * 1.25f + 4.f;
-        t.kcap = std::min(maxk, std::max(8u, (uint32_t)std::ceil(want)));
+        t.kcap = std::min(kcap_limit(maxk), std::max(8u, (uint32_t)std::ceil(want)));
       }
       t.leaf = l;
       tasks.push_back(t);

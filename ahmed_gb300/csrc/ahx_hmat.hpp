@@ -111,6 +111,14 @@ inline uint32_t maxk_of(uint32_t n1, uint32_t n2, uint32_t rankmax) {
   return maxk > rankmax ? rankmax : maxk;
 }
 
+// Largest useful ACA column capacity of a leaf with rank bound kmax.  The
+// reference allocates kmax + 1 columns (Include/ACA.h:231-232) because its
+// column loop takes one more cross when the row loop stops at k == kmax
+// (Include/ACA.h:311-334); that cross decides between success (no pivot left)
+// and failure.  A capacity of kmax + 1 therefore never overflows, and the
+// retry loops of the assembly end.
+inline uint32_t kcap_limit(uint32_t kmax) { return kmax + 1u; }
+
 template <class T>
 int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
   if (v.empty()) return AHX_OK;

@@ -158,10 +158,12 @@ int ahx_helm_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint
                    double tol, uint32_t m, uint32_t maxit, uint32_t* iters, double* resid);
 /* Agglomeration (agglH, H/agglH.cpp:111-272; the recmpr branch of matgenGeH_sqntl,
  * Include/matgen_sqntl.h:32-55): bottom up, a non-diagonal block whose sons are all
- * low-rank leaves becomes one low-rank leaf when the recompressed union (relative
- * threshold eps, rank <= max_rank; unify_sons_, H/agglH.cpp:14-107) stores no more;
- * leaf indices are then compacted as fill_gaps does.  Unions with dense sons are not
- * formed.  Once per assembly.  nmerged (may be NULL): blocks merged. */
+ * leaves becomes one low-rank leaf when the recompressed union (relative threshold
+ * eps, rank <= max_rank; unify_sons_, H/agglH.cpp:14-107) stores no more; leaf
+ * indices are then compacted as fill_gaps does.  Dense sons enter the union in
+ * factored form (D times the identity), and a union of dense sons only is
+ * recompressed as the parent block itself.  Once per assembly.  nmerged (may be
+ * NULL): blocks merged. */
 int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged);
 /* The same for the Helmholtz leaves (agglH with T = dcomp, H/agglH.cpp:291-305).
  * Agglomeration changes the block tree: the handle's other kind of leaves (real
@@ -288,8 +290,9 @@ int ahx_mlp_predict(ahx_mlp* M, const float* X, uint32_t n, float* out);
  * device synchronisation of cudaMalloc/cudaFree, and hosts that own every
  * device allocation and only lend buffers.  The scratch comes from a fixed
  * 8 MiB array inside the library (present on every GPU that loads it, until
- * exit); a block needs 256 + 8*(2*(n1+n2)*kmax + 2*kmax^2 + 3*kmax) +
- * 4*(n1+n2) bytes and larger requests return AHX_ERR_ARG.
+ * exit); with c = kmax + 1 ACA columns (the reference's capacity) a block needs
+ * 256 + 8*(2*(n1+n2)*c + 2*c^2 + 3*c) + 4*(n1+n2) bytes; larger requests, and
+ * n1 or n2 above 2^20 or kmax above 2^16, return AHX_ERR_ARG.
  * Inputs (device): px/py/pz = point coordinates in permuted order; the block
  * is rows b1..b1+n1-1, columns b2..b2+n2-1, ACA start row i0 (< n1), kernel
  * diagonal 1/(4 pi h), accuracy eps, at most kmax ACA steps (the reference's
@@ -297,8 +300,9 @@ int ahx_mlp_predict(ahx_mlp* M, const float* X, uint32_t n, float* out);
  * recompressed factors (kt columns, mblock layout), info[3] = {status
  * (1 = low rank, 0 = ACA failed: fill the block densely), ACA rank, kt}.
  * The kernel is queued on `stream` (NULL = default stream); the call does not
- * wait for it.  The first call on a device resolves the array's device address
- * (make it before any stream capture).  All calls share the array: calls whose
+ * wait for it.  The first call on a device (and the first after its context was
+ * created again, e.g. after cudaDeviceReset) resolves the array's device address:
+ * make it before any stream capture.  All calls share the array: calls whose
  * kernels overlap on the GPU race, so serialise them. */
 int ahx_aca_block_noalloc(const double* px, const double* py, const double* pz, uint32_t b1,
                           uint32_t n1, uint32_t b2, uint32_t n2, uint32_t i0, double h, double eps,

@@ -129,3 +129,16 @@ def test_python_mirror_dispatches_by_element_type(monkeypatch):
                      ("ahx_helm_gmres", None), ("ahx_gmres", None)]
     monkeypatch.undo()
     H.close()
+
+
+def test_noalloc_refuses_oversized_blocks_before_device_work():
+    """Sizes whose n1 + n2 wraps 32 bits, or rank bounds beyond the fixed scratch
+    array, are refused with AHX_ERR_ARG before any CUDA call (no GPU needed)."""
+    import ctypes as C
+
+    L = _capi.lib()
+    fake = C.c_void_p(0x1000)  # never dereferenced: the call returns first
+    for n1, n2, kmax in ((1 << 31, 1 << 31, 4), (100, 100, 1 << 20), (3000, 3000, 500)):
+        rc = L.ahx_aca_block_noalloc(fake, fake, fake, 0, n1, 0, n2, 0, 0.1, 1e-6, kmax, fake, fake, fake, None)
+        assert rc == _capi.AHX_ERR_ARG
+        assert b"scratch" in L.ahx_last_error()

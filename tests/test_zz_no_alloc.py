@@ -24,7 +24,8 @@ KMAX = 64
 
 
 def _scratch_bytes(n1, n2, kmax):
-    return 256 + 8 * (2 * (n1 + n2) * kmax + 2 * kmax * kmax + 3 * kmax) + 4 * (n1 + n2)
+    c = kmax + 1  # ACA column capacity: the reference allocates kmax + 1 columns
+    return 256 + 8 * (2 * (n1 + n2) * c + 2 * c * c + 3 * c) + 4 * (n1 + n2)
 
 
 def _noalloc(torch, pts_dev, leaf, h, eps):
@@ -94,3 +95,10 @@ def test_noalloc_rejects_blocks_beyond_the_scratch():
                                            C.c_void_p(info.data_ptr()), None)
     assert rc == _capi.AHX_ERR_ARG
     assert b"scratch" in _capi.lib().ahx_last_error()
+    # sizes whose n1 + n2 wraps 32 bits are refused too, before any size arithmetic
+    for n1, n2, kmax in ((1 << 31, 1 << 31, 4), (100, 100, 1 << 20)):
+        rc = _capi.lib().ahx_aca_block_noalloc(p, p, p, 0, n1, 0, n2, 0, 0.1, 1e-6, kmax,
+                                               C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()),
+                                               C.c_void_p(info.data_ptr()), None)
+        assert rc == _capi.AHX_ERR_ARG
+        assert b"scratch" in _capi.lib().ahx_last_error()
