@@ -944,6 +944,111 @@ void or_matvec(const or_hmat* H, double d, uint32_t p, const double* X, double* 
 }
 
 /* ------------------------------------------------------------------------ */
+/* CPU baseline of bounded samples                                            */
+
+typedef void (*or_dgemm_t)(const char*, const char*, const int*, const int*, const int*, const double*,
+                           const double*, const int*, const double*, const int*, const double*, double*,
+                           const int*);
+typedef void (*or_dgemv_t)(const char*, const int*, const int*, const double*, const double*, const int*,
+                           const double*, const int*, const double*, double*, const int*);
+static or_dgemm_t g_dgemm = NULL;
+static or_dgemv_t g_dgemv = NULL;
+
+void or_set_blas(void* dgemm, void* dgemv) {
+  g_dgemm = (or_dgemm_t)dgemm;
+  g_dgemv = (or_dgemv_t)dgemv;
+}
+
+void or_assemble_list(or_hmat* H, double h, double eps, uint32_t rankmax, int nthreads,
+                      const uint32_t* leaves, uint32_t count) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t q = 0; q < (int64_t)count; ++q) apprx_leaf(H, h, eps, rankmax, leaves[q]);
+}
+
+/* C = alpha op(A) B + beta C with op = T (transa 'T') or N, column-major */
+static void mm(char ta, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+               double beta, double* Cm, int ldc) {
+  if (g_dgemm) {
+    const char tb = 'N';
+    g_dgemm(&ta, &tb, &m, &n, &k, &alpha, A, &lda, B, &ldb, &beta, Cm, &ldc);
+    return;
+  }
+  for (int c = 0; c < n; ++c)
+    for (int i = 0; i < m; ++i) {
+      double s = 0.0;
+      for (int l = 0; l < k; ++l) s += (ta == 'T' ? A[l + (size_t)i * lda] : A[i + (size_t)l * lda]) * B[l + (size_t)c * ldb];
+      Cm[i + (size_t)c * ldc] = alpha * s + beta * Cm[i + (size_t)c * ldc];
+    }
+}
+
+/* y = alpha op(A) x + y */
+static void mv(char ta, int m, int n, double alpha, const double* A, int lda, const double* x, double* y) {
+  if (g_dgemv) {
+    const int one = 1;
+    const double b1 = 1.0;
+    g_dgemv(&ta, &m, &n, &alpha, A, &lda, x, &one, &b1, y, &one);
+    return;
+  }
+  if (ta == 'N') {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) y[i] += alpha * A[i + (size_t)j * lda] * x[j];
+  } else {
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < m; ++i) s += A[i + (size_t)j * lda] * x[i];
+      y[j] += alpha * s;
+    }
+  }
+}
+
+static void leaf_gem(const or_hmat* H, uint32_t l, double d, uint32_t p, const double* X, uint64_t ldX,
+                     double* Y, uint64_t ldY, double* tmp) {
+  const or_leaf* L = &H->leaves[l];
+  const double* A = H->data[l];
+  const int n1 = (int)L->n1, n2 = (int)L->n2, lx = (int)ldX, ly = (int)ldY;
+  if (!A) return;
+  const double* x = X + L->b2;
+  double* y = Y + L->b1;
+  if (H->rank[l] > 0) {
+    const int k = H->rank[l];
+    const double* V = A + (size_t)k * n1;
+    if (p == 1) { /* mltaLrMVec_: t = V^T x, y += d U t */
+      for (int r = 0; r < k; ++r) tmp[r] = 0.0;
+      mv('T', n2, k, 1.0, V, n2, x, tmp);
+      mv('N', n1, k, d, A, n1, tmp, y);
+    } else { /* mltaLrMGeM_: gemhm then gemma */
+      mm('T', k, (int)p, n2, 1.0, V, n2, x, lx, 0.0, tmp, k);
+      mm('N', n1, (int)p, k, d, A, n1, tmp, k, 1.0, y, ly);
+    }
+  } else if (H->rank[l] < 0) {
+    if (p == 1) mv('N', n1, n2, d, A, n1, x, y);
+    else mm('N', n1, (int)p, n2, d, A, n1, x, lx, 1.0, y, ly);
+  }
+}
+
+void or_matvec_layers(const or_hmat* H, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+                      uint64_t ldY, int nthreads, const uint32_t* leaves, const uint32_t* group_start,
+                      uint32_t ngroups, const uint32_t* layer_start, uint32_t nlayers) {
+  set_threads(nthreads);
+  uint32_t kmax = 1;
+  for (uint32_t q = 0; q < group_start[ngroups]; ++q)
+    if (H->rank[leaves[q]] > (int32_t)kmax) kmax = (uint32_t)H->rank[leaves[q]];
+#pragma omp parallel
+  {
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)kmax * p);
+    for (uint32_t q = 0; q < nlayers; ++q) {
+#pragma omp for schedule(dynamic, 4)
+      for (int64_t g = (int64_t)layer_start[q]; g < (int64_t)layer_start[q + 1]; ++g)
+        for (uint32_t e = group_start[g]; e < group_start[g + 1]; ++e)
+          leaf_gem(H, leaves[e], d, p, X, ldX, Y, ldY, tmp);
+      /* the implicit barrier of the omp for ends the layer */
+    }
+    free(tmp);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* solvers: GMRes (solvers/GMRES.cpp:32-181), CG (solvers/CG.cpp:31-113)      */
 
 static double nrm2(size_t n, const double* x) { return sqrt(dot((uint32_t)n, x, x)); }

@@ -58,6 +58,27 @@ void or_set_leaf(or_hmat* H, uint32_t l, int32_t rank, const double* data);
 /* Y += d A X, X/Y column-major n x p with leading dimension n. nthreads<=0: all */
 void or_matvec(const or_hmat* H, double d, uint32_t p, const double* X, double* Y, int nthreads);
 
+/* ---- CPU baseline of bounded samples (bench.py's reference arm) ---------- */
+/* Fortran BLAS dgemm_/dgemv_ supplied by the caller (e.g. the OpenBLAS that
+ * scipy bundles), used by or_matvec_layers as the reference uses BLAS in
+ * mltaLrMGeM_/mltaGeMGeM (H/mblock.cpp:141-154, Include/mblock.h:105-109).
+ * NULL: plain C loops. */
+void or_set_blas(void* dgemm, void* dgemv);
+/* Assemble the listed leaves only (apprx_unsym per leaf, OpenMP dynamic). */
+void or_assemble_list(or_hmat* H, double h, double eps, uint32_t rankmax, int nthreads,
+                      const uint32_t* leaves, uint32_t count);
+/* Y += d A_S X over a set S of assembled leaves, X/Y column-major with leading
+ * dimensions ldX/ldY.  S is given as groups of leaves that share one row
+ * cluster (leaves[group_start[g] .. group_start[g+1]-1]), and the groups as
+ * layers (groups layer_start[q] .. layer_start[q+1]-1) whose row clusters are
+ * pairwise disjoint: the threads share the groups of one layer, so no two
+ * threads write the same rows and no private accumulators are needed.  Per
+ * leaf, mltaGeM_ (H/mblock.cpp:141-154, 225-238): low rank T = V^T X then
+ * Y += d U T; dense Y += d A X (p = 1: the vector forms scpr/axpy and gemv). */
+void or_matvec_layers(const or_hmat* H, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
+                      uint64_t ldY, int nthreads, const uint32_t* leaves, const uint32_t* group_start,
+                      uint32_t ngroups, const uint32_t* layer_start, uint32_t nlayers);
+
 /* GMRES(m) and CG as the reference solvers (return 0 converged, 1 not). */
 uint32_t or_gmres(const or_hmat* H, const double* b, double* x, double* eps, uint32_t m,
                   uint32_t* nsteps, int nthreads);

@@ -63,6 +63,9 @@ def lib():
         L.or_aca_block.argtypes = [vp, dbl, u32, u32, u32, u32, dbl, u32, u32, vp, vp, vp]
         L.or_recompress.restype = u32
         L.or_recompress.argtypes = [u32, u32, u32, vp, vp, dbl, u32]
+        L.or_set_blas.argtypes = [vp, vp]
+        L.or_assemble_list.argtypes = [vp, dbl, dbl, u32, i32, vp, u32]
+        L.or_matvec_layers.argtypes = [vp, dbl, u32, vp, C.c_uint64, vp, C.c_uint64, i32, vp, vp, u32, vp, u32]
         _lib = L
     return _lib
 
@@ -154,6 +157,21 @@ class OracleH:
         r = lib().or_cg(self._H, _p(b), _p(x), C.byref(e), C.byref(ns), nthreads)
         return r, e.value, ns.value
 
+    def assemble_list(self, leaves, eps=1e-6, rankmax=2**31, nthreads=0):
+        """Assemble only the listed leaves (a bounded sample of the matrix)."""
+        sel = np.ascontiguousarray(leaves, dtype=np.uint32)
+        lib().or_assemble_list(self._H, self.h, eps, min(rankmax, 2**32 - 1), nthreads, _p(sel), len(sel))
+
+    def matvec_layers(self, plan, X, Y, d=1.0, nthreads=0):
+        """Y += d A_S X over the leaves of `plan` (layered_groups), X and Y of shape
+        (p, n) (rows are right-hand sides, i.e. n x p column-major, ld n)."""
+        order, gs, ls = plan
+        assert X.flags.c_contiguous and Y.flags.c_contiguous
+        p = 1 if X.ndim == 1 else X.shape[0]
+        lib().or_matvec_layers(self._H, d, p, _p(X), self.n, _p(Y), self.n, nthreads, _p(order), _p(gs),
+                               len(gs) - 1, _p(ls), len(ls) - 1)
+        return Y
+
     def dense(self):
         """Full matrix in permuted order (small n only)."""
         op, _ = self.perm()
@@ -164,6 +182,59 @@ class OracleH:
         D = np.sqrt((dx * dx + dy * dy) + dz * dz)  # same rounding as or_entry
         np.fill_diagonal(D, self.h)
         return 1.0 / ((4.0 * np.pi) * D)
+
+
+def layered_groups(leaves, sel):
+    """Groups the selected leaves by row cluster (b1, n1) and the groups into
+    layers of pairwise disjoint row clusters (nesting depth in the cluster tree:
+    two clusters either nest or are disjoint).  Returns (order, group_start,
+    layer_start) as uint32 arrays for OracleH.matvec_layers."""
+    sel = np.asarray(sel, dtype=np.int64)
+    key = {}
+    for l in sel:
+        key.setdefault((int(leaves[l, 0]), int(leaves[l, 1])), []).append(int(l))
+    clusters = sorted(key, key=lambda c: (c[0], -c[1]))
+    depth, stack = {}, []
+    for b1, n1 in clusters:
+        while stack and stack[-1] <= b1:
+            stack.pop()
+        depth[(b1, n1)] = len(stack)
+        stack.append(b1 + n1)
+    layers = sorted(set(depth.values()))
+    order, gs, ls = [], [0], [0]
+    for q in layers:
+        for c in clusters:
+            if depth[c] == q:
+                order.extend(key[c])
+                gs.append(len(order))
+        ls.append(len(gs) - 1)
+    u = lambda a: np.asarray(a, dtype=np.uint32)
+    return u(order), u(gs), u(ls)
+
+
+def use_host_blas():
+    """Routes the sampled products through the OpenBLAS that scipy bundles
+    (dgemm_/dgemv_, one thread per caller; the reference calls BLAS in the same
+    places).  Returns a description, or None when no such library is found."""
+    import glob
+    try:
+        import scipy
+    except ImportError:
+        return None
+    d = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    cand = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+    for path in cand:
+        try:
+            B = C.CDLL(path)
+            gemm = C.cast(B.scipy_dgemm_, C.c_void_p).value
+            gemv = C.cast(B.scipy_dgemv_, C.c_void_p).value
+            B.scipy_openblas_set_num_threads(1)
+        except (OSError, AttributeError):
+            continue
+        lib().or_set_blas(gemm, gemv)
+        use_host_blas._keep = B
+        return os.path.basename(path) + " dgemm_/dgemv_, 1 thread per OpenMP thread"
+    return None
 
 
 def ref_available():
