@@ -49,6 +49,10 @@ SIGNATURES = [
     ("ahx_hmat_set_leaves", _i32, [_vp, _vp, _vp, _vp]),
     ("ahx_hmat_storage_bytes", _u64, [_vp, _i32]),
     ("ahx_hmat_prepare", _i32, [_vp, _i32]),
+    ("ahx_hmat_release", _i32, [_vp, _i32]),
+    ("ahx_hmat_stream_bytes", _i32, [_vp, _i32, _vp]),
+    ("ahx_timing", _i32, [_i32]),
+    ("ahx_timing_read", _i32, [_vp, _vp, _i32]),
     ("ahx_matvec", _i32, [_vp, _i32, _dbl, _u32, _vp, _u64, _vp, _u64]),
     ("ahx_gmres", _i32, [_vp, _i32, _u32, _vp, _u64, _vp, _u64, _dbl, _u32, _u32, _vp, _vp]),
     ("ahx_cg", _i32, [_vp, _u32, _vp, _u64, _vp, _u64, _dbl, _u32, _vp, _vp]),

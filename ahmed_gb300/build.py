@@ -17,7 +17,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 # -ffp-contract=off: the tree arithmetic must round exactly like the reference's x86-64 build
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp"]
 
-CU_SOURCES = ["ahx_aca.cu", "ahx_matvec.cu", "ahx_matvec_tc.cu", "ahx_matvec_df.cu", "ahx_capi.cu", "ahx_solve.cu",
+CU_SOURCES = ["ahx_aca.cu", "ahx_matvec.cu", "ahx_matvec_tc.cu", "ahx_matvec_umma.cu", "ahx_matvec_df.cu", "ahx_capi.cu", "ahx_solve.cu",
               "ahx_mlp.cu", "ahx_aca_helm.cu", "ahx_io.cu",
               "ahx_aggl.cu", "ahx_matvec_z.cu", "ahx_solve_z.cu"]
 CXX_SOURCES = ["ahx_tree.cpp"]

@@ -10,6 +10,7 @@
 
 #include "ahx_aca.cuh"
 #include "ahx_hmat.hpp"
+#include "ahx_umma.cuh"
 
 namespace ahx {
 
@@ -423,6 +424,97 @@ int build_mixed_streams(ProdCopy& pc, int prec, const std::vector<PlanLeaf>& lea
   return AHX_OK;
 }
 
+bool um_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("AHX_UMMA");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+int prepare_um(ahx_hmat* H) {
+  ProdCopy& pc = H->prod[kFP32];
+  if (pc.um_valid) return AHX_OK;
+  std::vector<PlanLeaf> pls;
+  ScopedBuf tmp;
+  const double* src = nullptr;
+  int rc;
+  if ((rc = full_leaves(H, pls, tmp, src))) return rc;
+  UmLayout L;
+  int sms = 0;
+  AHX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
+  const uint32_t grid = (uint32_t)std::max(sms, 1);
+  // AHX_UM_KPIECE: V-sweep tiles longer than this are split along K (default 4096)
+  const char* kp = std::getenv("AHX_UM_KPIECE");
+  build_um_layout(pls, H->tree.n, grid, L, (kp && *kp) ? (uint32_t)std::strtoul(kp, nullptr, 10) : 4096u);
+  AHX_CUDA(um_init_attributes());
+  pc.release_um();
+  if ((rc = pc.um_vstream.reserve(std::max<uint64_t>(L.vbytes, 16)))) return rc;
+  if ((rc = pc.um_rstream.reserve(std::max<uint64_t>(L.rbytes, 16)))) return rc;
+  if ((rc = upload(pc.um_vtiles, L.vtiles, H->stream))) return rc;
+  if ((rc = upload(pc.um_rtiles, L.rtiles, H->stream))) return rc;
+  if ((rc = upload(pc.um_zero, L.zero, H->stream))) return rc;
+  if ((rc = upload(pc.um_vranges, L.vranges, H->stream))) return rc;
+  if ((rc = upload(pc.um_rranges, L.rranges, H->stream))) return rc;
+  // Z rows: X rows, T rows, 64 floats each (the widest pass)
+  const uint64_t zrows = H->tree.n + (uint64_t)L.t_rows + 1;
+  if ((rc = pc.um_z.reserve(zrows * 64 * sizeof(float)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.um_z.p, 0, zrows * 64 * sizeof(float), H->stream));
+  if ((rc = pc.err.reserve(sizeof(int)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), H->stream));
+  {
+    DevBuf de, db;
+    if ((rc = upload(de, L.entries, H->stream))) return rc;
+    if ((rc = upload(db, L.vbuild, H->stream))) {
+      de.release();
+      return rc;
+    }
+    cudaError_t ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.vbuild.size(), de.as<UmEntry>(), src,
+                                     pc.um_vstream.as<unsigned char>(), H->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(H->stream);
+    db.release();
+    if (ce == cudaSuccess && (rc = upload(db, L.rbuild, H->stream)) == AHX_OK) {
+      ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.rbuild.size(), de.as<UmEntry>(), src,
+                           pc.um_rstream.as<unsigned char>(), H->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(H->stream);
+    }
+    db.release();
+    de.release();
+    if (rc) return rc;
+    AHX_CUDA(ce);
+  }
+  tmp.release();
+  pc.um_nv = (uint32_t)L.vtiles.size();
+  pc.um_nr = (uint32_t)L.rtiles.size();
+  pc.um_nzero = (uint32_t)L.zero.size();
+  pc.um_trows = L.t_rows;
+  pc.um_grid = grid;
+  pc.um_payload = L.payload_bytes;
+  pc.um_stream_bytes = L.stream_bytes;
+  pc.um_valid = true;
+  return AHX_OK;
+}
+
+UmPlan um_plan(ProdCopy& pc, uint64_t n) {
+  UmPlan pl;
+  pl.vtiles = pc.um_vtiles.as<UmTile>();
+  pl.rtiles = pc.um_rtiles.as<UmTile>();
+  pl.vranges = pc.um_vranges.as<uint32_t>();
+  pl.rranges = pc.um_rranges.as<uint32_t>();
+  pl.grid = pc.um_grid;
+  pl.nvtiles = pc.um_nv;
+  pl.nrtiles = pc.um_nr;
+  pl.vstream = pc.um_vstream.as<unsigned char>();
+  pl.rstream = pc.um_rstream.as<unsigned char>();
+  pl.zero = pc.um_zero.as<UmRange>();
+  pl.nzero = pc.um_nzero;
+  pl.n = n;
+  pl.t_rows = pc.um_trows;
+  pl.z = pc.um_z.as<float>();
+  pl.err = pc.err.as<int>();
+  return pl;
+}
+
 TcPlan mixed_plan(const ProdCopy& pc, uint64_t n) {
   TcPlan pl;
   pl.vunits = pc.vunits.as<TcVUnit>();
@@ -467,7 +559,15 @@ int product_device(ahx_hmat* H, int prec, double d, uint32_t p, const double* X,
     set_error("transposed products use the FP64 leaves");
     return AHX_ERR_ARG;
   }
-  int rc = prepare_product(H, prec);
+  int rc;
+  if (prec == kFP32 && p >= 2 && um_enabled()) {
+    // FP32 leaves, several right-hand sides: the tcgen05 sweeps
+    if ((rc = prepare_um(H))) return rc;
+    const UmPlan pl = um_plan(H->prod[kFP32], H->tree.n);
+    AHX_CUDA(launch_matvec_um(pl, d, p, X, ldX, Y, ldY, H->stream));
+    return AHX_OK;
+  }
+  rc = prepare_product(H, prec);
   if (rc) return rc;
   ProdCopy& pc = H->prod[prec];
   if (prec == kDF64) {
@@ -971,8 +1071,33 @@ int ahx_hmat_set_leaves(ahx_hmat* H, const int32_t* ranks, const double* data,
 uint64_t ahx_hmat_storage_bytes(ahx_hmat* H, int precision) {
   if (!H || !H->assembled) return 0;
   if (ensure_device(H)) return 0;
+  if (precision == kFP32 && um_enabled()) {
+    if (prepare_um(H)) return 0;
+    return H->prod[kFP32].um_payload;
+  }
   if (prepare_product(H, precision)) return 0;
   return H->prod[precision].bytes;
+}
+
+int ahx_hmat_stream_bytes(ahx_hmat* H, int precision, uint64_t* out) {
+  if (!H || !out || precision != kFP32) return AHX_ERR_ARG;
+  if (!H->assembled) return AHX_ERR_STATE;
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  if ((rc = prepare_um(H))) return rc;
+  *out = H->prod[kFP32].um_stream_bytes;
+  return AHX_OK;
+}
+
+int ahx_timing(int enable) {
+  um_timing_enable(enable != 0);
+  return AHX_OK;
+}
+
+int ahx_timing_read(double* ms2, uint64_t* count2, int reset) {
+  if (!ms2 || !count2) return AHX_ERR_ARG;
+  um_timing_read(ms2, count2, reset != 0);
+  return AHX_OK;
 }
 
 int ahx_hmat_prepare(ahx_hmat* H, int precision) {
@@ -983,7 +1108,18 @@ int ahx_hmat_prepare(ahx_hmat* H, int precision) {
   }
   int rc = ensure_device(H);
   if (rc) return rc;
+  if (precision == kFP32 && um_enabled()) return prepare_um(H);
   return prepare_product(H, precision);
+}
+
+int ahx_hmat_release(ahx_hmat* H, int precision) {
+  if (!H || precision < 0 || precision >= kNumPrecisions) return AHX_ERR_ARG;
+  if (precision == kFP64) return AHX_OK;  // the handle's own leaves
+  int rc = ensure_device(H);
+  if (rc) return rc;
+  AHX_CUDA(cudaStreamSynchronize(H->stream));
+  H->prod[precision].release_all();
+  return AHX_OK;
 }
 
 namespace {

@@ -54,6 +54,18 @@ struct ProdCopy {
   DevBuf vstream, rstream, vunits, runits, sides, vranges, rranges, treduce, xb, xf, yr, t, err;
   uint32_t nvunits = 0, nrunits = 0, grid = 0, t_rows = 0, ntreduce = 0, pmax = 16;
   uint32_t unit_bytes = 0;  // unit cap the streams were built with
+  // FP32 leaves on the tcgen05 path (ahx_umma.cuh), products of >= 2 right-hand sides
+  bool um_valid = false;
+  DevBuf um_vstream, um_rstream, um_vtiles, um_rtiles, um_zero, um_z, um_vranges, um_rranges;
+  uint32_t um_nv = 0, um_nr = 0, um_nzero = 0, um_trows = 0, um_grid = 0;
+  uint64_t um_payload = 0, um_stream_bytes = 0;
+  void release_um() {
+    for (DevBuf* b : {&um_vstream, &um_rstream, &um_vtiles, &um_rtiles, &um_zero, &um_z, &um_vranges, &um_rranges})
+      b->release();
+    um_valid = false;
+    um_nv = um_nr = um_nzero = um_trows = um_grid = 0;
+    um_payload = um_stream_bytes = 0;
+  }
   void release_all() {
     for (DevBuf* b : {&lr, &dn, &leaves, &order, &tleaves, &torder, &vstream, &rstream, &vunits, &runits, &sides,
                       &vranges, &rranges, &treduce, &xb, &xf, &yr, &t, &err})
@@ -61,6 +73,7 @@ struct ProdCopy {
     valid = false;
     bytes = 0;
     nleaves = ntleaves = nvunits = nrunits = grid = t_rows = ntreduce = 0;
+    release_um();
   }
 };
 
@@ -165,6 +178,9 @@ struct ahx_hmat {
 
 namespace ahx {
 int prepare_product(ahx_hmat* H, int prec);
+// FP32 leaves as tcgen05 streams (ahx_umma.cuh); AHX_UMMA=0 keeps every FP32 product on the mma.sync sweeps
+int prepare_um(ahx_hmat* H);
+bool um_enabled();
 // kDF64 product scratch for p right-hand sides (the split X), ahead of graph capture
 int prepare_df_x(ahx::ProdCopy& pc, uint64_t n, uint32_t p);
 // Y += d A X in double-float over a leaf table and pc.lr (the split FP64 arena)

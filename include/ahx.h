@@ -186,6 +186,19 @@ int ahx_hmat_set_leaves(ahx_hmat* H, const int32_t* ranks, const double* data,
 uint64_t ahx_hmat_storage_bytes(ahx_hmat* H, int precision);
 /* prepare the product copy at a precision (done lazily by the product otherwise) */
 int ahx_hmat_prepare(ahx_hmat* H, int precision);
+/* free the product copy of a precision (AHX_FP32, AHX_BF16, AHX_DF64; the FP64
+ * leaves stay); the next product at that precision prepares it again.  No
+ * reference counterpart: freembls (Include/H.h:34-45) frees the leaves themselves. */
+int ahx_hmat_release(ahx_hmat* H, int precision);
+/* bytes of the FP32 tcgen05 product streams (leaf images, chunk heads, padding) */
+int ahx_hmat_stream_bytes(ahx_hmat* H, int precision, uint64_t* out);
+/* CUDA-event timing of the product sweeps (measurement instrumentation, no
+ * reference counterpart): enable != 0 records events around every launch of the
+ * FP32 tensor-core sweeps; ahx_timing_read returns per kind (0 = V sweep,
+ * 1 = rows sweep) the summed milliseconds and launch counts (it synchronises),
+ * and forgets them when reset != 0. */
+int ahx_timing(int enable);
+int ahx_timing_read(double* ms2, uint64_t* count2, int reset);
 
 /* Y += d A X for p right-hand sides, column-major with leading dimensions ldX, ldY.
  * X and Y may be host or device pointers (host data are staged through the

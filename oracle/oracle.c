@@ -978,7 +978,8 @@ static void mm(char ta, int m, int n, int k, double alpha, const double* A, int 
     for (int i = 0; i < m; ++i) {
       double s = 0.0;
       for (int l = 0; l < k; ++l) s += (ta == 'T' ? A[l + (size_t)i * lda] : A[i + (size_t)l * lda]) * B[l + (size_t)c * ldb];
-      Cm[i + (size_t)c * ldc] = alpha * s + beta * Cm[i + (size_t)c * ldc];
+      /* beta = 0 ignores C (BLAS semantics: it may hold anything) */
+      Cm[i + (size_t)c * ldc] = alpha * s + (beta != 0.0 ? beta * Cm[i + (size_t)c * ldc] : 0.0);
     }
 }
 
