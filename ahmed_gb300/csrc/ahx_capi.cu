@@ -512,6 +512,13 @@ UmPlan um_plan(ProdCopy& pc, uint64_t n) {
   pl.t_rows = pc.um_trows;
   pl.z = pc.um_z.as<float>();
   pl.err = pc.err.as<int>();
+  // AHX_UM_DRAIN: chunks of 32 K positions accumulated by the tensor core before
+  // the round-to-nearest FP32 add in registers (default 1)
+  static const uint32_t drain = [] {
+    const char* e = std::getenv("AHX_UM_DRAIN");
+    return (e && *e) ? (uint32_t)std::max(1ul, std::strtoul(e, nullptr, 10)) : 1u;
+  }();
+  pl.drain = drain;
   return pl;
 }
 

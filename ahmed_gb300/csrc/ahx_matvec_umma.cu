@@ -38,9 +38,9 @@ namespace {
 using namespace ptx;
 
 constexpr uint32_t kPiece = kUmN * kUmKc * 4;           // 16 KB: largest B image / A piece
-constexpr uint32_t kRing = 128u << 10;                  // ring of chunk images (+ their B lo images)
+constexpr uint32_t kRing = 160u << 10;                  // ring of chunk images (+ their B lo images)
 constexpr uint32_t kSlots = 16;                         // chunk records of the ring
-constexpr uint32_t kA = 4;                              // A stages
+constexpr uint32_t kA = 2;                              // A stages
 constexpr uint32_t kAcc = 4;                            // tensor-memory accumulators (128 columns each)
 constexpr uint32_t kSRow = 65;                          // staging row stride (floats): conflict-free
 constexpr uint32_t kOffA = kRing;
@@ -71,6 +71,7 @@ struct KArgs {
   double d;
   uint32_t pg;          // right-hand sides of this pass
   uint32_t mode;        // 0: V sweep (T out), 1: rows sweep (Y out)
+  uint32_t drain;       // chunks accumulated in tensor memory per drain (>= 1)
   int* err;
 };
 
@@ -230,13 +231,17 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      uint32_t c = 0;
+      // Chunks accumulate in one tensor-memory accumulator for a drain group
+      // (a.drain chunks of one tile, or the rest of the tile); the group's
+      // last chunk commits the accumulator to the epilogue.
+      uint32_t c = 0, gi = 0, gpos = 0;
+      bool gfirst = false;
       bool issued = false;
       while (true) {
-        const uint32_t sl = c % kSlots, as = c % kA, q = c % kAcc;
+        const uint32_t sl = c % kSlots, as = c % kA, q = gi % kAcc;
         if (!wait_bar(S.aready(as), (c / kA) & 1, a.err)) break;
         const uint32_t so = S.slot_off()[sl];
-        if (c >= kAcc && !wait_bar(S.accempty(q), (c / kAcc - 1) & 1, a.err)) break;
+        if (gpos == 0 && gi >= kAcc && !wait_bar(S.accempty(q), (gi / kAcc - 1) & 1, a.err)) break;
         if (so == kStop) {
           // forward the stop to the epilogue (both arrivals of the phase)
           volatile uint32_t* f = &S.acchdr(q)->flags;
@@ -246,7 +251,8 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
           break;
         }
         const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
-        const UmHead h = *E.head();
+        UmHead h = *E.head();
+        if (gpos == 0) gfirst = h.flags & kUmFirst;
         tc_fence_after();
         const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
         const uint32_t idesc = umma_idesc_tf32(128, n16);
@@ -257,16 +263,21 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         const uint32_t d = tmem + q * kUmN;
         for (uint32_t kk = 0; kk < (uint32_t)h.kc / 8u; ++kk) {
           const uint64_t da = umma_desc_sw128(sa + kk * 32u, 1024u);
-          umma_tf32(d, da, umma_desc(sb + kk * 256u, 128u, sbo), idesc, kk > 0 ? 1u : 0u);
+          umma_tf32(d, da, umma_desc(sb + kk * 256u, 128u, sbo), idesc, (kk > 0 || gpos > 0) ? 1u : 0u);
           umma_tf32(d, da, umma_desc(sl2 + kk * 256u, 128u, sbo), idesc, 1u);
         }
         umma_commit(S.bempty(sl));
         umma_commit(S.aempty(as));
-        *S.acchdr(q) = h;
-        umma_commit(S.accfull(q));
-        mbar_arrive(S.accfull(q));  // publishes the head (release)
         issued = true;
         ++c;
+        if (++gpos == a.drain || (h.flags & kUmLast)) {
+          h.flags = (h.flags & ~kUmFirst) | (gfirst ? kUmFirst : 0u);
+          *S.acchdr(q) = h;
+          umma_commit(S.accfull(q));
+          mbar_arrive(S.accfull(q));  // publishes the head (release)
+          gpos = 0;
+          ++gi;
+        }
       }
       // the MMAs issued last have completed before the tensor memory is freed
       if (issued) wait_bar(S.aempty((c - 1) % kA), ((c - 1) / kA) & 1, a.err);
@@ -300,14 +311,14 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         }
       }
     };
-    auto finalize = [&](uint32_t c) {
+    auto finalize = [&](uint32_t c, const float4 (&vf)[4]) {
       const uint32_t so = S.slot_off()[c % kSlots], as = c % kA;
       const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
       const UmHead h = *E.head();
       if (gather && 4 * kb < h.kc) {
         unsigned char* atom = S.astage(as) + g * 1024u;
-        const float x[4][4] = {{vc[0].x, vc[0].y, vc[0].z, vc[0].w}, {vc[1].x, vc[1].y, vc[1].z, vc[1].w},
-                               {vc[2].x, vc[2].y, vc[2].z, vc[2].w}, {vc[3].x, vc[3].y, vc[3].z, vc[3].w}};
+        const float x[4][4] = {{vf[0].x, vf[0].y, vf[0].z, vf[0].w}, {vf[1].x, vf[1].y, vf[1].z, vf[1].w},
+                               {vf[2].x, vf[2].y, vf[2].z, vf[2].w}, {vf[3].x, vf[3].y, vf[3].z, vf[3].w}};
 #pragma unroll
         for (uint32_t t = 0; t < 4; ++t) {
           float hi[4], lo[4];
@@ -335,33 +346,39 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
       __syncwarp();
       if (lane == 0) mbar_arrive(S.aready(as));
     };
+    // One step per chunk c: the loads of chunk c go into one register set while
+    // chunk c - 1 is finalised from the other (ping-pong: the loads have a whole
+    // step to land).  Returns false when the role is done.
     bool have_prev = false;
-    for (uint32_t c = 0;; ++c) {
+    auto step = [&](uint32_t c, float4 (&vload)[4], float4 (&vfin)[4]) -> bool {
       const uint32_t sl = c % kSlots;
-      if (!wait_bar(S.bfull(sl), (c / kSlots) & 1, a.err)) break;
+      if (!wait_bar(S.bfull(sl), (c / kSlots) & 1, a.err)) return false;
       const uint32_t so = S.slot_off()[sl];
       const bool stop = so == kStop;
       if (!stop) {
         const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
         const UmHead h = *E.head();
-        load(h, E.idx(), vn);
+        load(h, E.idx(), vload);
       }
       if (have_prev) {
         // the A stage of chunk c - 1 is free once the MMAs of chunk c - 1 - kA are done
         const uint32_t cp = c - 1;
-        if (cp >= kA && !wait_bar(S.aempty(cp % kA), (cp / kA - 1) & 1, a.err)) break;
-        finalize(cp);
+        if (cp >= kA && !wait_bar(S.aempty(cp % kA), (cp / kA - 1) & 1, a.err)) return false;
+        finalize(cp, vfin);
       }
-#pragma unroll
-      for (uint32_t i = 0; i < 4; ++i) vc[i] = vn[i];
       have_prev = !stop;
       if (stop) {
         // pass the stop on to the MMA issuer through this chunk's A stage
-        if (c >= kA && !wait_bar(S.aempty(c % kA), (c / kA - 1) & 1, a.err)) break;
+        if (c >= kA && !wait_bar(S.aempty(c % kA), (c / kA - 1) & 1, a.err)) return false;
         __syncwarp();
         if (lane == 0) mbar_arrive(S.aready(c % kA));
-        break;
+        return false;
       }
+      return true;
+    };
+    for (uint32_t c = 0;; c += 2) {
+      if (!step(c, vn, vc)) break;
+      if (!step(c + 1, vc, vn)) break;
     }
   } else {
     // ---------------- epilogue
@@ -614,6 +631,7 @@ cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const d
   a.z = pl.z;
   a.err = pl.err;
   a.pg = pg;
+  a.drain = std::max<uint32_t>(1u, pl.drain);
   if (pl.nvtiles) {
     a.tiles = pl.vtiles;
     a.ranges = pl.vranges;

@@ -140,6 +140,7 @@ struct UmPlan {
   uint32_t t_rows = 0;
   float* z = nullptr;      // Z rows: X rows (n) then T rows (t_rows), 64 floats each (P used)
   int* err = nullptr;
+  uint32_t drain = 1;      // chunks accumulated in tensor memory per drain into registers
 };
 
 cudaError_t um_init_attributes();

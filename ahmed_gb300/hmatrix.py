@@ -250,6 +250,10 @@ class HMatrix:
     def prepare(self, precision="fp64"):
         check(lib().ahx_hmat_prepare(self._h, _prec(precision)))
 
+    def release(self, precision):
+        """Frees the product copy of a precision (not the FP64 leaves)."""
+        check(lib().ahx_hmat_release(self._h, _prec(precision)))
+
     # -- Helmholtz leaves (mblock<dcomp>) ---------------------------------
     def helmholtz_assemble(self, wavenumber, h=None, eps=1e-6, rankmax=2**32 - 1):
         """The Helmholtz H-matrix exp(ikr)/(4 pi r) (diagonal exp(ikh)/(4 pi h)) on this

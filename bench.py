@@ -1,4 +1,16 @@
-"""Benchmark: batched H-matvec on one GB300 (and the CPU reference path beside it).
+"""Benchmark: H-matvec and GMRES on one GB300 (and the CPU reference path beside it).
+
+Default workload (--workload headline): N = 1,048,576 uniform random points on
+the unit-cube surface (seed 4), Laplace kernel with diagonal 1/(4 pi h), h = half
+the smallest nearest-neighbour distance, bounding-box tree, leaf 64, eta 0.8, ACA
+eps 1e-6; 64 right-hand sides.  A step is one product Y += A X with all 64
+right-hand sides, FP32 leaves on the tensor cores (error per right-hand side
+against the FP64 product <= 1e-6); `value` counts vector products per second.
+The same line carries the BF16-factor product with its error, the plain FP64
+product, and GMRES(50) to a 1e-8 FP64 residual (mixed and plain, median of 3
+solves).  The leaf streams (tens of GB) are larger than L2: no flush.
+
+The --workload sphere case below is the N = 65,536 sphere benchmark:
 
 Workload (Laplace single-layer collocation on the unit sphere):
   N = 65,536 Fibonacci-sphere points, K(x,y) = 1/(4 pi |x-y|), diagonal
@@ -758,21 +770,321 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# Headline workload: N = 1,048,576 uniform random points on the unit-cube surface
+# (seed 4), Laplace kernel, bounding-box tree, leaf 64, eta 0.8, ACA eps 1e-6,
+# 64 right-hand sides; products, and GMRES(50) to a 1e-8 FP64 residual.
+HL_N, HL_P, HL_LEAF = 1 << 20, 64, 64
+HEADLINE = {
+    "workload": "laplace-cube-1048576-64rhs",
+    "points": "uniform random points on the unit-cube surface (numpy PCG64 seed 4)",
+    "n": HL_N, "rhs": HL_P, "tree": "bbx", "leaf": HL_LEAF, "eta": ETA, "eps": EPS,
+    "kernel": "1/(4 pi r)",
+    "diag": "1/(4 pi h), h = smallest nearest-neighbour distance / 2 (with the mean spacing the "
+            "matrix of a random cloud is indefinite and GMRES stagnates)",
+    "x": "X ~ U[-1, 1] (seed 5)",
+    "gmres": "GMRES(50) to a 1e-8 relative FP64 residual, b ~ N(0, 1) (seed 6)",
+    "l2": "inputs larger than L2 (no flush)",
+}
+METRIC_HL = "H-matvec/s & GMRES solves/s"
+
+
+def _min_nn_host(P):
+    """Smallest nearest-neighbour distance (host, scipy k-d tree): the CPU arm sets
+    h without the library."""
+    from scipy.spatial import cKDTree
+
+    d, _ = cKDTree(P).query(P, k=2)
+    return float(d[:, 1].min())
+
+
+def cpu_sample(n, p, leaf, steps, warmup, threads, frac=8, seed=9):
+    """The reference path on the host cores, on a bounded sample of the headline
+    matrix: 1/frac of its leaves (uniform random, seeded) assembled by the oracle
+    (apprx_unsym per leaf), multiplied with the reference's BLAS calls per leaf
+    (mltaGeM_, H/mblock.cpp:141-154) by OpenMP threads sharing row-disjoint leaf
+    groups.  The product cost is a sum over leaves, so the full product's time is
+    the sample's times frac.  GMRES per right-hand side (solvers/GMRES.cpp:80-181)
+    costs per step one single-vector product and the Gram-Schmidt work of the
+    step (timed on full-length vectors, averaged over a 50-step cycle)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from ahmed_gb300 import geometry as G
+
+    P = G.cube_surface(n, 4)
+    h = _min_nn_host(P) / 2
+    Ho = O.OracleH(P, O.TREE_BBX, leaf, ETA, h)
+    lv = Ho.leaves()
+    nl = len(lv)
+    sel = np.sort(np.random.default_rng(seed).choice(nl, nl // frac, replace=False))
+    blas = O.use_host_blas()
+    t0 = time.perf_counter()
+    Ho.assemble_list(sel, EPS, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    plan = O.layered_groups(lv, sel)
+    scale = nl / len(sel)
+    X = np.random.default_rng(5).uniform(-1.0, 1.0, (p, n))
+    Y = np.zeros_like(X)
+    for _ in range(max(1, warmup)):
+        Ho.matvec_layers(plan, X, Y, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        Ho.matvec_layers(plan, X, Y, nthreads=threads)
+    t_prod = (time.perf_counter() - t0) / steps
+    x1 = X[0].copy()
+    y1 = np.zeros(n)
+    Ho.matvec_layers(plan, x1, y1, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        Ho.matvec_layers(plan, x1, y1, nthreads=threads)
+    t_prod1 = (time.perf_counter() - t0) / 3
+    # Gram-Schmidt of a 50-step cycle: step i takes i + 1 dots and axpys over n
+    V = np.random.default_rng(1).standard_normal((26, n))
+    w = np.random.default_rng(2).standard_normal(n)
+    t0 = time.perf_counter()
+    for i in range(25):
+        w -= (V[i] @ w) * V[i]
+    np.linalg.norm(w)
+    t_orth = (time.perf_counter() - t0) / 25 * 25.5  # mean step of the cycle: 25.5 vectors
+    return {"products_per_s": p / (t_prod * scale), "product_s_full": t_prod * scale,
+            "product1_s_full": t_prod1 * scale, "gmres_step_s": t_prod1 * scale + t_orth,
+            "assembly_s_sample": t_asm, "assembly_s_full_estimate": t_asm * scale,
+            "sample_leaves": int(len(sel)), "leaves": int(nl), "scale": scale, "blas": blas,
+            "cores": threads}
+
+
+def _cpu_desc(c, steps):
+    return (f"{c['sample_leaves']} of the {c['leaves']} leaves of the same matrix (1/{c['scale']:.0f}, uniform "
+            f"random, seed 9) assembled by the oracle and multiplied {steps} times with 64 right-hand "
+            f"sides (reference BLAS calls per leaf: {c['blas'] or 'C loops'}); the full product's time is "
+            f"the sample's x {c['scale']:.2f}")
+
+
+def run_reference_headline(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    c = cpu_sample(HL_N, HL_P, HL_LEAF, max(1, args.steps), max(1, args.warmup // 3), threads)
+    val = c["products_per_s"]
+    line = {
+        "impl": "reference", "metric": METRIC_HL, "value": val, "unit": "vector products/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": c["product_s_full"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": dict(HEADLINE),
+        "cpu_baseline": {"value": val, "unit": "vector products/s", "cores": threads, "kind": "port",
+                         "sample": _cpu_desc(c, args.steps)},
+        "e2e": {"value": val, "unit": "vector products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "details": {"cpu": c},
+    }
+    print(json.dumps(line))
+
+
+def _kernel_bytes(H, p):
+    """Algorithmic bytes of the two FP32 sweeps of one product: V sweep = V factors
+    + X read; rows sweep = U factors + dense leaves + Y read and written (FP64)."""
+    lv = H.leaves()
+    r = H.ranks()
+    n1, n2 = lv[:, 1].astype(np.int64), lv[:, 3].astype(np.int64)
+    lr = r > 0
+    v = 4 * int((n2[lr] * r[lr]).sum())
+    u = 4 * int((n1[lr] * r[lr]).sum())
+    d = 4 * int((n1[r < 0] * n2[r < 0]).sum())
+    return {"v_sweep": v + 8 * p * H.n, "rows_sweep": u + d + 16 * p * H.n}
+
+
+def run_headline(args):
+    import torch
+    import ahmed_gb300 as A
+    from ahmed_gb300 import _capi
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, p = HL_N, HL_P
+    P = A.geometry.cube_surface(n, 4)
+    t0 = time.perf_counter()
+    h = A.min_nn(P) / 2
+    H = A.HMatrix(P, "bbx", bmin=HL_LEAF, eta=ETA, device=local)
+    t_tree = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    H.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    H.matgenGeH_omp(h, EPS)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    ranks = H.ranks()
+    L = _capi.lib()
+    X = torch.from_numpy(np.random.default_rng(5).uniform(-1.0, 1.0, (p, n))).to(dev)
+    Y = torch.zeros_like(X)
+    t0 = time.perf_counter()
+    H.prepare("fp32")
+    torch.cuda.synchronize()
+    t_prep32 = time.perf_counter() - t0
+    H.prepare("fp64")
+    launches = {}
+
+    def timed(prec, steps, warmup, kernel_times=False):
+        for _ in range(warmup):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        ms2, cnt2 = np.zeros(2), np.zeros(2, np.uint64)
+        if kernel_times:
+            L.ahx_timing_read(ms2.ctypes.data, cnt2.ctypes.data, 1)
+            L.ahx_timing(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = L.ahx_kernel_launches()
+        e0.record(stream)
+        for _ in range(steps):
+            H.mltaGeHVec(1.0, X, Y, precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches[prec] = int(L.ahx_kernel_launches() - l0)
+        ms = e0.elapsed_time(e1)
+        if kernel_times:
+            L.ahx_timing_read(ms2.ctypes.data, cnt2.ctypes.data, 1)
+            L.ahx_timing(0)
+        if ws > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps, (ms2 / np.maximum(cnt2, 1), cnt2)
+
+    with ClockSampler(local) as cs:
+        ms32, (kms, kcnt) = timed("fp32", args.steps, args.warmup, kernel_times=True)
+    clocks = cs.summary()
+    ms64, _ = timed("fp64", 2, 1)
+    Y64 = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Y64, precision="fp64")
+    Y32 = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Y32, precision="fp32")
+    torch.cuda.synchronize()
+    err32 = float(((Y32 - Y64).norm(dim=1) / Y64.norm(dim=1)).max())
+    del Y32
+    # end to end through the public API: pinned host X and Y, copies inside the timed region
+    Xh = torch.from_numpy(np.random.default_rng(5).uniform(-1.0, 1.0, (p, n))).pin_memory()
+    Yh = torch.zeros_like(Xh).pin_memory()
+    for _ in range(2):
+        H.mltaGeHVec(1.0, Xh.numpy(), Yh.numpy(), precision="fp32")
+    torch.cuda.synchronize()
+    ne2e = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        H.mltaGeHVec(1.0, Xh.numpy(), Yh.numpy(), precision="fp32")
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ne2e
+    # BF16 factors beside it (the C5 storage of the task), with its error per right-hand side
+    H.release("fp32")
+    t0 = time.perf_counter()
+    H.prepare("bf16")
+    torch.cuda.synchronize()
+    t_prepb = time.perf_counter() - t0
+    msb, _ = timed("bf16", max(3, args.steps // 2), 2)
+    Yb = torch.zeros_like(X)
+    H.mltaGeHVec(1.0, X, Yb, precision="bf16")
+    torch.cuda.synchronize()
+    errb = float(((Yb - Y64).norm(dim=1) / Y64.norm(dim=1)).max())
+    del Yb, Y64, Y
+    # GMRES(50) to 1e-8: mixed (BF16/FP32 inner solves, FP64 refinement) and plain FP64, 3 solves each
+    B = torch.from_numpy(np.random.default_rng(6).standard_normal((p, n))).to(dev)
+    gm = {}
+    for prec in ("bf16", "fp64"):
+        runs = []
+        for _ in range(args.gmres_solves):
+            Xs = torch.zeros_like(B)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st, rr, its = H.GMRes(B, Xs, 1e-8, 50, args.gmres_cap, precision=prec)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            R = B.clone()
+            H.mltaGeHVec(-1.0, Xs, R, precision="fp64")
+            true = float((R.norm(dim=1) / B.norm(dim=1)).max())
+            runs.append({"s": dt, "converged": st == 0, "max_iters": int(its.max()),
+                         "true_max_resid": true})
+            del Xs, R
+        secs = sorted(r["s"] for r in runs)
+        med = secs[len(secs) // 2]
+        ok = all(r["converged"] and r["true_max_resid"] <= 1e-8 for r in runs)
+        gm[prec] = {"median_s": med, "solves_per_s": (p / med) if ok else None, "runs": runs}
+    if gm["bf16"]["solves_per_s"] and gm["fp64"]["solves_per_s"]:
+        gm["mixed_over_plain"] = gm["bf16"]["solves_per_s"] / gm["fp64"]["solves_per_s"]
+    peak, peak_kind = _peaks()
+    kb = _kernel_bytes(H, p)
+    total_alg = H.storage_bytes("fp64") // 2 + p * n * 24  # FP32 payload + X read + Y read and written
+    dom = 1 if kms[1] >= kms[0] else 0
+    dom_bytes = kb["rows_sweep"] if dom == 1 else kb["v_sweep"]
+    achieved = dom_bytes / (kms[dom] * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("umma_rows_sweep_fp32_64rhs_cube1048576")
+        except Exception:
+            traffic = None
+    value = ws * p / (ms32 * 1e-3)
+    line = {
+        "metric": METRIC_HL, "value": value, "unit": "vector products/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(HEADLINE),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": ("um_sweep_kernel rows sweep" if dom == 1 else "um_sweep_kernel V sweep"),
+                     "kernel_ms": float(kms[dom]), "kernel_algorithmic_bytes": dom_bytes,
+                     "step": {"algorithmic_bytes": total_alg, "achieved": total_alg / (ms32 * 1e-3) / 1e9,
+                              "frac": total_alg / (ms32 * 1e-3) / 1e9 / peak}},
+        "e2e": {"value": ws * p / e2e_s, "unit": "vector products/s", "h2d_bytes_per_step": p * n * 16,
+                "d2h_bytes_per_step": p * n * 8},
+        "gpu_launches": launches.get("fp32"),
+        "clocks": clocks,
+        "gmres": {"mixed_bf16_solves_per_s": gm["bf16"]["solves_per_s"], "plain_fp64_solves_per_s":
+                  gm["fp64"]["solves_per_s"], "mixed_over_plain": gm.get("mixed_over_plain"), "detail": gm},
+        "details": {"tree_s": t_tree, "assembly_s": t_asm, "leaves": int(H.nleaves),
+                    "lowrank_leaves": int((ranks >= 0).sum()), "avg_rank": float(ranks[ranks >= 0].mean()),
+                    "fp64_leaf_bytes": int(H.storage_bytes("fp64")), "fp32_prepare_s": t_prep32,
+                    "bf16_prepare_s": t_prepb, "fp32_max_rel_err_per_rhs": err32,
+                    "plain_fp64_ms": ms64, "fp32_over_fp64_product": ms64 / ms32,
+                    "bf16_ms": msb, "bf16_max_rel_err_per_rhs": errb,
+                    "sweep_ms": {"v": float(kms[0]), "rows": float(kms[1])}, "sweep_bytes": kb},
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        c = cpu_sample(n, p, HL_LEAF, 3, 1, threads)
+        line["cpu_baseline"] = {"value": c["products_per_s"], "unit": "vector products/s", "cores": threads,
+                                "kind": "port", "sample": _cpu_desc(c, 3),
+                                "gmres_solves_per_s_estimate": 1.0 / (c["gmres_step_s"] * gm["fp64"]["runs"][0]["max_iters"]),
+                                "gmres_step_s": c["gmres_step_s"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ahx", choices=["ahx", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--autotune", type=int, default=1, help="1: tune the stream bucketing before timing")
     ap.add_argument("--n", type=int, default=N_POINTS,
                     help="number of points (smaller cases are for profiling only)")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cube-large", "batch", "product", "predictor", "helmholtz",
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "sphere", "cube-large", "batch", "product", "predictor", "helmholtz",
                              "zhmat", "aggl"],
-                    help="sphere: the default product benchmark; cube-large: N = 2^20 "
-                         "cube surface, 64 right-hand sides, products and GMRES; batch: "
-                         "256 uneven instances, one launch per product, batched GMRES")
+                    help="headline (default): N = 2^20 cube surface, leaf 64, 64 right-hand sides, FP32 "
+                         "products on the tensor cores and GMRES(50); sphere: N = 65,536 sphere, 16 "
+                         "right-hand sides; cube-large: the same N = 2^20 workload with BF16 factors; "
+                         "batch: 256 uneven instances, one launch per product, batched GMRES")
+    ap.add_argument("--gmres-solves", type=int, default=3, help="headline: timed GMRES solves per form (median)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--geometry", default="sphere", choices=["sphere", "cube"], help="product workload")
     ap.add_argument("--leaf", type=int, default=BMIN, help="product workload")
@@ -794,7 +1106,12 @@ def main():
     if args.n != N_POINTS:
         set_size(args.n)
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "sphere":
+            run_reference(args)
+        else:
+            run_reference_headline(args)
+    elif args.workload == "headline":
+        run_headline(args)
     elif args.workload == "cube-large":
         run_large(args)
     elif args.workload == "batch":
@@ -810,7 +1127,7 @@ def main():
     elif args.workload == "aggl":
         run_aggl(args)
     else:
-        run_gpu(args)
+        run_gpu(args)  # sphere
 
 
 if __name__ == "__main__":
