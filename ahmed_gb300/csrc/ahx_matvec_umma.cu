@@ -2,25 +2,27 @@
 // tensor-memory accumulators) over FP32 leaf streams; the layout, the sweeps
 // and the precision scheme are described in ahx_umma.cuh.
 //
-// One persistent CTA per SM, 10 warps with fixed roles:
+// One persistent CTA per SM, 14 warps with fixed roles:
 //   warp 0      producer: walks the CTA's contiguous range of tiles (ranges
 //               balanced by bytes; descriptors fetched 32 at a time) and
 //               bulk-copies (cp.async.bulk) each chunk image (indices, head, B)
 //               into a byte ring of kRing bytes, as far ahead as the ring and
-//               its kSlots slot records allow; each ring entry also reserves
-//               room for the chunk's B lo image
+//               its kSlots slot records allow
 //   warp 1      MMA issuer (one thread) and owner of the tensor memory: per
-//               chunk, 2 * kc / 8 tcgen05.mma (B hi and B lo parts) into one
+//               chunk, 2 * kc / 8 tcgen05.mma (B as copied, which the tensor
+//               core reads truncated to TF32, and its remainder image) into one
 //               of four 128-column accumulators, then tcgen05.commit to the
-//               ring slot, the A stage and the accumulator
-//   warps 2-5   A gather: 16-byte loads of the chunk's Z values one chunk
-//               ahead, split into TF32 hi/lo parts and stored in one of kA A
-//               stages (128-byte-swizzled K-major); the TF32 split of the B
-//               image into hi (in place) and lo images; then the stage is
-//               released to the MMA issuer
-//   warps 6-9   epilogue: tensor memory -> registers (round-to-nearest FP32
-//               adds per chunk), and at the end of a tile the sum, staged
-//               through shared memory, into Y (FP64, in place) or T
+//               ring slot, the stage and the accumulator
+//   warps 2-5   stage filling: 16-byte loads of the chunk's Z values one chunk
+//               ahead, split into TF32 hi/lo parts and stored as A in one of
+//               kA stages (128-byte-swizzled K-major), and the remainder image
+//               B - trunc(B) beside it; then the stage is released to the MMA
+//               issuer
+//   warps 6-13  epilogue, two warps per tensor-memory lane quadrant (columns
+//               0-63 and 64-127): each thread adds its accumulator row to
+//               registers (round-to-nearest FP32) per chunk; at the end of a
+//               tile the hi and lo rows are summed through shared memory into
+//               Y (FP64, in place) or T
 // Every wait is bounded: on timeout the kernel raises the error word and all
 // roles return after the copies and MMAs they started have completed.
 #include <algorithm>
@@ -38,24 +40,26 @@ namespace {
 using namespace ptx;
 
 constexpr uint32_t kPiece = kUmN * kUmKc * 4;           // 16 KB: largest B image / A piece
-constexpr uint32_t kRing = 160u << 10;                  // ring of chunk images (+ their B lo images)
+constexpr uint32_t kRing = 120u << 10;                  // ring of chunk images (head + B)
 constexpr uint32_t kSlots = 16;                         // chunk records of the ring
-constexpr uint32_t kA = 2;                              // A stages
+constexpr uint32_t kA = 2;                              // stages (A + the B remainder image)
 constexpr uint32_t kAcc = 4;                            // tensor-memory accumulators (128 columns each)
 constexpr uint32_t kSRow = 65;                          // staging row stride (floats): conflict-free
-constexpr uint32_t kOffA = kRing;
-constexpr uint32_t kOffStaging = kOffA + kA * kPiece;
-constexpr uint32_t kOffAccHdr = kOffStaging + 64 * kSRow * 4;
+constexpr uint32_t kOffA = kRing;                       // stage i: A at kOffA + 2 i kPiece, B lo after it
+constexpr uint32_t kOffStaging = kOffA + 2 * kA * kPiece;
+constexpr uint32_t kStagingBytes = 64 * kSRow * 4;      // per column half
+constexpr uint32_t kOffAccHdr = kOffStaging + 2 * kStagingBytes;
 constexpr uint32_t kOffSlotOff = kOffAccHdr + kAcc * sizeof(UmHead);
 constexpr uint32_t kOffEnd = kOffSlotOff + kSlots * 4;   // producer's end positions (u64)
 constexpr uint32_t kOffBar = kOffEnd + kSlots * 8;
 constexpr uint32_t kNumBars = 2 * kSlots + 2 * kA + 2 * kAcc;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
 constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;   // + alignment slack of the dynamic base
-constexpr uint32_t kThreads = 320;
+constexpr uint32_t kThreads = 448;
+constexpr uint32_t kEpiWarps = 8;                       // epilogue warps: each arrives on accempty
 constexpr uint32_t kTmemCols = kAcc * kUmN;             // all 512 columns
 constexpr uint32_t kStop = 0xffffffffu;                 // slot record of the stop marker
-constexpr uint32_t kMaxEntry = kUmIdxBytes + 32 + 2 * kPiece;
+constexpr uint32_t kMaxEntry = kUmIdxBytes + 32 + kPiece;
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 // the gather keeps one chunk unconverted: two entries (and the wrap gap) fit the ring
 static_assert(3 * kMaxEntry <= kRing, "ring size");
@@ -78,8 +82,11 @@ struct KArgs {
 struct Smem {
   unsigned char* base;
   __device__ unsigned char* ring() const { return base; }
-  __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + i * kPiece; }
-  __device__ float* staging() const { return reinterpret_cast<float*>(base + kOffStaging); }
+  __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + 2 * i * kPiece; }
+  __device__ unsigned char* lostage(uint32_t i) const { return base + kOffA + (2 * i + 1) * kPiece; }
+  __device__ float* staging(uint32_t half) const {
+    return reinterpret_cast<float*>(base + kOffStaging + half * kStagingBytes);
+  }
   __device__ UmHead* acchdr(uint32_t a) const { return reinterpret_cast<UmHead*>(base + kOffAccHdr) + a; }
   __device__ uint32_t* slot_off() const { return reinterpret_cast<uint32_t*>(base + kOffSlotOff); }
   __device__ uint64_t* endpos() const { return reinterpret_cast<uint64_t*>(base + kOffEnd); }
@@ -93,7 +100,7 @@ struct Smem {
   __device__ uint32_t* tmem_slot() const { return reinterpret_cast<uint32_t*>(base + kOffTmem); }
 };
 
-// a chunk image in the ring: [indices (hdr - 32 bytes)] [UmHead] [B] [B lo]
+// a chunk image in the ring: [indices (hdr - 32 bytes)] [UmHead] [B]
 struct Entry {
   const unsigned char* img;
   uint32_t hdr;
@@ -102,8 +109,15 @@ struct Entry {
   __device__ unsigned char* b() const { return const_cast<unsigned char*>(img) + hdr; }
 };
 
+// Bounded wait; it also gives up as soon as another role has raised the error
+// word, so that one failed wait ends the whole CTA quickly.
 __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, int* err) {
-  return mbar_wait_sleep(bar, parity, err);
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 1023u) == 1023u && *reinterpret_cast<volatile int*>(err)) return false;
+  }
+  atomicExch(err, 1);
+  return false;
 }
 
 // (hi, lo) TF32 parts of x: hi = x rounded to 10 fraction bits (to nearest,
@@ -115,9 +129,16 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
   lo = x - hi;
 }
 
+// The remainder of x beyond its TF32 truncation, x - trunc(x) (exact): the
+// tensor core reads an FP32 operand as its truncation to TF32 (10 fraction
+// bits), so the copied B and this image carry x to 2^-21 relative.
+__device__ __forceinline__ float tf32_rest(float x) {
+  return x - __uint_as_float(__float_as_uint(x) & 0xffffe000u);
+}
+
 // ---------------------------------------------------------------------------
 template <int P>
-__global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   extern __shared__ unsigned char smem_raw[];
   // 1024-byte alignment of the shared-window offset (swizzle atoms, core matrices)
   const Smem S{smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u)};
@@ -134,12 +155,13 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
     }
     for (uint32_t i = 0; i < kAcc; ++i) {
       mbar_init(S.accfull(i), 2);
-      mbar_init(S.accempty(i), 4);
+      mbar_init(S.accempty(i), kEpiWarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // A rows >= 2P are never gathered: zero them once (they only feed D rows that are never read)
-  for (uint32_t i = threadIdx.x; i < kA * (kPiece / 16); i += kThreads)
+  // A rows of absent right-hand sides are never gathered: zero the stages once
+  // (those rows only feed D rows that are never read)
+  for (uint32_t i = threadIdx.x; i < 2 * kA * (kPiece / 16); i += kThreads)
     reinterpret_cast<uint4*>(S.astage(0))[i] = make_uint4(0u, 0u, 0u, 0u);
   fence_proxy_async();
   if (warp == 1) {
@@ -197,7 +219,7 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         const uint64_t cstride = (uint64_t)hdr + (uint64_t)n8 * kUmKc * 4;
         for (uint32_t c = 0; c < nch; ++c) {
           const uint32_t kc = c + 1 == nch ? klast : kUmKc;
-          const uint32_t bbytes = n8 * kc * 4, sz = hdr + 2 * bbytes;
+          const uint32_t bbytes = n8 * kc * 4, sz = hdr + bbytes;
           uint64_t p0 = pos;
           if ((p0 % kRing) + sz > kRing) p0 += kRing - p0 % kRing;  // no entry wraps
           if (!reserve(p0, sz)) {
@@ -225,7 +247,9 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
       }
       // every bulk copy issued has landed before the CTA may exit: the chunks
       // not yet consumed (the older ones were consumed, hence landed)
-      for (uint32_t i = oldest; i < it; ++i) wait_bar(S.bfull(i % kSlots), (i / kSlots) & 1, a.err);
+      // (bounded, but not cut short by another role's error: a copy in flight
+      // must not land after the CTA has exited)
+      for (uint32_t i = oldest; i < it; ++i) mbar_wait_sleep(S.bfull(i % kSlots), (i / kSlots) & 1, a.err);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -259,7 +283,7 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         const uint32_t sbo = (uint32_t)h.kc * 32u;  // (kc / 4) core matrices of 128 bytes per 8-row group
         const uint32_t sa = smem_u32(S.astage(as));
         const uint32_t sb = smem_u32(E.b());
-        const uint32_t sl2 = sb + (uint32_t)h.n8 * h.kc * 4u;  // B lo image
+        const uint32_t sl2 = smem_u32(S.lostage(as));  // B remainder image
         const uint32_t d = tmem + q * kUmN;
         for (uint32_t kk = 0; kk < (uint32_t)h.kc / 8u; ++kk) {
           const uint64_t da = umma_desc_sw128(sa + kk * 32u, 1024u);
@@ -280,23 +304,24 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         }
       }
       // the MMAs issued last have completed before the tensor memory is freed
-      if (issued) wait_bar(S.aempty((c - 1) % kA), ((c - 1) / kA) & 1, a.err);
+      // (bounded, not cut short by another role's error)
+      if (issued) mbar_wait_sleep(S.aempty((c - 1) % kA), ((c - 1) / kA) & 1, a.err);
     }
     __syncwarp();
   } else if (warp < 6) {
-    // ---------------- A gather + B split
-    // A (128 x kc, TF32) in the 128-byte-swizzled K-major layout: atom g = rows
-    // 8 g .. 8 g + 7 (right-hand sides 4 g .. 4 g + 3, hi and lo parts: row
-    // 2 j + s), 1024 bytes, 16-byte chunk kb (k = 4 kb .. 4 kb + 3) of row r at
-    // chunk kb ^ r.  Lane (kb = lane % 8, g = 4 q + lane / 8) loads Z rows
-    // 4 kb .. 4 kb + 3, right-hand sides 4 g .. 4 g + 3 (four 16-byte loads),
-    // splits them into TF32 parts and stores its eight 16-byte row chunks
-    // (conflict-free: the eight lanes of one atom fill all 32 banks).  Loads run
-    // one chunk ahead of the stores.  All four warps then split the B image.
+    // ---------------- stage filling (A + the B remainder image)
+    // A (128 x kc, TF32) in the 128-byte-swizzled K-major layout, rows m < 64
+    // the hi parts of right-hand sides j = m, rows 64 + j their lo parts; atom
+    // g = rows 8 g .. 8 g + 7 (1024 bytes), 16-byte chunk kb (k = 4 kb .. 4 kb
+    // + 3) of row r at chunk kb ^ r.  Lane (kb = lane % 8, t = 4 q + lane / 8)
+    // loads Z rows 4 kb .. 4 kb + 3 of right-hand sides 4 t .. 4 t + 3 (four
+    // 16-byte loads), splits them and stores eight 16-byte row chunks (hi rows
+    // 4 t + i, lo rows 64 + 4 t + i).  Loads run one chunk ahead of the stores.
+    // All four warps then write the B remainder image.
     const uint32_t q = warp - 2;
     const uint32_t tid = threadIdx.x - 64;        // 0 .. 127
-    const uint32_t kb = lane & 7, g = 4 * q + (lane >> 3);
-    const bool gather = 4 * g < (uint32_t)P;      // this lane's right-hand sides exist
+    const uint32_t kb = lane & 7, t4 = 4 * q + (lane >> 3);
+    const bool gather = 4 * t4 < (uint32_t)P;     // this lane's right-hand sides exist
     float4 vn[4], vc[4];
 #pragma unroll
     for (uint32_t i = 0; i < 4; ++i) vn[i] = vc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -307,7 +332,7 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
         v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (gather && kp < h.kvalid) {
           const uint32_t zr = (h.flags & kUmContig) ? h.zsrc + kp : ix[kp];
-          v[i] = __ldg(reinterpret_cast<const float4*>(a.z + (uint64_t)zr * P + 4 * g));
+          v[i] = __ldg(reinterpret_cast<const float4*>(a.z + (uint64_t)zr * P + 4 * t4));
         }
       }
     };
@@ -316,31 +341,27 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
       const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
       const UmHead h = *E.head();
       if (gather && 4 * kb < h.kc) {
-        unsigned char* atom = S.astage(as) + g * 1024u;
+        unsigned char* Ast = S.astage(as);
         const float x[4][4] = {{vf[0].x, vf[0].y, vf[0].z, vf[0].w}, {vf[1].x, vf[1].y, vf[1].z, vf[1].w},
                                {vf[2].x, vf[2].y, vf[2].z, vf[2].w}, {vf[3].x, vf[3].y, vf[3].z, vf[3].w}};
 #pragma unroll
-        for (uint32_t t = 0; t < 4; ++t) {
+        for (uint32_t i = 0; i < 4; ++i) {
           float hi[4], lo[4];
 #pragma unroll
-          for (uint32_t i = 0; i < 4; ++i) split_tf32(x[i][t], hi[i], lo[i]);
-          const uint32_t r0 = 2 * t, r1 = 2 * t + 1;
-          *reinterpret_cast<float4*>(atom + r0 * 128u + ((kb ^ r0) << 4)) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-          *reinterpret_cast<float4*>(atom + r1 * 128u + ((kb ^ r1) << 4)) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+          for (uint32_t k = 0; k < 4; ++k) split_tf32(x[k][i], hi[k], lo[k]);
+          const uint32_t mh = 4 * t4 + i, ml = 64 + mh, r = mh & 7;  // ml & 7 == r
+          *reinterpret_cast<float4*>(Ast + (mh >> 3) * 1024u + r * 128u + ((kb ^ r) << 4)) =
+              make_float4(hi[0], hi[1], hi[2], hi[3]);
+          *reinterpret_cast<float4*>(Ast + (ml >> 3) * 1024u + r * 128u + ((kb ^ r) << 4)) =
+              make_float4(lo[0], lo[1], lo[2], lo[3]);
         }
       }
-      float4* B = reinterpret_cast<float4*>(E.b());
+      const float4* B = reinterpret_cast<const float4*>(E.b());
+      float4* L = reinterpret_cast<float4*>(S.lostage(as));
       const uint32_t nv = (uint32_t)h.n8 * h.kc / 4;
-      float4* L = B + nv;
       for (uint32_t e = tid; e < nv; e += 128) {
         const float4 b = B[e];
-        float4 hi, lo;
-        split_tf32(b.x, hi.x, lo.x);
-        split_tf32(b.y, hi.y, lo.y);
-        split_tf32(b.z, hi.z, lo.z);
-        split_tf32(b.w, hi.w, lo.w);
-        B[e] = hi;
-        L[e] = lo;
+        L[e] = make_float4(tf32_rest(b.x), tf32_rest(b.y), tf32_rest(b.z), tf32_rest(b.w));
       }
       fence_proxy_async();  // generic writes -> the tensor core's (async proxy) reads
       __syncwarp();
@@ -383,16 +404,16 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
   } else {
     // ---------------- epilogue
     const uint32_t q = warp & 3;                  // tensor-memory lane quadrant of this warp
-    const uint32_t et = threadIdx.x - 192;        // 0 .. 127
-    const bool active = 32 * q < 2 * (uint32_t)P;
-    // Lanes 2 j and 2 j + 1 hold D rows of the hi and lo parts of right-hand
-    // side j; each chunk they exchange halves so that lane 2 j + s keeps the
-    // sums hi + lo of the columns c = 2 i + s: acc[i] = T[j][2 i + s].
-    const uint32_t sp = lane & 1;
-    float acc[kUmN / 2];
+    const uint32_t half = (warp - 6) >> 2;        // columns 64 half .. 64 half + 63
+    const uint32_t et = (threadIdx.x - 192) & 127;  // 0 .. 127 within the column half's warps
+    const uint32_t j = 32 * (q & 1) + lane;       // right-hand side of this lane's row
+    const bool active = j < (uint32_t)P;          // per lane: guards only the staging writes
+    const bool qactive = 32 * (q & 1) < (uint32_t)P;  // warp-uniform: the quadrant holds rows
+    const bool lo_row = q >= 2;                   // rows 64 .. 127: lo parts
+    float acc[64];
 #pragma unroll
-    for (int c = 0; c < (int)kUmN / 2; ++c) acc[c] = 0.f;
-    float* Sg = S.staging();
+    for (int c = 0; c < 64; ++c) acc[c] = 0.f;
+    float* Sg = S.staging(half);
     uint32_t ai = 0;
     while (true) {
       const uint32_t qa = ai % kAcc, ka = ai / kAcc;
@@ -402,20 +423,16 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
       tc_fence_after();
       const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
       const bool first = h.flags & kUmFirst;
-      if (active) {
+      // tcgen05.ld / wait::ld are warp-collective: warp-uniform condition only
+      if (qactive && 64 * half < n16) {
 #pragma unroll
-        for (uint32_t gg = 0; gg < kUmN / 32; ++gg) {
-          if (32 * gg < n16) {
+        for (uint32_t gg = 0; gg < 2; ++gg) {
+          if (64 * half + 32 * gg < n16) {
             float v[32];
-            tmem_ld32(tmem + ((32 * q) << 16) + qa * kUmN + 32 * gg, v);
+            tmem_ld32(tmem + ((32 * q) << 16) + qa * kUmN + 64 * half + 32 * gg, v);
             tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              const float mine = sp ? v[2 * i + 1] : v[2 * i];
-              const float give = sp ? v[2 * i] : v[2 * i + 1];
-              const float t = mine + __shfl_xor_sync(0xffffffffu, give, 1);
-              acc[16 * gg + i] = first ? t : acc[16 * gg + i] + t;
-            }
+            for (int i = 0; i < 32; ++i) acc[32 * gg + i] = first ? v[i] : acc[32 * gg + i] + v[i];
           }
         }
       }
@@ -423,38 +440,39 @@ __global__ void __maxnreg__(200) um_sweep_kernel(KArgs a) {
       __syncwarp();
       if (lane == 0) mbar_arrive(S.accempty(qa));
       ++ai;
-      if (!(h.flags & kUmLast)) continue;
-      // ---- end of the tile: out through the staging tile, 64 columns at a time
+      if (!(h.flags & kUmLast) || 64 * half >= h.nout) continue;
+      // ---- end of the tile: hi rows, then lo rows added, through the staging tile
+      const uint32_t bid = 1 + half;
+      named_bar(bid, 128);  // the staging tile is free
+      if (active && !lo_row) {
 #pragma unroll
-      for (uint32_t half = 0; half < 2; ++half) {
-        if (64 * half >= h.nout) break;
-        named_bar(1, 128);  // the staging tile is free
-        if (active) {
-          float* row = Sg + (16 * q + (lane >> 1)) * kSRow + sp;
+        for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] = acc[c];
+      }
+      named_bar(bid, 128);
+      if (active && lo_row) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) row[2 * i] = acc[32 * half + i];
-        }
-        named_bar(1, 128);
-        const uint32_t nh = min(64u, (uint32_t)h.nout - 64 * half);
-        const uint32_t row0 = h.out + 64 * half;
-        if (a.mode == 1) {
-          for (uint32_t e = et; e < a.pg * 64; e += 128) {
-            const uint32_t jj = e >> 6, c = e & 63;
-            if (c < nh) {
-              double* yp = a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy;
-              *yp += a.d * (double)Sg[jj * kSRow + c];
-            }
+        for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] += acc[c];
+      }
+      named_bar(bid, 128);
+      const uint32_t nh = min(64u, (uint32_t)h.nout - 64 * half);
+      const uint32_t row0 = h.out + 64 * half;
+      if (a.mode == 1) {
+        for (uint32_t e = et; e < a.pg * 64; e += 128) {
+          const uint32_t jj = e >> 6, c = e & 63;
+          if (c < nh) {
+            double* yp = a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy;
+            *yp += a.d * (double)Sg[jj * kSRow + c];
           }
-        } else {
-          const bool red = h.flags & kUmRed;
-          for (uint32_t e = et; e < (uint32_t)P * 64; e += 128) {
-            const uint32_t jj = e % P, c = e / P;
-            if (c < nh) {
-              float* tp = a.tout + (uint64_t)(row0 + c) * P + jj;
-              const float v = Sg[jj * kSRow + c];
-              if (red) atomicAdd(tp, v);
-              else *tp = v;
-            }
+        }
+      } else {
+        const bool red = h.flags & kUmRed;
+        for (uint32_t e = et; e < (uint32_t)P * 64; e += 128) {
+          const uint32_t jj = e % P, c = e / P;
+          if (c < nh) {
+            float* tp = a.tout + (uint64_t)(row0 + c) * P + jj;
+            const float v = Sg[jj * kSRow + c];
+            if (red) atomicAdd(tp, v);
+            else *tp = v;
           }
         }
       }
