@@ -19,10 +19,17 @@
 // leaves live in one libahx handle (trees on the host, bit-identical to the
 // reference's; leaves on the GPU).  mblock<T> objects are host views that
 // copy a leaf back from the device when their data is asked for.
-// MATGEN_T: the GPU generators are the Laplace collocation kernel (mblock<double>
-// leaves) and the Helmholtz kernel exp(ikr)/(4 pi r) (mblock<dcomp> leaves); the
-// generator object passes h (diagonal 1/(4 pi h), resp. exp(ikh)/(4 pi h)) through
-// `geth()` and, for dcomp, the wavenumber through `getk()`.
+// MATGEN_T: the kernels are evaluated on the GPU by this library, not through the
+// generator object's cmpbl / scale (Include/matgen_omp.h:27-33).  The matgen_*
+// functions therefore accept only the library's generator types (or types derived
+// from them), and refuse any other MATGEN_T at compile time:
+//   LaplaceGenerator{h}        K = 1/(4 pi r), diagonal 1/(4 pi h)  (mblock<double>, mblock<float>)
+//   HelmholtzGenerator{h, k}   K = exp(ikr)/(4 pi r), diagonal exp(ikh)/(4 pi h)
+//                              (mblock<dcomp>, mblock<scomp>)
+// GMRes / CG run on the GPU for the library's operators (HMatrixOperator,
+// ZHMatrixOperator) only; a call with any other Matrix<T> does not compile.  The
+// operators have no preconditioner: the reference's Matrix::precond_apply
+// (solvers/GMRES.cpp:73,128, solvers/CG.cpp:71) is the identity for them.
 #ifndef AHX_AHMED_HPP
 #define AHX_AHMED_HPP
 
@@ -259,6 +266,34 @@ void freembls(blcluster* bl, mblock<T>**& A) {
   A = nullptr;
 }
 
+// The generators whose kernels this library evaluates on the GPU.  A program's own
+// MATGEN_T may derive from one of them (keeping its other members); any other
+// generator type is refused at compile time, since its cmpbl / scale would not be
+// called.
+struct LaplaceGenerator {
+  double h;  // diagonal 1/(4 pi h)
+  double geth() const { return h; }
+};
+struct HelmholtzGenerator {
+  double h;  // diagonal exp(ikh)/(4 pi h)
+  double k;  // wavenumber
+  double geth() const { return h; }
+  double getk() const { return k; }
+};
+
+template <class T, class MATGEN_T>
+inline void check_generator() {
+  constexpr bool real = std::is_same<T, double>::value || std::is_same<T, float>::value;
+  constexpr bool cplx = std::is_same<T, dcomp>::value || std::is_same<T, scomp>::value;
+  static_assert(real || cplx, "ahx_ahmed: mblock<T> with T = double, float, dcomp or scomp");
+  static_assert(!real || std::is_base_of<LaplaceGenerator, MATGEN_T>::value,
+                "ahx_ahmed: real leaves are assembled from ahx_ahmed::LaplaceGenerator (or a type derived "
+                "from it); a generator's own cmpbl/scale are not evaluated on the GPU");
+  static_assert(!cplx || std::is_base_of<HelmholtzGenerator, MATGEN_T>::value,
+                "ahx_ahmed: complex leaves are assembled from ahx_ahmed::HelmholtzGenerator (or a type "
+                "derived from it); a generator's own cmpbl/scale are not evaluated on the GPU");
+}
+
 template <class MATGEN_T>
 void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankmax, const double*) {
   check(ahx_assemble(bl->handle(), MatGen.geth(), eps, rankmax));
@@ -285,6 +320,7 @@ void assemble_leaves(MATGEN_T& MatGen, blcluster* bl, double eps, unsigned rankm
 template <class T, class MATGEN_T>
 void matgenGeH_omp(MATGEN_T& MatGen, unsigned nblcks, blcluster* bl, double eps, unsigned rankmax,
                    mblock<T>** A) {
+  check_generator<T, MATGEN_T>();
   assemble_leaves(MatGen, bl, eps, rankmax, (const T*)nullptr);
   for (unsigned i = 0; i < nblcks; ++i) {
     delete A[i];
@@ -620,11 +656,19 @@ double spctrlnrm(Matrix<T>& A, const unsigned it_num = 10) {
   return std::sqrt(d);
 }
 
+// The solvers run on the GPU for the library's operators only: the overloads
+// below take HMatrixOperator / ZHMatrixOperator, and this template (an exact
+// match for every other type, preferred over a derived-to-base conversion) is
+// deleted, so GMRes / CG on a program's own Matrix<T> do not compile.
+template <class M, class T>
+unsigned GMRes(const M& A, T* const b, T* const x, double& eps, const unsigned m, unsigned& nsteps) = delete;
+template <class M, class T>
+unsigned CG(const M& A, T* const b, T* const x, double& eps, unsigned& nsteps) = delete;
+
 // solvers/GMRES.cpp:80: returns 0 converged, 1 not; eps and nsteps updated
-inline unsigned GMRes(const Matrix<double>& A, double* const b, double* const x, double& eps,
+inline unsigned GMRes(const HMatrixOperator& A, double* const b, double* const x, double& eps,
                       const unsigned m, unsigned& nsteps) {
-  const HMatrixOperator* H = dynamic_cast<const HMatrixOperator*>(&A);
-  if (!H) throw std::invalid_argument("ahx_ahmed: GMRes runs on an HMatrixOperator");
+  const HMatrixOperator* H = &A;
   uint32_t its = 0;
   double res = 0.0;
   const int rc = ahx_gmres(H->bl->handle(), AHX_FP64, 1, b, A.n, x, A.n, eps, m, nsteps, &its, &res);
@@ -643,10 +687,9 @@ struct ZHMatrixOperator : public Matrix<dcomp> {
 };
 
 // solvers/GMRES.cpp:246: complex GMRes
-inline unsigned GMRes(const Matrix<dcomp>& A, dcomp* const b, dcomp* const x, double& eps, const unsigned m,
+inline unsigned GMRes(const ZHMatrixOperator& A, dcomp* const b, dcomp* const x, double& eps, const unsigned m,
                       unsigned& nsteps) {
-  const ZHMatrixOperator* H = dynamic_cast<const ZHMatrixOperator*>(&A);
-  if (!H) throw std::invalid_argument("ahx_ahmed: complex GMRes runs on a ZHMatrixOperator");
+  const ZHMatrixOperator* H = &A;
   uint32_t its = 0;
   double res = 0.0;
   const int rc = ahx_helm_gmres(H->bl->handle(), AHX_FP64, 1, reinterpret_cast<const double*>(b), A.n,
@@ -658,10 +701,9 @@ inline unsigned GMRes(const Matrix<dcomp>& A, dcomp* const b, dcomp* const x, do
 }
 
 // solvers/CG.cpp:31
-inline unsigned CG(const Matrix<double>& A, double* const b, double* const x, double& eps,
+inline unsigned CG(const HMatrixOperator& A, double* const b, double* const x, double& eps,
                    unsigned& nsteps) {
-  const HMatrixOperator* H = dynamic_cast<const HMatrixOperator*>(&A);
-  if (!H) throw std::invalid_argument("ahx_ahmed: CG runs on an HMatrixOperator");
+  const HMatrixOperator* H = &A;
   uint32_t its = 0;
   double res = 0.0;
   const int rc = ahx_cg(H->bl->handle(), 1, b, A.n, x, A.n, eps, nsteps, &its, &res);

@@ -19,15 +19,14 @@ struct dof {
   double getradius2() const { return 0.0; }
 };
 
-struct LaplaceGen {  // the MATGEN_T of this example: K = 1/(4 pi r), diagonal 1/(4 pi h)
-  double h;
-  double geth() const { return h; }
+// the MATGEN_T of this example: K = 1/(4 pi r), diagonal 1/(4 pi h)
+struct LaplaceGen : LaplaceGenerator {
+  explicit LaplaceGen(double hh) : LaplaceGenerator{hh} {}
 };
 
-struct HelmholtzGen {  // mblock<dcomp> leaves: exp(ikr)/(4 pi r), diagonal exp(ikh)/(4 pi h)
-  double h, k;
-  double geth() const { return h; }
-  double getk() const { return k; }
+// mblock<dcomp> leaves: exp(ikr)/(4 pi r), diagonal exp(ikh)/(4 pi h)
+struct HelmholtzGen : HelmholtzGenerator {
+  HelmholtzGen(double hh, double kk) : HelmholtzGenerator{hh, kk} {}
 };
 
 int main(int argc, char** argv) {

@@ -13,6 +13,7 @@ Usage:  python tests/golden/make_golden.py            (Laplace cases)
                                                        products, GMRes)
         python tests/golden/make_golden.py zmbls      (savembls files of mblock<dcomp> leaves)
         python tests/golden/make_golden.py zaggl      (agglH of mblock<dcomp> leaves)
+        python tests/golden/make_golden.py cg         (the reference's CG, solvers/CG.cpp:31-113)
 """
 import os
 import sys
@@ -348,8 +349,49 @@ def zaggl():
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB) leaves {out['nleaves_before']} -> {R.nleaves}")
 
 
+# CG (solvers/CG.cpp:31-113) on positive definite diagonal variants: h = mean
+# spacing / 2 on the Fibonacci sphere, h = smallest spacing / 2 on the random
+# cube surface (with the mean spacing a random cloud's matrix is indefinite);
+# a converging solve and one stopped by its step limit.
+CG_CASES = {"fib4096": "mean", "cube3000": "min"}
+
+
+def _min_nn(P):
+    from scipy.spatial import cKDTree
+
+    d, _ = cKDTree(P).query(P, k=2)
+    return float(d[:, 1].min())
+
+
+def cg():
+    if not O.ref_available():
+        sys.exit("reference build missing: run oracle/ref/build_ref.sh first")
+    out = {}
+    for name, diag in CG_CASES.items():
+        gen, bmin = CASES[name]
+        P = gen()
+        h = (O.mean_nn(P) if diag == "mean" else _min_nn(P)) / 2.0
+        n = P.shape[0]
+        b = np.random.default_rng(3).standard_normal(n)
+        R = O.RefH(P, O.TREE_BBX, bmin, ETA, h)
+        R.assemble(EPS, nthreads=1)
+        for tag, steps in (("conv", 300), ("cap", 8)):
+            x = np.zeros(n)
+            ret, e, ns = R.cg(b, x, 1e-8, steps)
+            out[f"{name}_{tag}"] = np.array([ret, e, ns], np.float64)
+            out[f"{name}_{tag}_x"] = x
+            print(f"{name} {tag}: ret {ret} eps {e:.3e} steps {ns}")
+        out[f"{name}_b"] = b
+        out[f"{name}_h"] = np.float64(h)
+    path = os.path.join(HERE, "cg.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
+    if len(sys.argv) > 1 and sys.argv[1] == "cg":
+        cg()
+    elif len(sys.argv) > 1 and sys.argv[1] == "helmholtz":
         helmholtz()
     elif len(sys.argv) > 1 and sys.argv[1] == "mbls":
         mbls()

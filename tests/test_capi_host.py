@@ -142,3 +142,30 @@ def test_noalloc_refuses_oversized_blocks_before_device_work():
         rc = L.ahx_aca_block_noalloc(fake, fake, fake, 0, n1, 0, n2, 0, 0.1, 1e-6, kmax, fake, fake, fake, None)
         assert rc == _capi.AHX_ERR_ARG
         assert b"scratch" in L.ahx_last_error()
+
+
+@pytest.mark.parametrize("case", ["sphere65536-leaf32", "cube1048576-leaf64"])
+def test_trees_at_benchmark_sizes_match_oracle(case):
+    """The block-cluster trees of the benchmarked workloads (Fibonacci sphere N =
+    65,536 with leaf 32; uniform cube surface N = 2^20, seed 4, with leaf 64;
+    bounding-box bisection, eta 0.8) equal the oracle's bit for bit: both
+    permutations and the DFS leaf list (Include/cluster_bbx.h:100-128,
+    cluster/blcluster.cpp:40-66).  The oracle's trees are pinned to the
+    reference's own on the golden cases."""
+    import oracle as O
+
+    if case.startswith("sphere"):
+        P, leaf = A.geometry.fibonacci_sphere(65536), 32
+    else:
+        P, leaf = A.geometry.cube_surface(1 << 20, 4), 64
+    H = A.HMatrix(P, "bbx", bmin=leaf, eta=0.8)
+    Ho = O.OracleH(P, O.TREE_BBX, leaf, 0.8, 1.0)
+    op, po = H.perm()
+    oo, opo = Ho.perm()
+    assert np.array_equal(op, oo) and np.array_equal(po, opo)
+    assert np.array_equal(H.leaves(), Ho.leaves())
+    if case.startswith("sphere"):
+        Hp = A.HMatrix(P, "pca", bmin=leaf, eta=0.8)
+        Hpo = O.OracleH(P, O.TREE_PCA, leaf, 0.8, 1.0)
+        assert np.array_equal(Hp.perm()[0], Hpo.perm()[0])
+        assert np.array_equal(Hp.leaves(), Hpo.leaves())

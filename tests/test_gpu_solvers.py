@@ -132,6 +132,36 @@ def test_cg_matches_oracle(pair):
     assert _relerr(x, xo) <= 1e-6
 
 
+@pytest.mark.parametrize("case", ["fib4096", "cube3000"])
+@pytest.mark.parametrize("tag,steps", [("conv", 300), ("cap", 8)])
+def test_cg_matches_reference(golden, case, tag, steps):
+    """ahx_cg against the reference's own CG (solvers/CG.cpp:31-113, fixture
+    tests/golden/cg.npz) on leaves assembled by the oracle, which is pinned to
+    the reference's assembly: status, step count and solution."""
+    g, c = golden(case), golden("cg")
+    h = float(c[f"{case}_h"])
+    Ho = O.OracleH(g["points"], O.TREE_BBX, 32, 0.8, h)
+    Ho.assemble(1e-6, nthreads=4)
+    H = A.HMatrix(g["points"], "bbx")
+    chunks = [Ho.leaf_data(l) for l in range(Ho.nleaves)]
+    offs = np.zeros(len(chunks) + 1, np.uint64)
+    offs[1:] = np.cumsum([q.size for q in chunks])
+    H.set_leaves(Ho.ranks(), np.concatenate(chunks), offs)
+    ret_r, eps_r, ns_r = c[f"{case}_{tag}"]
+    xr = c[f"{case}_{tag}_x"]
+    x = np.zeros(H.n)
+    ret, eps, its = H.CG(c[f"{case}_b"], x, 1e-8, steps)
+    assert ret == int(ret_r)
+    if ret == 0:
+        assert abs(int(its[0]) - int(ns_r)) <= 2
+        assert eps[0] < 1e-8
+        assert _relerr(x, xr) <= 1e-5
+    else:
+        assert int(its[0]) == int(ns_r)
+        assert abs(eps[0] - eps_r) <= 1e-3 * eps_r
+        assert _relerr(x, xr) <= 1e-4
+
+
 def test_batch_product_and_gmres_match_instances():
     sizes = [(A.geometry.sphere_surface, 2100, 1), (A.geometry.ellipsoid_surface, 3300, 2),
              (A.geometry.cube_surface, 2600, 3)]

@@ -110,3 +110,26 @@ def test_gmres_matches_reference(golden, case, tag):
     else:
         assert ns == int(ns_r)
         assert abs(eps - eps_r) <= 1e-3 * eps_r
+
+
+@pytest.mark.parametrize("case", ["fib4096", "cube3000"])
+@pytest.mark.parametrize("tag,steps", [("conv", 300), ("cap", 8)])
+def test_cg_matches_reference(golden, case, tag, steps):
+    """The oracle's CG (solvers/CG.cpp:31-113) against the reference's own CG on its
+    own assembly: a converging solve and one stopped by the step limit."""
+    g, c = golden(case), golden("cg")
+    H = _oracle(g, O.TREE_BBX, h=float(c[f"{case}_h"]))
+    H.assemble(float(g["eps"]), nthreads=2)
+    ret_r, eps_r, ns_r = c[f"{case}_{tag}"]
+    x = np.zeros(H.n)
+    ret, eps, ns = H.cg(c[f"{case}_b"], x, 1e-8, steps, nthreads=2)
+    assert ret == int(ret_r)
+    xr = c[f"{case}_{tag}_x"]
+    if ret == 0:
+        assert abs(int(ns) - int(ns_r)) <= 2
+        assert eps < 1e-8
+        assert np.linalg.norm(x - xr) <= 1e-5 * np.linalg.norm(xr)
+    else:
+        assert ns == int(ns_r)
+        assert abs(eps - eps_r) <= 1e-3 * eps_r
+        assert np.linalg.norm(x - xr) <= 1e-4 * np.linalg.norm(xr)
