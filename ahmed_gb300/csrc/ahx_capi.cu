@@ -456,30 +456,47 @@ int prepare_um(ahx_hmat* H) {
   if ((rc = upload(pc.um_zero, L.zero, H->stream))) return rc;
   if ((rc = upload(pc.um_vranges, L.vranges, H->stream))) return rc;
   if ((rc = upload(pc.um_rranges, L.rranges, H->stream))) return rc;
-  // Z rows: X rows, T rows, 64 floats each (the widest pass)
+  if ((rc = upload(pc.um_vcranges, L.vcranges, H->stream))) return rc;
+  if ((rc = upload(pc.um_rcranges, L.rcranges, H->stream))) return rc;
+  if ((rc = pc.um_vzidx.reserve(std::max<uint64_t>(L.vchunks * kUmIdxBytes, 16)))) return rc;
+  if ((rc = pc.um_rzidx.reserve(std::max<uint64_t>(L.rchunks * kUmIdxBytes, 16)))) return rc;
+  // Z rows: X rows, T rows, one 256-byte row of FP16 pairs each (64 right-hand-side slots)
   const uint64_t zrows = H->tree.n + (uint64_t)L.t_rows + 1;
-  if ((rc = pc.um_z.reserve(zrows * 64 * sizeof(float)))) return rc;
-  AHX_CUDA(cudaMemsetAsync(pc.um_z.p, 0, zrows * 64 * sizeof(float), H->stream));
+  if ((rc = pc.um_z.reserve(zrows * kUmZPitch))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.um_z.p, 0, zrows * kUmZPitch, H->stream));
+  // FP32 accumulation rows of split V tiles (zero between products)
+  if ((rc = pc.um_tacc.reserve(std::max<uint64_t>((uint64_t)L.tacc_rows * 64 * sizeof(float), 16)))) return rc;
+  AHX_CUDA(cudaMemsetAsync(pc.um_tacc.p, 0, std::max<uint64_t>((uint64_t)L.tacc_rows * 64 * sizeof(float), 16),
+                           H->stream));
+  if ((rc = pc.um_xmax.reserve(64 * sizeof(uint32_t)))) return rc;
   if ((rc = pc.err.reserve(sizeof(int)))) return rc;
   AHX_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), H->stream));
   {
-    DevBuf de, db;
-    if ((rc = upload(de, L.entries, H->stream))) return rc;
-    if ((rc = upload(db, L.vbuild, H->stream))) {
-      de.release();
-      return rc;
-    }
-    cudaError_t ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.vbuild.size(), de.as<UmEntry>(), src,
-                                     pc.um_vstream.as<unsigned char>(), H->stream);
+    ScopedBuf de, db, dj, dts;
+    if ((rc = dts.reserve(std::max<uint64_t>((uint64_t)L.t_rows * sizeof(float), 16)))) return rc;
+    if ((rc = upload(dj, L.tjobs, H->stream))) return rc;
+    cudaError_t ce = launch_um_tscale(dj.as<UmTJob>(), (uint32_t)L.tjobs.size(), src, dts.as<float>(), H->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(H->stream);
-    db.release();
-    if (ce == cudaSuccess && (rc = upload(db, L.rbuild, H->stream)) == AHX_OK) {
-      ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.rbuild.size(), de.as<UmEntry>(), src,
-                           pc.um_rstream.as<unsigned char>(), H->stream);
+    dj.release();
+    if (ce == cudaSuccess) {
+      if ((rc = upload(de, L.entries, H->stream))) return rc;
+      if ((rc = upload(db, L.vbuild, H->stream))) {
+        de.release();
+        return rc;
+      }
+      ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.vbuild.size(), de.as<UmEntry>(), src, dts.as<float>(),
+                           H->tree.n, pc.um_vstream.as<unsigned char>(), pc.um_vzidx.as<uint32_t>(), H->stream);
       if (ce == cudaSuccess) ce = cudaStreamSynchronize(H->stream);
+      db.release();
+      if (ce == cudaSuccess && (rc = upload(db, L.rbuild, H->stream)) == AHX_OK) {
+        ce = launch_um_build(db.as<UmBuild>(), (uint32_t)L.rbuild.size(), de.as<UmEntry>(), src, dts.as<float>(),
+                             H->tree.n, pc.um_rstream.as<unsigned char>(), pc.um_rzidx.as<uint32_t>(), H->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(H->stream);
+      }
     }
     db.release();
     de.release();
+    dts.release();
     if (rc) return rc;
     AHX_CUDA(ce);
   }
@@ -501,6 +518,10 @@ UmPlan um_plan(ProdCopy& pc, uint64_t n) {
   pl.rtiles = pc.um_rtiles.as<UmTile>();
   pl.vranges = pc.um_vranges.as<uint32_t>();
   pl.rranges = pc.um_rranges.as<uint32_t>();
+  pl.vcranges = pc.um_vcranges.as<uint32_t>();
+  pl.rcranges = pc.um_rcranges.as<uint32_t>();
+  pl.vzidx = pc.um_vzidx.as<uint32_t>();
+  pl.rzidx = pc.um_rzidx.as<uint32_t>();
   pl.grid = pc.um_grid;
   pl.nvtiles = pc.um_nv;
   pl.nrtiles = pc.um_nr;
@@ -510,15 +531,10 @@ UmPlan um_plan(ProdCopy& pc, uint64_t n) {
   pl.nzero = pc.um_nzero;
   pl.n = n;
   pl.t_rows = pc.um_trows;
-  pl.z = pc.um_z.as<float>();
+  pl.z = pc.um_z.as<uint16_t>();
+  pl.tacc = pc.um_tacc.as<float>();
+  pl.xmax = pc.um_xmax.as<uint32_t>();
   pl.err = pc.err.as<int>();
-  // AHX_UM_DRAIN: chunks of 32 K positions accumulated by the tensor core before
-  // the round-to-nearest FP32 add in registers (default 1)
-  static const uint32_t drain = [] {
-    const char* e = std::getenv("AHX_UM_DRAIN");
-    return (e && *e) ? (uint32_t)std::max(1ul, std::strtoul(e, nullptr, 10)) : 1u;
-  }();
-  pl.drain = drain;
   return pl;
 }
 

@@ -56,11 +56,13 @@ struct ProdCopy {
   uint32_t unit_bytes = 0;  // unit cap the streams were built with
   // FP32 leaves on the tcgen05 path (ahx_umma.cuh), products of >= 2 right-hand sides
   bool um_valid = false;
-  DevBuf um_vstream, um_rstream, um_vtiles, um_rtiles, um_zero, um_z, um_vranges, um_rranges;
+  DevBuf um_vstream, um_rstream, um_vtiles, um_rtiles, um_zero, um_z, um_vranges, um_rranges, um_tacc, um_xmax;
+  DevBuf um_vcranges, um_rcranges, um_vzidx, um_rzidx;
   uint32_t um_nv = 0, um_nr = 0, um_nzero = 0, um_trows = 0, um_grid = 0;
   uint64_t um_payload = 0, um_stream_bytes = 0;
   void release_um() {
-    for (DevBuf* b : {&um_vstream, &um_rstream, &um_vtiles, &um_rtiles, &um_zero, &um_z, &um_vranges, &um_rranges})
+    for (DevBuf* b : {&um_vstream, &um_rstream, &um_vtiles, &um_rtiles, &um_zero, &um_z, &um_vranges, &um_rranges,
+                      &um_tacc, &um_xmax, &um_vcranges, &um_rcranges, &um_vzidx, &um_rzidx})
       b->release();
     um_valid = false;
     um_nv = um_nr = um_nzero = um_trows = um_grid = 0;

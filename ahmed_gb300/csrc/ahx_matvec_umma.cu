@@ -1,28 +1,28 @@
 // H-matrix product on the fifth-generation tensor cores (tcgen05.mma with
-// tensor-memory accumulators) over FP32 leaf streams; the layout, the sweeps
-// and the precision scheme are described in ahx_umma.cuh.
+// tensor-memory accumulators, kind::f16) over leaf streams of FP16 pairs; the
+// layout, the sweeps and the precision scheme are described in ahx_umma.cuh.
 //
 // One persistent CTA per SM, 14 warps with fixed roles:
 //   warp 0      producer: walks the CTA's contiguous range of tiles (ranges
-//               balanced by bytes; descriptors fetched 32 at a time) and
-//               bulk-copies (cp.async.bulk) each chunk image (indices, head, B)
-//               into a byte ring of kRing bytes, as far ahead as the ring and
-//               its kSlots slot records allow
+//               balanced by bytes; descriptors fetched 32 at a time); the Z-row
+//               indices of the chunk kLidx ahead go into a small queue (cp.async,
+//               one word per lane); each chunk image is bulk-copied
+//               (cp.async.bulk) into one of kSlots ring slots together with its
+//               Z rows (one bulk copy per run of consecutive rows)
 //   warp 1      MMA issuer (one thread) and owner of the tensor memory: per
-//               chunk, 2 * kc / 8 tcgen05.mma (B as copied, which the tensor
-//               core reads truncated to TF32, and its remainder image) into one
-//               of four 128-column accumulators, then tcgen05.commit to the
-//               ring slot, the stage and the accumulator
-//   warps 2-5   stage filling: 16-byte loads of the chunk's Z values one chunk
-//               ahead, split into TF32 hi/lo parts and stored as A in one of
-//               kA stages (128-byte-swizzled K-major), and the remainder image
-//               B - trunc(B) beside it; then the stage is released to the MMA
-//               issuer
+//               chunk, 2 * kc / 16 tcgen05.mma (first and second FP16 part of
+//               B) into one of four 128-column accumulators, then
+//               tcgen05.commit to the ring slot, the A stage and the
+//               accumulator
+//   warps 2-5   A stages: the chunk's Z rows (K x 128 FP16, row-major in the
+//               slot) transposed into the K-major canonical layout with
+//               ldmatrix.trans / stmatrix, one of kA stages
 //   warps 6-13  epilogue, two warps per tensor-memory lane quadrant (columns
-//               0-63 and 64-127): each thread adds its accumulator row to
-//               registers (round-to-nearest FP32) per chunk; at the end of a
-//               tile the hi and lo rows are summed through shared memory into
-//               Y (FP64, in place) or T
+//               0-63 and 64-127): each thread adds its accumulator row, times
+//               the chunk's scale, to registers (round-to-nearest FP32) per
+//               chunk; at the end of a tile the rows of the two parts are
+//               summed through shared memory into Y (FP64, in place) or into
+//               T rows (split into FP16 pairs; FP32 atomics for split tiles)
 // Every wait is bounded: on timeout the kernel raises the error word and all
 // roles return after the copies and MMAs they started have completed.
 #include <algorithm>
@@ -30,6 +30,8 @@
 #include <map>
 #include <mutex>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "ahx_ptx.cuh"
 #include "ahx_umma.cuh"
@@ -39,74 +41,83 @@ namespace {
 
 using namespace ptx;
 
-constexpr uint32_t kPiece = kUmN * kUmKc * 4;           // 16 KB: largest B image / A piece
-constexpr uint32_t kRing = 120u << 10;                  // ring of chunk images (head + B)
-constexpr uint32_t kSlots = 16;                         // chunk records of the ring
-constexpr uint32_t kA = 2;                              // stages (A + the B remainder image)
-constexpr uint32_t kAcc = 4;                            // tensor-memory accumulators (128 columns each)
-constexpr uint32_t kSRow = 65;                          // staging row stride (floats): conflict-free
-constexpr uint32_t kOffA = kRing;                       // stage i: A at kOffA + 2 i kPiece, B lo after it
-constexpr uint32_t kOffStaging = kOffA + 2 * kA * kPiece;
-constexpr uint32_t kStagingBytes = 64 * kSRow * 4;      // per column half
-constexpr uint32_t kOffAccHdr = kOffStaging + 2 * kStagingBytes;
-constexpr uint32_t kOffSlotOff = kOffAccHdr + kAcc * sizeof(UmHead);
-constexpr uint32_t kOffEnd = kOffSlotOff + kSlots * 4;   // producer's end positions (u64)
-constexpr uint32_t kOffBar = kOffEnd + kSlots * 8;
-constexpr uint32_t kNumBars = 2 * kSlots + 2 * kA + 2 * kAcc;
+// ---- shared-memory plan (offsets from the 1024-byte aligned base)
+constexpr uint32_t kSlots = 6;                            // ring slots (chunk image + its Z rows)
+constexpr uint32_t kLidx = 6;                             // Z-row indices are fetched this many chunks ahead
+constexpr uint32_t kQ = 8;                                // index queue entries (> kLidx)
+constexpr uint32_t kImgHead = 0;                          // slot offset of the chunk head
+constexpr uint32_t kImgB = kImgHead + 32;                 // slot offset of the b1 image
+constexpr uint32_t kImgMax = kUmN * kUmKc * 4;            // b1 + b2 images of the largest chunk
+constexpr uint32_t kZRowPitch = kUmZPitch;                // Z rows in a slot, as in global memory
+constexpr uint32_t kZOff = (kImgB + kImgMax + 127) / 128 * 128;
+constexpr uint32_t kSlotBytes = (kZOff + kUmKc * kZRowPitch + 127) / 128 * 128;
+constexpr uint32_t kA = 3;                                // A stages
+constexpr uint32_t kAStage = 128 * kUmKc * 2;             // 128 rows x 32 K positions, FP16
+constexpr uint32_t kAcc = 4;                              // tensor-memory accumulators (128 columns each)
+constexpr uint32_t kSRow = 65;                            // staging row stride (floats): conflict-free
+constexpr uint32_t kOffA = kSlots * kSlotBytes;
+constexpr uint32_t kOffStaging = kOffA + kA * kAStage;
+constexpr uint32_t kStagingBytes = 64 * kSRow * 4;        // per column half
+constexpr uint32_t kOffYs = kOffStaging + 2 * kStagingBytes;   // 64 doubles: Y factor per right-hand side
+constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
+constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
+constexpr uint32_t kOffIdxQ = kOffMeta + kSlots * 16;     // index queue: kQ x 32 words
+constexpr uint32_t kOffBar = kOffIdxQ + kQ * kUmKc * 4;
+constexpr uint32_t kNumBars = 3 * kSlots + 2 * kA + 2 * kAcc;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
-constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;   // + alignment slack of the dynamic base
+constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;     // + alignment slack of the dynamic base
 constexpr uint32_t kThreads = 448;
-constexpr uint32_t kEpiWarps = 8;                       // epilogue warps: each arrives on accempty
-constexpr uint32_t kTmemCols = kAcc * kUmN;             // all 512 columns
-constexpr uint32_t kStop = 0xffffffffu;                 // slot record of the stop marker
-constexpr uint32_t kMaxEntry = kUmIdxBytes + 32 + kPiece;
+constexpr uint32_t kEpiWarps = 8;                         // epilogue warps: each arrives on accempty
+constexpr uint32_t kTmemCols = kAcc * kUmN;               // all 512 columns
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
-// the gather keeps one chunk unconverted: two entries (and the wrap gap) fit the ring
-static_assert(3 * kMaxEntry <= kRing, "ring size");
+static_assert(kQ > kLidx, "the queue entry of a chunk is read before a later prefetch reuses it");
+
+// per-slot record written by the producer
+struct SlotMeta {
+  uint32_t hdr;       // bytes before the image pair in the stream (32); 0: stop marker
+  uint32_t pad[3];
+};
 
 struct KArgs {
   const UmTile* tiles;
   const uint32_t* ranges;  // per CTA: first tile (gridDim.x + 1 entries), balanced by bytes
+  const uint32_t* cranges; // per CTA: first chunk (gridDim.x + 1 entries)
+  const uint32_t* zidx;    // Z-row indices, 32 per chunk
   const unsigned char* stream;
-  const float* z;       // Z rows (P floats each)
-  float* tout;          // V sweep: T rows (P floats each)
+  uint16_t* z;          // Z rows (FP16 pairs), X rows then T rows
+  float* tacc;          // FP32 accumulation rows of split V tiles
+  const uint32_t* xmax; // max |X_j| of the pass (FP32 bits)
   double* y;            // rows sweep: Y (column-major, ldY), first column of this pass
   uint64_t ldy;
+  uint64_t n;           // rows of X: Z row of T row t is n + t
   double d;
-  uint32_t pg;          // right-hand sides of this pass
+  uint32_t pg;          // right-hand sides of this pass (<= 64)
   uint32_t mode;        // 0: V sweep (T out), 1: rows sweep (Y out)
-  uint32_t drain;       // chunks accumulated in tensor memory per drain (>= 1)
   int* err;
 };
 
 struct Smem {
   unsigned char* base;
-  __device__ unsigned char* ring() const { return base; }
-  __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + 2 * i * kPiece; }
-  __device__ unsigned char* lostage(uint32_t i) const { return base + kOffA + (2 * i + 1) * kPiece; }
+  __device__ unsigned char* slot(uint32_t i) const { return base + i * kSlotBytes; }
+  __device__ const UmHead* head(uint32_t i) const { return reinterpret_cast<const UmHead*>(slot(i) + kImgHead); }
+  __device__ uint32_t* idxq(uint32_t i) const { return reinterpret_cast<uint32_t*>(base + kOffIdxQ) + i * kUmKc; }
+  __device__ unsigned char* zrow(uint32_t i, uint32_t k) const { return slot(i) + kZOff + k * kZRowPitch; }
+  __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + i * kAStage; }
   __device__ float* staging(uint32_t half) const {
     return reinterpret_cast<float*>(base + kOffStaging + half * kStagingBytes);
   }
+  __device__ double* ys() const { return reinterpret_cast<double*>(base + kOffYs); }
   __device__ UmHead* acchdr(uint32_t a) const { return reinterpret_cast<UmHead*>(base + kOffAccHdr) + a; }
-  __device__ uint32_t* slot_off() const { return reinterpret_cast<uint32_t*>(base + kOffSlotOff); }
-  __device__ uint64_t* endpos() const { return reinterpret_cast<uint64_t*>(base + kOffEnd); }
+  __device__ SlotMeta* meta(uint32_t i) const { return reinterpret_cast<SlotMeta*>(base + kOffMeta) + i; }
   __device__ uint32_t bar(uint32_t i) const { return smem_u32(base + kOffBar + 8 * i); }
-  __device__ uint32_t bfull(uint32_t i) const { return bar(i); }
-  __device__ uint32_t bempty(uint32_t i) const { return bar(kSlots + i); }
-  __device__ uint32_t aready(uint32_t i) const { return bar(2 * kSlots + i); }
-  __device__ uint32_t aempty(uint32_t i) const { return bar(2 * kSlots + kA + i); }
-  __device__ uint32_t accfull(uint32_t i) const { return bar(2 * kSlots + 2 * kA + i); }
-  __device__ uint32_t accempty(uint32_t i) const { return bar(2 * kSlots + 2 * kA + kAcc + i); }
+  __device__ uint32_t fimg(uint32_t i) const { return bar(i); }
+  __device__ uint32_t fz(uint32_t i) const { return bar(kSlots + i); }
+  __device__ uint32_t empty(uint32_t i) const { return bar(2 * kSlots + i); }
+  __device__ uint32_t aready(uint32_t i) const { return bar(3 * kSlots + i); }
+  __device__ uint32_t aempty(uint32_t i) const { return bar(3 * kSlots + kA + i); }
+  __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + 2 * kA + i); }
+  __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + 2 * kA + kAcc + i); }
   __device__ uint32_t* tmem_slot() const { return reinterpret_cast<uint32_t*>(base + kOffTmem); }
-};
-
-// a chunk image in the ring: [indices (hdr - 32 bytes)] [UmHead] [B]
-struct Entry {
-  const unsigned char* img;
-  uint32_t hdr;
-  __device__ const UmHead* head() const { return reinterpret_cast<const UmHead*>(img + hdr - 32); }
-  __device__ const uint32_t* idx() const { return reinterpret_cast<const uint32_t*>(img); }
-  __device__ unsigned char* b() const { return const_cast<unsigned char*>(img) + hdr; }
 };
 
 // Bounded wait; it also gives up as soon as another role has raised the error
@@ -120,34 +131,31 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, int* err
   return false;
 }
 
-// (hi, lo) TF32 parts of x: hi = x rounded to 10 fraction bits (to nearest,
-// ties away from zero: add half a TF32 unit to the magnitude bits, clear the 13
-// low bits), lo = x - hi (exact).  lo keeps up to 13 significant bits, of which
-// the tensor core uses 11: the pair carries x to 2^-22 relative.
-__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
-  lo = x - hi;
+// Power of two s with |v| / s in [2^13, 2^14) for the largest |v| = m (1 for m = 0).
+__host__ __device__ __forceinline__ int scale_exp(double m) {
+  if (!(m > 0.0)) return 0;
+  int ex;
+  frexp(m, &ex);  // m = f 2^ex, f in [0.5, 1)
+  return ex - 14;
 }
 
-// The remainder of x beyond its TF32 truncation, x - trunc(x) (exact): the
-// tensor core reads an FP32 operand as its truncation to TF32 (10 fraction
-// bits), so the copied B and this image carry x to 2^-21 relative.
-__device__ __forceinline__ float tf32_rest(float x) {
-  return x - __uint_as_float(__float_as_uint(x) & 0xffffe000u);
+// the two FP16 parts of v (v already scaled into the FP16 range)
+__device__ __forceinline__ void split_h16(float v, __half& h1, __half& h2) {
+  h1 = __float2half_rn(v);
+  h2 = __float2half_rn(v - __half2float(h1));
 }
 
 // ---------------------------------------------------------------------------
-template <int P>
 __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   extern __shared__ unsigned char smem_raw[];
-  // 1024-byte alignment of the shared-window offset (swizzle atoms, core matrices)
   const Smem S{smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u)};
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
     for (uint32_t i = 0; i < kSlots; ++i) {
-      mbar_init(S.bfull(i), 1);
-      mbar_init(S.bempty(i), 1);
+      mbar_init(S.fimg(i), 1);
+      mbar_init(S.fz(i), 1);
+      mbar_init(S.empty(i), 1);
     }
     for (uint32_t i = 0; i < kA; ++i) {
       mbar_init(S.aready(i), 4);
@@ -159,11 +167,18 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // A rows of absent right-hand sides are never gathered: zero the stages once
-  // (those rows only feed D rows that are never read)
-  for (uint32_t i = threadIdx.x; i < 2 * kA * (kPiece / 16); i += kThreads)
-    reinterpret_cast<uint4*>(S.astage(0))[i] = make_uint4(0u, 0u, 0u, 0u);
+  // Z rows of a slot past a chunk's K are read into A rows that meet zero B
+  // values: they must hold finite numbers, so every slot's rows start at zero
+  for (uint32_t i = threadIdx.x; i < kSlots * (kUmKc * kZRowPitch / 16); i += kThreads) {
+    const uint32_t sl = i / (kUmKc * kZRowPitch / 16), o = i % (kUmKc * kZRowPitch / 16);
+    reinterpret_cast<uint4*>(S.slot(sl) + kZOff)[o] = make_uint4(0u, 0u, 0u, 0u);
+  }
   fence_proxy_async();
+  if (threadIdx.x < 64) {
+    // Y factor of right-hand side j: 1 / (the scale of X_j)
+    const float m = __uint_as_float(a.xmax[threadIdx.x]);
+    S.ys()[threadIdx.x] = ldexp(1.0, scale_exp((double)m));
+  }
   if (warp == 1) {
     tmem_alloc(smem_u32(S.tmem_slot()), kTmemCols);
     tmem_relinquish();
@@ -174,20 +189,21 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   const uint32_t tmem = *S.tmem_slot();
 
   if (warp == 0) {
-    // ---------------- producer (lane 0 issues; the warp fetches descriptors)
-    uint32_t it = 0, oldest = 0;
-    uint64_t pos = 0, done = 0;
+    // ---------------- producer
+    const uint32_t cb0 = a.cranges[blockIdx.x], ncb = a.cranges[blockIdx.x + 1] - cb0;
+    uint32_t c = 0;  // chunks issued
     bool ok = true;
-    // Frees ring slots (and their bytes, in order) until chunk `it` may take
-    // `sz` bytes at position p0; lane 0 only.
-    auto reserve = [&](uint64_t p0, uint32_t sz) -> bool {
-      while (oldest < it && (it - oldest >= kSlots || p0 + sz > done + kRing)) {
-        if (!wait_bar(S.bempty(oldest % kSlots), (oldest / kSlots) & 1, a.err)) return false;
-        done = S.endpos()[oldest % kSlots];
-        ++oldest;
-      }
-      return true;
+    // lane 0: the slot of chunk cc is free (its previous chunk has been consumed)
+    auto slot_free = [&](uint32_t cc) -> bool {
+      return cc < kSlots || wait_bar(S.empty(cc % kSlots), ((cc / kSlots) - 1) & 1, a.err);
     };
+    // all lanes: the Z-row indices of chunk cc into the queue (one group per chunk, empty past the end)
+    auto prefetch = [&](uint32_t cc) {
+      if (cc < ncb)
+        cp_async4(smem_u32(S.idxq(cc % kQ) + lane), a.zidx + (uint64_t)(cb0 + cc) * kUmKc + lane);
+      cp_async_commit();
+    };
+    for (uint32_t i = 0; i < kLidx; ++i) prefetch(i);
     const uint32_t t0 = a.ranges[blockIdx.x], t1 = a.ranges[blockIdx.x + 1];
     auto fetch = [&](uint32_t tb, uint4& w0, uint4& w1) {
       const uint32_t t = tb + lane;
@@ -209,64 +225,83 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         c1 = n1;
         fetch(t + 32, n0, n1);
       }
-      // UmTile words: src (x, y), nchunks z, n8 | hdr << 16 w; klast (c1.x & 0xffff)
+      // UmTile words: src (c0.x, c0.y), nchunks c0.z, n8 | hdr << 16 c0.w;
+      // klast | kvlast << 16 c1.x
       const uint32_t w_sl = __shfl_sync(0xffffffffu, c0.x, r), w_sh = __shfl_sync(0xffffffffu, c0.y, r);
       const uint32_t nch = __shfl_sync(0xffffffffu, c0.z, r), w3 = __shfl_sync(0xffffffffu, c0.w, r);
-      const uint32_t klast = __shfl_sync(0xffffffffu, c1.x, r) & 0xffffu;
-      if (lane == 0) {
-        const uint64_t tsrc = (uint64_t)w_sl | ((uint64_t)w_sh << 32);
-        const uint32_t n8 = w3 & 0xffffu, hdr = w3 >> 16;
-        const uint64_t cstride = (uint64_t)hdr + (uint64_t)n8 * kUmKc * 4;
-        for (uint32_t c = 0; c < nch; ++c) {
-          const uint32_t kc = c + 1 == nch ? klast : kUmKc;
-          const uint32_t bbytes = n8 * kc * 4, sz = hdr + bbytes;
-          uint64_t p0 = pos;
-          if ((p0 % kRing) + sz > kRing) p0 += kRing - p0 % kRing;  // no entry wraps
-          if (!reserve(p0, sz)) {
-            ok = false;
-            break;
-          }
-          const uint32_t sl = it % kSlots, off = (uint32_t)(p0 % kRing);
-          S.endpos()[sl] = p0 + sz;
-          S.slot_off()[sl] = off | (hdr << 24);
-          mbar_expect_tx(S.bfull(sl), hdr + bbytes);
-          bulk_g2s(smem_u32(S.ring() + off), a.stream + tsrc + (uint64_t)c * cstride, hdr + bbytes, S.bfull(sl));
-          pos = p0 + sz;
-          ++it;
+      const uint32_t w4 = __shfl_sync(0xffffffffu, c1.x, r);
+      const uint64_t tsrc = (uint64_t)w_sl | ((uint64_t)w_sh << 32);
+      const uint32_t n8 = w3 & 0xffffu, hdr = w3 >> 16;
+      const uint32_t klast = w4 & 0xffffu, kvlast = w4 >> 16;
+      const uint64_t cstride = (uint64_t)hdr + (uint64_t)n8 * kUmKc * 4;
+      for (uint32_t ch = 0; ch < nch; ++ch) {
+        const bool lastc = ch + 1 == nch;
+        const uint32_t kc = lastc ? klast : kUmKc, kv = lastc ? kvlast : kUmKc;
+        const uint32_t bytes = hdr + n8 * kc * 4;
+        const uint32_t sl = c % kSlots;
+        bool okl = true;
+        if (lane == 0) okl = slot_free(c);
+        ok = __shfl_sync(0xffffffffu, okl ? 1u : 0u, 0) != 0;
+        if (!ok) break;
+        // this chunk's indices landed (at most kLidx later groups pending)
+        prefetch(c + kLidx);
+        cp_async_wait<kLidx>();
+        const uint32_t zr = S.idxq(c % kQ)[lane];
+        if (lane == 0) {
+          S.meta(sl)->hdr = hdr;
+          mbar_expect_tx(S.fimg(sl), bytes);
+          bulk_g2s(smem_u32(S.slot(sl) + kImgB - hdr), a.stream + tsrc + (uint64_t)ch * cstride, bytes,
+                   S.fimg(sl));
+          mbar_expect_tx(S.fz(sl), kv * kZRowPitch);
         }
+        __syncwarp();
+        // Z rows [0, kv): one bulk copy per run of consecutive rows, issued by the run's first lane
+        const uint32_t prev = __shfl_up_sync(0xffffffffu, zr, 1);
+        const bool start = lane < kv && (lane == 0 || zr != prev + 1u);
+        const uint32_t starts = __ballot_sync(0xffffffffu, start);
+        if (start) {
+          const uint32_t later = lane < 31 ? starts >> (lane + 1) : 0u;
+          const uint32_t end = later ? lane + 1 + (uint32_t)(__ffs(later) - 1) : kv;
+          bulk_g2s(smem_u32(S.zrow(sl, lane)), reinterpret_cast<const unsigned char*>(a.z) + (uint64_t)zr * kZRowPitch,
+                   (end - lane) * kZRowPitch, S.fz(sl));
+        }
+        ++c;
       }
-      ok = __shfl_sync(0xffffffffu, ok ? 1u : 0u, 0) != 0;
-      it = __shfl_sync(0xffffffffu, it, 0);
     }
+    cp_async_wait<0>();
     if (lane == 0) {
-      if (ok && reserve(pos, 0)) {
-        // stop marker: a slot record without an image
-        const uint32_t sl = it % kSlots;
-        S.slot_off()[sl] = kStop;
-        mbar_arrive(S.bfull(sl));
+      bool stopped = false;
+      if (ok && slot_free(c)) {
+        // stop marker: a slot record without an image; both full barriers complete
+        const uint32_t sl = c % kSlots;
+        S.meta(sl)->hdr = 0u;
+        mbar_arrive(S.fimg(sl));
+        mbar_arrive(S.fz(sl));
+        stopped = true;
       }
-      // every bulk copy issued has landed before the CTA may exit: the chunks
-      // not yet consumed (the older ones were consumed, hence landed)
-      // (bounded, but not cut short by another role's error: a copy in flight
-      // must not land after the CTA has exited)
-      for (uint32_t i = oldest; i < it; ++i) mbar_wait_sleep(S.bfull(i % kSlots), (i / kSlots) & 1, a.err);
+      // every bulk copy issued has landed before the CTA may exit (bounded, but
+      // not cut short by another role's error: a copy in flight must not land
+      // after the CTA has exited).  Older chunks were consumed, hence landed;
+      // so was chunk c - kSlots once the stop marker took its slot (its
+      // barriers have moved on by a phase since).
+      const uint32_t keep = stopped ? kSlots - 1 : kSlots;
+      const uint32_t lo = c > keep ? c - keep : 0u;
+      for (uint32_t i = lo; i < c; ++i) {
+        mbar_wait_sleep(S.fimg(i % kSlots), (i / kSlots) & 1, a.err);
+        mbar_wait_sleep(S.fz(i % kSlots), (i / kSlots) & 1, a.err);
+      }
     }
     __syncwarp();
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      // Chunks accumulate in one tensor-memory accumulator for a drain group
-      // (a.drain chunks of one tile, or the rest of the tile); the group's
-      // last chunk commits the accumulator to the epilogue.
-      uint32_t c = 0, gi = 0, gpos = 0;
-      bool gfirst = false;
+      uint32_t c = 0;
       bool issued = false;
       while (true) {
-        const uint32_t sl = c % kSlots, as = c % kA, q = gi % kAcc;
+        const uint32_t sl = c % kSlots, as = c % kA, q = c % kAcc;
         if (!wait_bar(S.aready(as), (c / kA) & 1, a.err)) break;
-        const uint32_t so = S.slot_off()[sl];
-        if (gpos == 0 && gi >= kAcc && !wait_bar(S.accempty(q), (gi / kAcc - 1) & 1, a.err)) break;
-        if (so == kStop) {
+        if (c >= kAcc && !wait_bar(S.accempty(q), ((c / kAcc) - 1) & 1, a.err)) break;
+        if (S.meta(sl)->hdr == 0u) {
           // forward the stop to the epilogue (both arrivals of the phase)
           volatile uint32_t* f = &S.acchdr(q)->flags;
           *f = kUmStop;
@@ -274,34 +309,28 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           mbar_arrive(S.accfull(q));
           break;
         }
-        const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
-        UmHead h = *E.head();
-        if (gpos == 0) gfirst = h.flags & kUmFirst;
+        if (!wait_bar(S.fimg(sl), (c / kSlots) & 1, a.err)) break;
+        const UmHead h = *S.head(sl);
         tc_fence_after();
         const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
-        const uint32_t idesc = umma_idesc_tf32(128, n16);
-        const uint32_t sbo = (uint32_t)h.kc * 32u;  // (kc / 4) core matrices of 128 bytes per 8-row group
+        const uint32_t idesc = umma_idesc_f16(128, n16);
+        const uint32_t sbo = (uint32_t)h.kc * 16u;  // 8 rows x kc FP16 per core-matrix row group
         const uint32_t sa = smem_u32(S.astage(as));
-        const uint32_t sb = smem_u32(E.b());
-        const uint32_t sl2 = smem_u32(S.lostage(as));  // B remainder image
+        const uint32_t sb1 = smem_u32(S.slot(sl) + kImgB);
+        const uint32_t sb2 = sb1 + (uint32_t)h.n8 * h.kc * 2u;
         const uint32_t d = tmem + q * kUmN;
-        for (uint32_t kk = 0; kk < (uint32_t)h.kc / 8u; ++kk) {
-          const uint64_t da = umma_desc_sw128(sa + kk * 32u, 1024u);
-          umma_tf32(d, da, umma_desc(sb + kk * 256u, 128u, sbo), idesc, (kk > 0 || gpos > 0) ? 1u : 0u);
-          umma_tf32(d, da, umma_desc(sl2 + kk * 256u, 128u, sbo), idesc, 1u);
+        for (uint32_t s = 0; s < (uint32_t)h.kc / 16u; ++s) {
+          const uint64_t da = umma_desc(sa + s * 256u, 128u, 512u);
+          umma_f16(d, da, umma_desc(sb1 + s * 256u, 128u, sbo), idesc, s > 0 ? 1u : 0u);
+          umma_f16(d, da, umma_desc(sb2 + s * 256u, 128u, sbo), idesc, 1u);
         }
-        umma_commit(S.bempty(sl));
+        umma_commit(S.empty(sl));
         umma_commit(S.aempty(as));
+        *S.acchdr(q) = h;
+        umma_commit(S.accfull(q));
+        mbar_arrive(S.accfull(q));  // publishes the head (release)
         issued = true;
         ++c;
-        if (++gpos == a.drain || (h.flags & kUmLast)) {
-          h.flags = (h.flags & ~kUmFirst) | (gfirst ? kUmFirst : 0u);
-          *S.acchdr(q) = h;
-          umma_commit(S.accfull(q));
-          mbar_arrive(S.accfull(q));  // publishes the head (release)
-          gpos = 0;
-          ++gi;
-        }
       }
       // the MMAs issued last have completed before the tensor memory is freed
       // (bounded, not cut short by another role's error)
@@ -309,97 +338,33 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     }
     __syncwarp();
   } else if (warp < 6) {
-    // ---------------- stage filling (A + the B remainder image)
-    // A (128 x kc, TF32) in the 128-byte-swizzled K-major layout, rows m < 64
-    // the hi parts of right-hand sides j = m, rows 64 + j their lo parts; atom
-    // g = rows 8 g .. 8 g + 7 (1024 bytes), 16-byte chunk kb (k = 4 kb .. 4 kb
-    // + 3) of row r at chunk kb ^ r.  Lane (kb = lane % 8, t = 4 q + lane / 8)
-    // loads Z rows 4 kb .. 4 kb + 3 of right-hand sides 4 t .. 4 t + 3 (four
-    // 16-byte loads), splits them and stores eight 16-byte row chunks (hi rows
-    // 4 t + i, lo rows 64 + 4 t + i).  Loads run one chunk ahead of the stores.
-    // All four warps then write the B remainder image.
+    // ---------------- A stages: Z rows (K x 128 FP16, row-major) -> K-major canonical
+    // 8 x 8 tiles (mt, kt): rows m = 8 mt .. 8 mt + 7, K positions 8 kt .. 8 kt + 7;
+    // source rows k = 8 kt + i at byte column 16 mt of the slot's Z rows,
+    // destination core matrix at mt * 512 + kt * 128 (rows 16 bytes apart).
+    // Each warp moves 16 tiles with four ldmatrix.x4.trans / stmatrix.x4 pairs
+    // (lanes 8 i .. 8 i + 7 address tile i of an instruction).
     const uint32_t q = warp - 2;
-    const uint32_t tid = threadIdx.x - 64;        // 0 .. 127
-    const uint32_t kb = lane & 7, t4 = 4 * q + (lane >> 3);
-    const bool gather = 4 * t4 < (uint32_t)P;     // this lane's right-hand sides exist
-    float4 vn[4], vc[4];
+    for (uint32_t c = 0;; ++c) {
+      const uint32_t sl = c % kSlots, as = c % kA;
+      if (!__all_sync(0xffffffffu, wait_bar(S.fz(sl), (c / kSlots) & 1, a.err))) break;
+      const bool stop = S.meta(sl)->hdr == 0u;
+      if (c >= kA && !__all_sync(0xffffffffu, wait_bar(S.aempty(as), ((c / kA) - 1) & 1, a.err))) break;
+      if (!stop) {
+        const uint32_t dst0 = smem_u32(S.astage(as));
 #pragma unroll
-    for (uint32_t i = 0; i < 4; ++i) vn[i] = vc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto load = [&](const UmHead& h, const uint32_t* ix, float4 (&v)[4]) {
-#pragma unroll
-      for (uint32_t i = 0; i < 4; ++i) {
-        const uint32_t kp = 4 * kb + i;
-        v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gather && kp < h.kvalid) {
-          const uint32_t zr = (h.flags & kUmContig) ? h.zsrc + kp : ix[kp];
-          v[i] = __ldg(reinterpret_cast<const float4*>(a.z + (uint64_t)zr * P + 4 * t4));
+        for (uint32_t g = 0; g < 4; ++g) {
+          const uint32_t T = q * 16 + g * 4 + (lane >> 3);
+          const uint32_t mt = T & 15u, kt = T >> 4;
+          uint32_t r[4];
+          ldsm_x4_t(r, smem_u32(S.zrow(sl, kt * 8 + (lane & 7)) + mt * 16));
+          stsm_x4(dst0 + mt * 512u + kt * 128u + (lane & 7) * 16u, r);
         }
+        fence_proxy_async();  // generic writes -> the tensor core's (async proxy) reads
       }
-    };
-    auto finalize = [&](uint32_t c, const float4 (&vf)[4]) {
-      const uint32_t so = S.slot_off()[c % kSlots], as = c % kA;
-      const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
-      const UmHead h = *E.head();
-      if (gather && 4 * kb < h.kc) {
-        unsigned char* Ast = S.astage(as);
-        const float x[4][4] = {{vf[0].x, vf[0].y, vf[0].z, vf[0].w}, {vf[1].x, vf[1].y, vf[1].z, vf[1].w},
-                               {vf[2].x, vf[2].y, vf[2].z, vf[2].w}, {vf[3].x, vf[3].y, vf[3].z, vf[3].w}};
-#pragma unroll
-        for (uint32_t i = 0; i < 4; ++i) {
-          float hi[4], lo[4];
-#pragma unroll
-          for (uint32_t k = 0; k < 4; ++k) split_tf32(x[k][i], hi[k], lo[k]);
-          const uint32_t mh = 4 * t4 + i, ml = 64 + mh, r = mh & 7;  // ml & 7 == r
-          *reinterpret_cast<float4*>(Ast + (mh >> 3) * 1024u + r * 128u + ((kb ^ r) << 4)) =
-              make_float4(hi[0], hi[1], hi[2], hi[3]);
-          *reinterpret_cast<float4*>(Ast + (ml >> 3) * 1024u + r * 128u + ((kb ^ r) << 4)) =
-              make_float4(lo[0], lo[1], lo[2], lo[3]);
-        }
-      }
-      const float4* B = reinterpret_cast<const float4*>(E.b());
-      float4* L = reinterpret_cast<float4*>(S.lostage(as));
-      const uint32_t nv = (uint32_t)h.n8 * h.kc / 4;
-      for (uint32_t e = tid; e < nv; e += 128) {
-        const float4 b = B[e];
-        L[e] = make_float4(tf32_rest(b.x), tf32_rest(b.y), tf32_rest(b.z), tf32_rest(b.w));
-      }
-      fence_proxy_async();  // generic writes -> the tensor core's (async proxy) reads
       __syncwarp();
       if (lane == 0) mbar_arrive(S.aready(as));
-    };
-    // One step per chunk c: the loads of chunk c go into one register set while
-    // chunk c - 1 is finalised from the other (ping-pong: the loads have a whole
-    // step to land).  Returns false when the role is done.
-    bool have_prev = false;
-    auto step = [&](uint32_t c, float4 (&vload)[4], float4 (&vfin)[4]) -> bool {
-      const uint32_t sl = c % kSlots;
-      if (!wait_bar(S.bfull(sl), (c / kSlots) & 1, a.err)) return false;
-      const uint32_t so = S.slot_off()[sl];
-      const bool stop = so == kStop;
-      if (!stop) {
-        const Entry E{S.ring() + (so & 0xffffffu), so >> 24};
-        const UmHead h = *E.head();
-        load(h, E.idx(), vload);
-      }
-      if (have_prev) {
-        // the A stage of chunk c - 1 is free once the MMAs of chunk c - 1 - kA are done
-        const uint32_t cp = c - 1;
-        if (cp >= kA && !wait_bar(S.aempty(cp % kA), (cp / kA - 1) & 1, a.err)) return false;
-        finalize(cp, vfin);
-      }
-      have_prev = !stop;
-      if (stop) {
-        // pass the stop on to the MMA issuer through this chunk's A stage
-        if (c >= kA && !wait_bar(S.aempty(c % kA), (c / kA - 1) & 1, a.err)) return false;
-        __syncwarp();
-        if (lane == 0) mbar_arrive(S.aready(c % kA));
-        return false;
-      }
-      return true;
-    };
-    for (uint32_t c = 0;; c += 2) {
-      if (!step(c, vn, vc)) break;
-      if (!step(c + 1, vc, vn)) break;
+      if (stop) break;
     }
   } else {
     // ---------------- epilogue
@@ -407,9 +372,9 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     const uint32_t half = (warp - 6) >> 2;        // columns 64 half .. 64 half + 63
     const uint32_t et = (threadIdx.x - 192) & 127;  // 0 .. 127 within the column half's warps
     const uint32_t j = 32 * (q & 1) + lane;       // right-hand side of this lane's row
-    const bool active = j < (uint32_t)P;          // per lane: guards only the staging writes
-    const bool qactive = 32 * (q & 1) < (uint32_t)P;  // warp-uniform: the quadrant holds rows
-    const bool lo_row = q >= 2;                   // rows 64 .. 127: lo parts
+    const bool active = j < a.pg;                 // per lane: guards only the staging writes
+    const bool qactive = 32 * (q & 1) < a.pg;     // warp-uniform: the quadrant holds rows
+    const bool second = q >= 2;                   // rows 64 .. 127: the second parts
     float acc[64];
 #pragma unroll
     for (int c = 0; c < 64; ++c) acc[c] = 0.f;
@@ -423,6 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       tc_fence_after();
       const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
       const bool first = h.flags & kUmFirst;
+      const float sc = h.scale;
       // tcgen05.ld / wait::ld are warp-collective: warp-uniform condition only
       if (qactive && 64 * half < n16) {
 #pragma unroll
@@ -432,7 +398,8 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
             tmem_ld32(tmem + ((32 * q) << 16) + qa * kUmN + 64 * half + 32 * gg, v);
             tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 32; ++i) acc[32 * gg + i] = first ? v[i] : acc[32 * gg + i] + v[i];
+            for (int i = 0; i < 32; ++i)
+              acc[32 * gg + i] = first ? v[i] * sc : fmaf(v[i], sc, acc[32 * gg + i]);
           }
         }
       }
@@ -441,15 +408,15 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       if (lane == 0) mbar_arrive(S.accempty(qa));
       ++ai;
       if (!(h.flags & kUmLast) || 64 * half >= h.nout) continue;
-      // ---- end of the tile: hi rows, then lo rows added, through the staging tile
+      // ---- end of the tile: first-part rows, then second-part rows added, through the staging tile
       const uint32_t bid = 1 + half;
       named_bar(bid, 128);  // the staging tile is free
-      if (active && !lo_row) {
+      if (active && !second) {
 #pragma unroll
         for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] = acc[c];
       }
       named_bar(bid, 128);
-      if (active && lo_row) {
+      if (active && second) {
 #pragma unroll
         for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] += acc[c];
       }
@@ -461,18 +428,23 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           const uint32_t jj = e >> 6, c = e & 63;
           if (c < nh) {
             double* yp = a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy;
-            *yp += a.d * (double)Sg[jj * kSRow + c];
+            *yp += a.d * S.ys()[jj] * (double)Sg[jj * kSRow + c];
           }
         }
+      } else if (h.flags & kUmRed) {
+        for (uint32_t e = et; e < a.pg * 64; e += 128) {
+          const uint32_t jj = e % a.pg, c = e / a.pg;
+          if (c < nh) atomicAdd(a.tacc + (uint64_t)(h.tacc + 64 * half + c) * 64 + jj, Sg[jj * kSRow + c]);
+        }
       } else {
-        const bool red = h.flags & kUmRed;
-        for (uint32_t e = et; e < (uint32_t)P * 64; e += 128) {
-          const uint32_t jj = e % P, c = e / P;
+        for (uint32_t e = et; e < a.pg * 64; e += 128) {
+          const uint32_t jj = e % a.pg, c = e / a.pg;
           if (c < nh) {
-            float* tp = a.tout + (uint64_t)(row0 + c) * P + jj;
-            const float v = Sg[jj * kSRow + c];
-            if (red) atomicAdd(tp, v);
-            else *tp = v;
+            __half h1, h2;
+            split_h16(Sg[jj * kSRow + c], h1, h2);
+            __half* zp = reinterpret_cast<__half*>(a.z) + (a.n + row0 + c) * (kUmZPitch / 2);
+            zp[jj] = h1;
+            zp[64 + jj] = h2;
           }
         }
       }
@@ -487,42 +459,123 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   }
 }
 
-// X (FP64, column-major, ld ldX), columns 0 .. pg-1 -> Z rows 0 .. n-1 (P FP32
-// each, zero beyond pg); T rows of split V tiles zeroed.
-template <int P>
-__global__ void um_prep_kernel(const double* __restrict__ X, uint64_t ldX, uint64_t n, uint32_t pg,
-                               float* __restrict__ z, const UmRange* __restrict__ zero, uint32_t nzero) {
-  __shared__ float tile[32][P + 1];
-  const uint64_t nblk = (n + 31) / 32;
-  for (uint64_t b = blockIdx.x; b < nblk; b += gridDim.x) {
-    const uint64_t r0 = b * 32;
-    for (uint32_t e = threadIdx.x; e < 32u * P; e += blockDim.x) {
-      const uint32_t row = e & 31, col = e >> 5;
-      float v = 0.f;
-      if (col < pg && r0 + row < n) v = (float)X[(r0 + row) + (uint64_t)col * ldX];
-      tile[row][col] = v;
-    }
-    __syncthreads();
-    for (uint32_t e = threadIdx.x; e < 32u * P; e += blockDim.x) {
-      const uint32_t col = e % P, row = e / P;
-      if (r0 + row < n) z[(r0 + row) * P + col] = tile[row][col];
-    }
-    __syncthreads();
+// max |X_j| over the rows, j < pg (FP32 bits, atomicMax; the words start at 0)
+__global__ void __launch_bounds__(256) um_xmax_kernel(const double* __restrict__ X, uint64_t ldX, uint64_t n,
+                                                      uint32_t pg, uint32_t* __restrict__ xmax) {
+  __shared__ float wm[8][64];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint32_t j = 0; j < pg; ++j) {
+    float m = 0.f;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+      m = fmaxf(m, (float)fabs(X[r + (uint64_t)j * ldX]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) wm[warp][j] = m;
   }
-  float* t = z + n * P;
-  for (uint32_t r = blockIdx.x; r < nzero; r += gridDim.x) {
-    const UmRange R = zero[r];
-    for (uint32_t e = threadIdx.x; e < R.count * (uint32_t)P; e += blockDim.x) t[(uint64_t)R.row * P + e] = 0.f;
+  __syncthreads();
+  if (threadIdx.x < pg) {
+    float m = 0.f;
+    for (uint32_t w = 0; w < 8; ++w) m = fmaxf(m, wm[w][threadIdx.x]);
+    atomicMax(xmax + threadIdx.x, __float_as_uint(m));
   }
 }
 
-// One CTA per tile: chunk heads, Z-row indices and B images from the FP64 arena.
+// X (FP64, column-major, ld ldX), columns 0 .. pg-1 -> Z rows 0 .. n-1: X_j
+// scaled by a power of two (its largest |value| into [2^13, 2^14)) and split
+// into two FP16 parts; slots >= pg are zero.
+__global__ void __launch_bounds__(256) um_prep_kernel(const double* __restrict__ X, uint64_t ldX, uint64_t n,
+                                                      uint32_t pg, const uint32_t* __restrict__ xmax,
+                                                      uint16_t* __restrict__ z) {
+  __shared__ double tile[64][33];
+  __shared__ double sx[64];
+  if (threadIdx.x < 64) {
+    const float m = __uint_as_float(xmax[threadIdx.x]);
+    sx[threadIdx.x] = ldexp(1.0, -scale_exp((double)m));
+  }
+  __syncthreads();
+  const uint64_t nblk = (n + 31) / 32;
+  for (uint64_t b = blockIdx.x; b < nblk; b += gridDim.x) {
+    const uint64_t r0 = b * 32;
+    for (uint32_t e = threadIdx.x; e < 32u * 64u; e += blockDim.x) {
+      const uint32_t row = e & 31, col = e >> 5;
+      double v = 0.0;
+      if (col < pg && r0 + row < n) v = X[(r0 + row) + (uint64_t)col * ldX] * sx[col];
+      tile[col][row] = v;
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < 32u * 64u; e += blockDim.x) {
+      const uint32_t col = e & 63, row = e >> 6;
+      if (r0 + row < n) {
+        const double v = tile[col][row];
+        const __half h1 = __double2half(v);
+        const __half h2 = __double2half(v - (double)__half2float(h1));
+        __half* zp = reinterpret_cast<__half*>(z) + (r0 + row) * (kUmZPitch / 2);
+        zp[col] = h1;
+        zp[64 + col] = h2;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// split V tiles: FP32 accumulation rows -> Z rows (FP16 pairs); the rows are zeroed again
+__global__ void __launch_bounds__(256) um_tconv_kernel(const UmRange* __restrict__ ranges, uint32_t nranges,
+                                                       float* __restrict__ tacc, uint16_t* __restrict__ z,
+                                                       uint64_t n) {
+  for (uint32_t r = blockIdx.x; r < nranges; r += gridDim.x) {
+    const UmRange R = ranges[r];
+    for (uint32_t e = threadIdx.x; e < R.count * 64u; e += blockDim.x) {
+      const uint32_t c = e >> 6, jj = e & 63;
+      float* tp = tacc + (uint64_t)(R.off + c) * 64 + jj;
+      const float v = *tp;
+      *tp = 0.f;
+      __half h1, h2;
+      split_h16(v, h1, h2);
+      __half* zp = reinterpret_cast<__half*>(z) + (n + R.row + c) * (kUmZPitch / 2);
+      zp[jj] = h1;
+      zp[64 + jj] = h2;
+    }
+  }
+}
+
+// T-row scales: one warp per low-rank leaf; s_t = 2^-e with ||V_t||_1 = f 2^e, f in [0.5, 1)
+__global__ void __launch_bounds__(256) um_tscale_kernel(const UmTJob* __restrict__ jobs, uint32_t njobs,
+                                                        const double* __restrict__ a64,
+                                                        float* __restrict__ tscale) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t jb = w0; jb < njobs; jb += nw) {
+    const UmTJob J = jobs[jb];
+    for (uint32_t col = 0; col < J.rank; ++col) {
+      const double* v = a64 + J.vbase + (uint64_t)col * J.n2;
+      double s = 0.0;
+      for (uint32_t i = lane; i < J.n2; i += 32) s += fabs(v[i]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        int ex = 0;
+        if (s > 0.0) frexp(s, &ex);
+        ex = max(-100, min(100, ex));
+        tscale[J.trow + col] = ldexpf(1.f, -ex);
+      }
+    }
+  }
+}
+
+// One CTA per tile: chunk heads, Z-row indices and the FP16 image pairs from
+// the FP64 arena (V values times the T-row scale, U values divided by it).
 __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict__ tiles,
                                                        const UmEntry* __restrict__ entries,
                                                        const double* __restrict__ a64,
-                                                       unsigned char* __restrict__ stream) {
+                                                       const float* __restrict__ tscale, uint64_t n,
+                                                       unsigned char* __restrict__ stream,
+                                                       uint32_t* __restrict__ zidx) {
   const UmBuild T = tiles[blockIdx.x];
   __shared__ int32_t ent[kUmN];
+  __shared__ double vals[kUmN * kUmKc];
+  __shared__ double red[8];
   const bool byN = T.flags & kUmByN, contig = T.flags & kUmContig;
   const uint32_t tid = threadIdx.x;
   if (byN) {
@@ -536,7 +589,7 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
   }
   uint64_t off = T.src;
   for (uint32_t c = 0; c < T.nchunks; ++c) {
-    const uint32_t kb = c * kUmKc, kval = min(kUmKc, T.K - kb), kc = (kval + 7u) & ~7u;
+    const uint32_t kb = c * kUmKc, kval = min(kUmKc, T.K - kb), kc = (kval + 15u) & ~15u;
     unsigned char* img = stream + off;
     unsigned char* B = img + T.hdr;
     if (!byN) {
@@ -558,27 +611,9 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
       }
       __syncthreads();
     }
-    if (tid == 0) {
-      UmHead h{};
-      h.zsrc = contig ? T.zrow0 + kb : 0u;
-      h.kc = (uint16_t)kc;
-      h.kvalid = (uint16_t)kval;
-      h.n8 = T.n8;
-      h.nout = (uint16_t)T.nout;
-      h.out = T.out;
-      h.flags = (c == 0 ? kUmFirst : 0u) | (c + 1 == T.nchunks ? kUmLast : 0u) | (T.flags & (kUmContig | kUmRed));
-      h.tile = blockIdx.x;
-      *reinterpret_cast<UmHead*>(B - 32) = h;
-    }
-    if (!contig && tid < kUmKc) {
-      uint32_t zr = 0;
-      if (tid < kval && ent[tid] >= 0) {
-        const UmEntry E = entries[T.e0 + ent[tid]];
-        zr = E.zrow0 + (kb + tid - E.k0);
-      }
-      reinterpret_cast<uint32_t*>(img)[tid] = zr;
-    }
+    // values of the chunk and their largest magnitude
     const uint32_t cnt = (uint32_t)T.n8 * kc;
+    double m = 0.0;
     for (uint32_t e = tid; e < cnt; e += blockDim.x) {
       uint32_t nn, kk;
       if (byN) {
@@ -588,18 +623,76 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
         nn = e % T.n8;
         kk = e / T.n8;
       }
-      float v = 0.f;
+      double v = 0.0;
       if (nn < T.nout && kk < kval) {
         const int32_t ei = byN ? ent[nn] : ent[kk];
         if (ei >= 0) {
           const UmEntry E = entries[T.e0 + ei];
           const uint32_t K = kb + kk;
-          if (K >= E.k0 && K < E.k0 + E.kn && nn >= E.n0 && nn < E.n0 + E.nn)
-            v = (float)a64[E.base + (uint64_t)(K - E.k0) * E.sk + (uint64_t)(nn - E.n0) * E.sn];
+          if (K >= E.k0 && K < E.k0 + E.kn && nn >= E.n0 && nn < E.n0 + E.nn) {
+            v = a64[E.base + (uint64_t)(K - E.k0) * E.sk + (uint64_t)(nn - E.n0) * E.sn];
+            if (byN) v *= (double)tscale[T.out + nn];                               // V column of T row out + nn
+            else if (E.zrow0 >= n) v /= (double)tscale[E.zrow0 - n + (K - E.k0)];  // U column of a T row
+          }
         }
       }
-      *reinterpret_cast<float*>(B + (nn >> 3) * (kc * 32u) + (kk >> 2) * 128u + (nn & 7u) * 16u + (kk & 3u) * 4u) = v;
+      vals[e] = v;
+      m = fmax(m, fabs(v));
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((tid & 31) == 0) red[tid >> 5] = m;
+    __syncthreads();
+    double mx = 0.0;
+    for (uint32_t w = 0; w < blockDim.x / 32; ++w) mx = fmax(mx, red[w]);
+    const int se = max(-120, min(120, scale_exp(mx)));
+    const double inv = ldexp(1.0, -se);
+    if (tid == 0) {
+      UmHead h{};
+      h.zsrc = contig ? T.zrow0 + kb : 0u;
+      h.kc = (uint16_t)kc;
+      h.kvalid = (uint16_t)kval;
+      h.n8 = T.n8;
+      h.nout = (uint16_t)T.nout;
+      h.out = T.out;
+      h.flags = (c == 0 ? kUmFirst : 0u) | (c + 1 == T.nchunks ? kUmLast : 0u) | (T.flags & (kUmContig | kUmRed));
+      h.scale = ldexpf(1.f, se);
+      h.tacc = T.tacc;
+      h.tile = blockIdx.x;
+      *reinterpret_cast<UmHead*>(B - 32) = h;
+    }
+    if (tid < kUmKc) {
+      // Z rows of the chunk's K positions (positions past kval unused)
+      uint32_t zr = 0;
+      if (tid < kval) {
+        if (contig) {
+          zr = T.zrow0 + kb + tid;
+        } else if (ent[tid] >= 0) {
+          const UmEntry E = entries[T.e0 + ent[tid]];
+          zr = E.zrow0 + (kb + tid - E.k0);
+        }
+      }
+      zidx[(uint64_t)(T.cbase + c) * kUmKc + tid] = zr;
+    }
+    __half* B1 = reinterpret_cast<__half*>(B);
+    __half* B2 = B1 + (size_t)T.n8 * kc;
+    for (uint32_t e = tid; e < cnt; e += blockDim.x) {
+      uint32_t nn, kk;
+      if (byN) {
+        kk = e % kc;
+        nn = e / kc;
+      } else {
+        nn = e % T.n8;
+        kk = e / T.n8;
+      }
+      const double v = vals[e] * inv;
+      const __half h1 = __double2half(v);
+      const __half h2 = __double2half(v - (double)__half2float(h1));
+      const uint32_t o = (nn >> 3) * (kc * 8u) + (kk >> 3) * 64u + (nn & 7u) * 8u + (kk & 7u);  // in FP16 units
+      B1[o] = h1;
+      B2[o] = h2;
+    }
+    __syncthreads();
     off += T.hdr + (uint64_t)T.n8 * kc * 4;
   }
 }
@@ -613,7 +706,6 @@ std::mutex g_tmu;
 bool g_timing = false;
 std::vector<TimingRec> g_trecs;
 
-template <int P>
 cudaError_t launch_sweep(const KArgs& a, int kind, uint32_t grid, cudaStream_t s) {
   TimingRec r{kind, nullptr, nullptr};
   bool timed = false;
@@ -626,7 +718,7 @@ cudaError_t launch_sweep(const KArgs& a, int kind, uint32_t grid, cudaStream_t s
     cudaEventCreate(&r.e1);
     cudaEventRecord(r.e0, s);
   }
-  um_sweep_kernel<P><<<grid, kThreads, kSmemBytes, s>>>(a);
+  um_sweep_kernel<<<grid, kThreads, kSmemBytes, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (timed) {
     cudaEventRecord(r.e1, s);
@@ -636,39 +728,52 @@ cudaError_t launch_sweep(const KArgs& a, int kind, uint32_t grid, cudaStream_t s
   return e;
 }
 
-template <int P>
 cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const double* X, uint64_t ldX, double* Y,
                    uint64_t ldY, cudaStream_t s) {
   const uint64_t nblk = (pl.n + 31) / 32;
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(nblk, (uint64_t)pl.grid * 8));
-  um_prep_kernel<P><<<grid, 256, 0, s>>>(X + (uint64_t)r0 * ldX, ldX, pl.n, pg, pl.z, pl.zero, pl.nzero);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaMemsetAsync(pl.xmax, 0, 64 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  uint64_t launches = 1;
+  const double* Xp = X + (uint64_t)r0 * ldX;
+  const unsigned gx = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((pl.n + 255) / 256, (uint64_t)pl.grid * 4));
+  um_xmax_kernel<<<gx, 256, 0, s>>>(Xp, ldX, pl.n, pg, pl.xmax);
+  um_prep_kernel<<<grid, 256, 0, s>>>(Xp, ldX, pl.n, pg, pl.xmax, pl.z);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  uint64_t launches = 2;
   KArgs a{};
   a.z = pl.z;
+  a.tacc = pl.tacc;
+  a.xmax = pl.xmax;
   a.err = pl.err;
   a.pg = pg;
-  a.drain = std::max<uint32_t>(1u, pl.drain);
+  a.n = pl.n;
   if (pl.nvtiles) {
     a.tiles = pl.vtiles;
     a.ranges = pl.vranges;
+    a.cranges = pl.vcranges;
+    a.zidx = pl.vzidx;
     a.stream = pl.vstream;
-    a.tout = pl.z + pl.n * P;
     a.mode = 0;
-    if ((e = launch_sweep<P>(a, 0, pl.grid, s)) != cudaSuccess) return e;
+    if ((e = launch_sweep(a, 0, pl.grid, s)) != cudaSuccess) return e;
+    ++launches;
+  }
+  if (pl.nzero) {
+    um_tconv_kernel<<<std::min<uint32_t>(pl.nzero, pl.grid * 4), 256, 0, s>>>(pl.zero, pl.nzero, pl.tacc, pl.z,
+                                                                              pl.n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     ++launches;
   }
   if (pl.nrtiles) {
     a.tiles = pl.rtiles;
     a.ranges = pl.rranges;
+    a.cranges = pl.rcranges;
+    a.zidx = pl.rzidx;
     a.stream = pl.rstream;
-    a.tout = nullptr;
     a.y = Y + (uint64_t)r0 * ldY;
     a.ldy = ldY;
     a.d = d;
     a.mode = 1;
-    if ((e = launch_sweep<P>(a, 1, pl.grid, s)) != cudaSuccess) return e;
+    if ((e = launch_sweep(a, 1, pl.grid, s)) != cudaSuccess) return e;
     ++launches;
   }
   count_product_launches(launches);
@@ -676,34 +781,37 @@ cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const d
 }
 
 uint32_t round8(uint32_t x) { return (x + 7u) & ~7u; }
+uint32_t round16(uint32_t x) { return (x + 15u) & ~15u; }
 
 }  // namespace
 
 cudaError_t um_init_attributes() {
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(um_sweep_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes)))
-    return e;
-  if ((e = cudaFuncSetAttribute(um_sweep_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes)))
-    return e;
-  return cudaFuncSetAttribute(um_sweep_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+  return cudaFuncSetAttribute(um_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+}
+
+cudaError_t launch_um_tscale(const UmTJob* jobs, uint32_t njobs, const double* arena64, float* tscale,
+                             cudaStream_t s) {
+  if (njobs == 0) return cudaSuccess;
+  const uint32_t blocks = std::min<uint32_t>((njobs + 7) / 8, 65535u);
+  um_tscale_kernel<<<blocks, 256, 0, s>>>(jobs, njobs, arena64, tscale);
+  count_product_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_um_build(const UmBuild* tiles, uint32_t ntiles, const UmEntry* entries, const double* arena64,
-                            unsigned char* stream, cudaStream_t s) {
+                            const float* tscale, uint64_t n, unsigned char* stream, uint32_t* zidx,
+                            cudaStream_t s) {
   if (ntiles == 0) return cudaSuccess;
-  um_build_kernel<<<ntiles, 256, 0, s>>>(tiles, entries, arena64, stream);
+  um_build_kernel<<<ntiles, 256, 0, s>>>(tiles, entries, arena64, tscale, n, stream, zidx);
   count_product_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_matvec_um(const UmPlan& pl, double d, uint32_t p, const double* X, uint64_t ldX, double* Y,
                              uint64_t ldY, cudaStream_t s) {
-  for (uint32_t r0 = 0; r0 < p; r0 += 64) {
-    const uint32_t pg = std::min(64u, p - r0);
-    cudaError_t e;
-    if (pg <= 16) e = run_um<16>(pl, d, r0, pg, X, ldX, Y, ldY, s);
-    else if (pg <= 32) e = run_um<32>(pl, d, r0, pg, X, ldX, Y, ldY, s);
-    else e = run_um<64>(pl, d, r0, pg, X, ldX, Y, ldY, s);
+  for (uint32_t r0 = 0; r0 < p; r0 += kUmSlots) {
+    const uint32_t pg = std::min(kUmSlots, p - r0);
+    const cudaError_t e = run_um(pl, d, r0, pg, X, ldX, Y, ldY, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -766,7 +874,10 @@ void build_um_layout(const std::vector<PlanLeaf>& leaves, uint64_t n, uint32_t g
     for (uint32_t g0 = 0; g0 < nc; g0 += kUmN) {
       const uint32_t ng = std::min(kUmN, nc - g0);
       const bool red = npieces > 1;
-      if (red) L.zero.push_back({tc + g0, ng});
+      if (red) {
+        L.zero.push_back({tc + g0, ng, L.tacc_rows, 0u});
+        L.tacc_rows += ng;
+      }
       for (uint32_t pc = 0; pc < npieces; ++pc) {
         const uint32_t k0 = pc * kpiece, K = std::min(kpiece, n2 - k0);
         UmBuild B{};
@@ -778,6 +889,7 @@ void build_um_layout(const std::vector<PlanLeaf>& leaves, uint64_t n, uint32_t g
         B.flags = kUmContig | kUmByN | (red ? kUmRed : 0u);
         B.n8 = (uint16_t)round8(ng);
         B.hdr = 32;
+        B.tacc = red ? L.zero.back().off : 0u;
         B.nchunks = (K + kUmKc - 1) / kUmKc;
         for (size_t i = 0; i < ls.size(); ++i) {
           const PlanLeaf& q = leaves[ls[i]];
@@ -799,6 +911,11 @@ void build_um_layout(const std::vector<PlanLeaf>& leaves, uint64_t n, uint32_t g
     }
   }
   L.t_rows = t_rows;
+  for (size_t l = 0; l < leaves.size(); ++l)
+    if (leaves[l].rank > 0) {
+      const PlanLeaf& q = leaves[l];
+      L.tjobs.push_back({q.off + (uint64_t)q.rank * q.n1, q.n2, (uint32_t)q.rank, trow[l], 0u});
+    }
 
   // ---- rows sweep: finest row blocks (<= kUmN rows) of the row clusters
   std::vector<uint32_t> bd{0u, (uint32_t)n};
@@ -852,7 +969,7 @@ void build_um_layout(const std::vector<PlanLeaf>& leaves, uint64_t n, uint32_t g
     B.out = bs[i];
     B.flags = 0;
     B.n8 = (uint16_t)round8(B.nout);
-    B.hdr = (uint16_t)(32 + kUmIdxBytes);
+    B.hdr = 32;
     B.nchunks = (K + kUmKc - 1) / kUmKc;
     if (K > 0) L.rbuild.push_back(B);
     std::vector<UmEntry>().swap(es);
@@ -860,34 +977,49 @@ void build_um_layout(const std::vector<PlanLeaf>& leaves, uint64_t n, uint32_t g
 
   // ---- stream offsets and the kernel's tiles
   auto chunk_bytes = [](const UmBuild& B) {
-    const uint32_t klast = round8(B.K - (B.nchunks - 1) * kUmKc);
+    const uint32_t klast = round16(B.K - (B.nchunks - 1) * kUmKc);
     return (uint64_t)(B.nchunks - 1) * (B.hdr + (uint64_t)B.n8 * kUmKc * 4) + B.hdr + (uint64_t)B.n8 * klast * 4;
   };
-  auto place = [&](std::vector<UmBuild>& bl, std::vector<UmTile>& tl, uint64_t& bytes) {
+  auto place = [&](std::vector<UmBuild>& bl, std::vector<UmTile>& tl, uint64_t& bytes, uint64_t& chunks) {
     bytes = 0;
+    chunks = 0;
     tl.clear();
     for (UmBuild& B : bl) {
       B.src = bytes;
+      B.cbase = (uint32_t)chunks;
+      chunks += B.nchunks;
       bytes += chunk_bytes(B);
       UmTile T{};
       T.src = B.src;
       T.nchunks = B.nchunks;
       T.n8 = B.n8;
       T.hdr = B.hdr;
-      T.klast = (uint16_t)round8(B.K - (B.nchunks - 1) * kUmKc);
+      T.klast = (uint16_t)round16(B.K - (B.nchunks - 1) * kUmKc);
+      T.kvlast = (uint16_t)(B.K - (B.nchunks - 1) * kUmKc);
+      T.zrow0 = B.zrow0;
+      T.flags = B.flags & kUmContig;
       tl.push_back(T);
     }
   };
-  place(L.vbuild, L.vtiles, L.vbytes);
-  place(L.rbuild, L.rtiles, L.rbytes);
+  place(L.vbuild, L.vtiles, L.vbytes, L.vchunks);
+  place(L.rbuild, L.rtiles, L.rbytes, L.rchunks);
   // contiguous tile ranges per CTA, balanced by stream bytes
   auto ranges = [&](const std::vector<UmBuild>& bl, std::vector<uint32_t>& first) {
     std::vector<uint64_t> bytes(bl.size());
-    for (size_t t = 0; t < bl.size(); ++t) bytes[t] = chunk_bytes(bl[t]);
+    // stream bytes plus the chunks' Z rows (mostly L2 hits: weighted by half)
+    for (size_t t = 0; t < bl.size(); ++t) bytes[t] = chunk_bytes(bl[t]) + (uint64_t)bl[t].nchunks * kUmKc * kUmZRowBytes / 2;
     balance_ranges(bytes, std::max<uint32_t>(grid, 1), first);
   };
   ranges(L.vbuild, L.vranges);
   ranges(L.rbuild, L.rranges);
+  // the first chunk of every CTA's range
+  auto cranges = [&](const std::vector<UmBuild>& bl, const std::vector<uint32_t>& first, uint64_t chunks,
+                     std::vector<uint32_t>& out) {
+    out.resize(first.size());
+    for (size_t i = 0; i < first.size(); ++i) out[i] = first[i] < bl.size() ? bl[first[i]].cbase : (uint32_t)chunks;
+  };
+  cranges(L.vbuild, L.vranges, L.vchunks, L.vcranges);
+  cranges(L.rbuild, L.rranges, L.rchunks, L.rcranges);
   L.stream_bytes = L.vbytes + L.rbytes;
   for (const PlanLeaf& q : leaves)
     L.payload_bytes += 4ull * (q.rank >= 0 ? (uint64_t)q.rank * (q.n1 + q.n2) : (uint64_t)q.n1 * q.n2);

@@ -770,6 +770,99 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+def run_kernels(args):
+    """One small case of every kernel family, for per-kernel profiling captures (ncu
+    launch lists with DRAM bytes): the Laplace sphere at `--n` points (leaf 32, eta 0.8,
+    eps 1e-6): assembly (ACA, recompression, dense leaves), products with FP64 / FP32 /
+    BF16 / double-float leaves at 16 and 1 right-hand sides, the transposed product,
+    GMRES and CG; the symmetric tree; agglomeration (N = 4096); save and load of the
+    leaves; the rank predictor (features, training, prediction, hinted assembly); the
+    Helmholtz H-matrix (complex ACA and products); a batch of four instances."""
+    import tempfile as _tf
+
+    import torch
+    import ahmed_gb300 as A
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    G = A.geometry
+    n = args.n
+    P = G.fibonacci_sphere(n)
+    h = A.mean_nn(P)
+    H = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+    H.matgenGeH_omp(h, EPS)
+    rng = np.random.default_rng(1)
+    for p in (16, 1):
+        X = torch.from_numpy(rng.uniform(-1.0, 1.0, (p, n))).to(dev)
+        for prec in ("fp64", "fp32", "bf16", "df64"):
+            Y = torch.zeros_like(X)
+            for _ in range(2):
+                H.mltaGeHVec(1.0, X, Y, precision=prec)
+        H.mltaGeHhGeM(1.0, p, X, n, torch.zeros_like(X), n)
+    b = np.random.default_rng(3).standard_normal(n)
+    Hs = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+    Hs.matgenGeH_omp(h / 2.0, EPS)
+    Hs.GMRes(b, np.zeros(n), 1e-8, 30, 200)
+    Hs.GMRes(b, np.zeros(n), 1e-8, 30, 400, precision="fp32")
+    Hs.CG(b, np.zeros(n), 1e-8, 200)
+    Hs.spctrlnrm(5)
+    Hs.close()
+    with _tf.TemporaryDirectory() as d:
+        f = os.path.join(d, "leaves.mbls")
+        H.save(f)
+        H2 = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+        H2.load(f)
+        H2.close()
+    feats = H.features(EPS)
+    r = H.aca_ranks()
+    lv = H.leaves()
+    sel = (lv[:, 4] == 1) & (r >= 0)
+    M = A.RankPredictor(seed=0)
+    M.fit(feats[sel], r[sel], epochs=2, batch=1024, lr=2e-3)
+    pred = M.predict(feats)
+    Hh = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
+    Hh.assemble_hinted(h, EPS, np.where(lv[:, 4] == 1, pred, -1.0))
+    Hh.close()
+    H.close()
+    Psym = G.fibonacci_sphere(16384)
+    Hy = A.HMatrix(Psym, "bbx", bmin=BMIN, eta=ETA, symmetric=True)
+    Hy.matgenGeH_omp(A.mean_nn(Psym), EPS)
+    Xs = torch.from_numpy(rng.uniform(-1.0, 1.0, (16, Hy.n))).to(dev)
+    Hy.mltaGeHVec(1.0, Xs, torch.zeros_like(Xs))
+    Hy.close()
+    Pa = G.fibonacci_sphere(4096)
+    Ha = A.HMatrix(Pa, "bbx", bmin=BMIN, eta=ETA)
+    Ha.matgenGeH_omp(A.mean_nn(Pa), EPS)
+    Ha.agglH(EPS)
+    Ha.close()
+    Pz = G.sphere_surface(16384, 17)
+    Hz = A.HMatrix(Pz, "bbx", bmin=BMIN, eta=ETA)
+    Hz.helmholtz_aca_ranks(16.2, A.mean_nn(Pz), EPS)
+    Hz.helmholtz_assemble(16.2, A.mean_nn(Pz), EPS)
+    for p in (16, 1):
+        Xz = torch.from_numpy(rng.standard_normal((p, Hz.n)) + 1j * rng.standard_normal((p, Hz.n))).to(dev)
+        for prec in ("fp64", "fp32"):
+            Hz.mltaGeHVec(1.0, Xz, torch.zeros_like(Xz), precision=prec)
+    Ha2 = A.HMatrix(Pa, "bbx", bmin=BMIN, eta=ETA)
+    Ha2.helmholtz_assemble(5.0, A.mean_nn(Pa), EPS)
+    Ha2.helm_agglH(EPS)
+    Ha2.close()
+    Hz.close()
+    mats = []
+    for i, m in enumerate((2048, 3000, 5000, 8000)):
+        Pm = G.sphere_surface(m, 100 + i)
+        Hm = A.HMatrix(Pm, "bbx", bmin=BMIN, eta=ETA)
+        Hm.matgenGeH_omp(A.min_nn(Pm) / 2.0, EPS)
+        mats.append(Hm)
+    Bt = A.HBatch(mats, precision="bf16")
+    xb = np.random.default_rng(4).standard_normal(Bt.n)
+    Bt.matvec(1.0, xb, np.zeros(Bt.n))
+    Bt.gmres(xb, np.zeros(Bt.n), 1e-8, 30, 300)
+    Bt.close()
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": f"kernels-sphere-{n}", "ok": True}))
+
+
 # ---------------------------------------------------------------------------
 # Headline workload: N = 1,048,576 uniform random points on the unit-cube surface
 # (seed 4), Laplace kernel, bounding-box tree, leaf 64, eta 0.8, ACA eps 1e-6,
@@ -1079,7 +1172,7 @@ def main():
                     help="number of points (smaller cases are for profiling only)")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "sphere", "cube-large", "batch", "product", "predictor", "helmholtz",
-                             "zhmat", "aggl"],
+                             "zhmat", "aggl", "kernels"],
                     help="headline (default): N = 2^20 cube surface, leaf 64, 64 right-hand sides, FP32 "
                          "products on the tensor cores and GMRES(50); sphere: N = 65,536 sphere, 16 "
                          "right-hand sides; cube-large: the same N = 2^20 workload with BF16 factors; "
@@ -1126,6 +1219,8 @@ def main():
         run_zhmat(args)
     elif args.workload == "aggl":
         run_aggl(args)
+    elif args.workload == "kernels":
+        run_kernels(args)
     else:
         run_gpu(args)  # sphere
 
