@@ -2,25 +2,28 @@
 // tensor-memory accumulators, kind::f16) over leaf streams of FP16 pairs; the
 // layout, the sweeps and the precision scheme are described in ahx_umma.cuh.
 //
-// One persistent CTA per SM, 14 warps with fixed roles:
+// One persistent CTA per SM, 20 warps with fixed roles:
 //   warp 0      producer: walks the CTA's contiguous range of tiles (ranges
 //               balanced by bytes; descriptors fetched 32 at a time); the Z-row
 //               indices of the chunk kLidx ahead go into a small queue (cp.async,
-//               one word per lane); each chunk image is bulk-copied
+//               two words per lane); each chunk image is bulk-copied
 //               (cp.async.bulk) into one of kSlots ring slots together with its
 //               Z rows (one bulk copy per run of consecutive rows)
 //   warp 1      MMA issuer (one thread) and owner of the tensor memory: per
-//               chunk, 2 * kc / 16 tcgen05.mma (first and second FP16 part of
-//               B) into one of four 128-column accumulators, then
-//               tcgen05.commit to the ring slot, the A stage and the
-//               accumulator
-//   warps 2-5   A stages: the chunk's Z rows (K x 128 FP16, row-major in the
+//               chunk, kc / 16 tcgen05.mma of N = 128 + n16 (the first FP16
+//               part of B in rows 0 .. n8 - 1, the second in rows 128 ..
+//               128 + n8 - 1: one wide MMA per K step instead of two narrow
+//               ones, whose fixed issue cost dominates) into one of two
+//               256-column accumulators, then tcgen05.commit to the ring slot
+//               (which also frees the chunk's A stage) and the accumulator
+//   warps 2-3   A stages: the chunk's Z rows (K x 128 FP16, row-major in the
 //               slot) transposed into the K-major canonical layout with
 //               ldmatrix.trans / stmatrix, one of kA stages
-//   warps 6-13  epilogue, two warps per tensor-memory lane quadrant (columns
-//               0-63 and 64-127): each thread adds its accumulator row, times
-//               the chunk's scale, to registers (round-to-nearest FP32) per
-//               chunk; at the end of a tile the rows of the two parts are
+//   warps 4-19  epilogue, four warps per tensor-memory lane quadrant (output
+//               rows 0-31, 32-63, 64-95, 96-127): each thread adds its accumulator row
+//               (the two parts of B summed), times the chunk's scale, to
+//               registers (round-to-nearest FP32) per chunk; at the end of a
+//               tile the rows of the two parts of A are
 //               summed through shared memory into Y (FP64, in place) or into
 //               T rows (split into FP16 pairs; FP32 atomics for split tiles)
 // Every wait is bounded: on timeout the kernel raises the error word and all
@@ -42,7 +45,7 @@ namespace {
 using namespace ptx;
 
 // ---- shared-memory plan (offsets from the 1024-byte aligned base)
-constexpr uint32_t kSlots = 6;                            // ring slots (chunk image + its Z rows)
+constexpr uint32_t kSlots = 3;                            // ring slots (chunk image + its Z rows)
 constexpr uint32_t kLidx = 6;                             // Z-row indices are fetched this many chunks ahead
 constexpr uint32_t kQ = 8;                                // index queue entries (> kLidx)
 constexpr uint32_t kImgHead = 0;                          // slot offset of the chunk head
@@ -51,24 +54,31 @@ constexpr uint32_t kImgMax = kUmN * kUmKc * 4;            // b1 + b2 images of t
 constexpr uint32_t kZRowPitch = kUmZPitch;                // Z rows in a slot, as in global memory
 constexpr uint32_t kZOff = (kImgB + kImgMax + 127) / 128 * 128;
 constexpr uint32_t kSlotBytes = (kZOff + kUmKc * kZRowPitch + 127) / 128 * 128;
-constexpr uint32_t kA = 3;                                // A stages
-constexpr uint32_t kAStage = 128 * kUmKc * 2;             // 128 rows x 32 K positions, FP16
-constexpr uint32_t kAcc = 4;                              // tensor-memory accumulators (128 columns each)
-constexpr uint32_t kSRow = 65;                            // staging row stride (floats): conflict-free
+constexpr uint32_t kA = 2;                                // A stages
+constexpr uint32_t kAStage = 128 * kUmKc * 2;             // 128 rows x kUmKc K positions, FP16
+constexpr uint32_t kASbo = kUmKc * 16;                    // A stage: bytes per 8-row group
+constexpr uint32_t kAcc = 2;                              // tensor-memory accumulators (256 columns each)
+constexpr uint32_t kAccCols = 2 * kUmN;
+constexpr uint32_t kSRow = 33;                            // staging row stride (floats): conflict-free
 constexpr uint32_t kOffA = kSlots * kSlotBytes;
 constexpr uint32_t kOffStaging = kOffA + kA * kAStage;
-constexpr uint32_t kStagingBytes = 64 * kSRow * 4;        // per column half
-constexpr uint32_t kOffYs = kOffStaging + 2 * kStagingBytes;   // 64 doubles: Y factor per right-hand side
+constexpr uint32_t kStagingBytes = 64 * kSRow * 4;        // per quarter of the output rows
+constexpr uint32_t kOffYs = kOffStaging + 4 * kStagingBytes;   // 64 doubles: Y factor per right-hand side
 constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
 constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
 constexpr uint32_t kOffIdxQ = kOffMeta + kSlots * 16;     // index queue: kQ x 32 words
 constexpr uint32_t kOffBar = kOffIdxQ + kQ * kUmKc * 4;
-constexpr uint32_t kNumBars = 3 * kSlots + 2 * kA + 2 * kAcc;
+constexpr uint32_t kNumBars = 3 * kSlots + kA + 2 * kAcc;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
 constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;     // + alignment slack of the dynamic base
-constexpr uint32_t kThreads = 448;
-constexpr uint32_t kEpiWarps = 8;                         // epilogue warps: each arrives on accempty
-constexpr uint32_t kTmemCols = kAcc * kUmN;               // all 512 columns
+constexpr uint32_t kThreads = 640;
+constexpr uint32_t kTrWarps = 2;                          // A-stage warps: each arrives on aready
+constexpr uint32_t kEpiWarp0 = 2 + kTrWarps;              // first epilogue warp
+constexpr uint32_t kEpiWarps = 16;                        // epilogue warps: each arrives on accempty
+static_assert(kEpiWarp0 % 4 == 0, "epilogue warps cover the lane quadrants in order");
+constexpr uint32_t kTmemCols = kAcc * kAccCols;           // all 512 columns
+static_assert(kSlots > kA, "an A stage is free once its previous chunk's slot is released");
+static_assert(kUmKc == 64, "the producer and the A-stage warps handle two 32-position halves");
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 static_assert(kQ > kLidx, "the queue entry of a chunk is read before a later prefetch reuses it");
 
@@ -93,7 +103,33 @@ struct KArgs {
   double d;
   uint32_t pg;          // right-hand sides of this pass (<= 64)
   uint32_t mode;        // 0: V sweep (T out), 1: rows sweep (Y out)
+  uint32_t prof;        // 1: per-role cycle counters into g_um_prof
   int* err;
+};
+
+// Per-role cycle counters of the sweeps (diagnostics, off by default): summed
+// over CTAs, lane 0 of warps 0 (producer), 1 (MMA), 2 (A stages), 6 (epilogue).
+enum UmProf : uint32_t {
+  kPfProdTotal, kPfProdSlot, kPfProdIdx, kPfChunks,
+  kPfTrFz, kPfTrAempty, kPfTrWork, kPfPad7,
+  kPfMmaAready, kPfMmaAccempty, kPfMmaImg, kPfMmaIssue,
+  kPfEpiAccfull, kPfEpiDrain, kPfEpiTile, kPfKernel,
+  kPfCount = 16
+};
+__device__ unsigned long long g_um_prof[kPfCount];
+
+struct ProfClock {
+  bool on;
+  unsigned long long acc[4] = {0, 0, 0, 0};
+  __device__ explicit ProfClock(bool o) : on(o) {}
+  __device__ __forceinline__ long long now() const { return on ? clock64() : 0; }
+  __device__ __forceinline__ void add(int i, long long t0) {
+    if (on) acc[i] += (unsigned long long)(clock64() - t0);
+  }
+  __device__ void flush(uint32_t base) const {
+    if (!on) return;
+    for (int i = 0; i < 4; ++i) atomicAdd(&g_um_prof[base + i], acc[i]);
+  }
 };
 
 struct Smem {
@@ -103,8 +139,8 @@ struct Smem {
   __device__ uint32_t* idxq(uint32_t i) const { return reinterpret_cast<uint32_t*>(base + kOffIdxQ) + i * kUmKc; }
   __device__ unsigned char* zrow(uint32_t i, uint32_t k) const { return slot(i) + kZOff + k * kZRowPitch; }
   __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + i * kAStage; }
-  __device__ float* staging(uint32_t half) const {
-    return reinterpret_cast<float*>(base + kOffStaging + half * kStagingBytes);
+  __device__ float* staging(uint32_t quarter) const {
+    return reinterpret_cast<float*>(base + kOffStaging + quarter * kStagingBytes);
   }
   __device__ double* ys() const { return reinterpret_cast<double*>(base + kOffYs); }
   __device__ UmHead* acchdr(uint32_t a) const { return reinterpret_cast<UmHead*>(base + kOffAccHdr) + a; }
@@ -114,9 +150,8 @@ struct Smem {
   __device__ uint32_t fz(uint32_t i) const { return bar(kSlots + i); }
   __device__ uint32_t empty(uint32_t i) const { return bar(2 * kSlots + i); }
   __device__ uint32_t aready(uint32_t i) const { return bar(3 * kSlots + i); }
-  __device__ uint32_t aempty(uint32_t i) const { return bar(3 * kSlots + kA + i); }
-  __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + 2 * kA + i); }
-  __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + 2 * kA + kAcc + i); }
+  __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + kA + i); }
+  __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + kA + kAcc + i); }
   __device__ uint32_t* tmem_slot() const { return reinterpret_cast<uint32_t*>(base + kOffTmem); }
 };
 
@@ -157,10 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       mbar_init(S.fz(i), 1);
       mbar_init(S.empty(i), 1);
     }
-    for (uint32_t i = 0; i < kA; ++i) {
-      mbar_init(S.aready(i), 4);
-      mbar_init(S.aempty(i), 1);
-    }
+    for (uint32_t i = 0; i < kA; ++i) mbar_init(S.aready(i), kTrWarps);
     for (uint32_t i = 0; i < kAcc; ++i) {
       mbar_init(S.accfull(i), 2);
       mbar_init(S.accempty(i), kEpiWarps);
@@ -188,9 +220,14 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   tc_fence_after();
   const uint32_t tmem = *S.tmem_slot();
 
+  const bool pf = a.prof != 0 && lane == 0;
   if (warp == 0) {
     // ---------------- producer
+    ProfClock P(pf);
+    const long long tk0 = P.now();
     const uint32_t cb0 = a.cranges[blockIdx.x], ncb = a.cranges[blockIdx.x + 1] - cb0;
+    // L2: chunk images are read once (evict first); Z rows are read by many chunks (evict last)
+    const uint64_t pol_img = policy_evict_first(), pol_z = policy_evict_last();
     uint32_t c = 0;  // chunks issued
     bool ok = true;
     // lane 0: the slot of chunk cc is free (its previous chunk has been consumed)
@@ -199,8 +236,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     };
     // all lanes: the Z-row indices of chunk cc into the queue (one group per chunk, empty past the end)
     auto prefetch = [&](uint32_t cc) {
-      if (cc < ncb)
-        cp_async4(smem_u32(S.idxq(cc % kQ) + lane), a.zidx + (uint64_t)(cb0 + cc) * kUmKc + lane);
+      if (cc < ncb) {
+        const uint32_t* src = a.zidx + (uint64_t)(cb0 + cc) * kUmKc;
+        cp_async4(smem_u32(S.idxq(cc % kQ) + lane), src + lane);
+        cp_async4(smem_u32(S.idxq(cc % kQ) + 32 + lane), src + 32 + lane);
+      }
       cp_async_commit();
     };
     for (uint32_t i = 0; i < kLidx; ++i) prefetch(i);
@@ -240,30 +280,45 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         const uint32_t bytes = hdr + n8 * kc * 4;
         const uint32_t sl = c % kSlots;
         bool okl = true;
+        long long tp = P.now();
         if (lane == 0) okl = slot_free(c);
+        P.add(1, tp);
         ok = __shfl_sync(0xffffffffu, okl ? 1u : 0u, 0) != 0;
         if (!ok) break;
         // this chunk's indices landed (at most kLidx later groups pending)
         prefetch(c + kLidx);
+        tp = P.now();
         cp_async_wait<kLidx>();
-        const uint32_t zr = S.idxq(c % kQ)[lane];
+        P.add(2, tp);
+        const uint32_t zr0 = S.idxq(c % kQ)[lane], zr1 = S.idxq(c % kQ)[32 + lane];
         if (lane == 0) {
           S.meta(sl)->hdr = hdr;
           mbar_expect_tx(S.fimg(sl), bytes);
-          bulk_g2s(smem_u32(S.slot(sl) + kImgB - hdr), a.stream + tsrc + (uint64_t)ch * cstride, bytes,
-                   S.fimg(sl));
+          // head and b1 image, then the b2 image 128 rows after the b1 image's start
+          const unsigned char* src = a.stream + tsrc + (uint64_t)ch * cstride;
+          const uint32_t half_bytes = n8 * kc * 2;
+          bulk_g2s_hint(smem_u32(S.slot(sl) + kImgB - hdr), src, hdr + half_bytes, S.fimg(sl), pol_img);
+          bulk_g2s_hint(smem_u32(S.slot(sl) + kImgB + kUmN * kc * 2), src + hdr + half_bytes, half_bytes,
+                        S.fimg(sl), pol_img);
           mbar_expect_tx(S.fz(sl), kv * kZRowPitch);
         }
         __syncwarp();
-        // Z rows [0, kv): one bulk copy per run of consecutive rows, issued by the run's first lane
-        const uint32_t prev = __shfl_up_sync(0xffffffffu, zr, 1);
-        const bool start = lane < kv && (lane == 0 || zr != prev + 1u);
-        const uint32_t starts = __ballot_sync(0xffffffffu, start);
-        if (start) {
-          const uint32_t later = lane < 31 ? starts >> (lane + 1) : 0u;
-          const uint32_t end = later ? lane + 1 + (uint32_t)(__ffs(later) - 1) : kv;
-          bulk_g2s(smem_u32(S.zrow(sl, lane)), reinterpret_cast<const unsigned char*>(a.z) + (uint64_t)zr * kZRowPitch,
-                   (end - lane) * kZRowPitch, S.fz(sl));
+        // Z rows [0, kv): one bulk copy per run of consecutive rows (runs end at
+        // position 32 as well), issued by the run's first lane; two halves of 32
+#pragma unroll
+        for (uint32_t hf = 0; hf < 2; ++hf) {
+          const uint32_t zr = hf ? zr1 : zr0, p = 32 * hf + lane;
+          const uint32_t kvh = kv > 32 * hf ? min(32u, kv - 32 * hf) : 0u;  // valid positions of this half
+          const uint32_t prev = __shfl_up_sync(0xffffffffu, zr, 1);
+          const bool start = lane < kvh && (lane == 0 || zr != prev + 1u);
+          const uint32_t starts = __ballot_sync(0xffffffffu, start);
+          if (start) {
+            const uint32_t later = lane < 31 ? starts >> (lane + 1) : 0u;
+            const uint32_t end = later ? lane + 1 + (uint32_t)(__ffs(later) - 1) : kvh;
+            bulk_g2s_hint(smem_u32(S.zrow(sl, p)),
+                          reinterpret_cast<const unsigned char*>(a.z) + (uint64_t)zr * kZRowPitch,
+                          (end - lane) * kZRowPitch, S.fz(sl), pol_z);
+          }
         }
         ++c;
       }
@@ -290,17 +345,25 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         mbar_wait_sleep(S.fimg(i % kSlots), (i / kSlots) & 1, a.err);
         mbar_wait_sleep(S.fz(i % kSlots), (i / kSlots) & 1, a.err);
       }
+      P.add(0, tk0);
+      P.acc[3] = c;
+      P.flush(kPfProdTotal);
     }
     __syncwarp();
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
+      ProfClock P(pf);
       uint32_t c = 0;
       bool issued = false;
       while (true) {
         const uint32_t sl = c % kSlots, as = c % kA, q = c % kAcc;
+        long long tp = P.now();
         if (!wait_bar(S.aready(as), (c / kA) & 1, a.err)) break;
+        P.add(0, tp);
+        tp = P.now();
         if (c >= kAcc && !wait_bar(S.accempty(q), ((c / kAcc) - 1) & 1, a.err)) break;
+        P.add(1, tp);
         if (S.meta(sl)->hdr == 0u) {
           // forward the stop to the epilogue (both arrivals of the phase)
           volatile uint32_t* f = &S.acchdr(q)->flags;
@@ -309,135 +372,170 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           mbar_arrive(S.accfull(q));
           break;
         }
+        tp = P.now();
         if (!wait_bar(S.fimg(sl), (c / kSlots) & 1, a.err)) break;
+        P.add(2, tp);
+        tp = P.now();
         const UmHead h = *S.head(sl);
         tc_fence_after();
+        // B rows 0 .. n8-1: first parts; rows 128 .. 128 + n8 - 1: second parts
+        // (rows in between and past them are stale: their D columns are not read)
         const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
-        const uint32_t idesc = umma_idesc_f16(128, n16);
+        const uint32_t idesc = umma_idesc_f16(128, kUmN + n16);
         const uint32_t sbo = (uint32_t)h.kc * 16u;  // 8 rows x kc FP16 per core-matrix row group
         const uint32_t sa = smem_u32(S.astage(as));
-        const uint32_t sb1 = smem_u32(S.slot(sl) + kImgB);
-        const uint32_t sb2 = sb1 + (uint32_t)h.n8 * h.kc * 2u;
-        const uint32_t d = tmem + q * kUmN;
-        for (uint32_t s = 0; s < (uint32_t)h.kc / 16u; ++s) {
-          const uint64_t da = umma_desc(sa + s * 256u, 128u, 512u);
-          umma_f16(d, da, umma_desc(sb1 + s * 256u, 128u, sbo), idesc, s > 0 ? 1u : 0u);
-          umma_f16(d, da, umma_desc(sb2 + s * 256u, 128u, sbo), idesc, 1u);
-        }
+        const uint32_t sb = smem_u32(S.slot(sl) + kImgB);
+        const uint32_t d = tmem + q * kAccCols;
+        for (uint32_t s = 0; s < (uint32_t)h.kc / 16u; ++s)
+          umma_f16(d, umma_desc(sa + s * 256u, 128u, kASbo), umma_desc(sb + s * 256u, 128u, sbo), idesc,
+                   s > 0 ? 1u : 0u);
         umma_commit(S.empty(sl));
-        umma_commit(S.aempty(as));
         *S.acchdr(q) = h;
         umma_commit(S.accfull(q));
         mbar_arrive(S.accfull(q));  // publishes the head (release)
+        P.add(3, tp);
         issued = true;
         ++c;
       }
+      P.flush(kPfMmaAready);
       // the MMAs issued last have completed before the tensor memory is freed
       // (bounded, not cut short by another role's error)
-      if (issued) mbar_wait_sleep(S.aempty((c - 1) % kA), ((c - 1) / kA) & 1, a.err);
+      if (issued) mbar_wait_sleep(S.empty((c - 1) % kSlots), ((c - 1) / kSlots) & 1, a.err);
     }
     __syncwarp();
-  } else if (warp < 6) {
+  } else if (warp < kEpiWarp0) {
     // ---------------- A stages: Z rows (K x 128 FP16, row-major) -> K-major canonical
     // 8 x 8 tiles (mt, kt): rows m = 8 mt .. 8 mt + 7, K positions 8 kt .. 8 kt + 7;
     // source rows k = 8 kt + i at byte column 16 mt of the slot's Z rows,
-    // destination core matrix at mt * 512 + kt * 128 (rows 16 bytes apart).
-    // Each warp moves 16 tiles with four ldmatrix.x4.trans / stmatrix.x4 pairs
-    // (lanes 8 i .. 8 i + 7 address tile i of an instruction).
+    // destination core matrix at mt * kASbo + kt * 128 (rows 16 bytes apart).
+    // ldmatrix.x4.trans / stmatrix.x4 pairs move four tiles (lanes 8 i ..
+    // 8 i + 7 address tile i of an instruction).  A stage is
+    // free once the MMAs of its previous chunk are done: that chunk's slot
+    // release (tcgen05.commit to the slot's empty barrier).
     const uint32_t q = warp - 2;
+    ProfClock P(pf && warp == 2);
     for (uint32_t c = 0;; ++c) {
       const uint32_t sl = c % kSlots, as = c % kA;
+      long long tp = P.now();
       if (!__all_sync(0xffffffffu, wait_bar(S.fz(sl), (c / kSlots) & 1, a.err))) break;
+      P.add(0, tp);
       const bool stop = S.meta(sl)->hdr == 0u;
-      if (c >= kA && !__all_sync(0xffffffffu, wait_bar(S.aempty(as), ((c / kA) - 1) & 1, a.err))) break;
+      tp = P.now();
+      if (c >= kA) {
+        const uint32_t cp = c - kA;
+        if (!__all_sync(0xffffffffu, wait_bar(S.empty(cp % kSlots), (cp / kSlots) & 1, a.err))) break;
+      }
+      P.add(1, tp);
+      tp = P.now();
       if (!stop) {
         const uint32_t dst0 = smem_u32(S.astage(as));
+        // 128 tiles: each warp moves 64 in two batches of 8 instruction pairs, all
+        // loads of a batch before its stores (a store may alias a later load for
+        // the compiler, which would otherwise serialise each pair)
 #pragma unroll
-        for (uint32_t g = 0; g < 4; ++g) {
-          const uint32_t T = q * 16 + g * 4 + (lane >> 3);
-          const uint32_t mt = T & 15u, kt = T >> 4;
-          uint32_t r[4];
-          ldsm_x4_t(r, smem_u32(S.zrow(sl, kt * 8 + (lane & 7)) + mt * 16));
-          stsm_x4(dst0 + mt * 512u + kt * 128u + (lane & 7) * 16u, r);
+        for (uint32_t bt = 0; bt < 2; ++bt) {
+          uint32_t r[8][4];
+#pragma unroll
+          for (uint32_t g = 0; g < 8; ++g) {
+            const uint32_t T = q * 64 + bt * 32 + g * 4 + (lane >> 3);
+            const uint32_t mt = T & 15u, kt = T >> 4;
+            ldsm_x4_t(r[g], smem_u32(S.zrow(sl, kt * 8 + (lane & 7)) + mt * 16));
+          }
+#pragma unroll
+          for (uint32_t g = 0; g < 8; ++g) {
+            const uint32_t T = q * 64 + bt * 32 + g * 4 + (lane >> 3);
+            const uint32_t mt = T & 15u, kt = T >> 4;
+            stsm_x4(dst0 + mt * kASbo + kt * 128u + (lane & 7) * 16u, r[g]);
+          }
         }
         fence_proxy_async();  // generic writes -> the tensor core's (async proxy) reads
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(S.aready(as));
+      P.add(2, tp);
       if (stop) break;
     }
+    P.flush(kPfTrFz);
   } else {
     // ---------------- epilogue
     const uint32_t q = warp & 3;                  // tensor-memory lane quadrant of this warp
-    const uint32_t half = (warp - 6) >> 2;        // columns 64 half .. 64 half + 63
-    const uint32_t et = (threadIdx.x - 192) & 127;  // 0 .. 127 within the column half's warps
+    const uint32_t qr = (warp - kEpiWarp0) >> 2;  // output rows 32 qr .. 32 qr + 31 of the tile
+    const uint32_t et = (threadIdx.x - 32 * kEpiWarp0) & 127;  // 0 .. 127 within the quarter's warps
     const uint32_t j = 32 * (q & 1) + lane;       // right-hand side of this lane's row
     const bool active = j < a.pg;                 // per lane: guards only the staging writes
     const bool qactive = 32 * (q & 1) < a.pg;     // warp-uniform: the quadrant holds rows
     const bool second = q >= 2;                   // rows 64 .. 127: the second parts
-    float acc[64];
+    float acc[32];
 #pragma unroll
-    for (int c = 0; c < 64; ++c) acc[c] = 0.f;
-    float* Sg = S.staging(half);
+    for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+    float* Sg = S.staging(qr);
+    ProfClock P(pf && warp == kEpiWarp0);
     uint32_t ai = 0;
     while (true) {
       const uint32_t qa = ai % kAcc, ka = ai / kAcc;
+      long long tp = P.now();
       if (!wait_bar(S.accfull(qa), ka & 1, a.err)) break;
+      P.add(0, tp);
+      tp = P.now();
       const UmHead h = *S.acchdr(qa);
       if (h.flags & kUmStop) break;
       tc_fence_after();
-      const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
       const bool first = h.flags & kUmFirst;
       const float sc = h.scale;
-      // tcgen05.ld / wait::ld are warp-collective: warp-uniform condition only
-      if (qactive && 64 * half < n16) {
+      // tcgen05.ld / wait::ld are warp-collective: warp-uniform conditions only.
+      // Output row r of the tile: D column r (first parts of B) + column 128 + r
+      // (second parts).
+      if (qactive && 32 * qr < h.n8) {
+        const uint32_t t0 = tmem + ((32 * q) << 16) + qa * kAccCols + 32 * qr;
+        float v[32];
+        tmem_ld32(t0, v);
+        tmem_wait_ld();
 #pragma unroll
-        for (uint32_t gg = 0; gg < 2; ++gg) {
-          if (64 * half + 32 * gg < n16) {
-            float v[32];
-            tmem_ld32(tmem + ((32 * q) << 16) + qa * kUmN + 64 * half + 32 * gg, v);
-            tmem_wait_ld();
+        for (int i = 0; i < 32; ++i) acc[i] = first ? v[i] * sc : fmaf(v[i], sc, acc[i]);
+        tmem_ld32(t0 + kUmN, v);
+        tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 32; ++i)
-              acc[32 * gg + i] = first ? v[i] * sc : fmaf(v[i], sc, acc[32 * gg + i]);
-          }
-        }
+        for (int i = 0; i < 32; ++i) acc[i] = fmaf(v[i], sc, acc[i]);
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(S.accempty(qa));
       ++ai;
-      if (!(h.flags & kUmLast) || 64 * half >= h.nout) continue;
+      P.add(1, tp);
+      if (!(h.flags & kUmLast) || 32 * qr >= h.nout) continue;
+      tp = P.now();
       // ---- end of the tile: first-part rows, then second-part rows added, through the staging tile
-      const uint32_t bid = 1 + half;
+      const uint32_t bid = 1 + qr;
       named_bar(bid, 128);  // the staging tile is free
       if (active && !second) {
 #pragma unroll
-        for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] = acc[c];
+        for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] = acc[c];
       }
       named_bar(bid, 128);
       if (active && second) {
 #pragma unroll
-        for (int c = 0; c < 64; ++c) Sg[j * kSRow + c] += acc[c];
+        for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] += acc[c];
       }
       named_bar(bid, 128);
-      const uint32_t nh = min(64u, (uint32_t)h.nout - 64 * half);
-      const uint32_t row0 = h.out + 64 * half;
+      const uint32_t nh = min(32u, (uint32_t)h.nout - 32 * qr);
+      const uint32_t row0 = h.out + 32 * qr;
       if (a.mode == 1) {
-        for (uint32_t e = et; e < a.pg * 64; e += 128) {
-          const uint32_t jj = e >> 6, c = e & 63;
-          if (c < nh) {
-            double* yp = a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy;
-            *yp += a.d * S.ys()[jj] * (double)Sg[jj * kSRow + c];
-          }
+        // every Y element gets exactly one add (its row belongs to this tile
+        // only): a fire-and-forget reduction keeps the warp from waiting on
+        // the read of Y and gives the same rounding as y + v
+        for (uint32_t e = et; e < a.pg * 32; e += 128) {
+          const uint32_t jj = e >> 5, c = e & 31;
+          if (c < nh)
+            red_add_f64(a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy,
+                        a.d * S.ys()[jj] * (double)Sg[jj * kSRow + c]);
         }
       } else if (h.flags & kUmRed) {
-        for (uint32_t e = et; e < a.pg * 64; e += 128) {
+        for (uint32_t e = et; e < a.pg * 32; e += 128) {
           const uint32_t jj = e % a.pg, c = e / a.pg;
-          if (c < nh) atomicAdd(a.tacc + (uint64_t)(h.tacc + 64 * half + c) * 64 + jj, Sg[jj * kSRow + c]);
+          if (c < nh) atomicAdd(a.tacc + (uint64_t)(h.tacc + 32 * qr + c) * 64 + jj, Sg[jj * kSRow + c]);
         }
       } else {
-        for (uint32_t e = et; e < a.pg * 64; e += 128) {
+        for (uint32_t e = et; e < a.pg * 32; e += 128) {
           const uint32_t jj = e % a.pg, c = e / a.pg;
           if (c < nh) {
             __half h1, h2;
@@ -448,7 +546,9 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           }
         }
       }
+      P.add(2, tp);
     }
+    P.flush(kPfEpiAccfull);
   }
 
   tc_fence_before();
@@ -574,8 +674,8 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
                                                        uint32_t* __restrict__ zidx) {
   const UmBuild T = tiles[blockIdx.x];
   __shared__ int32_t ent[kUmN];
-  __shared__ double vals[kUmN * kUmKc];
   __shared__ double red[8];
+  static_assert(kUmKc <= kUmN, "per-position entry table");
   const bool byN = T.flags & kUmByN, contig = T.flags & kUmContig;
   const uint32_t tid = threadIdx.x;
   if (byN) {
@@ -611,11 +711,9 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
       }
       __syncthreads();
     }
-    // values of the chunk and their largest magnitude
+    // values of the chunk (recomputed in the second pass) and their largest magnitude
     const uint32_t cnt = (uint32_t)T.n8 * kc;
-    double m = 0.0;
-    for (uint32_t e = tid; e < cnt; e += blockDim.x) {
-      uint32_t nn, kk;
+    auto value = [&](uint32_t e, uint32_t& nn, uint32_t& kk) -> double {
       if (byN) {
         kk = e % kc;
         nn = e / kc;
@@ -636,8 +734,12 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
           }
         }
       }
-      vals[e] = v;
-      m = fmax(m, fabs(v));
+      return v;
+    };
+    double m = 0.0;
+    for (uint32_t e = tid; e < cnt; e += blockDim.x) {
+      uint32_t nn, kk;
+      m = fmax(m, fabs(value(e, nn, kk)));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -678,14 +780,7 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
     __half* B2 = B1 + (size_t)T.n8 * kc;
     for (uint32_t e = tid; e < cnt; e += blockDim.x) {
       uint32_t nn, kk;
-      if (byN) {
-        kk = e % kc;
-        nn = e / kc;
-      } else {
-        nn = e % T.n8;
-        kk = e / T.n8;
-      }
-      const double v = vals[e] * inv;
+      const double v = value(e, nn, kk) * inv;
       const __half h1 = __double2half(v);
       const __half h2 = __double2half(v - (double)__half2float(h1));
       const uint32_t o = (nn >> 3) * (kc * 8u) + (kk >> 3) * 64u + (nn & 7u) * 8u + (kk & 7u);  // in FP16 units
@@ -704,6 +799,7 @@ struct TimingRec {
 };
 std::mutex g_tmu;
 bool g_timing = false;
+bool g_prof = false;
 std::vector<TimingRec> g_trecs;
 
 cudaError_t launch_sweep(const KArgs& a, int kind, uint32_t grid, cudaStream_t s) {
@@ -747,6 +843,10 @@ cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const d
   a.err = pl.err;
   a.pg = pg;
   a.n = pl.n;
+  {
+    std::lock_guard<std::mutex> lk(g_tmu);
+    a.prof = g_prof ? 1u : 0u;
+  }
   if (pl.nvtiles) {
     a.tiles = pl.vtiles;
     a.ranges = pl.vranges;
@@ -1080,6 +1180,29 @@ extern "C" int ahx_um_host_product(uint64_t n, uint32_t nleaves, const uint32_t*
     info[1] = L.rtiles.size();
     info[2] = L.t_rows;
     info[3] = L.stream_bytes / 16;
+  }
+  return 0;
+}
+
+// Diagnostics hooks (not part of the drop-in interface): per-role cycle
+// counters of the tcgen05 sweeps, summed over CTAs and launches since the last
+// reset (16 words: producer total / slot waits / index waits / chunks; A-stage
+// warp fz waits / stage waits / work; MMA A waits / accumulator waits / image
+// waits / issue; epilogue accumulator waits / drains / tile ends).
+extern "C" int ahx_um_counters_enable(int enable) {
+  std::lock_guard<std::mutex> lk(ahx::g_tmu);
+  ahx::g_prof = enable != 0;
+  return 0;
+}
+
+extern "C" int ahx_um_counters(uint64_t* out16, int reset) {
+  if (cudaDeviceSynchronize() != cudaSuccess) return 2;
+  unsigned long long v[ahx::kPfCount];
+  if (cudaMemcpyFromSymbol(v, ahx::g_um_prof, sizeof(v)) != cudaSuccess) return 2;
+  for (int i = 0; i < (int)ahx::kPfCount; ++i) out16[i] = v[i];
+  if (reset) {
+    const unsigned long long z[ahx::kPfCount] = {};
+    if (cudaMemcpyToSymbol(ahx::g_um_prof, z, sizeof(z)) != cudaSuccess) return 2;
   }
   return 0;
 }

@@ -21,7 +21,7 @@
 //
 // Precision (the FP32 storage of this library, about 22 significant bits):
 // every stored value v is kept as two FP16 numbers, b1 = fp16(v / s) and
-// b2 = fp16(v / s - b1), with s a power of two per chunk of 32 K positions
+// b2 = fp16(v / s - b1), with s a power of two per chunk of 64 K positions
 // (the chunk's largest |v| / s lies in [2^13, 2^14)).  Z rows (X rows and T
 // rows) hold each of 64 right-hand-side slots the same way: 64 first parts,
 // then 64 second parts (256 bytes per row, rows kUmZPitch bytes apart); A's row
@@ -35,7 +35,7 @@
 // ||V_t||_1 s_t <= 1 and the matching U column by 1 / s_t, so that every T
 // row stays below 2^14 and no FP16 value overflows.
 //
-// Stream of each sweep: per tile, chunks of <= 32 K positions; each chunk
+// Stream of each sweep: per tile, chunks of <= 64 K positions; each chunk
 // image is [UmHead (32 B)] [b1 image] [b2 image], the images in the tensor
 // core's K-major, no-swizzle
 // canonical layout of 16-bit elements: core matrices of 8 rows x 16 bytes
@@ -43,7 +43,7 @@
 //     (n / 8) * (kc * 16) + (k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2
 // (leading-dimension byte offset 128, stride byte offset kc * 16; kc a
 // multiple of 16).  One bulk copy moves a chunk image into the kernel's ring.
-// The Z rows of every chunk (32 row indices per chunk, in chunk order, the
+// The Z rows of every chunk (64 row indices per chunk, in chunk order, the
 // positions past the chunk's K unused) are a separate array, so that the
 // kernel can fetch them well ahead of the images.
 #pragma once
@@ -56,7 +56,7 @@
 
 namespace ahx {
 
-constexpr uint32_t kUmKc = 32;    // K positions per chunk
+constexpr uint32_t kUmKc = 64;    // K positions per chunk
 constexpr uint32_t kUmN = 128;    // rows (N) per tile
 constexpr uint32_t kUmIdxBytes = kUmKc * 4;
 constexpr uint32_t kUmSlots = 64;           // right-hand-side slots of a Z row
@@ -74,7 +74,7 @@ enum UmFlags : uint32_t {
 
 struct UmHead {
   uint32_t zsrc;      // contiguous tiles: Z row of the chunk's k = 0
-  uint16_t kc;        // K of the chunk images (multiple of 16, <= 32)
+  uint16_t kc;        // K of the chunk images (multiple of 16, <= 64)
   uint16_t kvalid;    // positions >= kvalid are zero
   uint16_t n8;        // rows of the images (multiple of 8, <= 128)
   uint16_t nout;      // output rows of the tile (<= 128)
@@ -168,7 +168,7 @@ struct UmPlan {
   const uint32_t* rranges = nullptr;
   const uint32_t* vcranges = nullptr;  // per CTA: first chunk (grid + 1 entries)
   const uint32_t* rcranges = nullptr;
-  const uint32_t* vzidx = nullptr;     // Z-row indices, 32 per chunk
+  const uint32_t* vzidx = nullptr;     // Z-row indices, kUmKc per chunk
   const uint32_t* rzidx = nullptr;
   uint32_t grid = 0;
   uint32_t nvtiles = 0, nrtiles = 0;
