@@ -448,9 +448,12 @@ def run_product(args):
     ms = e0.elapsed_time(e1) / args.steps
     b = algorithmic_bytes(H, args.precision, args.rhs)
     sym = "-sym" if args.symmetric else ""
-    print(json.dumps({"workload": f"laplace-{args.geometry}-{n}-{args.rhs}rhs-{args.precision}{sym}", "ms": ms,
-                      "algorithmic_bytes": b, "achieved_gbs": b / (ms * 1e-3) / 1e9, "assembly_s": t_asm,
-                      "fp64_leaf_bytes": int(H.storage_bytes("fp64"))}))
+    out = {"workload": f"laplace-{args.geometry}-{n}-{args.rhs}rhs-{args.precision}{sym}", "ms": ms,
+           "algorithmic_bytes": b, "achieved_gbs": b / (ms * 1e-3) / 1e9, "assembly_s": t_asm,
+           "fp64_leaf_bytes": int(H.storage_bytes("fp64"))}
+    if args.precision == "fp32" and not args.symmetric:
+        out["sweep_bytes"] = _kernel_bytes(H, args.rhs)
+    print(json.dumps(out))
 
 
 def run_predictor(args):
@@ -1085,10 +1088,12 @@ def run_headline(args):
     torch.cuda.synchronize()
     errb = float(((Yb - Y64).norm(dim=1) / Y64.norm(dim=1)).max())
     del Yb, Y64, Y
-    # GMRES(50) to 1e-8: mixed (BF16/FP32 inner solves, FP64 refinement) and plain FP64, 3 solves each
+    # GMRES(50) to 1e-8: mixed (inner solves on the FP32-class tcgen05 product or on
+    # BF16 factors, FP64 refinement) and plain FP64, 3 solves each
     B = torch.from_numpy(np.random.default_rng(6).standard_normal((p, n))).to(dev)
     gm = {}
-    for prec in ("bf16", "fp64"):
+    H.prepare("fp32")
+    for prec in ("fp32", "bf16", "fp64"):
         runs = []
         for _ in range(args.gmres_solves):
             Xs = torch.zeros_like(B)
@@ -1107,8 +1112,10 @@ def run_headline(args):
         med = secs[len(secs) // 2]
         ok = all(r["converged"] and r["true_max_resid"] <= 1e-8 for r in runs)
         gm[prec] = {"median_s": med, "solves_per_s": (p / med) if ok else None, "runs": runs}
+    if gm["fp32"]["solves_per_s"] and gm["fp64"]["solves_per_s"]:
+        gm["mixed_over_plain"] = gm["fp32"]["solves_per_s"] / gm["fp64"]["solves_per_s"]
     if gm["bf16"]["solves_per_s"] and gm["fp64"]["solves_per_s"]:
-        gm["mixed_over_plain"] = gm["bf16"]["solves_per_s"] / gm["fp64"]["solves_per_s"]
+        gm["mixed_bf16_over_plain"] = gm["bf16"]["solves_per_s"] / gm["fp64"]["solves_per_s"]
     peak, peak_kind = _peaks()
     kb = _kernel_bytes(H, p)
     total_alg = H.storage_bytes("fp64") // 2 + p * n * 24  # FP32 payload + X read + Y read and written
@@ -1137,8 +1144,12 @@ def run_headline(args):
                 "d2h_bytes_per_step": p * n * 8},
         "gpu_launches": launches.get("fp32"),
         "clocks": clocks,
-        "gmres": {"mixed_bf16_solves_per_s": gm["bf16"]["solves_per_s"], "plain_fp64_solves_per_s":
-                  gm["fp64"]["solves_per_s"], "mixed_over_plain": gm.get("mixed_over_plain"), "detail": gm},
+        "gmres": {"mixed_fp32_solves_per_s": gm["fp32"]["solves_per_s"],
+                  "mixed_bf16_solves_per_s": gm["bf16"]["solves_per_s"], "plain_fp64_solves_per_s":
+                  gm["fp64"]["solves_per_s"], "mixed_over_plain": gm.get("mixed_over_plain"),
+                  "mixed_bf16_over_plain": gm.get("mixed_bf16_over_plain"),
+                  "restart": 50, "tol": 1e-8, "diag": "h = smallest nearest-neighbour distance / 2",
+                  "detail": gm},
         "details": {"tree_s": t_tree, "assembly_s": t_asm, "leaves": int(H.nleaves),
                     "lowrank_leaves": int((ranks >= 0).sum()), "avg_rank": float(ranks[ranks >= 0].mean()),
                     "fp64_leaf_bytes": int(H.storage_bytes("fp64")), "fp32_prepare_s": t_prep32,
