@@ -68,7 +68,7 @@ constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
 constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
 constexpr uint32_t kOffIdxQ = kOffMeta + kSlots * 16;     // index queue: kQ x 32 words
 constexpr uint32_t kOffBar = kOffIdxQ + kQ * kUmKc * 4;
-constexpr uint32_t kNumBars = 3 * kSlots + kA + 2 * kAcc;
+constexpr uint32_t kNumBars = 3 * kSlots + kA + 2 * kAcc + 4;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
 constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;     // + alignment slack of the dynamic base
 constexpr uint32_t kThreads = 640;
@@ -152,6 +152,7 @@ struct Smem {
   __device__ uint32_t aready(uint32_t i) const { return bar(3 * kSlots + i); }
   __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + kA + i); }
   __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + kA + kAcc + i); }
+  __device__ uint32_t quarter(uint32_t i) const { return bar(3 * kSlots + kA + 2 * kAcc + i); }
   __device__ uint32_t* tmem_slot() const { return reinterpret_cast<uint32_t*>(base + kOffTmem); }
 };
 
@@ -193,6 +194,7 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       mbar_init(S.empty(i), 1);
     }
     for (uint32_t i = 0; i < kA; ++i) mbar_init(S.aready(i), kTrWarps);
+    for (uint32_t i = 0; i < 4; ++i) mbar_init(S.quarter(i), 4);
     for (uint32_t i = 0; i < kAcc; ++i) {
       mbar_init(S.accfull(i), 2);
       mbar_init(S.accempty(i), kEpiWarps);
@@ -469,6 +471,16 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
 #pragma unroll
     for (int c = 0; c < 32; ++c) acc[c] = 0.f;
     float* Sg = S.staging(qr);
+    // the quarter's four warps meet on an mbarrier with bounded waits (no
+    // warp can be left waiting after another gave up on a failed wait)
+    uint32_t quses = 0;
+    auto qsync = [&]() -> bool {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(S.quarter(qr));
+      const bool ok = __all_sync(0xffffffffu, wait_bar(S.quarter(qr), quses & 1, a.err));
+      ++quses;
+      return ok;
+    };
     ProfClock P(pf && warp == kEpiWarp0);
     uint32_t ai = 0;
     while (true) {
@@ -505,18 +517,17 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       if (!(h.flags & kUmLast) || 32 * qr >= h.nout) continue;
       tp = P.now();
       // ---- end of the tile: first-part rows, then second-part rows added, through the staging tile
-      const uint32_t bid = 1 + qr;
-      named_bar(bid, 128);  // the staging tile is free
+      if (!qsync()) break;  // the staging tile is free
       if (active && !second) {
 #pragma unroll
         for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] = acc[c];
       }
-      named_bar(bid, 128);
+      if (!qsync()) break;
       if (active && second) {
 #pragma unroll
         for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] += acc[c];
       }
-      named_bar(bid, 128);
+      if (!qsync()) break;
       const uint32_t nh = min(32u, (uint32_t)h.nout - 32 * qr);
       const uint32_t row0 = h.out + 32 * qr;
       if (a.mode == 1) {
