@@ -11,13 +11,14 @@
 // compacted like fill_gaps_ (H/agglH.cpp:185-211).  The leaf arena is
 // rewritten in leaf order.
 //
-// A dense son D enters the union in factored form D I^T (its columns as U, an
+// A dense son D enters a union in factored form D I^T (its columns as U, an
 // identity as V), so that every union is one QR + SVD recompression of
 // [U_cat][V_cat]^T; the reference forms the dense block and takes its SVD
 // (mblock::unify_cols, H/mblock_D.cpp:804-860) with the same truncation rule.
-// The reference unifies the sons pairwise (columns, then rows) and truncates
-// after each step; this one-shot union truncates once.  Unions wider than
-// kMaxUnion columns are not formed.
+// As in the reference, the sons are united pairwise: the two sons of each
+// block row first (unify_cols), then the two truncated block rows (unify_rows),
+// with a truncation after each step.  Unions wider than kMaxUnion columns are
+// not formed.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -218,75 +219,138 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
       std::stable_sort(todo.begin(), todo.end(), [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
       size_t at = 0;
       while (at < todo.size()) {
-        std::vector<MergeTask> tasks;
-        std::vector<Seg2D> segs;
+        // Pairwise unions as the reference's unify_sons_ (H/agglH.cpp:40-86):
+        // phase A unites the sons of each block row (unify_cols: [U0 U1],
+        // diag(V0, V1), a dense son as (D, I)) and truncates; phase B unites the
+        // two truncated block rows (unify_rows: diag(U_top, U_bot), [V_top V_bot])
+        // and truncates again.  Both phases run as batches of merge tasks.
+        std::vector<MergeTask> tasksA, tasksB;
+        std::vector<Seg2D> segsA;
         std::vector<int32_t> which;
-        uint64_t wsz = 0, zsz = 0;
+        std::vector<int32_t> pairA[2];  // per candidate: its phase-A task (-1: empty pair)
+        uint64_t wszA = 0, zszA = 0, wszB = 0, zszB = 0;
+        const uint32_t e32 = (uint32_t)ew;
         for (; at < todo.size(); ++at) {
           const BNode& q = N[todo[at]];
-          const uint32_t k = union_width(q);
-          const bool all_dense = dense_sons(q);
-          kmax_round = std::max<uint64_t>(kmax_round, k);
-          const uint64_t need = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
-          if (!tasks.empty() && (wsz + need) * ew * sizeof(double) > budget) break;
-          MergeTask t{q.n1, q.n2, k, 0u, wsz, zsz};
-          // U = [U00 U01 0 0; 0 0 U10 U11], V = [V00 0 V10 0; 0 V01 0 V11]; a dense
-          // son contributes (D, I).  Four dense sons: U = the parent block, V = I (n2
-          // columns instead of 2 n2).
-          const uint32_t e32 = (uint32_t)ew;
-          if (all_dense) {
-            for (int s = 0; s < 4; ++s) {
-              const BNode& c = N[q.son[s]];
-              const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
-              segs.push_back(Seg2D{off[c.leaf] * ew, (wsz + (uint64_t)co * q.n1 + ro) * ew, c.n1 * e32, c.n2,
-                                   q.n1 * e32, 0u});
+          uint32_t kp[2] = {0, 0};
+          for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j) {
+              const BNode& c = N[q.son[2 * i + j]];
+              kp[i] += rank[c.leaf] < 0 ? c.n2 : (uint32_t)rank[c.leaf];
             }
-            segs.push_back(Seg2D{kSegIdentity, (wsz + (uint64_t)q.n1 * k) * ew, q.n2, q.n2, q.n2 * e32,
-                                 cplx ? 1u : 0u});
+          const uint32_t m0 = N[q.son[0]].n1, m1 = N[q.son[2]].n1;
+          const uint64_t needA = aca_ws_doubles(m0, q.n2, std::max(kp[0], 1u)) + merge_qrcp_doubles(kp[0]) +
+                                 aca_ws_doubles(m1, q.n2, std::max(kp[1], 1u)) + merge_qrcp_doubles(kp[1]);
+          const uint32_t kb = std::min(kp[0] + kp[1], 2 * max_rank);
+          const uint64_t needB = aca_ws_doubles(q.n1, q.n2, std::max(kb, 1u)) + merge_qrcp_doubles(kb);
+          if (!which.empty() && (wszA + needA + wszB + needB) * ew * sizeof(double) > budget) break;
+          kmax_round = std::max<uint64_t>(kmax_round, std::max(kp[0], kp[1]));
+          for (int i = 0; i < 2; ++i) {
+            if (kp[i] == 0) {
+              pairA[i].push_back(-1);
+              continue;
+            }
+            const uint32_t m = i ? m1 : m0, k = kp[i];
+            const uint32_t rb = N[q.son[2 * i]].b1;  // first row of this block row
+            MergeTask t{m, q.n2, k, 0u, wszA, zszA};
+            uint32_t col = 0;
+            for (int j = 0; j < 2; ++j) {
+              const BNode& c = N[q.son[2 * i + j]];
+              const bool dense = rank[c.leaf] < 0;
+              const uint32_t kc = dense ? c.n2 : (uint32_t)rank[c.leaf];
+              if (kc == 0) continue;
+              const uint32_t ro = c.b1 - rb, co = c.b2 - q.b2;
+              const uint64_t o = off[c.leaf];
+              const uint64_t vdst = wszA + (uint64_t)m * k + (uint64_t)col * q.n2 + co;
+              segsA.push_back(Seg2D{o * ew, (wszA + (uint64_t)col * m + ro) * ew, c.n1 * e32, kc, m * e32, 0u});
+              if (dense) segsA.push_back(Seg2D{kSegIdentity, vdst * ew, kc, kc, q.n2 * e32, cplx ? 1u : 0u});
+              else segsA.push_back(Seg2D{(o + (uint64_t)c.n1 * kc) * ew, vdst * ew, c.n2 * e32, kc, q.n2 * e32, 0u});
+              col += kc;
+            }
+            pairA[i].push_back((int32_t)tasksA.size());
+            tasksA.push_back(t);
+            wszA += aca_ws_doubles(m, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
+            zszA += m + q.n2 + 1;
           }
-          uint32_t col = 0;
-          for (int s = 0; s < 4 && !all_dense; ++s) {
-            const BNode& c = N[q.son[s]];
-            const bool dense = rank[c.leaf] < 0;
-            const uint32_t kc = dense ? c.n2 : (uint32_t)rank[c.leaf];
-            if (kc == 0) continue;
-            const uint32_t ro = c.b1 - q.b1, co = c.b2 - q.b2;
-            const uint64_t o = off[c.leaf];
-            const uint64_t vdst = wsz + (uint64_t)q.n1 * k + (uint64_t)col * q.n2 + co;
-            segs.push_back(Seg2D{o * ew, (wsz + (uint64_t)col * q.n1 + ro) * ew, c.n1 * e32, kc, q.n1 * e32, 0u});
-            if (dense) segs.push_back(Seg2D{kSegIdentity, vdst * ew, kc, kc, q.n2 * e32, cplx ? 1u : 0u});
-            else segs.push_back(Seg2D{(o + (uint64_t)c.n1 * kc) * ew, vdst * ew, c.n2 * e32, kc, q.n2 * e32, 0u});
-            col += kc;
-          }
-          tasks.push_back(t);
           which.push_back(todo[at]);
-          wsz += need;
-          zsz += q.n1 + q.n2 + 1;
+          wszB += needB;
+          zszB += q.n1 + q.n2 + 1;
         }
-        if ((rc = ws.reserve(std::max<uint64_t>(wsz, 1) * ew * sizeof(double)))) return rc;
-        if ((rc = zs.reserve(std::max<uint64_t>(zsz, 1) * sizeof(int)))) return rc;
-        AHX_CUDA(cudaMemsetAsync(ws.p, 0, wsz * ew * sizeof(double), H->stream));
-        if ((rc = upload(dsegs, segs, H->stream))) return rc;
-        AHX_CUDA(launch_copy2d(dsegs.as<Seg2D>(), (uint32_t)segs.size(), arena(), ws.as<double>(), H->stream));
-        if ((rc = upload(dtasks, tasks, H->stream))) return rc;
-        if ((rc = dres.reserve(tasks.size() * sizeof(AcaResult)))) return rc;
-        MergeParams p;
-        p.tasks = dtasks.as<MergeTask>();
-        p.ntasks = (uint32_t)tasks.size();
-        p.ws = ws.as<double>();
-        p.zs = zs.as<int>();
-        p.eps = eps;
-        p.res = dres.as<AcaResult>();
-        AHX_CUDA(cplx ? launch_zmerge(p, H->stream) : launch_merge(p, large == 1, H->stream));
-        std::vector<AcaResult> res(tasks.size());
-        AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, res.size() * sizeof(AcaResult), cudaMemcpyDeviceToHost,
-                                 H->stream));
-        AHX_CUDA(cudaStreamSynchronize(H->stream));
+        auto run_merge = [&](ScopedBuf& w, uint64_t wsz, uint64_t zsz, std::vector<MergeTask>& tasks,
+                             std::vector<Seg2D>& segs, const double* src,
+                             std::vector<AcaResult>& res) -> int {
+          res.assign(tasks.size(), AcaResult{});
+          if (tasks.empty()) return AHX_OK;
+          int r;
+          if ((r = w.reserve(std::max<uint64_t>(wsz, 1) * ew * sizeof(double)))) return r;
+          if ((r = zs.reserve(std::max<uint64_t>(zsz, 1) * sizeof(int)))) return r;
+          AHX_CUDA(cudaMemsetAsync(w.p, 0, wsz * ew * sizeof(double), H->stream));
+          if ((r = upload(dsegs, segs, H->stream))) return r;
+          AHX_CUDA(launch_copy2d(dsegs.as<Seg2D>(), (uint32_t)segs.size(), src, w.as<double>(), H->stream));
+          if ((r = upload(dtasks, tasks, H->stream))) return r;
+          if ((r = dres.reserve(tasks.size() * sizeof(AcaResult)))) return r;
+          MergeParams p;
+          p.tasks = dtasks.as<MergeTask>();
+          p.ntasks = (uint32_t)tasks.size();
+          p.ws = w.as<double>();
+          p.zs = zs.as<int>();
+          p.eps = eps;
+          p.res = dres.as<AcaResult>();
+          AHX_CUDA(cplx ? launch_zmerge(p, H->stream) : launch_merge(p, large == 1, H->stream));
+          AHX_CUDA(cudaMemcpyAsync(res.data(), dres.p, res.size() * sizeof(AcaResult), cudaMemcpyDeviceToHost,
+                                   H->stream));
+          AHX_CUDA(cudaStreamSynchronize(H->stream));
+          return AHX_OK;
+        };
+        std::vector<AcaResult> resA, resB;
+        if ((rc = run_merge(ws, wszA, zszA, tasksA, segsA, arena(), resA))) return rc;
+        // phase B: gather the truncated block rows (first kt columns of Un, Vn)
+        std::vector<Seg2D> segsB;
+        std::vector<int32_t> taskB(which.size(), -1);
+        uint64_t offB = 0;
+        for (size_t w = 0; w < which.size(); ++w) {
+          const BNode& q = N[which[w]];
+          uint32_t kt[2] = {0, 0};
+          for (int i = 0; i < 2; ++i)
+            if (pairA[i][w] >= 0) kt[i] = std::min(resA[pairA[i][w]].kt, max_rank);
+          const uint32_t k = kt[0] + kt[1];
+          const uint64_t needB = aca_ws_doubles(q.n1, q.n2, std::max(k, 1u)) + merge_qrcp_doubles(k);
+          if (k > 0) {
+            MergeTask t{q.n1, q.n2, k, 0u, offB, 0u};
+            uint32_t col = 0;
+            for (int i = 0; i < 2; ++i) {
+              if (kt[i] == 0) continue;
+              const MergeTask& ta = tasksA[pairA[i][w]];
+              const uint64_t un = ta.ws + (uint64_t)(ta.m + ta.n) * ta.k;  // Un (m x k), then Vn (n x k)
+              const uint64_t vn = un + (uint64_t)ta.m * ta.k;
+              const uint32_t ro = i ? N[q.son[0]].n1 : 0u;
+              segsB.push_back(Seg2D{un * ew, (offB + (uint64_t)col * q.n1 + ro) * ew, ta.m * e32, kt[i],
+                                    q.n1 * e32, 0u});
+              segsB.push_back(Seg2D{vn * ew, (offB + (uint64_t)q.n1 * k + (uint64_t)col * q.n2) * ew,
+                                    q.n2 * e32, kt[i], q.n2 * e32, 0u});
+              col += kt[i];
+            }
+            taskB[w] = (int32_t)tasksB.size();
+            tasksB.push_back(t);
+          }
+          offB += needB;
+        }
+        // zs offsets of phase B
+        {
+          uint64_t z = 0;
+          for (MergeTask& t : tasksB) {
+            t.zs = z;
+            z += t.m + t.n + 1;
+          }
+          zszB = z;
+        }
+        ScopedBuf wsB;
+        if ((rc = run_merge(wsB, offB, zszB, tasksB, segsB, ws.as<double>(), resB))) return rc;
         std::vector<CopyTask> copies;
-        for (size_t q = 0; q < tasks.size(); ++q) {
-          BNode& nd = N[which[q]];
+        for (size_t w = 0; w < which.size(); ++w) {
+          BNode& nd = N[which[w]];
           nd.decided = true;
-          const uint32_t kt = std::min(res[q].kt, max_rank);
+          const uint32_t kt = taskB[w] >= 0 ? std::min(resB[taskB[w]].kt, max_rank) : 0u;
           uint64_t pre = 0;
           for (int s = 0; s < 4; ++s) pre += size_of(N[nd.son[s]].leaf);
           const uint64_t post = (uint64_t)kt * (nd.n1 + nd.n2);
@@ -296,20 +360,19 @@ int agglomerate_impl(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerg
           uint64_t dst = 0;
           if (post && (rc = cplx ? zarena_append(H, post, dst) : arena_append(H, post, dst))) return rc;
           if (post) {
-            const MergeTask& t = tasks[q];
+            const MergeTask& t = tasksB[taskB[w]];
             const uint64_t un = t.ws + (uint64_t)(t.m + t.n) * t.k;  // Un follows U and V
-            const uint32_t e32 = (uint32_t)ew;
             copies.push_back(CopyTask{un * ew, (un + (uint64_t)t.m * t.k) * ew, dst * ew, t.m * e32, t.n * e32, kt, 0u});
           }
           rank[first] = (int32_t)kt;
           off[first] = dst;
-          leaf_node[first] = which[q];
+          leaf_node[first] = which[w];
           nd.leaf = first;
           ++merged;
         }
         if (!copies.empty()) {
           if ((rc = upload(dcopy, copies, H->stream))) return rc;
-          AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), ws.as<double>(), arena(),
+          AHX_CUDA(launch_copy_factors(dcopy.as<CopyTask>(), (uint32_t)copies.size(), wsB.as<double>(), arena(),
                                        H->stream));
           AHX_CUDA(cudaStreamSynchronize(H->stream));
         }

@@ -160,10 +160,10 @@ int ahx_helm_gmres(ahx_hmat* H, int precision, uint32_t p, const double* B, uint
  * Include/matgen_sqntl.h:32-55): bottom up, a non-diagonal block whose sons are all
  * leaves becomes one low-rank leaf when the recompressed union (relative threshold
  * eps, rank <= max_rank; unify_sons_, H/agglH.cpp:14-107) stores no more; leaf
- * indices are then compacted as fill_gaps does.  Dense sons enter the union in
- * factored form (D times the identity), and a union of dense sons only is
- * recompressed as the parent block itself.  Once per assembly.  nmerged (may be
- * NULL): blocks merged. */
+ * indices are then compacted as fill_gaps does.  As in the reference, the two
+ * sons of each block row are united first and truncated, then the two block
+ * rows.  Dense sons enter the unions in factored form (D times the identity).
+ * Once per assembly.  nmerged (may be NULL): blocks merged. */
 int ahx_agglomerate(ahx_hmat* H, double eps, uint32_t max_rank, uint32_t* nmerged);
 /* The same for the Helmholtz leaves (agglH with T = dcomp, H/agglH.cpp:291-305).
  * Agglomeration changes the block tree: the handle's other kind of leaves (real
