@@ -66,7 +66,8 @@ constexpr uint32_t kStagingBytes = 64 * kSRow * 4;        // per quarter of the 
 constexpr uint32_t kOffYs = kOffStaging + 4 * kStagingBytes;   // 64 doubles: Y factor per right-hand side
 constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
 constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
-constexpr uint32_t kOffIdxQ = kOffMeta + kSlots * 16;     // index queue: kQ x 32 words
+constexpr uint32_t kOffIssue = kOffMeta + kSlots * 16;    // per slot: clock of the copies' issue (diagnostics)
+constexpr uint32_t kOffIdxQ = kOffIssue + kSlots * 8;     // index queue: kQ x kUmKc words
 constexpr uint32_t kOffBar = kOffIdxQ + kQ * kUmKc * 4;
 constexpr uint32_t kNumBars = 3 * kSlots + kA + 2 * kAcc + 4;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
@@ -111,7 +112,7 @@ struct KArgs {
 // over CTAs, lane 0 of warps 0 (producer), 1 (MMA), 2 (A stages), 6 (epilogue).
 enum UmProf : uint32_t {
   kPfProdTotal, kPfProdSlot, kPfProdIdx, kPfChunks,
-  kPfTrFz, kPfTrAempty, kPfTrWork, kPfPad7,
+  kPfTrFz, kPfTrAempty, kPfTrWork, kPfZLatency,
   kPfMmaAready, kPfMmaAccempty, kPfMmaImg, kPfMmaIssue,
   kPfEpiAccfull, kPfEpiDrain, kPfEpiTile, kPfKernel,
   kPfCount = 16
@@ -137,6 +138,9 @@ struct Smem {
   __device__ unsigned char* slot(uint32_t i) const { return base + i * kSlotBytes; }
   __device__ const UmHead* head(uint32_t i) const { return reinterpret_cast<const UmHead*>(slot(i) + kImgHead); }
   __device__ uint32_t* idxq(uint32_t i) const { return reinterpret_cast<uint32_t*>(base + kOffIdxQ) + i * kUmKc; }
+  __device__ volatile long long* issued(uint32_t i) const {
+    return reinterpret_cast<volatile long long*>(base + kOffIssue) + i;
+  }
   __device__ unsigned char* zrow(uint32_t i, uint32_t k) const { return slot(i) + kZOff + k * kZRowPitch; }
   __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + i * kAStage; }
   __device__ float* staging(uint32_t quarter) const {
@@ -294,6 +298,7 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         P.add(2, tp);
         const uint32_t zr0 = S.idxq(c % kQ)[lane], zr1 = S.idxq(c % kQ)[32 + lane];
         if (lane == 0) {
+          if (pf) *S.issued(sl) = clock64();
           S.meta(sl)->hdr = hdr;
           mbar_expect_tx(S.fimg(sl), bytes);
           // head and b1 image, then the b2 image 128 rows after the b1 image's start
@@ -422,6 +427,7 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       if (!__all_sync(0xffffffffu, wait_bar(S.fz(sl), (c / kSlots) & 1, a.err))) break;
       P.add(0, tp);
       const bool stop = S.meta(sl)->hdr == 0u;
+      if (P.on && !stop) P.acc[3] += (unsigned long long)(clock64() - *S.issued(sl));  // issue -> Z landed
       tp = P.now();
       if (c >= kA) {
         const uint32_t cp = c - kA;
