@@ -714,7 +714,8 @@ def run_batch(args):
     in [2048, 32768] (numpy PCG64 seed 2), geometry uniform among the unit sphere, the
     ellipsoid (1, 0.5, 0.25) and the unit-cube surface with uniform random surface points;
     leaf 32, eta 0.8, ACA eps 1e-6; one right-hand side per instance b ~ N(0, 1) (seed 3);
-    GMRES(30) to 1e-8 with BF16/FP32 leaves and FP64 refinement, against plain FP64."""
+    GMRES(30) to 1e-8 with BF16 and with FP32-class leaves and FP64 refinement, against
+    plain FP64."""
     import torch
     import ahmed_gb300 as A
 
@@ -745,7 +746,7 @@ def run_batch(args):
            "fp64_arena_bytes": int(sum(H.storage_bytes("fp64") for H in mats))}
     b = np.random.default_rng(3).standard_normal(ntot)
     peak, _ = _peaks()
-    for prec in ("bf16", "fp64"):
+    for prec in ("bf16", "fp32", "fp64"):
         Bt = A.HBatch(mats, precision=prec)
         if prec != "fp64":
             Bt.prepare("df64")   # refinement residual copy, built with the streams (setup)
@@ -769,7 +770,9 @@ def run_batch(args):
                      "max_resid": float(rr.max()), "solves_per_s": k / dt}
         Bt.close()
     out["bf16"]["product_over_fp64"] = out["fp64"]["product_ms"] / out["bf16"]["product_ms"]
+    out["fp32"]["product_over_fp64"] = out["fp64"]["product_ms"] / out["fp32"]["product_ms"]
     out["gmres_mixed_over_plain"] = out["fp64"]["gmres_s"] / out["bf16"]["gmres_s"]
+    out["gmres_mixed_fp32_over_plain"] = out["fp64"]["gmres_s"] / out["fp32"]["gmres_s"]
     print(json.dumps(out))
 
 
