@@ -777,13 +777,13 @@ int gmres_driver(Operator& op, int prec, uint32_t p, const double* B, double* X,
       std::vector<double> res2(nsys, 0.0);
       const uint32_t budget = std::min(m, maxit - used);
       // the inner solve reduces r (relative to itself) only as far as the outer
-      // tolerance still needs, with a margin (0.3), and not below what the
+      // tolerance still needs, with a margin (0.5), and not below what the
       // storage precision's product supports: a later outer step does not
       // solve to the floor again
       double rmax = 0.0;
       for (uint32_t q = 0; q < nsys; ++q)
         if (!done[q]) rmax = std::max(rmax, resid[q]);
-      const double need = rmax > 0.0 ? 0.3 * tol / rmax : 1.0;
+      const double need = rmax > 0.0 ? 0.5 * tol / rmax : 1.0;
       const double itol = std::min(0.5, std::max(inner_prec == resid_prec ? 1e-12 : inner_tol, need));
       if ((rc = gmres_core(sv, inner_prec, rr.as<double>(), z.as<double>(), itol, m, budget, it2, res2, idone,
                            vbuf, rbuf, &graphs[inner_prec])))

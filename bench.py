@@ -822,11 +822,26 @@ def run_kernels(args):
     Hh = A.HMatrix(P, "bbx", bmin=BMIN, eta=ETA)
     Hh.assemble_hinted(h, EPS, np.where(lv[:, 4] == 1, pred, -1.0))
     Hh.close()
+    # the allocation-free ACA of one admissible block (points in cluster order on the device)
+    import ctypes as _C
+    from ahmed_gb300 import _capi
+    op, _ = H.perm()
+    pts = [torch.from_numpy(np.ascontiguousarray(P[op][:, i])).to(dev) for i in range(3)]
+    adm = np.nonzero((lv[:, 4] == 1) & (lv[:, 1].astype(np.int64) + lv[:, 3] <= 2048))[0]  # fits its 8 MiB scratch
+    b1, n1, b2, n2, _, _, i0 = (int(v) for v in lv[adm[len(adm) // 2]][:7])
+    Ub = torch.zeros(n1 * 32, dtype=torch.float64, device=dev)
+    Vb = torch.zeros(n2 * 32, dtype=torch.float64, device=dev)
+    info = torch.zeros(3, dtype=torch.int32, device=dev)
+    _capi.check(_capi.lib().ahx_aca_block_noalloc(
+        _C.c_void_p(pts[0].data_ptr()), _C.c_void_p(pts[1].data_ptr()), _C.c_void_p(pts[2].data_ptr()),
+        b1, n1, b2, n2, i0, h, EPS, 32, _C.c_void_p(Ub.data_ptr()), _C.c_void_p(Vb.data_ptr()),
+        _C.c_void_p(info.data_ptr()), None))
     Psym = G.fibonacci_sphere(16384)
     Hy = A.HMatrix(Psym, "bbx", bmin=BMIN, eta=ETA, symmetric=True)
     Hy.matgenGeH_omp(A.mean_nn(Psym), EPS)
     Xs = torch.from_numpy(rng.uniform(-1.0, 1.0, (16, Hy.n))).to(dev)
     Hy.mltaGeHVec(1.0, Xs, torch.zeros_like(Xs))
+    Hy.mltaGeHVec(1.0, Xs, torch.zeros_like(Xs), precision="fp32")  # mirror images for the streams
     Hy.close()
     Pa = G.fibonacci_sphere(4096)
     Ha = A.HMatrix(Pa, "bbx", bmin=BMIN, eta=ETA)
@@ -845,6 +860,8 @@ def run_kernels(args):
         Xz = torch.from_numpy(rng.standard_normal((p, Hz.n)) + 1j * rng.standard_normal((p, Hz.n))).to(dev)
         for prec in ("fp64", "fp32"):
             Hz.mltaGeHVec(1.0, Xz, torch.zeros_like(Xz), precision=prec)
+    xz1 = rng.standard_normal(Hz.n) + 1j * rng.standard_normal(Hz.n)
+    Hz.mltaGeHhVec(1.0, xz1, np.zeros_like(xz1))  # the adjoint
     mats = []
     for i, m in enumerate((2048, 3000, 5000, 8000)):
         Pm = G.sphere_surface(m, 100 + i)
@@ -866,6 +883,7 @@ def run_kernels(args):
     Hs.close()
     zb = np.random.default_rng(12).standard_normal(Hz.n) + 1j * np.random.default_rng(13).standard_normal(Hz.n)
     Hz.GMRes(zb, np.zeros_like(zb), 1e-8, 30, 20)
+    Hz.GMRes(zb, np.zeros_like(zb), 1e-8, 30, 20, precision="fp32")  # complex refinement
     Hz.close()
     Bt.gmres(xb, np.zeros(Bt.n), 1e-8, 30, 60)
     Bt.close()
