@@ -78,6 +78,20 @@ def _dist():
     return ws, rank, local
 
 
+def replica_max_ms(ms, ws, dev):
+    """Time of a step over all replicas (N > 1: every rank runs the whole workload
+    on its own GPU, no data-path collective): the slowest rank's, by one MAX
+    all-reduce of a one-element tensor on `dev` (the rank's GPU under NCCL; the
+    CPU under gloo in the tests)."""
+    if ws <= 1:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
 
@@ -216,11 +230,7 @@ def run_gpu(args):
         e1.record(stream)
         torch.cuda.synchronize()
         launches[prec] = A.lib().ahx_kernel_launches() - l0
-        ms = e0.elapsed_time(e1)
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replica_max_ms(e0.elapsed_time(e1), ws, dev)
         return ms / steps
 
     H.prepare("fp64")
@@ -1072,10 +1082,7 @@ def run_headline(args):
         if kernel_times:
             L.ahx_timing_read(ms2.ctypes.data, cnt2.ctypes.data, 1)
             L.ahx_timing(0)
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replica_max_ms(ms, ws, dev)
         return ms / steps, (ms2 / np.maximum(cnt2, 1), cnt2)
 
     with ClockSampler(local) as cs:
