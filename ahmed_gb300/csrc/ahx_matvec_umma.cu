@@ -4,21 +4,23 @@
 //
 // One persistent CTA per SM, 20 warps with fixed roles:
 //   warp 0      producer: walks the CTA's contiguous range of tiles (ranges
-//               balanced by bytes; descriptors fetched 32 at a time); the Z-row
-//               indices of the chunk kLidx ahead go into a small queue (cp.async,
-//               two words per lane); each chunk image is bulk-copied
-//               (cp.async.bulk) into one of kSlots ring slots together with its
-//               Z rows (one bulk copy per run of consecutive rows)
+//               balanced by bytes; descriptors fetched 32 at a time) and
+//               bulk-copies (cp.async.bulk) each chunk image into one of
+//               kSlots ring slots
 //   warp 1      MMA issuer (one thread) and owner of the tensor memory: per
 //               chunk, kc / 16 tcgen05.mma of N = 128 + n16 (the first FP16
 //               part of B in rows 0 .. n8 - 1, the second in rows 128 ..
 //               128 + n8 - 1: one wide MMA per K step instead of two narrow
 //               ones, whose fixed issue cost dominates) into one of two
-//               256-column accumulators, then tcgen05.commit to the ring slot
-//               (which also frees the chunk's A stage) and the accumulator
-//   warps 2-3   A stages: the chunk's Z rows (K x 128 FP16, row-major in the
-//               slot) transposed into the K-major canonical layout with
-//               ldmatrix.trans / stmatrix, one of kA stages
+//               256-column accumulators, A read MN-major from the slot, then
+//               tcgen05.commit to the ring slot and to the accumulator
+//   warps 2-3   Z rows: each gathers half of a chunk's Z rows (indices
+//               kLidx chunks ahead in a small queue, one bulk copy each) with
+//               16-byte cp.async straight into the slot's A operand: MN-major
+//               with the 128-byte swizzle (the row of K position p is the Z
+//               row itself, its first 64 FP16 values in one atom column, its
+//               second 64 in the next), so no transposition sits between the
+//               copies and the MMAs
 //   warps 4-19  epilogue, four warps per tensor-memory lane quadrant (output
 //               rows 0-31, 32-63, 64-95, 96-127): each thread adds its accumulator row
 //               (the two parts of B summed), times the chunk's scale, to
@@ -44,42 +46,43 @@ namespace {
 
 using namespace ptx;
 
-// ---- shared-memory plan (offsets from the 1024-byte aligned base)
-constexpr uint32_t kSlots = 3;                            // ring slots (chunk image + its Z rows)
+// ---- shared-memory plan (offsets from the dynamic base, which is 1024-byte aligned)
+constexpr uint32_t kSlots = 4;                            // ring slots (chunk image + its A operand)
 constexpr uint32_t kLidx = 6;                             // Z-row indices are fetched this many chunks ahead
-constexpr uint32_t kQ = 8;                                // index queue entries (> kLidx)
-constexpr uint32_t kImgHead = 0;                          // slot offset of the chunk head
-constexpr uint32_t kImgB = kImgHead + 32;                 // slot offset of the b1 image
+constexpr uint32_t kQ = 7;                                // index queue entries (> kLidx)
+constexpr uint32_t kZWarps = 2;                           // Z-row warps, each gathers kZPos positions of a chunk
+constexpr uint32_t kZPos = kUmKc / kZWarps;
+constexpr uint32_t kARegion = 128 * kUmKc * 2;            // A operand of a chunk: 128 x 64 FP16
+constexpr uint32_t kAHalf = kARegion / 2;                 // first parts (M 0-63) | second parts (M 64-127)
+constexpr uint32_t kAKStep = 16 * 128;                    // bytes of 16 K positions (two swizzle atoms)
+constexpr uint32_t kImgHead = 0;                          // image-slot offset of the chunk head
+constexpr uint32_t kImgB = kImgHead + 32;                 // image-slot offset of the b1 image
 constexpr uint32_t kImgMax = kUmN * kUmKc * 4;            // b1 + b2 images of the largest chunk
-constexpr uint32_t kZRowPitch = kUmZPitch;                // Z rows in a slot, as in global memory
-constexpr uint32_t kZOff = (kImgB + kImgMax + 127) / 128 * 128;
-constexpr uint32_t kSlotBytes = (kZOff + kUmKc * kZRowPitch + 127) / 128 * 128;
-constexpr uint32_t kA = 2;                                // A stages
-constexpr uint32_t kAStage = 128 * kUmKc * 2;             // 128 rows x kUmKc K positions, FP16
-constexpr uint32_t kASbo = kUmKc * 16;                    // A stage: bytes per 8-row group
+constexpr uint32_t kImgSlot = kImgB + kImgMax;
+constexpr uint32_t kZRowPitch = kUmZPitch;
+constexpr uint32_t kOffImg = kSlots * kARegion;           // the A operands first (1024-byte aligned)
 constexpr uint32_t kAcc = 2;                              // tensor-memory accumulators (256 columns each)
 constexpr uint32_t kAccCols = 2 * kUmN;
-constexpr uint32_t kSRow = 33;                            // staging row stride (floats): conflict-free
-constexpr uint32_t kOffA = kSlots * kSlotBytes;
-constexpr uint32_t kOffStaging = kOffA + kA * kAStage;
+constexpr uint32_t kSRow = 32;                            // staging row (floats), columns XOR-swizzled by the row
+constexpr uint32_t kOffStaging = kOffImg + kSlots * kImgSlot;
 constexpr uint32_t kStagingBytes = 64 * kSRow * 4;        // per quarter of the output rows
 constexpr uint32_t kOffYs = kOffStaging + 4 * kStagingBytes;   // 64 doubles: Y factor per right-hand side
 constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
 constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
 constexpr uint32_t kOffIssue = kOffMeta + kSlots * 16;    // per slot: clock of the copies' issue (diagnostics)
-constexpr uint32_t kOffIdxQ = kOffIssue + kSlots * 8;     // index queue: kQ x kUmKc words
-constexpr uint32_t kOffBar = kOffIdxQ + kQ * kUmKc * 4;
-constexpr uint32_t kNumBars = 3 * kSlots + kA + 2 * kAcc + 4;
+constexpr uint32_t kOffIdxQ = kOffIssue + kSlots * 8;     // index queues: per Z warp kQ x kZPos words
+constexpr uint32_t kOffBar = kOffIdxQ + kZWarps * kQ * kZPos * 4;
+constexpr uint32_t kNumBars = 3 * kSlots + kZWarps * kQ + 2 * kAcc + 4;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;
-constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024;     // + alignment slack of the dynamic base
+constexpr uint32_t kSmemBytes = kOffTmem + 16;
 constexpr uint32_t kThreads = 640;
-constexpr uint32_t kTrWarps = 2;                          // A-stage warps: each arrives on aready
-constexpr uint32_t kEpiWarp0 = 2 + kTrWarps;              // first epilogue warp
+constexpr uint32_t kEpiWarp0 = 2 + kZWarps;               // first epilogue warp
 constexpr uint32_t kEpiWarps = 16;                        // epilogue warps: each arrives on accempty
-static_assert(kEpiWarp0 % 4 == 0, "epilogue warps cover the lane quadrants in order");
+static_assert(kThreads == 32 * (kEpiWarp0 + kEpiWarps), "roles");
 constexpr uint32_t kTmemCols = kAcc * kAccCols;           // all 512 columns
-static_assert(kSlots > kA, "an A stage is free once its previous chunk's slot is released");
-static_assert(kUmKc == 64, "the producer and the A-stage warps handle two 32-position halves");
+static_assert(kTmemCols == 512, "tensor memory");
+static_assert(kImgSlot % 16 == 0 && kOffIdxQ % 16 == 0 && (kZPos * 4) % 16 == 0, "bulk-copy destinations");
+static_assert(kARegion % 1024 == 0, "swizzle atoms");
 static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 static_assert(kQ > kLidx, "the queue entry of a chunk is read before a later prefetch reuses it");
 
@@ -109,12 +112,12 @@ struct KArgs {
 };
 
 // Per-role cycle counters of the sweeps (diagnostics, off by default): summed
-// over CTAs, lane 0 of warps 0 (producer), 1 (MMA), 2 (A stages), 6 (epilogue).
+// over CTAs, lane 0 of warps 0 (producer), 1 (MMA), 2 (Z rows) and the first epilogue warp.
 enum UmProf : uint32_t {
-  kPfProdTotal, kPfProdSlot, kPfProdIdx, kPfChunks,
-  kPfTrFz, kPfTrAempty, kPfTrWork, kPfZLatency,
-  kPfMmaAready, kPfMmaAccempty, kPfMmaImg, kPfMmaIssue,
-  kPfEpiAccfull, kPfEpiDrain, kPfEpiTile, kPfKernel,
+  kPfProdTotal, kPfProdSlot, kPfProdSpare, kPfChunks,
+  kPfMmaImg, kPfMmaAccempty, kPfMmaFz, kPfMmaIssue,
+  kPfEpiAccfull, kPfEpiDrain, kPfEpiTile, kPfZLatency,
+  kPfZIdx, kPfZSlot, kPfZIssue, kPfZSpare,
   kPfCount = 16
 };
 __device__ unsigned long long g_um_prof[kPfCount];
@@ -135,14 +138,15 @@ struct ProfClock {
 
 struct Smem {
   unsigned char* base;
-  __device__ unsigned char* slot(uint32_t i) const { return base + i * kSlotBytes; }
-  __device__ const UmHead* head(uint32_t i) const { return reinterpret_cast<const UmHead*>(slot(i) + kImgHead); }
-  __device__ uint32_t* idxq(uint32_t i) const { return reinterpret_cast<uint32_t*>(base + kOffIdxQ) + i * kUmKc; }
+  __device__ unsigned char* areg(uint32_t i) const { return base + i * kARegion; }
+  __device__ unsigned char* img(uint32_t i) const { return base + kOffImg + i * kImgSlot; }
+  __device__ const UmHead* head(uint32_t i) const { return reinterpret_cast<const UmHead*>(img(i) + kImgHead); }
+  __device__ uint32_t* idxq(uint32_t w, uint32_t i) const {
+    return reinterpret_cast<uint32_t*>(base + kOffIdxQ) + (w * kQ + i) * kZPos;
+  }
   __device__ volatile long long* issued(uint32_t i) const {
     return reinterpret_cast<volatile long long*>(base + kOffIssue) + i;
   }
-  __device__ unsigned char* zrow(uint32_t i, uint32_t k) const { return slot(i) + kZOff + k * kZRowPitch; }
-  __device__ unsigned char* astage(uint32_t i) const { return base + kOffA + i * kAStage; }
   __device__ float* staging(uint32_t quarter) const {
     return reinterpret_cast<float*>(base + kOffStaging + quarter * kStagingBytes);
   }
@@ -153,12 +157,16 @@ struct Smem {
   __device__ uint32_t fimg(uint32_t i) const { return bar(i); }
   __device__ uint32_t fz(uint32_t i) const { return bar(kSlots + i); }
   __device__ uint32_t empty(uint32_t i) const { return bar(2 * kSlots + i); }
-  __device__ uint32_t aready(uint32_t i) const { return bar(3 * kSlots + i); }
-  __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + kA + i); }
-  __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + kA + kAcc + i); }
-  __device__ uint32_t quarter(uint32_t i) const { return bar(3 * kSlots + kA + 2 * kAcc + i); }
+  __device__ uint32_t idxbar(uint32_t w, uint32_t i) const { return bar(3 * kSlots + w * kQ + i); }
+  __device__ uint32_t accfull(uint32_t i) const { return bar(3 * kSlots + kZWarps * kQ + i); }
+  __device__ uint32_t accempty(uint32_t i) const { return bar(3 * kSlots + kZWarps * kQ + kAcc + i); }
+  __device__ uint32_t quarter(uint32_t i) const { return bar(3 * kSlots + kZWarps * kQ + 2 * kAcc + i); }
   __device__ uint32_t* tmem_slot() const { return reinterpret_cast<uint32_t*>(base + kOffTmem); }
 };
+
+// staging element (right-hand side j, column c): 32 floats per j, the columns
+// XOR-swizzled by j so that a warp's accesses along j or along c hit 32 banks
+__device__ __forceinline__ uint32_t stg(uint32_t j, uint32_t c) { return j * kSRow + (c ^ (j & 31u)); }
 
 // Bounded wait; it also gives up as soon as another role has raised the error
 // word, so that one failed wait ends the whole CTA quickly.
@@ -187,17 +195,23 @@ __device__ __forceinline__ void split_h16(float v, __half& h1, __half& h2) {
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
-  extern __shared__ unsigned char smem_raw[];
-  const Smem S{smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u)};
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const Smem S{smem_raw};
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the swizzle atoms of the A operands need a 1024-byte aligned base (the
+  // dynamic shared memory of a kernel without static shared memory starts there)
+  if (smem_u32(smem_raw) & 1023u) {
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+    return;
+  }
 
   if (threadIdx.x == 0) {
     for (uint32_t i = 0; i < kSlots; ++i) {
       mbar_init(S.fimg(i), 1);
-      mbar_init(S.fz(i), 1);
+      mbar_init(S.fz(i), 32 * kZWarps);  // one cp.async arrive per lane of the Z warps
       mbar_init(S.empty(i), 1);
     }
-    for (uint32_t i = 0; i < kA; ++i) mbar_init(S.aready(i), kTrWarps);
+    for (uint32_t i = 0; i < kZWarps * kQ; ++i) mbar_init(S.bar(3 * kSlots + i), 1);
     for (uint32_t i = 0; i < 4; ++i) mbar_init(S.quarter(i), 4);
     for (uint32_t i = 0; i < kAcc; ++i) {
       mbar_init(S.accfull(i), 2);
@@ -205,12 +219,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // Z rows of a slot past a chunk's K are read into A rows that meet zero B
-  // values: they must hold finite numbers, so every slot's rows start at zero
-  for (uint32_t i = threadIdx.x; i < kSlots * (kUmKc * kZRowPitch / 16); i += kThreads) {
-    const uint32_t sl = i / (kUmKc * kZRowPitch / 16), o = i % (kUmKc * kZRowPitch / 16);
-    reinterpret_cast<uint4*>(S.slot(sl) + kZOff)[o] = make_uint4(0u, 0u, 0u, 0u);
-  }
+  // A rows past a chunk's K meet zero B values: they must hold finite
+  // numbers, so every slot's A operand starts at zero (later chunks leave
+  // only Z values behind)
+  for (uint32_t i = threadIdx.x; i < kSlots * kARegion / 16; i += kThreads)
+    reinterpret_cast<uint4*>(S.areg(0))[i] = make_uint4(0u, 0u, 0u, 0u);
   fence_proxy_async();
   if (threadIdx.x < 64) {
     // Y factor of right-hand side j: 1 / (the scale of X_j)
@@ -231,25 +244,14 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     // ---------------- producer
     ProfClock P(pf);
     const long long tk0 = P.now();
-    const uint32_t cb0 = a.cranges[blockIdx.x], ncb = a.cranges[blockIdx.x + 1] - cb0;
-    // L2: chunk images are read once (evict first); Z rows are read by many chunks (evict last)
-    const uint64_t pol_img = policy_evict_first(), pol_z = policy_evict_last();
+    // L2: chunk images are read once (evict first)
+    const uint64_t pol_img = policy_evict_first();
     uint32_t c = 0;  // chunks issued
     bool ok = true;
     // lane 0: the slot of chunk cc is free (its previous chunk has been consumed)
     auto slot_free = [&](uint32_t cc) -> bool {
       return cc < kSlots || wait_bar(S.empty(cc % kSlots), ((cc / kSlots) - 1) & 1, a.err);
     };
-    // all lanes: the Z-row indices of chunk cc into the queue (one group per chunk, empty past the end)
-    auto prefetch = [&](uint32_t cc) {
-      if (cc < ncb) {
-        const uint32_t* src = a.zidx + (uint64_t)(cb0 + cc) * kUmKc;
-        cp_async4(smem_u32(S.idxq(cc % kQ) + lane), src + lane);
-        cp_async4(smem_u32(S.idxq(cc % kQ) + 32 + lane), src + 32 + lane);
-      }
-      cp_async_commit();
-    };
-    for (uint32_t i = 0; i < kLidx; ++i) prefetch(i);
     const uint32_t t0 = a.ranges[blockIdx.x], t1 = a.ranges[blockIdx.x + 1];
     auto fetch = [&](uint32_t tb, uint4& w0, uint4& w1) {
       const uint32_t t = tb + lane;
@@ -278,11 +280,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       const uint32_t w4 = __shfl_sync(0xffffffffu, c1.x, r);
       const uint64_t tsrc = (uint64_t)w_sl | ((uint64_t)w_sh << 32);
       const uint32_t n8 = w3 & 0xffffu, hdr = w3 >> 16;
-      const uint32_t klast = w4 & 0xffffu, kvlast = w4 >> 16;
+      const uint32_t klast = w4 & 0xffffu;  // (the valid positions, w4 >> 16, matter to no copy)
       const uint64_t cstride = (uint64_t)hdr + (uint64_t)n8 * kUmKc * 4;
       for (uint32_t ch = 0; ch < nch; ++ch) {
         const bool lastc = ch + 1 == nch;
-        const uint32_t kc = lastc ? klast : kUmKc, kv = lastc ? kvlast : kUmKc;
+        const uint32_t kc = lastc ? klast : kUmKc;
         const uint32_t bytes = hdr + n8 * kc * 4;
         const uint32_t sl = c % kSlots;
         bool okl = true;
@@ -291,12 +293,6 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         P.add(1, tp);
         ok = __shfl_sync(0xffffffffu, okl ? 1u : 0u, 0) != 0;
         if (!ok) break;
-        // this chunk's indices landed (at most kLidx later groups pending)
-        prefetch(c + kLidx);
-        tp = P.now();
-        cp_async_wait<kLidx>();
-        P.add(2, tp);
-        const uint32_t zr0 = S.idxq(c % kQ)[lane], zr1 = S.idxq(c % kQ)[32 + lane];
         if (lane == 0) {
           if (pf) *S.issued(sl) = clock64();
           S.meta(sl)->hdr = hdr;
@@ -304,54 +300,32 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           // head and b1 image, then the b2 image 128 rows after the b1 image's start
           const unsigned char* src = a.stream + tsrc + (uint64_t)ch * cstride;
           const uint32_t half_bytes = n8 * kc * 2;
-          bulk_g2s_hint(smem_u32(S.slot(sl) + kImgB - hdr), src, hdr + half_bytes, S.fimg(sl), pol_img);
-          bulk_g2s_hint(smem_u32(S.slot(sl) + kImgB + kUmN * kc * 2), src + hdr + half_bytes, half_bytes,
+          bulk_g2s_hint(smem_u32(S.img(sl) + kImgB - hdr), src, hdr + half_bytes, S.fimg(sl), pol_img);
+          bulk_g2s_hint(smem_u32(S.img(sl) + kImgB + kUmN * kc * 2), src + hdr + half_bytes, half_bytes,
                         S.fimg(sl), pol_img);
-          mbar_expect_tx(S.fz(sl), kv * kZRowPitch);
-        }
-        __syncwarp();
-        // Z rows [0, kv): one bulk copy per run of consecutive rows (runs end at
-        // position 32 as well), issued by the run's first lane; two halves of 32
-#pragma unroll
-        for (uint32_t hf = 0; hf < 2; ++hf) {
-          const uint32_t zr = hf ? zr1 : zr0, p = 32 * hf + lane;
-          const uint32_t kvh = kv > 32 * hf ? min(32u, kv - 32 * hf) : 0u;  // valid positions of this half
-          const uint32_t prev = __shfl_up_sync(0xffffffffu, zr, 1);
-          const bool start = lane < kvh && (lane == 0 || zr != prev + 1u);
-          const uint32_t starts = __ballot_sync(0xffffffffu, start);
-          if (start) {
-            const uint32_t later = lane < 31 ? starts >> (lane + 1) : 0u;
-            const uint32_t end = later ? lane + 1 + (uint32_t)(__ffs(later) - 1) : kvh;
-            bulk_g2s_hint(smem_u32(S.zrow(sl, p)),
-                          reinterpret_cast<const unsigned char*>(a.z) + (uint64_t)zr * kZRowPitch,
-                          (end - lane) * kZRowPitch, S.fz(sl), pol_z);
-          }
         }
         ++c;
       }
     }
-    cp_async_wait<0>();
     if (lane == 0) {
       bool stopped = false;
       if (ok && slot_free(c)) {
-        // stop marker: a slot record without an image; both full barriers complete
+        // stop marker: a slot record without an image (the MMA thread reads
+        // it after the image barrier and waits for no Z rows; the Z warps
+        // stop after the CTA's last chunk)
         const uint32_t sl = c % kSlots;
         S.meta(sl)->hdr = 0u;
         mbar_arrive(S.fimg(sl));
-        mbar_arrive(S.fz(sl));
         stopped = true;
       }
       // every bulk copy issued has landed before the CTA may exit (bounded, but
       // not cut short by another role's error: a copy in flight must not land
       // after the CTA has exited).  Older chunks were consumed, hence landed;
       // so was chunk c - kSlots once the stop marker took its slot (its
-      // barriers have moved on by a phase since).
+      // image barrier has moved on by a phase since).
       const uint32_t keep = stopped ? kSlots - 1 : kSlots;
       const uint32_t lo = c > keep ? c - keep : 0u;
-      for (uint32_t i = lo; i < c; ++i) {
-        mbar_wait_sleep(S.fimg(i % kSlots), (i / kSlots) & 1, a.err);
-        mbar_wait_sleep(S.fz(i % kSlots), (i / kSlots) & 1, a.err);
-      }
+      for (uint32_t i = lo; i < c; ++i) mbar_wait_sleep(S.fimg(i % kSlots), (i / kSlots) & 1, a.err);
       P.add(0, tk0);
       P.acc[3] = c;
       P.flush(kPfProdTotal);
@@ -361,12 +335,13 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     // ---------------- MMA issuer
     if (lane == 0) {
       ProfClock P(pf);
+      unsigned long long zlat = 0;
       uint32_t c = 0;
       bool issued = false;
       while (true) {
-        const uint32_t sl = c % kSlots, as = c % kA, q = c % kAcc;
+        const uint32_t sl = c % kSlots, q = c % kAcc;
         long long tp = P.now();
-        if (!wait_bar(S.aready(as), (c / kA) & 1, a.err)) break;
+        if (!wait_bar(S.fimg(sl), (c / kSlots) & 1, a.err)) break;
         P.add(0, tp);
         tp = P.now();
         if (c >= kAcc && !wait_bar(S.accempty(q), ((c / kAcc) - 1) & 1, a.err)) break;
@@ -380,21 +355,26 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           break;
         }
         tp = P.now();
-        if (!wait_bar(S.fimg(sl), (c / kSlots) & 1, a.err)) break;
+        if (!wait_bar(S.fz(sl), (c / kSlots) & 1, a.err)) break;
         P.add(2, tp);
+        if (P.on) zlat += (unsigned long long)(clock64() - *S.issued(sl));  // issue -> Z rows landed
         tp = P.now();
         const UmHead h = *S.head(sl);
+        // the Z rows came through cp.async (generic proxy), the tensor core
+        // reads them through the async proxy
+        fence_proxy_async();
         tc_fence_after();
         // B rows 0 .. n8-1: first parts; rows 128 .. 128 + n8 - 1: second parts
         // (rows in between and past them are stale: their D columns are not read)
         const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
-        const uint32_t idesc = umma_idesc_f16(128, kUmN + n16);
+        const uint32_t idesc = umma_idesc_f16(128, kUmN + n16) | kUmmaAMnMajor;
         const uint32_t sbo = (uint32_t)h.kc * 16u;  // 8 rows x kc FP16 per core-matrix row group
-        const uint32_t sa = smem_u32(S.astage(as));
-        const uint32_t sb = smem_u32(S.slot(sl) + kImgB);
+        const uint32_t sa = smem_u32(S.areg(sl));
+        const uint32_t sb = smem_u32(S.img(sl) + kImgB);
         const uint32_t d = tmem + q * kAccCols;
+        // A: M atoms (first / second parts) kAHalf apart, 8-position K atoms 1024 bytes apart
         for (uint32_t s = 0; s < (uint32_t)h.kc / 16u; ++s)
-          umma_f16(d, umma_desc(sa + s * 256u, 128u, kASbo), umma_desc(sb + s * 256u, 128u, sbo), idesc,
+          umma_f16(d, umma_desc_sw128(sa + s * kAKStep, kAHalf, 1024u), umma_desc(sb + s * 256u, 128u, sbo), idesc,
                    s > 0 ? 1u : 0u);
         umma_commit(S.empty(sl));
         *S.acchdr(q) = h;
@@ -404,66 +384,80 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
         issued = true;
         ++c;
       }
-      P.flush(kPfMmaAready);
+      P.flush(kPfMmaImg);
+      if (P.on) atomicAdd(&g_um_prof[kPfZLatency], zlat);
       // the MMAs issued last have completed before the tensor memory is freed
       // (bounded, not cut short by another role's error)
       if (issued) mbar_wait_sleep(S.empty((c - 1) % kSlots), ((c - 1) / kSlots) & 1, a.err);
     }
     __syncwarp();
   } else if (warp < kEpiWarp0) {
-    // ---------------- A stages: Z rows (K x 128 FP16, row-major) -> K-major canonical
-    // 8 x 8 tiles (mt, kt): rows m = 8 mt .. 8 mt + 7, K positions 8 kt .. 8 kt + 7;
-    // source rows k = 8 kt + i at byte column 16 mt of the slot's Z rows,
-    // destination core matrix at mt * kASbo + kt * 128 (rows 16 bytes apart).
-    // ldmatrix.x4.trans / stmatrix.x4 pairs move four tiles (lanes 8 i ..
-    // 8 i + 7 address tile i of an instruction).  A stage is
-    // free once the MMAs of its previous chunk are done: that chunk's slot
-    // release (tcgen05.commit to the slot's empty barrier).
-    const uint32_t q = warp - 2;
-    ProfClock P(pf && warp == 2);
-    for (uint32_t c = 0;; ++c) {
-      const uint32_t sl = c % kSlots, as = c % kA;
-      long long tp = P.now();
-      if (!__all_sync(0xffffffffu, wait_bar(S.fz(sl), (c / kSlots) & 1, a.err))) break;
-      P.add(0, tp);
-      const bool stop = S.meta(sl)->hdr == 0u;
-      if (P.on && !stop) P.acc[3] += (unsigned long long)(clock64() - *S.issued(sl));  // issue -> Z landed
-      tp = P.now();
-      if (c >= kA) {
-        const uint32_t cp = c - kA;
-        if (!__all_sync(0xffffffffu, wait_bar(S.empty(cp % kSlots), (cp / kSlots) & 1, a.err))) break;
+    // ---------------- Z rows: positions kZPos h .. kZPos h + kZPos - 1 of every chunk
+    const uint32_t h = warp - 2;
+    ProfClock P(pf && h == 0);
+    const uint32_t cb0 = a.cranges[blockIdx.x], ncb = a.cranges[blockIdx.x + 1] - cb0;
+    // L2: indices are read once (evict first); Z rows are read by many chunks (evict last)
+    const uint64_t pol_idx = policy_evict_first(), pol_z = policy_evict_last();
+    // lane 0: this warp's Z-row indices of chunk cc into its queue entry cc % kQ (nothing past the end)
+    auto prefetch = [&](uint32_t cc) {
+      if (lane == 0 && cc < ncb) {
+        const uint32_t e = cc % kQ;
+        mbar_expect_tx(S.idxbar(h, e), kZPos * 4);
+        bulk_g2s_hint(smem_u32(S.idxq(h, e)), a.zidx + (uint64_t)(cb0 + cc) * kUmKc + kZPos * h, kZPos * 4,
+                      S.idxbar(h, e), pol_idx);
       }
+    };
+    for (uint32_t i = 0; i < kLidx; ++i) prefetch(i);
+    // lanes 0-15 move the 16 pieces of 16 bytes of position 2 r, lanes 16-31
+    // those of position 2 r + 1 (positions past a chunk's K copy Z row 0, a
+    // finite row that meets zero B values).  Piece i = lane % 16 (FP16 values
+    // 8 i .. 8 i + 7 of the row) goes to the first-part (i < 8) or second-part
+    // half of the A operand, 16-byte column (i % 8) ^ (p % 8) of row p: the
+    // 128-byte swizzle
+    const uint32_t zpiece = lane & 15u, odd = lane >> 4;
+    const unsigned char* zsrc = reinterpret_cast<const unsigned char*>(a.z) + 16u * zpiece;
+    uint32_t c = 0;
+    for (; c < ncb; ++c) {
+      const uint32_t sl = c % kSlots, e = c % kQ;
+      long long tp = P.now();
+      if (!__all_sync(0xffffffffu, wait_bar(S.idxbar(h, e), (c / kQ) & 1, a.err))) break;
+      P.add(0, tp);
+      tp = P.now();
+      if (c >= kSlots && !__all_sync(0xffffffffu, wait_bar(S.empty(sl), ((c / kSlots) - 1) & 1, a.err))) break;
       P.add(1, tp);
       tp = P.now();
-      if (!stop) {
-        const uint32_t dst0 = smem_u32(S.astage(as));
-        // 128 tiles: each warp moves 64 in two batches of 8 instruction pairs, all
-        // loads of a batch before its stores (a store may alias a later load for
-        // the compiler, which would otherwise serialise each pair)
+      // index of position 2 r + odd (of this warp's positions) in zi[r]
+      uint32_t zi[kZPos / 2];
+      const uint4* q4 = reinterpret_cast<const uint4*>(S.idxq(h, e));
 #pragma unroll
-        for (uint32_t bt = 0; bt < 2; ++bt) {
-          uint32_t r[8][4];
-#pragma unroll
-          for (uint32_t g = 0; g < 8; ++g) {
-            const uint32_t T = q * 64 + bt * 32 + g * 4 + (lane >> 3);
-            const uint32_t mt = T & 15u, kt = T >> 4;
-            ldsm_x4_t(r[g], smem_u32(S.zrow(sl, kt * 8 + (lane & 7)) + mt * 16));
-          }
-#pragma unroll
-          for (uint32_t g = 0; g < 8; ++g) {
-            const uint32_t T = q * 64 + bt * 32 + g * 4 + (lane >> 3);
-            const uint32_t mt = T & 15u, kt = T >> 4;
-            stsm_x4(dst0 + mt * kASbo + kt * 128u + (lane & 7) * 16u, r[g]);
-          }
-        }
-        fence_proxy_async();  // generic writes -> the tensor core's (async proxy) reads
+      for (uint32_t v = 0; v < kZPos / 4; ++v) {
+        const uint4 w = q4[v];
+        zi[2 * v] = odd ? w.y : w.x;
+        zi[2 * v + 1] = odd ? w.w : w.z;
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(S.aready(as));
+      const uint32_t dst0 = smem_u32(S.areg(sl)) + (zpiece >> 3) * kAHalf + kZPos * h * 128u;
+#pragma unroll
+      for (uint32_t r = 0; r < kZPos / 2; ++r) {
+        const uint32_t p = 2 * r + odd;  // (kZPos h + p) % 8 = p % 8
+        cp_async16_hint(dst0 + p * 128u + (((zpiece & 7u) ^ (p & 7u)) << 4), zsrc + (uint64_t)zi[r] * kZRowPitch,
+                        pol_z);
+      }
+      cp_async_mbar_arrive(S.fz(sl));
       P.add(2, tp);
-      if (stop) break;
+      // the queue entry of chunk c + kLidx last held chunk c + kLidx - kQ < c,
+      // whose indices every lane of this warp has read
+      __syncwarp();
+      prefetch(c + kLidx);
     }
-    P.flush(kPfTrFz);
+    cp_async_commit();
+    cp_async_wait<0>();  // this lane's Z copies have landed
+    if (lane == 0) {
+      // index copies issued for chunks that were not taken (an early stop)
+      const uint32_t ie = min(ncb, c + kLidx);
+      for (uint32_t i = c; i < ie; ++i) mbar_wait_sleep(S.idxbar(h, i % kQ), (i / kQ) & 1, a.err);
+      P.flush(kPfZIdx);
+    }
+    __syncwarp();
   } else {
     // ---------------- epilogue
     const uint32_t q = warp & 3;                  // tensor-memory lane quadrant of this warp
@@ -526,12 +520,12 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       if (!qsync()) break;  // the staging tile is free
       if (active && !second) {
 #pragma unroll
-        for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] = acc[c];
+        for (int c = 0; c < 32; ++c) Sg[stg(j, c)] = acc[c];
       }
       if (!qsync()) break;
       if (active && second) {
 #pragma unroll
-        for (int c = 0; c < 32; ++c) Sg[j * kSRow + c] += acc[c];
+        for (int c = 0; c < 32; ++c) Sg[stg(j, c)] += acc[c];
       }
       if (!qsync()) break;
       const uint32_t nh = min(32u, (uint32_t)h.nout - 32 * qr);
@@ -544,19 +538,19 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
           const uint32_t jj = e >> 5, c = e & 31;
           if (c < nh)
             red_add_f64(a.y + (uint64_t)(row0 + c) + (uint64_t)jj * a.ldy,
-                        a.d * S.ys()[jj] * (double)Sg[jj * kSRow + c]);
+                        a.d * S.ys()[jj] * (double)Sg[stg(jj, c)]);
         }
       } else if (h.flags & kUmRed) {
         for (uint32_t e = et; e < a.pg * 32; e += 128) {
           const uint32_t jj = e % a.pg, c = e / a.pg;
-          if (c < nh) atomicAdd(a.tacc + (uint64_t)(h.tacc + 32 * qr + c) * 64 + jj, Sg[jj * kSRow + c]);
+          if (c < nh) atomicAdd(a.tacc + (uint64_t)(h.tacc + 32 * qr + c) * 64 + jj, Sg[stg(jj, c)]);
         }
       } else {
         for (uint32_t e = et; e < a.pg * 32; e += 128) {
           const uint32_t jj = e % a.pg, c = e / a.pg;
           if (c < nh) {
             __half h1, h2;
-            split_h16(Sg[jj * kSRow + c], h1, h2);
+            split_h16(Sg[stg(jj, c)], h1, h2);
             __half* zp = reinterpret_cast<__half*>(a.z) + (a.n + row0 + c) * (kUmZPitch / 2);
             zp[jj] = h1;
             zp[64 + jj] = h2;

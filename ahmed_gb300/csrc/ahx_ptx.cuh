@@ -99,6 +99,19 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// 16-byte asynchronous copy global -> shared that bypasses L1 (cp.async.cg),
+// with an L2 cache policy for the source line
+__device__ __forceinline__ void cp_async16_hint(uint32_t dst, const void* src, uint64_t policy) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "l"(policy)
+               : "memory");
+}
+
+// one arrive on the mbarrier once every earlier cp.async of this thread has
+// landed; the barrier's expected arrival count includes it (.noinc)
+__device__ __forceinline__ void cp_async_mbar_arrive(uint32_t bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
@@ -189,13 +202,14 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// The same, K-major with the 128-byte swizzle (layout type 2): atoms of 8 rows
-// x 128 bytes, 16-byte chunk c of row r stored at chunk c ^ r; atoms of
-// consecutive 8-row groups sbo bytes apart; the start address advances by the
-// byte offset of the K step inside the atom.
-__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
-         (1ull << 46) | (2ull << 61);
+// The same with the 128-byte swizzle (layout type 2): atoms of 8 rows x 128
+// bytes (1024-byte aligned), 16-byte chunk c of row r stored at chunk c ^ r.
+// MN-major operand: a row holds 64 consecutive M (or N) elements of one K
+// position, the 8 rows of an atom 8 consecutive K positions; lbo = bytes
+// between atoms adjacent in M (N), sbo = bytes between atoms adjacent in K.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | (2ull << 61);
 }
 
 // Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
@@ -210,6 +224,9 @@ __host__ __device__ constexpr uint32_t umma_idesc_tf32(uint32_t m, uint32_t n) {
 __host__ __device__ constexpr uint32_t umma_idesc_f16(uint32_t m, uint32_t n) {
   return (1u << 4) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
+
+// bit 15 of the instruction descriptor: A is MN-major (transposed)
+constexpr uint32_t kUmmaAMnMajor = 1u << 15;
 
 __device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
