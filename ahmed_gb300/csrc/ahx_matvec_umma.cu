@@ -36,6 +36,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include "ahx_ptx.cuh"
@@ -93,6 +95,7 @@ struct SlotMeta {
 };
 
 struct KArgs {
+  CUtensorMap zmap;        // Z rows as a 2D tensor (128 FP16 x rows), boxes of 64 x kZPos, 128-byte swizzle
   const UmTile* tiles;
   const uint32_t* ranges;  // per CTA: first tile (gridDim.x + 1 entries), balanced by bytes
   const uint32_t* cranges; // per CTA: first chunk (gridDim.x + 1 entries)
@@ -194,7 +197,7 @@ __device__ __forceinline__ void split_h16(float v, __half& h1, __half& h2) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(const __grid_constant__ KArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const Smem S{smem_raw};
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -208,7 +211,9 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
   if (threadIdx.x == 0) {
     for (uint32_t i = 0; i < kSlots; ++i) {
       mbar_init(S.fimg(i), 1);
-      mbar_init(S.fz(i), 32 * kZWarps);  // one cp.async arrive per lane of the Z warps
+      // per Z warp: one cp.async arrive per lane and one arrive (with the
+      // tensor copies' bytes, or none) by lane 0
+      mbar_init(S.fz(i), 33 * kZWarps);
       mbar_init(S.empty(i), 1);
     }
     for (uint32_t i = 0; i < kZWarps * kQ; ++i) mbar_init(S.bar(3 * kSlots + i), 1);
@@ -408,15 +413,18 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       }
     };
     for (uint32_t i = 0; i < kLidx; ++i) prefetch(i);
-    // lanes 0-15 move the 16 pieces of 16 bytes of position 2 r, lanes 16-31
-    // those of position 2 r + 1 (positions past a chunk's K copy Z row 0, a
-    // finite row that meets zero B values).  Piece i = lane % 16 (FP16 values
-    // 8 i .. 8 i + 7 of the row) goes to the first-part (i < 8) or second-part
-    // half of the A operand, 16-byte column (i % 8) ^ (p % 8) of row p: the
-    // 128-byte swizzle
+    // Consecutive rows (a contiguous tile: X rows of a V tile or of a dense
+    // leaf): two tensor copies, lane 0, of kZPos rows x 64 FP16 (first / second
+    // parts); the copy engine writes them with the 128-byte swizzle.  Other
+    // rows: lanes 0-15 move the 16 pieces of 16 bytes of position 2 r, lanes
+    // 16-31 those of position 2 r + 1 (positions past a chunk's K copy Z row
+    // 0, a finite row that meets zero B values).  Piece i = lane % 16 (FP16
+    // values 8 i .. 8 i + 7 of the row) goes to the first-part (i < 8) or
+    // second-part half of the A operand, 16-byte column (i % 8) ^ (p % 8) of
+    // row p: the same 128-byte swizzle.
     const uint32_t zpiece = lane & 15u, odd = lane >> 4;
     const unsigned char* zsrc = reinterpret_cast<const unsigned char*>(a.z) + 16u * zpiece;
-    uint32_t c = 0;
+    uint32_t c = 0, tma_recent = 0;  // bit i: chunk c - 1 - i came by tensor copies
     for (; c < ncb; ++c) {
       const uint32_t sl = c % kSlots, e = c % kQ;
       long long tp = P.now();
@@ -429,20 +437,35 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
       // index of position 2 r + odd (of this warp's positions) in zi[r]
       uint32_t zi[kZPos / 2];
       const uint4* q4 = reinterpret_cast<const uint4*>(S.idxq(h, e));
+      const uint32_t z0 = q4[0].x;
+      bool seq = true;
 #pragma unroll
       for (uint32_t v = 0; v < kZPos / 4; ++v) {
         const uint4 w = q4[v];
         zi[2 * v] = odd ? w.y : w.x;
         zi[2 * v + 1] = odd ? w.w : w.z;
+        seq &= zi[2 * v] == z0 + 4 * v + odd && zi[2 * v + 1] == z0 + 4 * v + 2 + odd;
       }
-      const uint32_t dst0 = smem_u32(S.areg(sl)) + (zpiece >> 3) * kAHalf + kZPos * h * 128u;
+      seq = __all_sync(0xffffffffu, seq);
+      const uint32_t dst0 = smem_u32(S.areg(sl)) + kZPos * h * 128u;
+      if (seq) {
+        if (lane == 0) {
+          mbar_expect_tx(S.fz(sl), kZPos * kUmZRowBytes);
+          tma_load_2d_hint(dst0, &a.zmap, 0, (int32_t)z0, S.fz(sl), pol_z);
+          tma_load_2d_hint(dst0 + kAHalf, &a.zmap, 64, (int32_t)z0, S.fz(sl), pol_z);
+        }
+      } else {
+        if (lane == 0) mbar_arrive(S.fz(sl));
+        const uint32_t dz = dst0 + (zpiece >> 3) * kAHalf;
 #pragma unroll
-      for (uint32_t r = 0; r < kZPos / 2; ++r) {
-        const uint32_t p = 2 * r + odd;  // (kZPos h + p) % 8 = p % 8
-        cp_async16_hint(dst0 + p * 128u + (((zpiece & 7u) ^ (p & 7u)) << 4), zsrc + (uint64_t)zi[r] * kZRowPitch,
-                        pol_z);
+        for (uint32_t r = 0; r < kZPos / 2; ++r) {
+          const uint32_t p = 2 * r + odd;  // (kZPos h + p) % 8 = p % 8
+          cp_async16_hint(dz + p * 128u + (((zpiece & 7u) ^ (p & 7u)) << 4), zsrc + (uint64_t)zi[r] * kZRowPitch,
+                          pol_z);
+        }
       }
       cp_async_mbar_arrive(S.fz(sl));
+      tma_recent = (tma_recent << 1) | (seq ? 1u : 0u);
       P.add(2, tp);
       // the queue entry of chunk c + kLidx last held chunk c + kLidx - kQ < c,
       // whose indices every lane of this warp has read
@@ -452,6 +475,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(KArgs a) {
     cp_async_commit();
     cp_async_wait<0>();  // this lane's Z copies have landed
     if (lane == 0) {
+      // tensor copies of the last kSlots chunks have landed (older chunks were
+      // consumed, hence landed; the wait gives up after its limit if the other
+      // Z warp never arrived, long after the copy itself)
+      for (uint32_t i = 0; i < kSlots && i < c; ++i)
+        if ((tma_recent >> i) & 1u) mbar_wait_sleep(S.fz((c - 1 - i) % kSlots), ((c - 1 - i) / kSlots) & 1, a.err);
       // index copies issued for chunks that were not taken (an early stop)
       const uint32_t ie = min(ncb, c + kLidx);
       for (uint32_t i = c; i < ie; ++i) mbar_wait_sleep(S.idxbar(h, i % kQ), (i / kQ) & 1, a.err);
@@ -835,6 +863,28 @@ cudaError_t launch_sweep(const KArgs& a, int kind, uint32_t grid, cudaStream_t s
   return e;
 }
 
+// Z rows (n + t_rows + 1 rows of 128 FP16, kUmZPitch bytes apart) as a 2D
+// tensor for the sweeps' tensor copies: boxes of 64 values x kZPos rows, 128-byte swizzle
+cudaError_t encode_zmap(CUtensorMap* m, const uint16_t* z, uint64_t zrows) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  if (!encode) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {kUmZRowBytes / 2, zrows};
+  const cuuint64_t strides[1] = {kUmZPitch};
+  const cuuint32_t box[2] = {64, kZPos};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<uint16_t*>(z), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const double* X, uint64_t ldX, double* Y,
                    uint64_t ldY, cudaStream_t s) {
   const uint64_t nblk = (pl.n + 31) / 32;
@@ -848,6 +898,7 @@ cudaError_t run_um(const UmPlan& pl, double d, uint32_t r0, uint32_t pg, const d
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   uint64_t launches = 2;
   KArgs a{};
+  if ((e = encode_zmap(&a.zmap, pl.z, pl.n + pl.t_rows + 1)) != cudaSuccess) return e;
   a.z = pl.z;
   a.tacc = pl.tacc;
   a.xmax = pl.xmax;

@@ -81,6 +81,18 @@ __device__ __forceinline__ void bulk_g2s_hint(uint32_t dst, const void* src, uin
       : "memory");
 }
 
+// 2D tensor copy global -> shared: the box of the tensor map (a CUtensorMap in
+// parameter or global memory) at element coordinates (x, y), completing on the
+// mbarrier, with an L2 cache policy
+__device__ __forceinline__ void tma_load_2d_hint(uint32_t dst, const void* map, int32_t x, int32_t y, uint32_t bar,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(bar), "l"(policy)
+      : "memory");
+}
+
 // L2 policies: data streamed once (evict first) and rows reused by many units (evict last)
 __device__ __forceinline__ uint64_t policy_evict_first() {
   uint64_t p;

@@ -178,7 +178,7 @@ struct UmPlan {
   uint32_t nzero = 0;
   uint64_t n = 0;          // rows of X / Y
   uint32_t t_rows = 0;
-  uint16_t* z = nullptr;   // Z rows: X rows (n) then T rows (t_rows), kUmZPitch bytes apart
+  uint16_t* z = nullptr;   // Z rows: X rows (n), T rows (t_rows), one spare row; kUmZPitch bytes apart
   float* tacc = nullptr;   // FP32 accumulation rows of split V tiles (64 floats each), zero between products
   uint32_t* xmax = nullptr;  // 64 words: max |X_j| of the pass (FP32 bits)
   int* err = nullptr;
