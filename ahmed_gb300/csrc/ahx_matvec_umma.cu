@@ -803,12 +803,15 @@ __global__ void __launch_bounds__(256) um_build_kernel(const UmBuild* __restrict
       *reinterpret_cast<UmHead*>(B - 32) = h;
     }
     if (tid < kUmKc) {
-      // Z rows of the chunk's K positions (positions past kval unused)
+      // Z rows of the chunk's K positions.  Past kval the rows meet zero B
+      // values: row 0 in indexed tiles; in contiguous tiles the run goes on, so
+      // that every chunk's rows stay one run for the sweeps' tensor copies
+      // (which read rows past the end of Z as zeros)
       uint32_t zr = 0;
-      if (tid < kval) {
-        if (contig) {
-          zr = T.zrow0 + kb + tid;
-        } else if (ent[tid] >= 0) {
+      if (contig) {
+        zr = T.zrow0 + kb + tid;
+      } else if (tid < kval) {
+        if (ent[tid] >= 0) {
           const UmEntry E = entries[T.e0 + ent[tid]];
           zr = E.zrow0 + (kb + tid - E.k0);
         }

@@ -43,9 +43,10 @@
 //     (n / 8) * (kc * 16) + (k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2
 // (leading-dimension byte offset 128, stride byte offset kc * 16; kc a
 // multiple of 16).  One bulk copy moves a chunk image into the kernel's ring.
-// The Z rows of every chunk (64 row indices per chunk, in chunk order, the
-// positions past the chunk's K unused) are a separate array, so that the
-// kernel can fetch them well ahead of the images.
+// The Z rows of every chunk (64 row indices per chunk, in chunk order; past
+// the chunk's K they meet zero B values: row 0, or in contiguous tiles the run
+// continued) are a separate array, so that the kernel can fetch them well
+// ahead of the images.
 #pragma once
 #include <cstdint>
 #include <vector>
