@@ -72,7 +72,7 @@ constexpr uint32_t kOffYs = kOffStaging + 4 * kStagingBytes;   // 64 doubles: Y 
 constexpr uint32_t kOffAccHdr = kOffYs + 64 * 8;
 constexpr uint32_t kOffMeta = kOffAccHdr + kAcc * sizeof(UmHead);
 constexpr uint32_t kOffIssue = kOffMeta + kSlots * 16;    // per slot: clock of the copies' issue (diagnostics)
-constexpr uint32_t kOffIdxQ = kOffIssue + kSlots * 8;     // index queues: per Z warp kQ x kZPos words
+constexpr uint32_t kOffIdxQ = (kOffIssue + kSlots * 8 + 15) / 16 * 16;  // index queues: per Z warp kQ x kZPos words
 constexpr uint32_t kOffBar = kOffIdxQ + kZWarps * kQ * kZPos * 4;
 constexpr uint32_t kNumBars = 3 * kSlots + kZWarps * kQ + 2 * kAcc + 4;
 constexpr uint32_t kOffTmem = kOffBar + kNumBars * 8;

@@ -62,7 +62,7 @@ constexpr uint32_t kUmN = 128;    // rows (N) per tile
 constexpr uint32_t kUmIdxBytes = kUmKc * 4;
 constexpr uint32_t kUmSlots = 64;           // right-hand-side slots of a Z row
 constexpr uint32_t kUmZRowBytes = 256;      // 64 first parts, 64 second parts (FP16)
-constexpr uint32_t kUmZPitch = 272;         // bytes between Z rows (16-byte skew: conflict-free row reads)
+constexpr uint32_t kUmZPitch = 272;         // bytes between Z rows (a multiple of 16: the row stride of the tensor copies)
 
 enum UmFlags : uint32_t {
   kUmFirst = 1u,    // first chunk of its tile
