@@ -8,8 +8,8 @@
 //               bulk-copies (cp.async.bulk) each chunk image into one of
 //               kSlots ring slots
 //   warp 1      MMA issuer (one thread) and owner of the tensor memory: per
-//               chunk, kc / 16 tcgen05.mma of N = 128 + n16 (the first FP16
-//               part of B in rows 0 .. n8 - 1, the second in rows 128 ..
+//               chunk, kc / 16 tcgen05.mma of N = 2 n16 (the first FP16
+//               part of B in rows 0 .. n8 - 1, the second in rows n16 ..
 //               128 + n8 - 1: one wide MMA per K step instead of two narrow
 //               ones, whose fixed issue cost dominates) into one of two
 //               256-column accumulators, A read MN-major from the slot, then
@@ -302,11 +302,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(const __grid_cons
           if (pf) *S.issued(sl) = clock64();
           S.meta(sl)->hdr = hdr;
           mbar_expect_tx(S.fimg(sl), bytes);
-          // head and b1 image, then the b2 image 128 rows after the b1 image's start
+          // head and b1 image, then the b2 image n16 rows after the b1 image's start
           const unsigned char* src = a.stream + tsrc + (uint64_t)ch * cstride;
-          const uint32_t half_bytes = n8 * kc * 2;
+          const uint32_t half_bytes = n8 * kc * 2, n16 = (n8 + 15u) & ~15u;
           bulk_g2s_hint(smem_u32(S.img(sl) + kImgB - hdr), src, hdr + half_bytes, S.fimg(sl), pol_img);
-          bulk_g2s_hint(smem_u32(S.img(sl) + kImgB + kUmN * kc * 2), src + hdr + half_bytes, half_bytes,
+          bulk_g2s_hint(smem_u32(S.img(sl) + kImgB + n16 * kc * 2), src + hdr + half_bytes, half_bytes,
                         S.fimg(sl), pol_img);
         }
         ++c;
@@ -369,10 +369,11 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(const __grid_cons
         // reads them through the async proxy
         fence_proxy_async();
         tc_fence_after();
-        // B rows 0 .. n8-1: first parts; rows 128 .. 128 + n8 - 1: second parts
-        // (rows in between and past them are stale: their D columns are not read)
+        // B rows 0 .. n8-1: first parts; rows n16 .. n16 + n8 - 1: second parts
+        // (rows in between and past them are stale: their D columns are not read);
+        // a narrow tile takes a narrow MMA
         const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
-        const uint32_t idesc = umma_idesc_f16(128, kUmN + n16) | kUmmaAMnMajor;
+        const uint32_t idesc = umma_idesc_f16(128, 2 * n16) | kUmmaAMnMajor;
         const uint32_t sbo = (uint32_t)h.kc * 16u;  // 8 rows x kc FP16 per core-matrix row group
         const uint32_t sa = smem_u32(S.areg(sl));
         const uint32_t sb = smem_u32(S.img(sl) + kImgB);
@@ -523,16 +524,18 @@ __global__ void __launch_bounds__(kThreads, 1) um_sweep_kernel(const __grid_cons
       const bool first = h.flags & kUmFirst;
       const float sc = h.scale;
       // tcgen05.ld / wait::ld are warp-collective: warp-uniform conditions only.
-      // Output row r of the tile: D column r (first parts of B) + column 128 + r
-      // (second parts).
+      // Output row r of the tile: D column r (first parts of B) + column n16 + r
+      // (second parts).  Rows r >= n8 read other columns (or columns past the
+      // MMA's N); they are never written out.
       if (qactive && 32 * qr < h.n8) {
         const uint32_t t0 = tmem + ((32 * q) << 16) + qa * kAccCols + 32 * qr;
+        const uint32_t n16 = ((uint32_t)h.n8 + 15u) & ~15u;
         float v[32];
         tmem_ld32(t0, v);
         tmem_wait_ld();
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] = first ? v[i] * sc : fmaf(v[i], sc, acc[i]);
-        tmem_ld32(t0 + kUmN, v);
+        tmem_ld32(t0 + n16, v);
         tmem_wait_ld();
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] = fmaf(v[i], sc, acc[i]);
